@@ -1,0 +1,238 @@
+"""final184_gb300 -- GB300-native voxel cone-tracing GI path of Final184 (Python host bindings).
+
+The compute path is libf184gi.so (hand-written sm_103a CUDA behind the C ABI in include/f184gi.h).  This module
+is a thin ctypes layer that keeps the reference renderer's pass shape: a frame calls voxelize -> mip -> trace
+(CMegaPipeline::Render, Foreground/Renderer/MegaPipeline.cpp:188-268).  Device buffers are passed as raw
+device pointers (e.g. torch.Tensor.data_ptr()); streams as cudaStream_t handles (int) or None.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import _abi
+from ._abi import (FMT_F16, FMT_F32, GRID_KEEP_COUNTS, Bounds, ConeParams, F184Error, GridDesc, GridFrame, Light,
+                   View, check, load)
+
+__all__ = ["VoxelGI", "Grid", "SyntheticScene", "Light", "Bounds", "View", "ConeParams", "GridDesc", "GridFrame",
+           "FMT_F32", "FMT_F16", "GRID_KEEP_COUNTS", "F184Error", "perspective", "ortho", "look_at", "mat4_inverse",
+           "make_light", "make_bounds", "default_cone_params", "frame_from_bounds", "make_view", "load"]
+
+
+def _fa(values, n):
+    return (C.c_float * n)(*[float(v) for v in np.asarray(values, dtype=np.float64).ravel()])
+
+
+def perspective(fovy_deg, aspect, near, far):
+    """CCamera::CalcPerspective (Foreground/SceneGraph/Camera.cpp:85-102), row-major 4x4."""
+    out = (C.c_float * 16)()
+    load().f184gi_camera_perspective(fovy_deg, aspect, near, far, out)
+    return np.array(out, dtype=np.float32).reshape(4, 4)
+
+
+def ortho(mag_x, mag_y, near, far):
+    """CCamera::CalcOrtho (Camera.cpp:104-111), row-major 4x4."""
+    out = (C.c_float * 16)()
+    load().f184gi_camera_ortho(mag_x, mag_y, near, far, out)
+    return np.array(out, dtype=np.float32).reshape(4, 4)
+
+
+def look_at(eye, target):
+    out = (C.c_float * 16)()
+    load().f184gi_camera_look_at(_fa(eye, 3), _fa(target, 3), out)
+    return np.array(out, dtype=np.float32).reshape(4, 4)
+
+
+def mat4_inverse(m):
+    out = (C.c_float * 16)()
+    check(load().f184gi_mat4_inverse(_fa(m, 16), out))
+    return np.array(out, dtype=np.float32).reshape(4, 4)
+
+
+def make_light(luminance, direction):
+    lt = Light()
+    for i in range(3):
+        lt.luminance[i] = float(luminance[i])
+        lt.direction[i] = float(direction[i])
+    return lt
+
+
+def make_bounds(mn, mx):
+    b = Bounds()
+    b.min.x, b.min.y, b.min.z = (float(v) for v in mn)
+    b.max.x, b.max.y, b.max.z = (float(v) for v in mx)
+    return b
+
+
+def frame_from_bounds(bounds, dim, light_dir):
+    """Grid placement + light frame computed on the host (bit-identical to the device's)."""
+    f = GridFrame()
+    check(load().f184gi_frame_from_bounds(C.byref(bounds), dim, _fa(light_dir, 3), C.byref(f)))
+    return f
+
+
+def default_cone_params():
+    p = ConeParams()
+    load().f184gi_cone_params_default(C.byref(p))
+    return p
+
+
+class SyntheticScene:
+    """Seeded scene (room + boxes/UV-spheres) owned by the library; arrays are numpy copies."""
+
+    def __init__(self, seed, target_tris, nobjects):
+        lib = load()
+        ptr = C.POINTER(_abi.Scene)()
+        check(lib.f184gi_scene_generate(seed, target_tris, nobjects, C.byref(ptr)))
+        self._ptr = ptr
+        s = ptr.contents
+        self.seed = seed
+        self.ntris = int(s.ntris)
+        self.nobjects = int(s.nobjects)
+        self.bounds = s.bounds
+        self.light = s.light
+        self.eye = np.array(s.eye, dtype=np.float32)
+        self.target = np.array(s.target, dtype=np.float32)
+        self._refresh()
+
+    def _refresh(self):
+        s = self._ptr.contents
+        n = self.ntris
+        self.tri_xyz = np.ctypeslib.as_array(s.tri_xyz, shape=(n * 9,)).copy()
+        self.albedo = np.ctypeslib.as_array(s.albedo, shape=(n,)).copy()
+        self.roughness = np.ctypeslib.as_array(s.roughness, shape=(n,)).copy()
+        self.object_first = np.ctypeslib.as_array(s.object_first, shape=(self.nobjects,)).copy()
+        self.object_count = np.ctypeslib.as_array(s.object_count, shape=(self.nobjects,)).copy()
+
+    def camera(self, i, seed=None):
+        eye = (C.c_float * 3)()
+        tgt = (C.c_float * 3)()
+        check(load().f184gi_scene_camera(self._ptr, self.seed if seed is None else seed, i, eye, tgt))
+        return np.array(eye, dtype=np.float32), np.array(tgt, dtype=np.float32)
+
+    def move_objects(self, seed, fraction, max_offset):
+        moved = (C.c_uint32 * self.nobjects)()
+        n = C.c_uint32()
+        check(load().f184gi_scene_move_objects(self._ptr, seed, fraction, max_offset, moved, C.byref(n)))
+        self._refresh()
+        return np.array(moved[: n.value], dtype=np.uint32)
+
+    def __del__(self):
+        try:
+            if self._ptr:
+                load().f184gi_scene_free(self._ptr)
+                self._ptr = None
+        except Exception:
+            pass
+
+
+class Grid:
+    def __init__(self, gi, handle, desc):
+        self.gi = gi
+        self.handle = handle
+        self.desc = desc
+
+    @property
+    def dim(self):
+        return self.desc.dim
+
+    def level_dim(self, level):
+        return self.desc.dim >> level
+
+
+def _stream(s):
+    if s is None:
+        return None
+    if hasattr(s, "cuda_stream"):
+        return C.c_void_p(s.cuda_stream)
+    return C.c_void_p(int(s))
+
+
+class VoxelGI:
+    """One f184gi context: resident grids plus the voxelize / mip / trace passes."""
+
+    def __init__(self, device=0, hbm_budget=0):
+        self.lib = load()
+        cfg = _abi.Config(device, 0, hbm_budget)
+        ctx = C.c_void_p()
+        check(self.lib.f184gi_create(C.byref(cfg), C.byref(ctx)))
+        self.ctx = ctx
+
+    def close(self):
+        if self.ctx:
+            check(self.lib.f184gi_destroy(self.ctx))
+            self.ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def memory_used(self):
+        v = C.c_uint64()
+        check(self.lib.f184gi_memory_used(self.ctx, C.byref(v)))
+        return v.value
+
+    def create_grid(self, dim, levels, fmt=FMT_F32, anisotropic=0, shadow_res=1024, flags=0):
+        d = GridDesc(dim, levels, fmt, anisotropic, shadow_res, flags)
+        h = C.c_uint32()
+        check(self.lib.f184gi_grid_create(self.ctx, C.byref(d), C.byref(h)))
+        return Grid(self, h.value, d)
+
+    def destroy_grid(self, grid):
+        check(self.lib.f184gi_grid_destroy(self.ctx, grid.handle))
+
+    def voxelize(self, grid, tri_ptr, albedo_ptr, ntris, light, bounds=None, dirty_ptr=None, ndirty=0, stream=None):
+        check(self.lib.f184gi_voxelize(self.ctx, grid.handle, tri_ptr, albedo_ptr, ntris,
+                                       C.byref(bounds) if bounds is not None else None, C.byref(light),
+                                       dirty_ptr, ndirty, _stream(stream)))
+
+    def mip(self, grid, levels=0, stream=None):
+        check(self.lib.f184gi_mip(self.ctx, grid.handle, levels, grid.desc.anisotropic, _stream(stream)))
+
+    def trace(self, grid, views, params=None, stream=None):
+        arr = (View * len(views))(*views)
+        check(self.lib.f184gi_trace(self.ctx, grid.handle, arr, len(views),
+                                    C.byref(params) if params is not None else None, _stream(stream)))
+
+    def gbuffer(self, tri_ptr, rough_ptr, ntris, view, tri_id_ptr=None, stream=None):
+        check(self.lib.f184gi_gbuffer(self.ctx, tri_ptr, rough_ptr, ntris, C.byref(view), tri_id_ptr,
+                                      _stream(stream)))
+
+    def sync(self, stream=None):
+        check(self.lib.f184gi_sync(self.ctx, _stream(stream)))
+
+    def frame(self, grid):
+        f = GridFrame()
+        check(self.lib.f184gi_grid_get_frame(self.ctx, grid.handle, C.byref(f)))
+        return f
+
+    def read_level(self, grid, level, direction=0):
+        d = grid.level_dim(level)
+        out = np.empty((d, d, d, 4), dtype=np.float32)
+        check(self.lib.f184gi_grid_read_level(self.ctx, grid.handle, level, direction, out.ctypes.data))
+        return out
+
+    def read_shadow(self, grid):
+        r = grid.desc.shadow_res
+        out = np.empty((r, r), dtype=np.float32)
+        check(self.lib.f184gi_grid_read_shadow(self.ctx, grid.handle, out.ctypes.data))
+        return out
+
+    def read_counts(self, grid):
+        d = grid.dim
+        out = np.empty((d, d, d), dtype=np.uint32)
+        check(self.lib.f184gi_grid_read_counts(self.ctx, grid.handle, out.ctypes.data))
+        return out
+
+
+def make_view(view_m, proj_m, width, height, depth_ptr, normal_ptr, rough_ptr, out_ptr, out_format=FMT_F32):
+    v = View()
+    for i, x in enumerate(np.asarray(view_m, dtype=np.float32).ravel()):
+        v.view[i] = float(x)
+    for i, x in enumerate(np.asarray(proj_m, dtype=np.float32).ravel()):
+        v.proj[i] = float(x)
+    v.width, v.height = width, height
+    v.depth, v.normal, v.roughness, v.out = depth_ptr, normal_ptr, rough_ptr, out_ptr
+    v.out_format = out_format
+    return v

@@ -1,0 +1,534 @@
+// api.cpp -- the f184gi C ABI: contexts, resident grids, the three passes and inspection.
+//
+// A context owns device memory under an optional HBM budget: resident grids (mip chain + shadow map + frame)
+// and per-pass scratch that grows on demand and is reused.  Calls are stream-ordered on the caller's stream;
+// kernels report overflow/timeout through a device status word that f184gi_sync and the inspection calls read.
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "frame.h"
+#include "gi_internal.h"
+#include "util.cuh"
+
+namespace f184 {
+
+namespace {
+thread_local std::string g_last_error;
+}
+
+int fail(int code, const std::string& msg) {
+    g_last_error = msg;
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+    if (e == cudaSuccess) return F184GI_OK;
+    g_last_error = std::string(what) + ": " + cudaGetErrorString(e);
+    return e == cudaErrorMemoryAllocation ? F184GI_ERR_OOM : F184GI_ERR_CUDA;
+}
+
+bool invert4(const double* m, double* inv) {
+    double a[4][8];
+    for (int r = 0; r < 4; ++r)
+        for (int c = 0; c < 8; ++c) a[r][c] = c < 4 ? m[r * 4 + c] : (c - 4 == r ? 1.0 : 0.0);
+    for (int c = 0; c < 4; ++c) {
+        int p = c;
+        for (int r = c + 1; r < 4; ++r)
+            if (std::fabs(a[r][c]) > std::fabs(a[p][c])) p = r;
+        if (a[p][c] == 0.0) return false;
+        if (p != c)
+            for (int k = 0; k < 8; ++k) std::swap(a[p][k], a[c][k]);
+        double iv = 1.0 / a[c][c];
+        for (int k = 0; k < 8; ++k) a[c][k] *= iv;
+        for (int r = 0; r < 4; ++r)
+            if (r != c) {
+                double f = a[r][c];
+                for (int k = 0; k < 8; ++k) a[r][k] -= f * a[c][k];
+            }
+    }
+    for (int r = 0; r < 4; ++r)
+        for (int c = 0; c < 4; ++c) inv[r * 4 + c] = a[r][c + 4];
+    return true;
+}
+
+int compute_frame(const f184gi_bounds& b, uint32_t dim, const float light_dir[3], f184gi_grid_frame* out) {
+    std::memset(out, 0, sizeof(*out));
+    const float mn[3] = {b.min.x, b.min.y, b.min.z}, mx[3] = {b.max.x, b.max.y, b.max.z};
+    frame_from_bounds(mn, mx, dim, light_dir, out);
+    return F184GI_OK;
+}
+
+}  // namespace f184
+
+using namespace f184;
+
+struct GridObj {
+    f184gi_grid_desc desc{};
+    ChainLayout chain{};
+    size_t chain_bytes = 0;
+    unsigned long long* shadow = nullptr;
+    size_t shadow_bytes = 0;
+    uint32_t* counts = nullptr;
+    size_t counts_bytes = 0;
+    f184gi_grid_frame* d_frame = nullptr;
+    bool voxelized = false;
+};
+
+struct f184gi_ctx {
+    int device = 0;
+    uint64_t budget = 0;
+    uint64_t used = 0;
+    std::map<uint32_t, GridObj> grids;
+    uint32_t next_id = 1;
+    Scratch raster, vox, trace, misc, keys;
+    uint32_t* d_status = nullptr;
+};
+
+namespace {
+
+int dev_alloc(f184gi_ctx* c, void** p, size_t bytes) {
+    *p = nullptr;
+    if (bytes == 0) return F184GI_OK;
+    if (c->budget && c->used + bytes > c->budget)
+        return fail(F184GI_ERR_BUDGET, "allocation of " + std::to_string(bytes) + " bytes exceeds the HBM budget");
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return fail(F184GI_ERR_OOM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    }
+    c->used += bytes;
+    return F184GI_OK;
+}
+
+void dev_free(f184gi_ctx* c, void* p, size_t bytes) {
+    if (!p) return;
+    cudaFree(p);
+    c->used -= bytes;
+}
+
+// Grow a scratch slot to at least `bytes` (contents are not preserved).
+int scratch_get(f184gi_ctx* c, Scratch& s, size_t bytes) {
+    if (s.bytes >= bytes) return F184GI_OK;
+    if (s.ptr) {
+        cudaError_t e = cudaDeviceSynchronize();  // the old buffer may still be in use by queued work
+        if (e != cudaSuccess) return cuda_fail(e, "scratch resize");
+        dev_free(c, s.ptr, s.bytes);
+        s.ptr = nullptr;
+        s.bytes = 0;
+    }
+    size_t want = bytes + bytes / 8;
+    int rc = dev_alloc(c, &s.ptr, want);
+    if (rc) return rc;
+    s.bytes = want;
+    return F184GI_OK;
+}
+
+bool pow2(uint32_t x) { return x && !(x & (x - 1)); }
+
+int check_desc(const f184gi_grid_desc* d) {
+    if (!d) return fail(F184GI_ERR_INVALID, "grid descriptor is null");
+    if (!pow2(d->dim) || d->dim < 16 || d->dim > 512) return fail(F184GI_ERR_INVALID, "grid dim must be a power of two in 16..512");
+    uint32_t maxl = 0;
+    for (uint32_t x = d->dim; x > 1; x >>= 1) ++maxl;  // log2(dim): keeps a 2^3 top level
+    if (d->levels < 1 || d->levels > maxl || d->levels > uint32_t(kMaxLevels))
+        return fail(F184GI_ERR_INVALID, "grid levels must be in 1..log2(dim)");
+    if (d->format != F184GI_FMT_F32 && d->format != F184GI_FMT_F16) return fail(F184GI_ERR_INVALID, "unknown grid format");
+    if (d->shadow_res < 64 || d->shadow_res > 8192) return fail(F184GI_ERR_INVALID, "shadow_res must be in 64..8192");
+    if (d->anisotropic > 1) return fail(F184GI_ERR_INVALID, "anisotropic must be 0 or 1");
+    return F184GI_OK;
+}
+
+ChainLayout layout_for(const f184gi_grid_desc& d, void* base) {
+    ChainLayout c{};
+    c.base = base;
+    c.dim = d.dim;
+    c.levels = d.levels;
+    c.format = d.format;
+    c.aniso = d.anisotropic;
+    c.esz = d.format == F184GI_FMT_F32 ? 16 : 8;
+    uint64_t off = 0;
+    for (uint32_t l = 0; l < d.levels; ++l) {
+        uint64_t dl = d.dim >> l;
+        c.ldim[l] = uint32_t(dl);
+        c.off[l] = off;
+        c.vol[l] = dl * dl * dl;
+        off += c.vol[l] * ((d.anisotropic && l > 0) ? 6 : 1);
+    }
+    return c;
+}
+
+uint64_t chain_elems(const f184gi_grid_desc& d) {
+    ChainLayout c = layout_for(d, nullptr);
+    uint32_t l = d.levels - 1;
+    return c.off[l] + c.vol[l] * ((d.anisotropic && l > 0) ? 6 : 1);
+}
+
+GridObj* find_grid(f184gi_ctx* c, uint32_t id) {
+    auto it = c->grids.find(id);
+    return it == c->grids.end() ? nullptr : &it->second;
+}
+
+int read_status(f184gi_ctx* c) {
+    uint32_t st = 0;
+    cudaError_t e = cudaMemcpy(&st, c->d_status, 4, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(e, "status read");
+    if (!st) return F184GI_OK;
+    cudaMemset(c->d_status, 0, 4);
+    if (st & kStatusTimeout) return fail(F184GI_ERR_TIMEOUT, "a bounded device wait expired");
+    if (st & kStatusOverflow) return fail(F184GI_ERR_OVERFLOW, "a bounded device structure overflowed");
+    return fail(F184GI_ERR_INVALID, "geometry outside the fixed-point range was skipped");
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* f184gi_last_error(void) { return g_last_error.c_str(); }
+int f184gi_abi_version(void) { return F184GI_ABI_VERSION; }
+
+int f184gi_create(const f184gi_config* cfg, f184gi_ctx** out) {
+    if (!out) return fail(F184GI_ERR_INVALID, "create: out is null");
+    *out = nullptr;
+    int device = cfg ? cfg->device : 0;
+    cudaError_t e = cudaSetDevice(device);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
+    f184gi_ctx* c = new f184gi_ctx();
+    c->device = device;
+    c->budget = cfg ? cfg->hbm_budget : 0;
+    void* st = nullptr;
+    int rc = dev_alloc(c, &st, 256);
+    if (rc) {
+        delete c;
+        return rc;
+    }
+    c->d_status = static_cast<uint32_t*>(st);
+    cudaMemset(c->d_status, 0, 4);
+    *out = c;
+    return F184GI_OK;
+}
+
+int f184gi_destroy(f184gi_ctx* c) {
+    if (!c) return fail(F184GI_ERR_INVALID, "destroy: null context");
+    cudaSetDevice(c->device);
+    cudaDeviceSynchronize();
+    for (auto& kv : c->grids) {
+        GridObj& g = kv.second;
+        dev_free(c, g.chain.base, g.chain_bytes);
+        dev_free(c, g.shadow, g.shadow_bytes);
+        dev_free(c, g.counts, g.counts_bytes);
+        dev_free(c, g.d_frame, sizeof(f184gi_grid_frame));
+    }
+    for (Scratch* s : {&c->raster, &c->vox, &c->trace, &c->misc, &c->keys}) dev_free(c, s->ptr, s->bytes);
+    dev_free(c, c->d_status, 256);
+    delete c;
+    return F184GI_OK;
+}
+
+int f184gi_memory_used(f184gi_ctx* c, uint64_t* bytes) {
+    if (!c || !bytes) return fail(F184GI_ERR_INVALID, "memory_used: null argument");
+    *bytes = c->used;
+    return F184GI_OK;
+}
+
+int f184gi_grid_bytes(const f184gi_grid_desc* d, uint64_t* bytes) {
+    int rc = check_desc(d);
+    if (rc) return rc;
+    if (!bytes) return fail(F184GI_ERR_INVALID, "grid_bytes: null output");
+    uint64_t esz = d->format == F184GI_FMT_F32 ? 16 : 8;
+    uint64_t b = chain_elems(*d) * esz + uint64_t(d->shadow_res) * d->shadow_res * 8 + sizeof(f184gi_grid_frame);
+    if (d->flags & F184GI_GRID_KEEP_COUNTS) b += uint64_t(d->dim) * d->dim * d->dim * 4;
+    *bytes = b;
+    return F184GI_OK;
+}
+
+int f184gi_grid_create(f184gi_ctx* c, const f184gi_grid_desc* d, uint32_t* grid) {
+    if (!c || !grid) return fail(F184GI_ERR_INVALID, "grid_create: null argument");
+    int rc = check_desc(d);
+    if (rc) return rc;
+    GridObj g;
+    g.desc = *d;
+    uint64_t esz = d->format == F184GI_FMT_F32 ? 16 : 8;
+    g.chain_bytes = chain_elems(*d) * esz;
+    void* base = nullptr;
+    if ((rc = dev_alloc(c, &base, g.chain_bytes))) return rc;
+    g.chain = layout_for(*d, base);
+    g.shadow_bytes = size_t(d->shadow_res) * d->shadow_res * 8;
+    void* sh = nullptr;
+    if ((rc = dev_alloc(c, &sh, g.shadow_bytes))) {
+        dev_free(c, base, g.chain_bytes);
+        return rc;
+    }
+    g.shadow = static_cast<unsigned long long*>(sh);
+    void* fr = nullptr;
+    if ((rc = dev_alloc(c, &fr, sizeof(f184gi_grid_frame)))) {
+        dev_free(c, base, g.chain_bytes);
+        dev_free(c, sh, g.shadow_bytes);
+        return rc;
+    }
+    g.d_frame = static_cast<f184gi_grid_frame*>(fr);
+    if (d->flags & F184GI_GRID_KEEP_COUNTS) {
+        g.counts_bytes = size_t(d->dim) * d->dim * d->dim * 4;
+        void* cp = nullptr;
+        if ((rc = dev_alloc(c, &cp, g.counts_bytes))) {
+            dev_free(c, base, g.chain_bytes);
+            dev_free(c, sh, g.shadow_bytes);
+            dev_free(c, fr, sizeof(f184gi_grid_frame));
+            return rc;
+        }
+        g.counts = static_cast<uint32_t*>(cp);
+        cudaMemset(g.counts, 0, g.counts_bytes);
+    }
+    cudaMemset(base, 0, g.chain_bytes);
+    cudaMemset(fr, 0, sizeof(f184gi_grid_frame));
+    uint32_t id = c->next_id++;
+    c->grids[id] = g;
+    *grid = id;
+    return F184GI_OK;
+}
+
+int f184gi_grid_destroy(f184gi_ctx* c, uint32_t grid) {
+    if (!c) return fail(F184GI_ERR_INVALID, "grid_destroy: null context");
+    GridObj* g = find_grid(c, grid);
+    if (!g) return fail(F184GI_ERR_NOTFOUND, "grid_destroy: unknown grid");
+    cudaDeviceSynchronize();
+    dev_free(c, g->chain.base, g->chain_bytes);
+    dev_free(c, g->shadow, g->shadow_bytes);
+    dev_free(c, g->counts, g->counts_bytes);
+    dev_free(c, g->d_frame, sizeof(f184gi_grid_frame));
+    c->grids.erase(grid);
+    return F184GI_OK;
+}
+
+int f184gi_voxelize(f184gi_ctx* c, uint32_t grid, const float* tri, const uint32_t* albedo, uint64_t ntris,
+                    const f184gi_bounds* bounds, const f184gi_light* light, const uint32_t* dirty, uint32_t ndirty,
+                    void* stream) {
+    if (!c || !light) return fail(F184GI_ERR_INVALID, "voxelize: null argument");
+    GridObj* g = find_grid(c, grid);
+    if (!g) return fail(F184GI_ERR_NOTFOUND, "voxelize: unknown grid");
+    if (ntris && (!tri || !albedo)) return fail(F184GI_ERR_INVALID, "voxelize: null triangle buffers");
+    if (ndirty && !dirty) return fail(F184GI_ERR_INVALID, "voxelize: null dirty list");
+    if (!bounds && ntris == 0) return fail(F184GI_ERR_INVALID, "voxelize: no triangles and no bounds");
+    float ld = light->direction[0] * light->direction[0] + light->direction[1] * light->direction[1] +
+               light->direction[2] * light->direction[2];
+    if (!(ld > 0.0f) || !std::isfinite(ld)) return fail(F184GI_ERR_INVALID, "voxelize: light direction is zero");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const f184gi_grid_desc& d = g->desc;
+    int rc = scratch_get(c, c->misc, 4096);
+    if (rc) return rc;
+    if ((rc = frame_launch(tri, ntris, bounds, d.dim, light->direction, g->d_frame, c->misc.ptr, s))) return rc;
+    // shadow map over the grid's light frame
+    RasterJob rj{};
+    rj.tri = tri;
+    rj.ntris = ntris;
+    rj.d_M = g->d_frame->light_clip;
+    rj.width = rj.height = d.shadow_res;
+    rj.keys = g->shadow;
+    if ((rc = scratch_get(c, c->raster, raster_scratch_bytes(ntris, d.shadow_res, d.shadow_res)))) return rc;
+    if ((rc = raster_launch(rj, c->raster.ptr, c->raster.bytes, c->d_status, s))) return rc;
+    VoxelizeJob vj{};
+    vj.tri = tri;
+    vj.albedo = albedo;
+    vj.ntris = ntris;
+    vj.d_frame = g->d_frame;
+    vj.light = *light;
+    vj.chain = g->chain;
+    vj.shadow_keys = g->shadow;
+    vj.shadow_res = d.shadow_res;
+    vj.counts = g->counts;
+    vj.dirty_bricks = dirty;
+    vj.ndirty = ndirty;
+    if ((rc = scratch_get(c, c->vox, voxelize_scratch_bytes(ntris, d.dim)))) return rc;
+    if ((rc = voxelize_launch(vj, c->vox.ptr, c->vox.bytes, c->d_status, s))) return rc;
+    g->voxelized = true;
+    return F184GI_OK;
+}
+
+int f184gi_mip(f184gi_ctx* c, uint32_t grid, uint32_t levels, uint32_t anisotropic, void* stream) {
+    if (!c) return fail(F184GI_ERR_INVALID, "mip: null context");
+    GridObj* g = find_grid(c, grid);
+    if (!g) return fail(F184GI_ERR_NOTFOUND, "mip: unknown grid");
+    if (anisotropic != g->desc.anisotropic) return fail(F184GI_ERR_INVALID, "mip: anisotropy differs from the grid's");
+    if (levels == 0 || levels > g->desc.levels) levels = g->desc.levels;
+    return mip_launch(g->chain, levels, c->d_status, static_cast<cudaStream_t>(stream));
+}
+
+void f184gi_cone_params_default(f184gi_cone_params* p) {
+    if (!p) return;
+    p->diffuse_cones = 5;
+    p->diffuse_tan_half = 0.57735026918962576f;
+    p->diffuse_tilt_deg = 60.0f;
+    p->step_factor = 0.5f;
+    p->max_distance = 0.0f;
+    p->alpha_stop = 0.999f;
+    p->start_offset = 1.0f;
+    p->min_spec_tan_half = 0.05f;
+    p->specular = 1;
+    p->pad = 0;
+}
+
+int f184gi_trace(f184gi_ctx* c, uint32_t grid, const f184gi_view* views, uint32_t nviews,
+                 const f184gi_cone_params* params, void* stream) {
+    if (!c || (nviews && !views)) return fail(F184GI_ERR_INVALID, "trace: null argument");
+    GridObj* g = find_grid(c, grid);
+    if (!g) return fail(F184GI_ERR_NOTFOUND, "trace: unknown grid");
+    TraceConsts tc{};
+    if (params)
+        tc.p = *params;
+    else
+        f184gi_cone_params_default(&tc.p);
+    // bounded marches: a cone advances at least step_factor/2 voxels per sample over at most max_distance
+    if (!(tc.p.step_factor >= 0.05f && tc.p.step_factor <= 4.0f) || !(tc.p.diffuse_tan_half > 0.0f) ||
+        !(tc.p.diffuse_tan_half <= 8.0f) || !(tc.p.min_spec_tan_half > 0.0f) || !(tc.p.start_offset >= 0.0f) ||
+        !(tc.p.start_offset <= 64.0f) || !(tc.p.max_distance <= 1.0e5f) || !(tc.p.alpha_stop > 0.0f) ||
+        !std::isfinite(tc.p.diffuse_tilt_deg) || (tc.p.diffuse_cones != 1 && tc.p.diffuse_cones != 5))
+        return fail(F184GI_ERR_INVALID, "trace: cone parameters out of range");
+    tc.tmax = tc.p.max_distance > 0.0f ? tc.p.max_distance : float(double(g->desc.dim) * std::sqrt(3.0));
+    double tilt = double(tc.p.diffuse_tilt_deg) * M_PI / 180.0;
+    tc.cos_tilt = float(std::cos(tilt));
+    tc.sin_tilt = float(std::sin(tilt));
+    std::vector<TraceView> tv(nviews);
+    for (uint32_t i = 0; i < nviews; ++i) {
+        const f184gi_view& v = views[i];
+        if (!v.depth || !v.normal || !v.roughness || !v.out || v.width == 0 || v.height == 0)
+            return fail(F184GI_ERR_INVALID, "trace: view " + std::to_string(i) + " has null buffers or zero size");
+        if (v.out_format != F184GI_FMT_F32 && v.out_format != F184GI_FMT_F16)
+            return fail(F184GI_ERR_INVALID, "trace: unknown output format");
+        double V[16], P[16], IV[16], IP[16];
+        for (int k = 0; k < 16; ++k) V[k] = v.view[k], P[k] = v.proj[k];
+        if (!invert4(V, IV) || !invert4(P, IP)) return fail(F184GI_ERR_INVALID, "trace: singular view or projection");
+        TraceView& t = tv[i];
+        for (int k = 0; k < 16; ++k) t.iview[k] = float(IV[k]), t.iproj[k] = float(IP[k]);
+        t.eye[0] = float(IV[3]);
+        t.eye[1] = float(IV[7]);
+        t.eye[2] = float(IV[11]);
+        t.width = v.width;
+        t.height = v.height;
+        t.depth = v.depth;
+        t.normal = v.normal;
+        t.rough = v.roughness;
+        t.out = v.out;
+        t.out_format = v.out_format;
+    }
+    int rc = scratch_get(c, c->trace, trace_scratch_bytes(nviews));
+    if (rc) return rc;
+    return trace_launch(g->chain, tc, g->d_frame, tv.data(), nviews, c->trace.ptr, c->trace.bytes,
+                        static_cast<cudaStream_t>(stream));
+}
+
+int f184gi_gbuffer(f184gi_ctx* c, const float* tri, const float* rough, uint64_t ntris, const f184gi_view* view,
+                   uint32_t* tri_id_out, void* stream) {
+    if (!c || !view || !tri || !rough) return fail(F184GI_ERR_INVALID, "gbuffer: null argument");
+    if (!view->depth || !view->normal || !view->roughness) return fail(F184GI_ERR_INVALID, "gbuffer: null G-buffer planes");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    RasterJob rj{};
+    rj.tri = tri;
+    rj.ntris = ntris;
+    // clip = proj * view, FP64
+    for (int r = 0; r < 4; ++r)
+        for (int k = 0; k < 4; ++k) {
+            double acc = 0.0;
+            for (int j = 0; j < 4; ++j) acc += double(view->proj[r * 4 + j]) * double(view->view[j * 4 + k]);
+            rj.M[r * 4 + k] = acc;
+        }
+    rj.d_M = nullptr;
+    rj.width = view->width;
+    rj.height = view->height;
+    int rc = scratch_get(c, c->keys, size_t(view->width) * view->height * 8);
+    if (rc) return rc;
+    rj.keys = static_cast<unsigned long long*>(c->keys.ptr);
+    if ((rc = scratch_get(c, c->raster, raster_scratch_bytes(ntris, view->width, view->height)))) return rc;
+    if ((rc = raster_launch(rj, c->raster.ptr, c->raster.bytes, c->d_status, s))) return rc;
+    double V[16], IV[16];
+    for (int k = 0; k < 16; ++k) V[k] = view->view[k];
+    if (!invert4(V, IV)) return fail(F184GI_ERR_INVALID, "gbuffer: singular view matrix");
+    const float eye[3] = {float(IV[3]), float(IV[7]), float(IV[11])};
+    return gbuffer_resolve_launch(rj.keys, view->width, view->height, tri, rough, view->view, eye,
+                                  const_cast<float*>(view->depth), const_cast<uint32_t*>(view->normal),
+                                  const_cast<uint16_t*>(view->roughness), tri_id_out, s);
+}
+
+int f184gi_sync(f184gi_ctx* c, void* stream) {
+    if (!c) return fail(F184GI_ERR_INVALID, "sync: null context");
+    cudaError_t e = cudaStreamSynchronize(static_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return cuda_fail(e, "sync");
+    return read_status(c);
+}
+
+int f184gi_frame_from_bounds(const f184gi_bounds* b, uint32_t dim, const float light_dir[3], f184gi_grid_frame* out) {
+    if (!b || !light_dir || !out) return fail(F184GI_ERR_INVALID, "frame_from_bounds: null argument");
+    if (dim < 4) return fail(F184GI_ERR_INVALID, "frame_from_bounds: dim too small");
+    return compute_frame(*b, dim, light_dir, out);
+}
+
+int f184gi_grid_get_frame(f184gi_ctx* c, uint32_t grid, f184gi_grid_frame* out) {
+    if (!c || !out) return fail(F184GI_ERR_INVALID, "grid_get_frame: null argument");
+    GridObj* g = find_grid(c, grid);
+    if (!g) return fail(F184GI_ERR_NOTFOUND, "grid_get_frame: unknown grid");
+    cudaError_t e = cudaMemcpy(out, g->d_frame, sizeof(*out), cudaMemcpyDeviceToHost);
+    return cuda_fail(e, "grid_get_frame");
+}
+
+int f184gi_grid_read_level(f184gi_ctx* c, uint32_t grid, uint32_t level, uint32_t dir, float* host) {
+    if (!c || !host) return fail(F184GI_ERR_INVALID, "grid_read_level: null argument");
+    GridObj* g = find_grid(c, grid);
+    if (!g) return fail(F184GI_ERR_NOTFOUND, "grid_read_level: unknown grid");
+    if (level >= g->desc.levels) return fail(F184GI_ERR_INVALID, "grid_read_level: level out of range");
+    if (dir > 0 && !(g->desc.anisotropic && level > 0 && dir < 6)) return fail(F184GI_ERR_INVALID, "grid_read_level: bad direction");
+    uint64_t d = g->chain.ldim[level];
+    size_t bytes = size_t(d * d * d) * 16;
+    int rc = scratch_get(c, c->misc, bytes);
+    if (rc) return rc;
+    cudaDeviceSynchronize();
+    if ((rc = read_level_launch(g->chain, level, dir, static_cast<float*>(c->misc.ptr), nullptr))) return rc;
+    cudaError_t e = cudaMemcpy(host, c->misc.ptr, bytes, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(e, "grid_read_level");
+    return read_status(c);
+}
+
+int f184gi_grid_read_shadow(f184gi_ctx* c, uint32_t grid, float* host) {
+    if (!c || !host) return fail(F184GI_ERR_INVALID, "grid_read_shadow: null argument");
+    GridObj* g = find_grid(c, grid);
+    if (!g) return fail(F184GI_ERR_NOTFOUND, "grid_read_shadow: unknown grid");
+    uint64_t n = uint64_t(g->desc.shadow_res) * g->desc.shadow_res;
+    std::vector<unsigned long long> keys(n);
+    cudaDeviceSynchronize();
+    cudaError_t e = cudaMemcpy(keys.data(), g->shadow, n * 8, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(e, "grid_read_shadow");
+    for (uint64_t i = 0; i < n; ++i) {
+        if (keys[i] == ~0ull) {
+            host[i] = 1.0f;
+        } else {
+            uint32_t b = uint32_t(keys[i] >> 32);
+            std::memcpy(&host[i], &b, 4);
+        }
+    }
+    return read_status(c);
+}
+
+int f184gi_grid_read_counts(f184gi_ctx* c, uint32_t grid, uint32_t* host) {
+    if (!c || !host) return fail(F184GI_ERR_INVALID, "grid_read_counts: null argument");
+    GridObj* g = find_grid(c, grid);
+    if (!g) return fail(F184GI_ERR_NOTFOUND, "grid_read_counts: unknown grid");
+    if (!g->counts) return fail(F184GI_ERR_INVALID, "grid_read_counts: grid was created without F184GI_GRID_KEEP_COUNTS");
+    cudaDeviceSynchronize();
+    cudaError_t e = cudaMemcpy(host, g->counts, g->counts_bytes, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(e, "grid_read_counts");
+    return read_status(c);
+}
+
+int f184gi_grid_level_ptr(f184gi_ctx* c, uint32_t grid, uint32_t level, void** ptr, uint64_t* bytes) {
+    if (!c || !ptr || !bytes) return fail(F184GI_ERR_INVALID, "grid_level_ptr: null argument");
+    GridObj* g = find_grid(c, grid);
+    if (!g) return fail(F184GI_ERR_NOTFOUND, "grid_level_ptr: unknown grid");
+    if (level >= g->desc.levels) return fail(F184GI_ERR_INVALID, "grid_level_ptr: level out of range");
+    const ChainLayout& ch = g->chain;
+    *ptr = static_cast<char*>(ch.base) + ch.off[level] * ch.esz;
+    *bytes = ch.vol[level] * ch.esz * ((ch.aniso && level > 0) ? 6 : 1);
+    return F184GI_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,128 @@
+// gi_device.cuh -- device helpers shared by the f184gi kernels.
+#pragma once
+
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <algorithm>
+#include <cmath>
+
+#include "gi_internal.h"
+
+namespace f184 {
+
+// ---- exact FP64: every operation rounded on its own, never contracted into an FMA ----
+__device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double dsub(double a, double b) { return __dsub_rn(a, b); }
+// row . (x, y, z, 1) in the order ((r0 x + r1 y) + r2 z) + r3
+__device__ __forceinline__ double drow(const double* r, double x, double y, double z) {
+    double s = dadd(dmul(r[0], x), dmul(r[1], y));
+    s = dadd(s, dmul(r[2], z));
+    return dadd(s, r[3]);
+}
+
+__device__ __forceinline__ int64_t floor_div64(int64_t a, int64_t b) {  // b > 0
+    int64_t q = a / b;
+    if ((a % b) != 0 && a < 0) --q;
+    return q;
+}
+
+// ---- Morton order of 8^3 bricks ----
+__host__ __device__ __forceinline__ uint32_t part1by2(uint32_t x) {
+    x &= 0x3ffu;
+    x = (x | (x << 16)) & 0x030000FFu;
+    x = (x | (x << 8)) & 0x0300F00Fu;
+    x = (x | (x << 4)) & 0x030C30C3u;
+    x = (x | (x << 2)) & 0x09249249u;
+    return x;
+}
+__host__ __device__ __forceinline__ uint32_t compact1by2(uint32_t x) {
+    x &= 0x09249249u;
+    x = (x | (x >> 2)) & 0x030C30C3u;
+    x = (x | (x >> 4)) & 0x0300F00Fu;
+    x = (x | (x >> 8)) & 0x030000FFu;
+    x = (x | (x >> 16)) & 0x000003FFu;
+    return x;
+}
+__host__ __device__ __forceinline__ uint32_t morton3(uint32_t x, uint32_t y, uint32_t z) {
+    return part1by2(x) | (part1by2(y) << 1) | (part1by2(z) << 2);
+}
+
+// element index of voxel (x, y, z) inside one volume of a level with `d` voxels per axis
+__host__ __device__ __forceinline__ uint64_t vox_index(uint32_t d, uint32_t x, uint32_t y, uint32_t z) {
+    if (d >= 8) {
+        uint32_t m = morton3(x >> 3, y >> 3, z >> 3);
+        return (uint64_t(m) << 9) | ((z & 7u) << 6) | ((y & 7u) << 3) | (x & 7u);
+    }
+    return (uint64_t(z) * d + y) * d + x;
+}
+
+// ---- voxel payload load/store ----
+__device__ __forceinline__ float4 load_vox(const void* base, uint32_t format, uint64_t idx) {
+    if (format == F184GI_FMT_F32) return __ldg(reinterpret_cast<const float4*>(base) + idx);
+    uint2 raw = __ldg(reinterpret_cast<const uint2*>(base) + idx);
+    __half2 a = *reinterpret_cast<__half2*>(&raw.x);
+    __half2 b = *reinterpret_cast<__half2*>(&raw.y);
+    float2 fa = __half22float2(a), fb = __half22float2(b);
+    return make_float4(fa.x, fa.y, fb.x, fb.y);
+}
+__device__ __forceinline__ void store_vox(void* base, uint32_t format, uint64_t idx, float4 v) {
+    if (format == F184GI_FMT_F32) {
+        reinterpret_cast<float4*>(base)[idx] = v;
+        return;
+    }
+    __half2 a = __floats2half2_rn(v.x, v.y), b = __floats2half2_rn(v.z, v.w);
+    uint2 raw;
+    raw.x = *reinterpret_cast<uint32_t*>(&a);
+    raw.y = *reinterpret_cast<uint32_t*>(&b);
+    reinterpret_cast<uint2*>(base)[idx] = raw;
+}
+
+__device__ __forceinline__ void set_status(uint32_t* st, uint32_t bit) {
+    if (st) atomicOr(st, bit);
+}
+
+// Bounded mbarrier wait on `parity`; returns false (and leaves the barrier) after `limit` polls.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, uint32_t limit) {
+    uint32_t addr = static_cast<uint32_t>(__cvta_generic_to_shared(bar));
+    for (uint32_t i = 0; i < limit; ++i) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(done)
+            : "r"(addr), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    uint32_t addr = static_cast<uint32_t>(__cvta_generic_to_shared(bar));
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(addr), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+    uint32_t addr = static_cast<uint32_t>(__cvta_generic_to_shared(bar));
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(addr), "r"(bytes) : "memory");
+}
+
+// 1-D bulk copy global -> shared, completion counted on `bar` (16-byte aligned, size % 16 == 0)
+__device__ __forceinline__ void bulk_g2s(void* smem_dst, const void* gsrc, uint32_t bytes, uint64_t* bar) {
+    uint32_t d = static_cast<uint32_t>(__cvta_generic_to_shared(smem_dst));
+    uint32_t b = static_cast<uint32_t>(__cvta_generic_to_shared(bar));
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(d),
+        "l"(gsrc), "r"(bytes), "r"(b)
+        : "memory");
+}
+
+__device__ __forceinline__ void fence_barrier_init() {
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+}  // namespace f184

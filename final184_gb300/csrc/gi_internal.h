@@ -1,0 +1,111 @@
+// gi_internal.h -- shared host-side declarations of the f184gi library (not part of the ABI).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+
+#include "../../include/f184gi.h"
+
+namespace f184 {
+
+constexpr int kMaxLevels = 11;
+constexpr int kBrickEdge = 8;
+constexpr int kBrickVox = 512;
+constexpr uint32_t kFixedFrac = 16;  // per-contribution injection weights are 16.16 fixed point
+
+// device status bits (set by kernels, read by f184gi_sync / inspection calls)
+constexpr uint32_t kStatusOverflow = 1u;
+constexpr uint32_t kStatusTimeout = 2u;
+constexpr uint32_t kStatusRange = 4u;  // geometry outside the fixed-point range was skipped
+
+int fail(int code, const std::string& msg);
+int cuda_fail(cudaError_t e, const char* what);
+bool invert4(const double* m, double* inv);
+
+// Grid placement computed on the host in FP64 (same operation order as the device variant).
+int compute_frame(const f184gi_bounds& b, uint32_t dim, const float light_dir[3], f184gi_grid_frame* out);
+
+// Element layout of one grid's mip chain.  Level l has dim_l = dim >> l voxels per axis; levels with
+// dim_l >= 8 are stored as 8^3 bricks in Morton order of the brick coordinates, voxels x-fastest inside a
+// brick; smaller levels are linear.  Anisotropic chains store six direction volumes per level >= 1.
+struct ChainLayout {
+    void* base;
+    uint32_t dim, levels, format, aniso;
+    uint32_t esz;                    // bytes per voxel (16 F32, 8 F16)
+    uint64_t off[kMaxLevels];        // element offset of level l (first direction volume)
+    uint64_t vol[kMaxLevels];        // elements of one volume of level l
+    uint32_t ldim[kMaxLevels];
+};
+
+// Host view of scratch memory used by one pass; grows on demand, kept by the context.
+struct Scratch {
+    void* ptr = nullptr;
+    size_t bytes = 0;
+};
+
+// ---- kernel launchers (defined in the .cu files) ----
+
+struct RasterJob {
+    const float* tri;       // 9 floats per triangle
+    uint64_t ntris;
+    double M[16];           // world -> clip (used when d_M is null)
+    const double* d_M;      // world -> clip in device memory (e.g. a device-computed frame), or null
+    uint32_t width, height;
+    unsigned long long* keys;  // width*height, output
+};
+// bytes of scratch a raster job needs
+size_t raster_scratch_bytes(uint64_t ntris, uint32_t width, uint32_t height);
+int raster_launch(const RasterJob& job, void* scratch, size_t scratch_bytes, uint32_t* d_status,
+                  cudaStream_t s);
+
+struct VoxelizeJob {
+    const float* tri;
+    const uint32_t* albedo;
+    uint64_t ntris;
+    const f184gi_grid_frame* d_frame;   // device copy of the frame
+    f184gi_light light;
+    ChainLayout chain;
+    const unsigned long long* shadow_keys;
+    uint32_t shadow_res;
+    uint32_t* counts;                   // optional (dim^3, linear)
+    const uint32_t* dirty_bricks;       // optional list (Morton brick indices of L0)
+    uint32_t ndirty;
+};
+size_t voxelize_scratch_bytes(uint64_t ntris, uint32_t dim);
+int voxelize_launch(const VoxelizeJob& job, void* scratch, size_t scratch_bytes, uint32_t* d_status,
+                    cudaStream_t s);
+
+// device-side frame from bounds (or from the triangles' AABB when bounds == nullptr)
+int frame_launch(const float* tri, uint64_t ntris, const f184gi_bounds* bounds, uint32_t dim,
+                 const float light_dir[3], f184gi_grid_frame* d_frame, void* scratch, cudaStream_t s);
+
+int mip_launch(const ChainLayout& chain, uint32_t levels, uint32_t* d_status, cudaStream_t s);
+
+struct TraceView {
+    float iview[16], iproj[16];     // inverses (FP32 of FP64 inverses)
+    float eye[3];
+    uint32_t width, height;
+    const float* depth;
+    const uint32_t* normal;
+    const uint16_t* rough;
+    void* out;
+    uint32_t out_format;
+};
+struct TraceConsts {
+    float tmax;
+    float cos_tilt, sin_tilt;
+    f184gi_cone_params p;
+};
+int trace_launch(const ChainLayout& chain, const TraceConsts& tc, const f184gi_grid_frame* d_frame,
+                 const TraceView* views, uint32_t nviews, void* scratch, size_t scratch_bytes, cudaStream_t s);
+size_t trace_scratch_bytes(uint32_t nviews);
+
+int gbuffer_resolve_launch(const unsigned long long* keys, uint32_t width, uint32_t height, const float* tri,
+                           const float* rough, const float view[16], const float eye[3], float* depth,
+                           uint32_t* normal, uint16_t* rough_out, uint32_t* tri_out, cudaStream_t s);
+
+int read_level_launch(const ChainLayout& chain, uint32_t level, uint32_t dir, float* d_out, cudaStream_t s);
+
+}  // namespace f184

@@ -1,0 +1,372 @@
+// raster.cu -- exact, tile-binned triangle rasterizer used for the shadow map and the G-buffer.
+//
+// Replaces the fixed-function depth-only raster of the reference's shadow pass
+// (Foreground/Renderer/ZOnlyRenderer.cpp:79-114, StaticMeshZOnlyVS Pipelang/Internal/main.lua:146-156) and the
+// G-buffer pass (GBufferRenderer.cpp:79-116).  Coverage and depth are exact functions of the input:
+//   clip = M * (x, y, z, 1) in FP64, clipped to 0 <= z <= w and |x|,|y| <= 16 w (Sutherland-Hodgman, FP64),
+//   vertices snapped to 1/16 pixel, coverage by inclusive int64 edge functions at pixel centres,
+//   depth = (e0 z0 + e1 z1 + e2 z2) * (1 / area) in FP64, rounded to FP32;
+//   per pixel the minimum of key = (depth bits << 32 | triangle index) wins.
+// Work is binned into 16x16 pixel tiles; one CTA rasterizes a tile in shared memory.
+#include "gi_device.cuh"
+#include "util.cuh"
+
+namespace f184 {
+namespace {
+
+constexpr int kTile = 16;
+constexpr double kGuard = 16.0;
+constexpr uint32_t kNone = 0xffffffffu;
+
+struct SubTri {
+    int32_t X[3], Y[3];
+    double Z[3];
+    double inv_area;
+    uint32_t tri;
+    uint16_t x0, x1, y0, y1;
+};
+
+struct V4 {
+    double x, y, z, w;
+};
+
+__device__ __forceinline__ double plane_dist(int k, const V4& v) {
+    switch (k) {
+        case 0: return v.z;
+        case 1: return dsub(v.w, v.z);
+        case 2: return dsub(dmul(kGuard, v.w), v.x);
+        case 3: return dadd(v.x, dmul(kGuard, v.w));
+        case 4: return dsub(dmul(kGuard, v.w), v.y);
+        default: return dadd(v.y, dmul(kGuard, v.w));
+    }
+}
+
+__device__ int clip_polygon(V4* poly, int n) {
+    V4 tmp[12];
+    for (int k = 0; k < 6; ++k) {
+        int m = 0;
+        for (int i = 0; i < n; ++i) {
+            V4 a = poly[i];
+            V4 b = poly[(i + 1) % n];
+            double da = plane_dist(k, a), db = plane_dist(k, b);
+            bool ina = da >= 0.0, inb = db >= 0.0;
+            if (ina) tmp[m++] = a;
+            if (ina != inb) {
+                double t = __ddiv_rn(da, dsub(da, db));
+                V4 r;
+                r.x = dadd(a.x, dmul(t, dsub(b.x, a.x)));
+                r.y = dadd(a.y, dmul(t, dsub(b.y, a.y)));
+                r.z = dadd(a.z, dmul(t, dsub(b.z, a.z)));
+                r.w = dadd(a.w, dmul(t, dsub(b.w, a.w)));
+                tmp[m++] = r;
+            }
+        }
+        n = m;
+        if (n < 3) return 0;
+        for (int i = 0; i < n; ++i) poly[i] = tmp[i];
+    }
+    return n;
+}
+
+__device__ bool snap(const V4& a, const V4& b, const V4& c, uint32_t W, uint32_t H, uint32_t tri, SubTri& s) {
+    const V4* v[3] = {&a, &b, &c};
+    int64_t X[3], Y[3];
+    double Z[3];
+    for (int i = 0; i < 3; ++i) {
+        if (!(v[i]->w > 0.0)) return false;
+        double nx = __ddiv_rn(v[i]->x, v[i]->w), ny = __ddiv_rn(v[i]->y, v[i]->w), nz = __ddiv_rn(v[i]->z, v[i]->w);
+        X[i] = __double2ll_rn(dmul(dadd(nx, 1.0), 8.0 * double(W)));
+        Y[i] = __double2ll_rn(dmul(dadd(ny, 1.0), 8.0 * double(H)));
+        Z[i] = nz;
+    }
+    int64_t area2 = (X[1] - X[0]) * (Y[2] - Y[0]) - (Y[1] - Y[0]) * (X[2] - X[0]);
+    if (area2 == 0) return false;
+    if (area2 < 0) {
+        int64_t t;
+        t = X[1], X[1] = X[2], X[2] = t;
+        t = Y[1], Y[1] = Y[2], Y[2] = t;
+        double tz = Z[1];
+        Z[1] = Z[2], Z[2] = tz;
+        area2 = -area2;
+    }
+    int64_t mnx = min(X[0], min(X[1], X[2])), mxx = max(X[0], max(X[1], X[2]));
+    int64_t mny = min(Y[0], min(Y[1], Y[2])), mxy = max(Y[0], max(Y[1], Y[2]));
+    int64_t x0 = max(int64_t(0), -floor_div64(-(mnx - 8), 16));
+    int64_t x1 = min(int64_t(W) - 1, floor_div64(mxx - 8, 16));
+    int64_t y0 = max(int64_t(0), -floor_div64(-(mny - 8), 16));
+    int64_t y1 = min(int64_t(H) - 1, floor_div64(mxy - 8, 16));
+    if (x0 > x1 || y0 > y1) return false;
+    for (int i = 0; i < 3; ++i) {
+        s.X[i] = int32_t(X[i]);
+        s.Y[i] = int32_t(Y[i]);
+        s.Z[i] = Z[i];
+    }
+    s.inv_area = __ddiv_rn(1.0, double(area2));
+    s.tri = tri;
+    s.x0 = uint16_t(x0), s.x1 = uint16_t(x1), s.y0 = uint16_t(y0), s.y1 = uint16_t(y1);
+    return true;
+}
+
+// Edge function of edge (a -> b) at fixed-point point (px, py).
+__device__ __forceinline__ int64_t edge(const SubTri& s, int a, int b, int64_t px, int64_t py) {
+    return int64_t(s.X[b] - s.X[a]) * (py - s.Y[a]) - int64_t(s.Y[b] - s.Y[a]) * (px - s.X[a]);
+}
+
+// Can the triangle cover any pixel centre of tile (tx, ty)?  Rejects tiles wholly outside one edge.
+__device__ __forceinline__ bool tile_may_overlap(const SubTri& s, int tx, int ty) {
+    int64_t px0 = int64_t(tx) * kTile * 16 + 8, px1 = px0 + (kTile - 1) * 16;
+    int64_t py0 = int64_t(ty) * kTile * 16 + 8, py1 = py0 + (kTile - 1) * 16;
+    const int ea[3] = {1, 2, 0}, eb[3] = {2, 0, 1};
+    for (int e = 0; e < 3; ++e) {
+        int64_t dx = s.X[eb[e]] - s.X[ea[e]], dy = s.Y[eb[e]] - s.Y[ea[e]];
+        // e(p) = dx (py - ya) - dy (px - xa): maximise over the tile corners
+        int64_t px = dy > 0 ? px0 : px1;
+        int64_t py = dx > 0 ? py1 : py0;
+        if (edge(s, ea[e], eb[e], px, py) < 0) return false;
+    }
+    return true;
+}
+
+struct RasterScratch {
+    SubTri* recs;          // ntris primary + overflow
+    uint32_t* ovf_count;   // [1]
+    uint32_t* tile_count;  // ntiles
+    uint32_t* tile_start;  // ntiles
+    uint32_t* tile_fill;   // ntiles
+    uint32_t* total;       // [1]
+    uint32_t* scan_tmp;
+    uint32_t* list;
+    uint64_t list_cap;
+    uint64_t ovf_cap;
+};
+
+__device__ __forceinline__ void visit_tiles(const SubTri& s, uint32_t rec, uint32_t tiles_x, uint32_t* tile_count,
+                                            const uint32_t* tile_start, uint32_t* tile_fill, uint32_t* list,
+                                            uint64_t list_cap, uint32_t* status, bool emit) {
+    int tx0 = s.x0 / kTile, tx1 = s.x1 / kTile, ty0 = s.y0 / kTile, ty1 = s.y1 / kTile;
+    bool small = (tx1 - tx0) <= 1 && (ty1 - ty0) <= 1;
+    for (int ty = ty0; ty <= ty1; ++ty)
+        for (int tx = tx0; tx <= tx1; ++tx) {
+            if (!small && !tile_may_overlap(s, tx, ty)) continue;
+            uint32_t t = uint32_t(ty) * tiles_x + uint32_t(tx);
+            if (!emit) {
+                atomicAdd(&tile_count[t], 1u);
+            } else {
+                uint64_t slot = uint64_t(tile_start[t]) + atomicAdd(&tile_fill[t], 1u);
+                if (slot < list_cap)
+                    list[slot] = rec;
+                else
+                    set_status(status, kStatusOverflow);
+            }
+        }
+}
+
+__global__ void raster_setup(const float* __restrict__ tri, uint64_t ntris, RasterJob job, RasterScratch sc,
+                             uint32_t tiles_x, uint32_t* status) {
+    uint64_t t = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (t >= ntris) return;
+    const double* M = job.d_M ? job.d_M : job.M;
+    V4 poly[12];
+    bool inside = true;
+    for (int v = 0; v < 3; ++v) {
+        double x = tri[t * 9 + v * 3], y = tri[t * 9 + v * 3 + 1], z = tri[t * 9 + v * 3 + 2];
+        poly[v].x = drow(M, x, y, z);
+        poly[v].y = drow(M + 4, x, y, z);
+        poly[v].z = drow(M + 8, x, y, z);
+        poly[v].w = drow(M + 12, x, y, z);
+        for (int k = 0; k < 6; ++k)
+            if (!(plane_dist(k, poly[v]) >= 0.0)) inside = false;
+    }
+    int n = 3;
+    if (!inside) n = clip_polygon(poly, 3);
+    bool primary_done = false;
+    for (int i = 1; i + 1 < n; ++i) {
+        SubTri s;
+        if (!snap(poly[0], poly[i], poly[i + 1], job.width, job.height, uint32_t(t), s)) continue;
+        uint64_t rec;
+        if (!primary_done) {
+            rec = t;
+            primary_done = true;
+        } else {
+            uint32_t k = atomicAdd(sc.ovf_count, 1u);
+            if (k >= sc.ovf_cap) {
+                set_status(status, kStatusOverflow);
+                continue;
+            }
+            rec = ntris + k;
+        }
+        sc.recs[rec] = s;
+        visit_tiles(s, uint32_t(rec), tiles_x, sc.tile_count, nullptr, nullptr, nullptr, 0, status, false);
+    }
+    if (!primary_done) sc.recs[t].tri = kNone;
+}
+
+__global__ void raster_emit(uint64_t ntris, RasterScratch sc, uint32_t tiles_x, uint32_t* status) {
+    uint64_t r = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    uint64_t nrec = ntris + min(uint64_t(*sc.ovf_count), sc.ovf_cap);
+    if (r >= nrec) return;
+    SubTri s = sc.recs[r];
+    if (s.tri == kNone) return;
+    visit_tiles(s, uint32_t(r), tiles_x, nullptr, sc.tile_start, sc.tile_fill, sc.list, sc.list_cap, status, true);
+}
+
+__global__ void __launch_bounds__(256) raster_tiles(RasterScratch sc, uint32_t tiles_x, uint32_t W, uint32_t H,
+                                                    unsigned long long* __restrict__ keys) {
+    __shared__ unsigned long long sk[kTile * kTile];
+    const uint32_t tile = blockIdx.x;
+    const int tx = int(tile % tiles_x), ty = int(tile / tiles_x);
+    sk[threadIdx.x] = ~0ull;
+    __syncthreads();
+    const uint32_t beg = sc.tile_start[tile], cnt = sc.tile_count[tile];
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t end = uint32_t(min(uint64_t(beg) + cnt, sc.list_cap));
+    for (uint32_t it = beg + warp; it < end; it += 8) {
+        const SubTri s = sc.recs[sc.list[it]];
+        int x0 = max(int(s.x0), tx * kTile), x1 = min(int(s.x1), tx * kTile + kTile - 1);
+        int y0 = max(int(s.y0), ty * kTile), y1 = min(int(s.y1), ty * kTile + kTile - 1);
+        if (x0 > x1 || y0 > y1) continue;
+        int w = x1 - x0 + 1, npx = w * (y1 - y0 + 1);
+        for (int p = int(lane); p < npx; p += 32) {
+            int px = x0 + p % w, py = y0 + p / w;
+            int64_t Px = int64_t(px) * 16 + 8, Py = int64_t(py) * 16 + 8;
+            int64_t e0 = edge(s, 1, 2, Px, Py);
+            int64_t e1 = edge(s, 2, 0, Px, Py);
+            int64_t e2 = edge(s, 0, 1, Px, Py);
+            if (e0 < 0 || e1 < 0 || e2 < 0) continue;
+            double z = dmul(double(e0), s.Z[0]);
+            z = dadd(z, dmul(double(e1), s.Z[1]));
+            z = dadd(z, dmul(double(e2), s.Z[2]));
+            z = dmul(z, s.inv_area);
+            float zf = __double2float_rn(z);
+            if (!(zf >= 0.0f)) zf = 0.0f;
+            if (zf > 1.0f) zf = 1.0f;
+            unsigned long long key = (uint64_t(__float_as_uint(zf)) << 32) | s.tri;
+            atomicMin(&sk[(py - ty * kTile) * kTile + (px - tx * kTile)], key);
+        }
+    }
+    __syncthreads();
+    int px = tx * kTile + int(threadIdx.x % kTile), py = ty * kTile + int(threadIdx.x / kTile);
+    if (px < int(W) && py < int(H)) keys[uint64_t(py) * W + px] = sk[threadIdx.x];
+}
+
+template <class T>
+T* carve(char*& p, uint64_t n) {
+    uintptr_t a = (reinterpret_cast<uintptr_t>(p) + 255) & ~uintptr_t(255);
+    T* r = reinterpret_cast<T*>(a);
+    p = reinterpret_cast<char*>(a + n * sizeof(T));
+    return r;
+}
+
+}  // namespace
+
+static uint64_t ovf_capacity(uint64_t ntris) { return ntris / 2 + 4096; }
+static uint64_t list_capacity(uint64_t ntris, uint32_t ntiles) { return ntris * 8 + uint64_t(ntiles) * 16 + 65536; }
+
+size_t raster_scratch_bytes(uint64_t ntris, uint32_t W, uint32_t H) {
+    uint32_t tiles = ((W + kTile - 1) / kTile) * ((H + kTile - 1) / kTile);
+    uint64_t recs = ntris + ovf_capacity(ntris);
+    return recs * sizeof(SubTri) + uint64_t(tiles) * 12 + scan_scratch_bytes(tiles) + list_capacity(ntris, tiles) * 4 +
+           16 * 256;
+}
+
+int raster_launch(const RasterJob& job, void* scratch, size_t scratch_bytes, uint32_t* d_status, cudaStream_t s) {
+    if (job.width == 0 || job.height == 0 || job.width > 8192 || job.height > 8192)
+        return fail(F184GI_ERR_INVALID, "raster: viewport out of range");
+    if (job.ntris >= 0xffff0000ull) return fail(F184GI_ERR_INVALID, "raster: too many triangles");
+    const uint32_t tiles_x = (job.width + kTile - 1) / kTile, tiles_y = (job.height + kTile - 1) / kTile;
+    const uint32_t ntiles = tiles_x * tiles_y;
+    if (scratch_bytes < raster_scratch_bytes(job.ntris, job.width, job.height))
+        return fail(F184GI_ERR_INVALID, "raster: scratch too small");
+    char* p = static_cast<char*>(scratch);
+    RasterScratch sc;
+    sc.ovf_cap = ovf_capacity(job.ntris);
+    sc.recs = carve<SubTri>(p, job.ntris + sc.ovf_cap);
+    sc.ovf_count = carve<uint32_t>(p, 1);
+    sc.total = carve<uint32_t>(p, 1);
+    sc.tile_count = carve<uint32_t>(p, ntiles);
+    sc.tile_start = carve<uint32_t>(p, ntiles);
+    sc.tile_fill = carve<uint32_t>(p, ntiles);
+    sc.scan_tmp = carve<uint32_t>(p, scan_scratch_bytes(ntiles) / 4);
+    sc.list_cap = list_capacity(job.ntris, ntiles);
+    sc.list = carve<uint32_t>(p, sc.list_cap);
+    cudaMemsetAsync(sc.ovf_count, 0, 4, s);
+    cudaMemsetAsync(sc.tile_count, 0, size_t(ntiles) * 4, s);
+    cudaMemsetAsync(sc.tile_fill, 0, size_t(ntiles) * 4, s);
+    if (job.ntris) {
+        uint32_t blocks = uint32_t((job.ntris + 127) / 128);
+        raster_setup<<<blocks, 128, 0, s>>>(job.tri, job.ntris, job, sc, tiles_x, d_status);
+    }
+    int rc = exclusive_scan(sc.tile_count, ntiles, sc.tile_start, sc.total, sc.scan_tmp, s);
+    if (rc) return rc;
+    if (job.ntris) {
+        uint64_t nrec = job.ntris + sc.ovf_cap;
+        raster_emit<<<uint32_t((nrec + 127) / 128), 128, 0, s>>>(job.ntris, sc, tiles_x, d_status);
+    }
+    raster_tiles<<<ntiles, 256, 0, s>>>(sc, tiles_x, job.width, job.height, job.keys);
+    return cuda_fail(cudaGetLastError(), "raster");
+}
+
+// ---------------- G-buffer resolve ----------------
+namespace {
+
+__device__ __forceinline__ uint32_t oct_encode(float3 n) {
+    float s = fabsf(n.x) + fabsf(n.y) + fabsf(n.z);
+    float x = n.x / s, y = n.y / s;
+    if (n.z < 0.0f) {
+        float ox = x, oy = y;
+        x = (1.0f - fabsf(oy)) * (ox >= 0.0f ? 1.0f : -1.0f);
+        y = (1.0f - fabsf(ox)) * (oy >= 0.0f ? 1.0f : -1.0f);
+    }
+    return uint32_t(__half_as_ushort(__float2half_rn(x))) | (uint32_t(__half_as_ushort(__float2half_rn(y))) << 16);
+}
+
+struct Mat3x4 {
+    float m[12];
+};
+
+__global__ void gbuffer_resolve(const unsigned long long* __restrict__ keys, uint32_t W, uint32_t H,
+                                const float* __restrict__ tri, const float* __restrict__ rough, Mat3x4 V, float3 eye,
+                                float* depth, uint32_t* normal, uint16_t* rough_out, uint32_t* tri_out) {
+    uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= uint64_t(W) * H) return;
+    unsigned long long k = keys[i];
+    if (k == ~0ull) {
+        depth[i] = 1.0f;
+        normal[i] = 0;
+        rough_out[i] = 0;
+        if (tri_out) tri_out[i] = 0xffffffffu;
+        return;
+    }
+    uint32_t t = uint32_t(k & 0xffffffffu);
+    depth[i] = __uint_as_float(uint32_t(k >> 32));
+    const float* p = tri + uint64_t(t) * 9;
+    float3 p0 = make_float3(p[0], p[1], p[2]), p1 = make_float3(p[3], p[4], p[5]), p2 = make_float3(p[6], p[7], p[8]);
+    float3 a = make_float3(p1.x - p0.x, p1.y - p0.y, p1.z - p0.z), b = make_float3(p2.x - p0.x, p2.y - p0.y, p2.z - p0.z);
+    float3 n = make_float3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+    float il = rsqrtf(fmaxf(n.x * n.x + n.y * n.y + n.z * n.z, 1e-30f));
+    n = make_float3(n.x * il, n.y * il, n.z * il);
+    if (n.x * (eye.x - p0.x) + n.y * (eye.y - p0.y) + n.z * (eye.z - p0.z) < 0.0f) n = make_float3(-n.x, -n.y, -n.z);
+    float3 nv = make_float3(V.m[0] * n.x + V.m[1] * n.y + V.m[2] * n.z, V.m[4] * n.x + V.m[5] * n.y + V.m[6] * n.z,
+                            V.m[8] * n.x + V.m[9] * n.y + V.m[10] * n.z);
+    float nl = rsqrtf(fmaxf(nv.x * nv.x + nv.y * nv.y + nv.z * nv.z, 1e-30f));
+    nv = make_float3(nv.x * nl, nv.y * nl, nv.z * nl);
+    normal[i] = oct_encode(nv);
+    rough_out[i] = __half_as_ushort(__float2half_rn(rough[t]));
+    if (tri_out) tri_out[i] = t;
+}
+
+}  // namespace
+
+int gbuffer_resolve_launch(const unsigned long long* keys, uint32_t W, uint32_t H, const float* tri,
+                           const float* rough, const float view[16], const float eye[3], float* depth,
+                           uint32_t* normal, uint16_t* rough_out, uint32_t* tri_out, cudaStream_t s) {
+    Mat3x4 V;
+    for (int i = 0; i < 12; ++i) V.m[i] = view[i];
+    uint64_t n = uint64_t(W) * H;
+    gbuffer_resolve<<<uint32_t((n + 255) / 256), 256, 0, s>>>(keys, W, H, tri, rough, V,
+                                                              make_float3(eye[0], eye[1], eye[2]), depth, normal,
+                                                              rough_out, tri_out);
+    return cuda_fail(cudaGetLastError(), "gbuffer_resolve");
+}
+
+}  // namespace f184

@@ -1,0 +1,265 @@
+// trace.cu -- per-pixel diffuse + specular cone trace over a G-buffer.
+//
+// Replaces the reference's indirect pass (Shader/Lighting/indirect.frag:104-243), which marches four
+// stochastic single rays per pixel through a one-level RG16UI volume.  Here each pixel traces five diffuse cones
+// (60-degree aperture: one along the normal, four tilted 60 degrees, in the frame of the reference's
+// make_coord_space, indirect.frag:71-86) and one specular cone whose tan(half aperture) is the G-buffer
+// roughness.  A cone steps by half its diameter, samples the mip chain quadrilinearly (trilinear inside a
+// level, linear between log2(diameter) levels, zero outside the grid) and composites front to back in FP32.
+// The G-buffer decode follows indirect.frag:44-58 and 189-196 (InvProj, then InvModelView).
+#include <vector>
+
+#include "gi_device.cuh"
+
+namespace f184 {
+namespace {
+
+__device__ __forceinline__ float3 f3(float x, float y, float z) { return make_float3(x, y, z); }
+__device__ __forceinline__ float3 add3(float3 a, float3 b) { return f3(a.x + b.x, a.y + b.y, a.z + b.z); }
+__device__ __forceinline__ float3 sub3(float3 a, float3 b) { return f3(a.x - b.x, a.y - b.y, a.z - b.z); }
+__device__ __forceinline__ float3 mul3(float3 a, float s) { return f3(a.x * s, a.y * s, a.z * s); }
+__device__ __forceinline__ float dot3(float3 a, float3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ float3 cross3(float3 a, float3 b) {
+    return f3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+__device__ __forceinline__ float3 norm3(float3 a) {
+    float l = sqrtf(dot3(a, a));
+    return l > 0.0f ? mul3(a, 1.0f / l) : a;
+}
+
+// make_coord_space, indirect.frag:71-86
+__device__ __forceinline__ void coord_space(float3 n, float3& x, float3& y, float3& z) {
+    z = n;
+    float3 h = z;
+    float ax = fabsf(h.x), ay = fabsf(h.y), az = fabsf(h.z);
+    if (ax <= ay && ax <= az)
+        h.x = 1.0f;
+    else if (ay <= ax && ay <= az)
+        h.y = 1.0f;
+    else
+        h.z = 1.0f;
+    z = norm3(z);
+    y = norm3(cross3(h, z));
+    x = norm3(cross3(z, y));
+}
+
+__device__ __forceinline__ float3 oct_decode(uint32_t p) {
+    float x = __half2float(__ushort_as_half(uint16_t(p & 0xffffu)));
+    float y = __half2float(__ushort_as_half(uint16_t(p >> 16)));
+    float3 v = f3(x, y, 1.0f - fabsf(x) - fabsf(y));
+    if (v.z < 0.0f) {
+        float ox = v.x, oy = v.y;
+        v.x = (1.0f - fabsf(oy)) * (ox >= 0.0f ? 1.0f : -1.0f);
+        v.y = (1.0f - fabsf(ox)) * (oy >= 0.0f ? 1.0f : -1.0f);
+    }
+    return norm3(v);
+}
+
+__device__ __forceinline__ float4 tri_sample(const ChainLayout& c, uint32_t l, uint64_t vol_off, float3 x) {
+    const int d = int(c.ldim[l]);
+    const float s = __int_as_float((127 - int(l)) << 23);  // 2^-l
+    float u[3] = {x.x * s - 0.5f, x.y * s - 0.5f, x.z * s - 0.5f};
+    int i0[3];
+    float f[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        float fl = floorf(u[a]);
+        i0[a] = int(fl);
+        f[a] = u[a] - fl;
+    }
+    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+    for (int dz = 0; dz < 2; ++dz) {
+        int z = i0[2] + dz;
+        float wz = dz ? f[2] : 1.0f - f[2];
+#pragma unroll
+        for (int dy = 0; dy < 2; ++dy) {
+            int y = i0[1] + dy;
+            float wy = dy ? f[1] : 1.0f - f[1];
+#pragma unroll
+            for (int dx = 0; dx < 2; ++dx) {
+                int xx = i0[0] + dx;
+                float wx = dx ? f[0] : 1.0f - f[0];
+                if (unsigned(z) < unsigned(d) && unsigned(y) < unsigned(d) && unsigned(xx) < unsigned(d)) {
+                    float w = wx * wy * wz;
+                    float4 v = load_vox(c.base, c.format, vol_off + vox_index(d, xx, y, z));
+                    acc.x += w * v.x;
+                    acc.y += w * v.y;
+                    acc.z += w * v.z;
+                    acc.w += w * v.w;
+                }
+            }
+        }
+    }
+    return acc;
+}
+
+__device__ __forceinline__ float4 level_sample(const ChainLayout& c, uint32_t l, float3 x, float3 dir) {
+    if (!c.aniso || l == 0) return tri_sample(c, l, c.off[l], x);
+    float w[3] = {dir.x * dir.x, dir.y * dir.y, dir.z * dir.z};
+    int sel[3] = {dir.x >= 0.0f ? 0 : 1, dir.y >= 0.0f ? 2 : 3, dir.z >= 0.0f ? 4 : 5};
+    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        float4 s = tri_sample(c, l, c.off[l] + uint64_t(sel[a]) * c.vol[l], x);
+        acc.x += w[a] * s.x;
+        acc.y += w[a] * s.y;
+        acc.z += w[a] * s.z;
+        acc.w += w[a] * s.w;
+    }
+    return acc;
+}
+
+__device__ float4 cone(const ChainLayout& c, const TraceConsts& tc, float3 o, float3 dir, float tan_half) {
+    float cr = 0.f, cg = 0.f, cb = 0.f, alpha = 0.f;
+    float t = tc.p.start_offset;
+    const float dimf = float(c.dim);
+    const float maxl = float(c.levels - 1);
+    while (t <= tc.tmax) {
+        float diam = fmaxf(1.0f, 2.0f * t * tan_half);
+        float lvl = fminf(fmaxf(log2f(diam), 0.0f), maxl);
+        float3 x = add3(o, mul3(dir, t));
+        float m = 2.0f * diam;
+        if (x.x < -m || x.y < -m || x.z < -m || x.x > dimf + m || x.y > dimf + m || x.z > dimf + m) break;
+        float fl = floorf(lvl);
+        uint32_t l0 = uint32_t(fl);
+        float f = lvl - fl;
+        float4 s = level_sample(c, l0, x, dir);
+        if (f > 0.0f && l0 + 1 < c.levels) {
+            float4 s1 = level_sample(c, l0 + 1, x, dir);
+            s.x = s.x + f * (s1.x - s.x);
+            s.y = s.y + f * (s1.y - s.y);
+            s.z = s.z + f * (s1.z - s.z);
+            s.w = s.w + f * (s1.w - s.w);
+        }
+        float tr = 1.0f - alpha;
+        cr += tr * s.x;
+        cg += tr * s.y;
+        cb += tr * s.z;
+        alpha += tr * s.w;
+        if (alpha >= tc.p.alpha_stop) break;
+        t += tc.p.step_factor * diam;
+    }
+    return make_float4(cr, cg, cb, alpha);
+}
+
+__device__ __forceinline__ void store_out(void* out, uint32_t fmt, uint64_t i, float4 v) {
+    if (fmt == F184GI_FMT_F32) {
+        reinterpret_cast<float4*>(out)[i] = v;
+    } else {
+        __half2 a = __floats2half2_rn(v.x, v.y), b = __floats2half2_rn(v.z, v.w);
+        uint2 raw;
+        raw.x = *reinterpret_cast<uint32_t*>(&a);
+        raw.y = *reinterpret_cast<uint32_t*>(&b);
+        reinterpret_cast<uint2*>(out)[i] = raw;
+    }
+}
+
+__device__ void trace_pixel(const ChainLayout& c, const TraceConsts& tc, const TraceView& v, float3 org, float inv_vs,
+                            uint32_t px, uint32_t py) {
+    const uint64_t npix = uint64_t(v.width) * v.height;
+    const uint64_t pi = uint64_t(py) * v.width + px;
+    float d = v.depth[pi];
+    if (!(d < 1.0f)) {
+        store_out(v.out, v.out_format, pi, make_float4(0.f, 0.f, 0.f, 0.f));
+        store_out(v.out, v.out_format, npix + pi, make_float4(0.f, 0.f, 0.f, 0.f));
+        return;
+    }
+    const float* ip = v.iproj;
+    const float* iv = v.iview;
+    float nx = (float(px) + 0.5f) / float(v.width) * 2.0f - 1.0f;
+    float ny = (float(py) + 0.5f) / float(v.height) * 2.0f - 1.0f;
+    float vp[4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) vp[r] = ip[r * 4 + 0] * nx + ip[r * 4 + 1] * ny + ip[r * 4 + 2] * d + ip[r * 4 + 3];
+    float3 cs = f3(vp[0] / vp[3], vp[1] / vp[3], vp[2] / vp[3]);
+    float3 wp = f3(iv[0] * cs.x + iv[1] * cs.y + iv[2] * cs.z + iv[3], iv[4] * cs.x + iv[5] * cs.y + iv[6] * cs.z + iv[7],
+                   iv[8] * cs.x + iv[9] * cs.y + iv[10] * cs.z + iv[11]);
+    float3 nv = oct_decode(v.normal[pi]);
+    float3 nw = norm3(f3(iv[0] * nv.x + iv[1] * nv.y + iv[2] * nv.z, iv[4] * nv.x + iv[5] * nv.y + iv[6] * nv.z,
+                         iv[8] * nv.x + iv[9] * nv.y + iv[10] * nv.z));
+    float rough = __half2float(__ushort_as_half(v.rough[pi]));
+    float3 pv = f3((wp.x - org.x) * inv_vs, (wp.y - org.y) * inv_vs, (wp.z - org.z) * inv_vs);
+    float3 o = add3(pv, mul3(nw, tc.p.start_offset));
+    float3 bx, by, bz;
+    coord_space(nw, bx, by, bz);
+    float4 acc;
+    if (tc.p.diffuse_cones >= 5) {
+        float4 c0 = cone(c, tc, o, bz, tc.p.diffuse_tan_half);
+        acc = make_float4(0.25f * c0.x, 0.25f * c0.y, 0.25f * c0.z, 0.25f * c0.w);
+        const float cphi[4] = {1.f, 0.f, -1.f, 0.f}, sphi[4] = {0.f, 1.f, 0.f, -1.f};
+#pragma unroll 1
+        for (int k = 0; k < 4; ++k) {
+            float3 side = add3(mul3(bx, cphi[k]), mul3(by, sphi[k]));
+            float3 dir = norm3(add3(mul3(bz, tc.cos_tilt), mul3(side, tc.sin_tilt)));
+            float4 ck = cone(c, tc, o, dir, tc.p.diffuse_tan_half);
+            acc.x += 0.1875f * ck.x;
+            acc.y += 0.1875f * ck.y;
+            acc.z += 0.1875f * ck.z;
+            acc.w += 0.1875f * ck.w;
+        }
+    } else {
+        acc = cone(c, tc, o, bz, tc.p.diffuse_tan_half);
+    }
+    store_out(v.out, v.out_format, pi, acc);
+    float4 sp = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (tc.p.specular) {
+        float3 vd = norm3(sub3(wp, f3(v.eye[0], v.eye[1], v.eye[2])));
+        float dn = dot3(vd, nw);
+        float3 rd = norm3(sub3(vd, mul3(nw, 2.0f * dn)));
+        float th = fmaxf(rough, tc.p.min_spec_tan_half);
+        sp = cone(c, tc, o, rd, th);
+    }
+    store_out(v.out, v.out_format, npix + pi, sp);
+}
+
+// One CTA = one 16x8 pixel tile of one view; tiles of all views are enumerated in view order.
+__global__ void __launch_bounds__(128) trace_kernel(ChainLayout c, TraceConsts tc, const f184gi_grid_frame* __restrict__ fr,
+                                                    const TraceView* __restrict__ views,
+                                                    const uint32_t* __restrict__ tile_base, uint32_t nviews) {
+    uint32_t tile = blockIdx.x;
+    uint32_t vi = 0;
+    while (vi + 1 < nviews && tile >= tile_base[vi + 1]) ++vi;
+    const TraceView& v = views[vi];
+    uint32_t local = tile - tile_base[vi];
+    uint32_t tiles_x = (v.width + 15) / 16;
+    uint32_t px = (local % tiles_x) * 16 + (threadIdx.x & 15);
+    uint32_t py = (local / tiles_x) * 8 + (threadIdx.x >> 4);
+    if (px >= v.width || py >= v.height) return;
+    // world -> L0 voxel units: (p - origin) * (inv_voxel_fixed / 256), all scalings exact
+    float3 org = f3(float(fr->origin[0]), float(fr->origin[1]), float(fr->origin[2]));
+    float inv_vs = float(fr->inv_voxel_fixed * (1.0 / 256.0));
+    trace_pixel(c, tc, v, org, inv_vs, px, py);
+}
+
+}  // namespace
+
+size_t trace_scratch_bytes(uint32_t nviews) { return size_t(nviews) * sizeof(TraceView) + size_t(nviews + 1) * 4 + 512; }
+
+int trace_launch(const ChainLayout& c, const TraceConsts& tc, const f184gi_grid_frame* d_frame, const TraceView* views,
+                 uint32_t nviews, void* scratch, size_t scratch_bytes, cudaStream_t s) {
+    if (nviews == 0) return F184GI_OK;
+    if (scratch_bytes < trace_scratch_bytes(nviews)) return fail(F184GI_ERR_INVALID, "trace: scratch too small");
+    // host staging of the view table (views + tile prefix), copied once per call
+    std::vector<unsigned char> host(trace_scratch_bytes(nviews));
+    TraceView* hv = reinterpret_cast<TraceView*>(host.data());
+    uint32_t* hb = reinterpret_cast<uint32_t*>(host.data() + size_t(nviews) * sizeof(TraceView));
+    uint32_t tiles = 0;
+    for (uint32_t i = 0; i < nviews; ++i) {
+        hv[i] = views[i];
+        hb[i] = tiles;
+        tiles += ((views[i].width + 15) / 16) * ((views[i].height + 7) / 8);
+    }
+    hb[nviews] = tiles;
+    cudaError_t e = cudaMemcpyAsync(scratch, host.data(), host.size(), cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) return cuda_fail(e, "trace: view table");
+    // the staging buffer must outlive the async copy
+    e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cuda_fail(e, "trace: view table sync");
+    const TraceView* dv = static_cast<const TraceView*>(scratch);
+    const uint32_t* db = reinterpret_cast<const uint32_t*>(static_cast<const unsigned char*>(scratch) + size_t(nviews) * sizeof(TraceView));
+    trace_kernel<<<tiles, 128, 0, s>>>(c, tc, d_frame, dv, db, nviews);
+    return cuda_fail(cudaGetLastError(), "trace");
+}
+
+}  // namespace f184

@@ -1,0 +1,399 @@
+// voxelize.cu -- conservative voxelization with shadow-mapped direct-light injection into 8^3 bricks.
+//
+// Replaces the reference's VoxelGS/VoxelPS pair (Pipelang/Internal/main.lua:83-144, 242-275), which projects
+// each triangle on its dominant axis and stores an RGB565 albedo + normal per covered pixel centre with
+// last-writer-wins imageStore.  Here a voxel is covered when the triangle and the closed voxel box overlap
+// (separating-axis test), decided exactly in integers on vertices snapped to 1/256 voxel (FP64 snap).  Each
+// covering triangle adds its Lambert weight |dot(-L, n)| * albedo (the term of Shader/Lighting/indirect.frag:60-62,
+// 167) as 16.16 fixed point with integer atomics, so sums and counts are independent of triangle order.  The
+// voxel's radiance is luminance * shadow(voxel centre) * mean weight, the shadow test being indirect.frag:160-165's
+// compare with a two-voxel bias, evaluated in FP64 against the shadow map rasterized by raster.cu.
+//
+// Pipeline: setup (snap, weight, count overlapped bricks) -> scan -> emit (triangle lists per brick) ->
+// one CTA per brick accumulates in shared memory, resolves and writes the brick once.
+#include "gi_device.cuh"
+#include "util.cuh"
+
+namespace f184 {
+namespace {
+
+constexpr int64_t kFix = 256;     // fixed-point units per voxel
+constexpr int64_t kHalf = 128;
+constexpr int64_t kBrickFix = 2048;  // units per brick edge
+constexpr int64_t kMaxQ = int64_t(1) << 19;
+constexpr uint32_t kInvalid = 0xffffffffu;
+
+__constant__ float c_albedo_lut[256];  // (i / 255)^2.2
+
+struct TriRec {
+    int32_t q[9];    // snapped vertices (x0 y0 z0 x1 ...), 24.8 voxel fixed point
+    uint32_t wq[3];  // injection weight per channel, 16.16 fixed point; wq[0] = kInvalid marks skipped
+};
+
+struct VoxScratch {
+    TriRec* recs;
+    uint32_t* brick_count;
+    uint32_t* brick_start;
+    uint32_t* brick_fill;
+    uint32_t* total;
+    uint32_t* scan_tmp;
+    uint32_t* dirty_mask;  // nbricks bits, null = all bricks
+    uint32_t* list;
+    uint64_t list_cap;
+};
+
+__device__ __forceinline__ int64_t iabs64(int64_t x) { return x < 0 ? -x : x; }
+__device__ __forceinline__ int64_t sar7_floor(int64_t x) { return x >> 7; }         // floor(x / 128)
+__device__ __forceinline__ int64_t sar7_ceil(int64_t x) { return -((-x) >> 7); }    // ceil(x / 128)
+__device__ __forceinline__ int32_t clamp32(int64_t x) {
+    return int32_t(x > int64_t(INT32_MAX) ? int64_t(INT32_MAX) : (x < int64_t(INT32_MIN) ? int64_t(INT32_MIN) : x));
+}
+
+// Exact closed-set overlap of a triangle (fixed-point q) with the axis-aligned box of centre c, half size h.
+__device__ bool tri_box_sat(const int32_t* q, const int64_t c[3], int64_t h) {
+    int64_t v[3][3];
+    for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b) v[a][b] = int64_t(q[a * 3 + b]) - c[b];
+    for (int b = 0; b < 3; ++b) {
+        int64_t mn = min(v[0][b], min(v[1][b], v[2][b])), mx = max(v[0][b], max(v[1][b], v[2][b]));
+        if (mn > h || mx < -h) return false;
+    }
+    int64_t e0[3], e1[3];
+    for (int b = 0; b < 3; ++b) {
+        e0[b] = v[1][b] - v[0][b];
+        e1[b] = v[2][b] - v[0][b];
+    }
+    int64_t n[3] = {e0[1] * e1[2] - e0[2] * e1[1], e0[2] * e1[0] - e0[0] * e1[2], e0[0] * e1[1] - e0[1] * e1[0]};
+    int64_t s = n[0] * v[0][0] + n[1] * v[0][1] + n[2] * v[0][2];
+    int64_t r = h * (iabs64(n[0]) + iabs64(n[1]) + iabs64(n[2]));
+    if (s > r || s < -r) return false;
+    for (int e = 0; e < 3; ++e) {
+        int64_t ed[3];
+        for (int b = 0; b < 3; ++b) ed[b] = v[(e + 1) % 3][b] - v[e][b];
+        for (int ax = 0; ax < 3; ++ax) {
+            int64_t a0 = 0, a1 = 0, a2 = 0;
+            if (ax == 0) a1 = ed[2], a2 = -ed[1];
+            if (ax == 1) a0 = -ed[2], a2 = ed[0];
+            if (ax == 2) a0 = ed[1], a1 = -ed[0];
+            int64_t p0 = a0 * v[0][0] + a1 * v[0][1] + a2 * v[0][2];
+            int64_t p1 = a0 * v[1][0] + a1 * v[1][1] + a2 * v[1][2];
+            int64_t p2 = a0 * v[2][0] + a1 * v[2][1] + a2 * v[2][2];
+            int64_t rr = h * (iabs64(a0) + iabs64(a1) + iabs64(a2));
+            if (min(p0, min(p1, p2)) > rr || max(p0, max(p1, p2)) < -rr) return false;
+        }
+    }
+    return true;
+}
+
+// voxel range touched by the triangle's AABB (closed boxes), clamped to the grid
+__device__ __forceinline__ void voxel_range(const int32_t* q, uint32_t dim, int32_t lo[3], int32_t hi[3]) {
+    for (int a = 0; a < 3; ++a) {
+        int64_t mn = min(q[a], min(q[3 + a], q[6 + a])), mx = max(q[a], max(q[3 + a], q[6 + a]));
+        lo[a] = int32_t(max(int64_t(0), -floor_div64(-(mn - kFix), kFix)));
+        hi[a] = int32_t(min(int64_t(dim) - 1, floor_div64(mx, kFix)));
+    }
+}
+
+template <bool kEmit>
+__device__ void visit_bricks(const TriRec& r, uint32_t t, uint32_t dim, const VoxScratch& sc, uint32_t* status) {
+    int32_t lo[3], hi[3];
+    voxel_range(r.q, dim, lo, hi);
+    int32_t b0[3], b1[3];
+    for (int a = 0; a < 3; ++a) b0[a] = lo[a] >> 3, b1[a] = hi[a] >> 3;
+    bool single = b0[0] == b1[0] && b0[1] == b1[1] && b0[2] == b1[2];
+    for (int bz = b0[2]; bz <= b1[2]; ++bz)
+        for (int by = b0[1]; by <= b1[1]; ++by)
+            for (int bx = b0[0]; bx <= b1[0]; ++bx) {
+                uint32_t m = morton3(bx, by, bz);
+                if (sc.dirty_mask && !((sc.dirty_mask[m >> 5] >> (m & 31)) & 1u)) continue;
+                if (!single) {
+                    const int64_t c[3] = {bx * kBrickFix + kBrickFix / 2, by * kBrickFix + kBrickFix / 2,
+                                          bz * kBrickFix + kBrickFix / 2};
+                    if (!tri_box_sat(r.q, c, kBrickFix / 2)) continue;
+                }
+                if (!kEmit) {
+                    atomicAdd(&sc.brick_count[m], 1u);
+                } else {
+                    uint64_t slot = uint64_t(sc.brick_start[m]) + atomicAdd(&sc.brick_fill[m], 1u);
+                    if (slot < sc.list_cap)
+                        sc.list[slot] = t;
+                    else
+                        set_status(status, kStatusOverflow);
+                }
+            }
+}
+
+__global__ void vox_setup(const float* __restrict__ tri, const uint32_t* __restrict__ albedo, uint64_t ntris,
+                          const f184gi_grid_frame* __restrict__ fr, uint32_t dim, VoxScratch sc, uint32_t* status) {
+    uint64_t t = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (t >= ntris) return;
+    TriRec r;
+    bool ok = true;
+    const float* p = tri + t * 9;
+    for (int i = 0; i < 9; ++i) {
+        int a = i % 3;
+        double d = dsub(double(p[i]), fr->origin[a]);
+        double s = dmul(d, fr->inv_voxel_fixed);
+        int64_t q = __double2ll_rn(s);
+        if (q >= kMaxQ || q <= -kMaxQ) {
+            ok = false;
+            q = 0;
+        }
+        r.q[i] = int32_t(q);
+    }
+    if (!ok) set_status(status, kStatusRange);
+    if (ok) {
+        int64_t e0[3], e1[3];
+        for (int a = 0; a < 3; ++a) {
+            e0[a] = int64_t(r.q[3 + a]) - r.q[a];
+            e1[a] = int64_t(r.q[6 + a]) - r.q[a];
+        }
+        int64_t n0 = e0[1] * e1[2] - e0[2] * e1[1], n1 = e0[2] * e1[0] - e0[0] * e1[2],
+                n2 = e0[0] * e1[1] - e0[1] * e1[0];
+        if (n0 == 0 && n1 == 0 && n2 == 0) ok = false;
+        int32_t lo[3], hi[3];
+        voxel_range(r.q, dim, lo, hi);
+        if (lo[0] > hi[0] || lo[1] > hi[1] || lo[2] > hi[2]) ok = false;
+    }
+    if (!ok) {
+        r.wq[0] = r.wq[1] = r.wq[2] = kInvalid;
+        sc.recs[t] = r;
+        return;
+    }
+    // injection weight |dot(-L, n)| * albedo, FP32
+    float3 a = make_float3(p[3] - p[0], p[4] - p[1], p[5] - p[2]);
+    float3 b = make_float3(p[6] - p[0], p[7] - p[1], p[8] - p[2]);
+    float3 n = make_float3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+    float len = sqrtf(n.x * n.x + n.y * n.y + n.z * n.z);
+    float wi0 = -float(fr->light_dir[0]), wi1 = -float(fr->light_dir[1]), wi2 = -float(fr->light_dir[2]);
+    float cosv = len > 0.0f ? fabsf(wi0 * n.x + wi1 * n.y + wi2 * n.z) / len : 0.0f;
+    uint32_t al = albedo[t];
+    for (int c = 0; c < 3; ++c) {
+        float w = cosv * c_albedo_lut[(al >> (8 * c)) & 255u];
+        r.wq[c] = min(__float2uint_rn(w * 65536.0f), 65536u);
+    }
+    sc.recs[t] = r;
+    visit_bricks<false>(r, uint32_t(t), dim, sc, status);
+}
+
+__global__ void vox_emit(uint64_t ntris, uint32_t dim, VoxScratch sc, uint32_t* status) {
+    uint64_t t = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (t >= ntris) return;
+    TriRec r = sc.recs[t];
+    if (r.wq[0] == kInvalid) return;
+    visit_bricks<true>(r, uint32_t(t), dim, sc, status);
+}
+
+__global__ void vox_dirty_mask(const uint32_t* dirty, uint32_t ndirty, uint32_t nbricks, uint32_t* mask) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < ndirty && dirty[i] < nbricks) atomicOr(&mask[dirty[i] >> 5], 1u << (dirty[i] & 31));
+}
+
+// Per-axis separating test prepared for one (triangle, brick) item: with m = 2 (voxel - brick origin) + 1
+// (odd, 1..15), the voxel centre is 128 m + brick offset and the axis test reads lo <= a . m <= hi.
+struct AxisTest {
+    int32_t ax, ay, az, lo, hi;
+};
+
+__global__ void __launch_bounds__(256) vox_bricks(VoxScratch sc, const f184gi_grid_frame* __restrict__ fr,
+                                                  uint32_t dim, ChainLayout chain, f184gi_light light,
+                                                  const unsigned long long* __restrict__ shadow, uint32_t res,
+                                                  uint32_t* counts, const uint32_t* __restrict__ dirty,
+                                                  uint32_t* status) {
+    __shared__ uint32_t s_sum[3][512];
+    __shared__ uint32_t s_cnt[512];
+    const uint32_t m = dirty ? dirty[blockIdx.x] : blockIdx.x;
+    const uint32_t nb = dim >> 3;
+    if (m >= nb * nb * nb) return;
+    const int32_t bx = int32_t(compact1by2(m)), by = int32_t(compact1by2(m >> 1)), bz = int32_t(compact1by2(m >> 2));
+    for (int i = threadIdx.x; i < 512; i += 256) {
+        s_sum[0][i] = s_sum[1][i] = s_sum[2][i] = 0;
+        s_cnt[i] = 0;
+    }
+    __syncthreads();
+    const uint32_t beg = sc.brick_start[m];
+    const uint32_t end = uint32_t(min(uint64_t(beg) + sc.brick_count[m], sc.list_cap));
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int64_t base[3] = {int64_t(bx) * kBrickFix, int64_t(by) * kBrickFix, int64_t(bz) * kBrickFix};
+    for (uint32_t it = beg + warp; it < end; it += 8) {
+        const uint32_t t = sc.list[it];
+        const TriRec r = sc.recs[t];
+        int32_t lo[3], hi[3];
+        voxel_range(r.q, dim, lo, hi);
+        lo[0] = max(lo[0], bx * 8), hi[0] = min(hi[0], bx * 8 + 7);
+        lo[1] = max(lo[1], by * 8), hi[1] = min(hi[1], by * 8 + 7);
+        lo[2] = max(lo[2], bz * 8), hi[2] = min(hi[2], bz * 8 + 7);
+        if (lo[0] > hi[0] || lo[1] > hi[1] || lo[2] > hi[2]) continue;
+        // vertices relative to the brick origin (|v| < 2^20)
+        int64_t v[3][3];
+        for (int a = 0; a < 3; ++a)
+            for (int b = 0; b < 3; ++b) v[a][b] = int64_t(r.q[a * 3 + b]) - base[b];
+        // lanes 0..8 prepare the nine edge x axis tests, lane 9 the plane test; then broadcast
+        AxisTest my{0, 0, 0, 0, 0};
+        int64_t pn[3] = {0, 0, 0}, plo = 0, phi = 0;
+        if (lane < 9) {
+            int e = lane / 3, ax = lane % 3;
+            int64_t ed[3];
+            for (int b = 0; b < 3; ++b) ed[b] = v[(e + 1) % 3][b] - v[e][b];
+            int64_t a0 = 0, a1 = 0, a2 = 0;
+            if (ax == 0) a1 = ed[2], a2 = -ed[1];
+            if (ax == 1) a0 = -ed[2], a2 = ed[0];
+            if (ax == 2) a0 = ed[1], a1 = -ed[0];
+            int64_t p0 = a0 * v[0][0] + a1 * v[0][1] + a2 * v[0][2];
+            int64_t p1 = a0 * v[1][0] + a1 * v[1][1] + a2 * v[1][2];
+            int64_t p2 = a0 * v[2][0] + a1 * v[2][1] + a2 * v[2][2];
+            int64_t rr = kHalf * (iabs64(a0) + iabs64(a1) + iabs64(a2));
+            int64_t pmin = min(p0, min(p1, p2)), pmax = max(p0, max(p1, p2));
+            // overlap iff pmin - rr <= 128 (a . m) <= pmax + rr
+            my.ax = int32_t(a0), my.ay = int32_t(a1), my.az = int32_t(a2);
+            my.lo = clamp32(sar7_ceil(pmin - rr));
+            my.hi = clamp32(sar7_floor(pmax + rr));
+        }
+        {
+            int64_t e0[3], e1[3];
+            for (int b = 0; b < 3; ++b) {
+                e0[b] = v[1][b] - v[0][b];
+                e1[b] = v[2][b] - v[0][b];
+            }
+            pn[0] = e0[1] * e1[2] - e0[2] * e1[1];
+            pn[1] = e0[2] * e1[0] - e0[0] * e1[2];
+            pn[2] = e0[0] * e1[1] - e0[1] * e1[0];
+            int64_t s = pn[0] * v[0][0] + pn[1] * v[0][1] + pn[2] * v[0][2];
+            int64_t rr = kHalf * (iabs64(pn[0]) + iabs64(pn[1]) + iabs64(pn[2]));
+            // overlap iff s - rr <= 128 (n . m) <= s + rr
+            plo = sar7_ceil(s - rr);
+            phi = sar7_floor(s + rr);
+        }
+        AxisTest ax[9];
+#pragma unroll
+        for (int k = 0; k < 9; ++k) {
+            ax[k].ax = __shfl_sync(0xffffffffu, my.ax, k);
+            ax[k].ay = __shfl_sync(0xffffffffu, my.ay, k);
+            ax[k].az = __shfl_sync(0xffffffffu, my.az, k);
+            ax[k].lo = __shfl_sync(0xffffffffu, my.lo, k);
+            ax[k].hi = __shfl_sync(0xffffffffu, my.hi, k);
+        }
+        const int nx = hi[0] - lo[0] + 1, ny = hi[1] - lo[1] + 1, nz = hi[2] - lo[2] + 1;
+        const int nvox = nx * ny * nz;
+        for (int p = int(lane); p < nvox; p += 32) {
+            int lx = lo[0] - bx * 8 + p % nx, ly = lo[1] - by * 8 + (p / nx) % ny, lz = lo[2] - bz * 8 + p / (nx * ny);
+            int32_t mx = 2 * lx + 1, my2 = 2 * ly + 1, mz = 2 * lz + 1;
+            bool hit = true;
+#pragma unroll
+            for (int k = 0; k < 9; ++k) {
+                int32_t d = ax[k].ax * mx + ax[k].ay * my2 + ax[k].az * mz;
+                hit = hit && d >= ax[k].lo && d <= ax[k].hi;
+            }
+            if (hit) {
+                int64_t d = pn[0] * mx + pn[1] * my2 + pn[2] * mz;
+                hit = d >= plo && d <= phi;
+            }
+            if (hit) {
+                int li = lz * 64 + ly * 8 + lx;
+                atomicAdd(&s_sum[0][li], r.wq[0]);
+                atomicAdd(&s_sum[1][li], r.wq[1]);
+                atomicAdd(&s_sum[2][li], r.wq[2]);
+                atomicAdd(&s_cnt[li], 1u);
+            }
+        }
+    }
+    __syncthreads();
+    // resolve: radiance = luminance * shadow * mean weight, opacity 1 where covered
+    const double* M = fr->light_clip;
+    const double half_res = 0.5 * double(res);
+    for (int li = threadIdx.x; li < 512; li += 256) {
+        int lx = li & 7, ly = (li >> 3) & 7, lz = li >> 6;
+        uint32_t cnt = s_cnt[li];
+        float4 out = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (cnt) {
+            if (cnt >= 65536u) set_status(status, kStatusOverflow);
+            int64_t ijk[3] = {bx * 8 + lx, by * 8 + ly, bz * 8 + lz};
+            double cw[3];
+            for (int a = 0; a < 3; ++a) cw[a] = dadd(fr->origin[a], dmul(dadd(double(ijk[a]), 0.5), fr->voxel_size));
+            double x = drow(M + 0, cw[0], cw[1], cw[2]);
+            double y = drow(M + 4, cw[0], cw[1], cw[2]);
+            double z = drow(M + 8, cw[0], cw[1], cw[2]);
+            double tx = floor(dmul(dadd(x, 1.0), half_res)), ty = floor(dmul(dadd(y, 1.0), half_res));
+            bool lit = true;
+            if (tx >= 0.0 && ty >= 0.0 && tx < double(res) && ty < double(res)) {
+                unsigned long long k = shadow[uint64_t(ty) * res + uint64_t(tx)];
+                double sd = k == ~0ull ? 1.0 : double(__uint_as_float(uint32_t(k >> 32)));
+                lit = dsub(z, fr->shadow_bias) <= sd;
+            }
+            float scale = lit ? (1.0f / 65536.0f) / float(cnt) : 0.0f;
+            out.x = light.luminance[0] * (float(s_sum[0][li]) * scale);
+            out.y = light.luminance[1] * (float(s_sum[1][li]) * scale);
+            out.z = light.luminance[2] * (float(s_sum[2][li]) * scale);
+            out.w = 1.0f;
+        }
+        store_vox(chain.base, chain.format, chain.off[0] + (uint64_t(m) << 9) + li, out);
+        if (counts) {
+            uint64_t lin = (uint64_t(bz * 8 + lz) * dim + uint64_t(by * 8 + ly)) * dim + uint64_t(bx * 8 + lx);
+            counts[lin] = cnt;
+        }
+    }
+}
+
+template <class T>
+T* carve(char*& p, uint64_t n) {
+    uintptr_t a = (reinterpret_cast<uintptr_t>(p) + 255) & ~uintptr_t(255);
+    T* r = reinterpret_cast<T*>(a);
+    p = reinterpret_cast<char*>(a + n * sizeof(T));
+    return r;
+}
+
+uint64_t list_capacity(uint64_t ntris, uint32_t nbricks) { return ntris * 6 + uint64_t(nbricks) * 2 + 65536; }
+
+bool g_lut_ready = false;
+
+}  // namespace
+
+size_t voxelize_scratch_bytes(uint64_t ntris, uint32_t dim) {
+    uint32_t nb = dim / 8, nbricks = nb * nb * nb;
+    return ntris * sizeof(TriRec) + uint64_t(nbricks) * 12 + scan_scratch_bytes(nbricks) + (nbricks / 32 + 1) * 4 +
+           list_capacity(ntris, nbricks) * 4 + 16 * 256;
+}
+
+int voxelize_launch(const VoxelizeJob& job, void* scratch, size_t scratch_bytes, uint32_t* d_status, cudaStream_t s) {
+    const uint32_t dim = job.chain.dim;
+    if (dim < 16 || dim > 512 || (dim & (dim - 1))) return fail(F184GI_ERR_INVALID, "voxelize: dim must be 2^k in 16..512");
+    if (job.ntris >= 0xffff0000ull) return fail(F184GI_ERR_INVALID, "voxelize: too many triangles");
+    if (scratch_bytes < voxelize_scratch_bytes(job.ntris, dim)) return fail(F184GI_ERR_INVALID, "voxelize: scratch too small");
+    if (!g_lut_ready) {
+        float lut[256];
+        for (int i = 0; i < 256; ++i) lut[i] = float(std::pow(double(i) / 255.0, 2.2));
+        cudaError_t e = cudaMemcpyToSymbol(c_albedo_lut, lut, sizeof(lut));
+        if (e != cudaSuccess) return cuda_fail(e, "voxelize: albedo table");
+        g_lut_ready = true;
+    }
+    const uint32_t nb = dim / 8, nbricks = nb * nb * nb;
+    char* p = static_cast<char*>(scratch);
+    VoxScratch sc;
+    sc.recs = carve<TriRec>(p, job.ntris);
+    sc.brick_count = carve<uint32_t>(p, nbricks);
+    sc.brick_start = carve<uint32_t>(p, nbricks);
+    sc.brick_fill = carve<uint32_t>(p, nbricks);
+    sc.total = carve<uint32_t>(p, 1);
+    sc.scan_tmp = carve<uint32_t>(p, scan_scratch_bytes(nbricks) / 4);
+    uint32_t* mask = carve<uint32_t>(p, nbricks / 32 + 1);
+    sc.list_cap = list_capacity(job.ntris, nbricks);
+    sc.list = carve<uint32_t>(p, sc.list_cap);
+    sc.dirty_mask = nullptr;
+    cudaMemsetAsync(sc.brick_count, 0, size_t(nbricks) * 4, s);
+    cudaMemsetAsync(sc.brick_fill, 0, size_t(nbricks) * 4, s);
+    if (job.ndirty) {
+        sc.dirty_mask = mask;
+        cudaMemsetAsync(mask, 0, size_t(nbricks / 32 + 1) * 4, s);
+        vox_dirty_mask<<<(job.ndirty + 255) / 256, 256, 0, s>>>(job.dirty_bricks, job.ndirty, nbricks, mask);
+    }
+    if (job.ntris) vox_setup<<<uint32_t((job.ntris + 127) / 128), 128, 0, s>>>(job.tri, job.albedo, job.ntris, job.d_frame, dim, sc, d_status);
+    int rc = exclusive_scan(sc.brick_count, nbricks, sc.brick_start, sc.total, sc.scan_tmp, s);
+    if (rc) return rc;
+    if (job.ntris) vox_emit<<<uint32_t((job.ntris + 127) / 128), 128, 0, s>>>(job.ntris, dim, sc, d_status);
+    uint32_t nblocks = job.ndirty ? job.ndirty : nbricks;
+    vox_bricks<<<nblocks, 256, 0, s>>>(sc, job.d_frame, dim, job.chain, job.light, job.shadow_keys, job.shadow_res,
+                                       job.counts, job.ndirty ? job.dirty_bricks : nullptr, d_status);
+    return cuda_fail(cudaGetLastError(), "voxelize");
+}
+
+}  // namespace f184

@@ -1,0 +1,244 @@
+/*
+ * f184gi.h -- C ABI of the GB300 voxel global-illumination path.
+ *
+ * The path has three passes, driven in the same order as the reference renderer's frame:
+ *   f184gi_voxelize  -- shadow map + conservative voxelization with direct-light injection
+ *                       (replaces CZOnlyRenderer::RenderList, Foreground/Renderer/ZOnlyRenderer.h:21-22,
+ *                        and CVoxelizeRenderer::RenderList, Foreground/Renderer/VoxelizeRenderer.h:21-22,
+ *                        as called from CMegaPipeline::Render, Foreground/Renderer/MegaPipeline.cpp:188-223)
+ *   f184gi_mip       -- 3D mip chain of the radiance/opacity grid (the reference volume has one level,
+ *                       Foreground/Renderer/MegaPipeline.cpp:474-482; this pass has no reference counterpart)
+ *   f184gi_trace     -- per-pixel diffuse + specular cone trace over a G-buffer
+ *                       (replaces the lighting_indirect fullscreen pass, Foreground/Renderer/MegaPipeline.cpp:241-268,
+ *                        shader Shader/Lighting/indirect.frag:104-243)
+ *
+ * Conventions
+ *  - Every entry point returns an int status: 0 = ok, negative = error; f184gi_last_error() returns a
+ *    thread-local message for the last failure on the calling thread.
+ *  - Buffers passed as `const float*` etc. to the pass calls are DEVICE pointers unless the name says host.
+ *    Work is stream-ordered on the caller's cudaStream_t, passed as `void*` (NULL = legacy default stream).
+ *  - Matrices are row-major 4x4 floats acting on column vectors (v' = M v), the memory layout of
+ *    tc::Matrix4 (Math/Matrix4.h).  The reference transposes them before upload to GLSL
+ *    (Foreground/SceneGraph/SceneView.cpp:28-30); this ABI takes them untransposed.
+ *  - One context owns its device buffers; it is not thread-safe (like CMegaPipeline, MegaPipeline.cpp:374-375):
+ *    callers serialise calls on one context.  Separate contexts may be used from separate threads.
+ */
+#ifndef F184GI_H
+#define F184GI_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define F184GI_ABI_VERSION 1
+
+/* status codes */
+#define F184GI_OK 0
+#define F184GI_ERR_INVALID (-1)  /* bad argument (null pointer, size out of range, unknown handle) */
+#define F184GI_ERR_CUDA (-2)     /* a CUDA runtime call failed */
+#define F184GI_ERR_OOM (-3)      /* device allocation failed */
+#define F184GI_ERR_BUDGET (-4)   /* request does not fit the context's HBM budget */
+#define F184GI_ERR_OVERFLOW (-5) /* a bounded device structure overflowed (result invalid) */
+#define F184GI_ERR_TIMEOUT (-6)  /* a bounded wait expired */
+#define F184GI_ERR_NOTFOUND (-7) /* unknown grid / request id */
+#define F184GI_ERR_CANCELLED (-8)
+
+/* ---- boundary value types (layout-compatible with the reference Math library) ---- */
+
+/* tc::Vector3 (Math/Vector3.h), 12 bytes */
+typedef struct f184gi_vec3 {
+    float x, y, z;
+} f184gi_vec3;
+
+/* tc::BoundingBox (Math/BoundingBox.h:321-325): Min, pad, Max, pad -- 32 bytes */
+typedef struct f184gi_bounds {
+    f184gi_vec3 min;
+    float pad0;
+    f184gi_vec3 max;
+    float pad1;
+} f184gi_bounds;
+
+/* The sun as the reference binds it (PerLightConstants, MegaPipeline.cpp:95-99, 264-265):
+ * luminance = Color * Intensity (Foreground/SceneGraph/Light.h:18),
+ * direction = the light node's world -Z (MegaPipeline.cpp:110), i.e. the direction light travels.
+ * Lambert uses -direction (indirect.frag:167). */
+typedef struct f184gi_light {
+    float luminance[3];
+    float direction[3];
+} f184gi_light;
+
+/* storage formats of the radiance/opacity grid (RGB = radiance premultiplied by opacity, A = opacity) */
+#define F184GI_FMT_F32 0u /* float4 per voxel, 16 B */
+#define F184GI_FMT_F16 1u /* half4  per voxel,  8 B */
+
+/* grid flags */
+#define F184GI_GRID_KEEP_COUNTS 1u /* also keep the per-voxel contribution count (u32, L0) for inspection */
+
+typedef struct f184gi_grid_desc {
+    uint32_t dim;         /* voxels per axis at L0: power of two, 16..512 */
+    uint32_t levels;      /* mip levels including L0: 1..log2(dim) */
+    uint32_t format;      /* F184GI_FMT_* */
+    uint32_t anisotropic; /* 0 = isotropic mips, 1 = 6-direction anisotropic mips (levels >= 1) */
+    uint32_t shadow_res;  /* shadow map texels per side: 64..8192 */
+    uint32_t flags;       /* F184GI_GRID_* */
+} f184gi_grid_desc;
+
+/* Placement of the grid in the world, derived from the scene bounds in FP64 (read back with f184gi_grid_get_frame).
+ * voxel v = floor((p - origin) / voxel_size). */
+typedef struct f184gi_grid_frame {
+    double origin[3];
+    double voxel_size;
+    double inv_voxel_fixed; /* 256 / voxel_size: world -> 24.8 voxel fixed point */
+    double light_clip[16];  /* world -> shadow clip space (row-major), z in [0,1] */
+    double shadow_bias;     /* clip-z bias of the shadow compare (two voxels along the light) */
+    double light_dir[3];    /* normalised direction of travel */
+} f184gi_grid_frame;
+
+/* One view over one G-buffer (the trace's inputs).  The G-buffer layout:
+ *   depth     FP32 per pixel, NDC depth of `proj` (the value the reference's depth attachment holds,
+ *             decoded with InvProj as indirect.frag:50-55 does); >= 1.0 marks background.
+ *   normal    2 x FP16 per pixel (packed in a u32, low half = x): octahedral encoding of the view-space
+ *             unit normal (the reference stores view-space normals, Pipelang/Internal/main.lua:56).
+ *   roughness FP16 per pixel (the reference's Target2.g, main.lua:238).
+ * Row y = 0 is the top of the image (uv.y = (y + 0.5) / height, as the reference's fullscreen pass). */
+typedef struct f184gi_view {
+    float view[16]; /* world -> view, row-major */
+    float proj[16]; /* view -> clip, row-major (CCamera::CalcPerspective convention) */
+    uint32_t width, height;
+    const float* depth;
+    const uint32_t* normal;
+    const uint16_t* roughness;
+    void* out;           /* 2 * width * height RGBA: [diffuse.rgb, occlusion] then [specular.rgb, alpha] */
+    uint32_t out_format; /* F184GI_FMT_F32 (float4) or F184GI_FMT_F16 (half4) */
+    uint32_t pad;
+} f184gi_view;
+
+/* Cone-trace parameters; f184gi_cone_params_default fills the defaults noted below. */
+typedef struct f184gi_cone_params {
+    uint32_t diffuse_cones;  /* 5 (1 along the normal + 4 tilted) or 1 */
+    float diffuse_tan_half;  /* tan(30 deg): 60-degree aperture */
+    float diffuse_tilt_deg;  /* 60: tilt of the side cones from the normal */
+    float step_factor;       /* 0.5: step = step_factor * cone diameter */
+    float max_distance;      /* in L0 voxels; <= 0 means the grid diagonal */
+    float alpha_stop;        /* 0.999: stop a cone once its opacity reaches this */
+    float start_offset;      /* 1.0: origin offset along the normal, in L0 voxels */
+    float min_spec_tan_half; /* 0.05: specular cone tan(half aperture) = max(roughness, this) */
+    uint32_t specular;       /* 1 = trace the specular cone */
+    uint32_t pad;
+} f184gi_cone_params;
+
+typedef struct f184gi_config {
+    int device;              /* CUDA device ordinal */
+    uint32_t flags;
+    uint64_t hbm_budget;     /* bytes the context may hold on the device; 0 = no limit */
+} f184gi_config;
+
+typedef struct f184gi_ctx f184gi_ctx;
+
+/* ---- context and grids ---- */
+const char* f184gi_last_error(void);
+int f184gi_abi_version(void);
+int f184gi_create(const f184gi_config* cfg, f184gi_ctx** out);
+int f184gi_destroy(f184gi_ctx* ctx);
+/* bytes currently held on the device by the context */
+int f184gi_memory_used(f184gi_ctx* ctx, uint64_t* bytes);
+
+/* Allocate a radiance/opacity grid with its mip chain and shadow map.  Grids stay resident until destroyed. */
+int f184gi_grid_create(f184gi_ctx* ctx, const f184gi_grid_desc* desc, uint32_t* grid);
+int f184gi_grid_destroy(f184gi_ctx* ctx, uint32_t grid);
+/* bytes a grid with this descriptor occupies (grid + mips + shadow map + scratch reserve) */
+int f184gi_grid_bytes(const f184gi_grid_desc* desc, uint64_t* bytes);
+
+/* ---- the three passes ---- */
+
+/* Voxelize `ntris` triangles (tri_xyz: 9 floats per triangle, device) with per-triangle RGBA8 albedo
+ * (device, R in the low byte) into `grid`, injecting the directional light through a shadow map that this
+ * call rasterizes.  bounds (host pointer) fixes the grid placement; NULL = the triangles' own AABB,
+ * reduced on the device.  dirty_bricks (device, brick indices in Morton order) limits the rewrite to those
+ * 8^3 bricks of L0 (ndirty = 0: whole grid); the shadow map is always rebuilt. */
+int f184gi_voxelize(f184gi_ctx* ctx, uint32_t grid, const float* tri_xyz, const uint32_t* albedo,
+                    uint64_t ntris, const f184gi_bounds* bounds, const f184gi_light* light,
+                    const uint32_t* dirty_bricks, uint32_t ndirty, void* stream);
+
+/* Build mip levels 1..levels-1 from L0 (levels = 0: all levels of the grid). */
+int f184gi_mip(f184gi_ctx* ctx, uint32_t grid, uint32_t levels, uint32_t anisotropic, void* stream);
+
+/* Cone-trace every pixel of every view against `grid`; params NULL = defaults. */
+int f184gi_trace(f184gi_ctx* ctx, uint32_t grid, const f184gi_view* views, uint32_t nviews,
+                 const f184gi_cone_params* params, void* stream);
+
+void f184gi_cone_params_default(f184gi_cone_params* p);
+
+/* ---- supporting passes ---- */
+
+/* Rasterize a G-buffer for one camera (the reference's GBufferRenderer pass,
+ * Foreground/Renderer/GBufferRenderer.cpp:79-116 with main.lua:32-58,227-240): flat face normals facing the
+ * camera, per-triangle roughness (device FP32), depth of view->proj.  Writes view->depth/normal/roughness
+ * (device buffers owned by the caller).  Fragment ties resolve to the lowest triangle index. */
+int f184gi_gbuffer(f184gi_ctx* ctx, const float* tri_xyz, const float* roughness, uint64_t ntris,
+                   const f184gi_view* view, uint32_t* tri_id_out, void* stream);
+
+/* Wait for the stream, then report (and clear) errors that kernels flagged on the device since the last
+ * check: F184GI_ERR_OVERFLOW (a bounded structure overflowed), F184GI_ERR_TIMEOUT (a bounded wait expired). */
+int f184gi_sync(f184gi_ctx* ctx, void* stream);
+
+/* ---- inspection (host copies; synchronise the stream) ---- */
+int f184gi_grid_get_frame(f184gi_ctx* ctx, uint32_t grid, f184gi_grid_frame* out);
+/* level as linear FP32 RGBA, x fastest: dim_l^3 * 4 floats (anisotropic: direction `dir` 0..5 for level >= 1) */
+int f184gi_grid_read_level(f184gi_ctx* ctx, uint32_t grid, uint32_t level, uint32_t dir, float* host_rgba);
+/* shadow map as FP32 depth (1.0 = empty), shadow_res^2 floats, row 0 first */
+int f184gi_grid_read_shadow(f184gi_ctx* ctx, uint32_t grid, float* host_depth);
+/* per-voxel contribution counts at L0 (needs F184GI_GRID_KEEP_COUNTS), linear x fastest */
+int f184gi_grid_read_counts(f184gi_ctx* ctx, uint32_t grid, uint32_t* host_counts);
+/* device pointer and byte size of one level (for callers that sample the chain themselves) */
+int f184gi_grid_level_ptr(f184gi_ctx* ctx, uint32_t grid, uint32_t level, void** dev_ptr, uint64_t* bytes);
+
+/* Host computation of the grid frame that f184gi_voxelize derives from `bounds` (bit-identical to it). */
+int f184gi_frame_from_bounds(const f184gi_bounds* bounds, uint32_t dim, const float light_dir[3],
+                             f184gi_grid_frame* out);
+
+/* ---- host helpers mirroring Foreground/SceneGraph/Camera.cpp ---- */
+/* CCamera::CalcPerspective (Camera.cpp:85-102): fovy in degrees */
+void f184gi_camera_perspective(float fovy_deg, float aspect, float near_clip, float far_clip, float out[16]);
+/* CCamera::CalcOrtho (Camera.cpp:104-111) */
+void f184gi_camera_ortho(float mag_x, float mag_y, float near_clip, float far_clip, float out[16]);
+/* view matrix of a camera at `eye` looking at `target` with +Y up: the inverse of the camera node's world
+ * transform (SceneView.cpp:28), camera looking down its local -Z */
+void f184gi_camera_look_at(const float eye[3], const float target[3], float out[16]);
+/* general 4x4 inverse (FP64 internally); returns 0, or F184GI_ERR_INVALID when singular */
+int f184gi_mat4_inverse(const float m[16], float out[16]);
+
+/* ---- seeded synthetic scenes (host memory owned by the library) ---- */
+typedef struct f184gi_scene {
+    uint64_t ntris;
+    uint32_t nobjects;
+    uint32_t pad;
+    float* tri_xyz;           /* 9 floats per triangle */
+    uint32_t* albedo;         /* RGBA8 per triangle */
+    float* roughness;         /* per triangle, uniform [0.1, 0.9] */
+    uint32_t* object_first;   /* first triangle of each object (room = object 0) */
+    uint32_t* object_count;   /* triangles per object */
+    f184gi_bounds bounds;
+    f184gi_light light;
+    float eye[3], target[3];  /* seeded camera inside the room */
+} f184gi_scene;
+
+/* Room (6 quads bounding [-10,10]^3) + nobjects boxes/UV-spheres (half each) with ~target_tris triangles
+ * in total, seeded by `seed` (splitmix64 -> xoshiro256**). */
+int f184gi_scene_generate(uint64_t seed, uint64_t target_tris, uint32_t nobjects, f184gi_scene** out);
+void f184gi_scene_free(f184gi_scene* scene);
+/* Rigidly move `fraction` of the objects (seeded) by up to `max_offset` world units; the moved objects'
+ * indices go to moved_out (capacity nobjects), their count to nmoved. */
+int f184gi_scene_move_objects(f184gi_scene* scene, uint64_t seed, float fraction, float max_offset,
+                              uint32_t* moved_out, uint32_t* nmoved);
+/* view i of a seeded camera path inside the room */
+int f184gi_scene_camera(const f184gi_scene* scene, uint64_t seed, uint32_t i, float eye[3], float target[3]);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* F184GI_H */

@@ -1,0 +1,156 @@
+"""CUDA path vs the CPU oracle on seeded scenes (run on a GPU).
+
+Bit-exact: grid frame, shadow map, voxel occupancy and contribution counts, G-buffer depth and triangle ids,
+grid bytes under a shuffled triangle order, dirty-brick re-voxelization vs full voxelization.
+Within REL_TOL (1e-3, relative with an absolute floor of 1e-2, see gi_case.py): injected radiance, mip levels,
+cone-traced pixels.
+"""
+import numpy as np
+import pytest
+
+from gi_case import REL_TOL, Case, rel_err
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def case(lib):
+    c = Case()
+    c.voxelize()
+    c.mip()
+    c.gbuffer()
+    return c
+
+
+@pytest.fixture(scope="module")
+def oracle_l0(case, orc):
+    fo = case.oracle_frame()
+    sd = orc.shadow_depth(orc.raster(orc.frame_matrix(fo), case.res, case.res, case.sc.tri_xyz))
+    l0, cnt = orc.voxelize(fo, case.dim, case.res, case.sc.tri_xyz, case.sc.albedo, case.oracle_light(), sd)
+    return fo, sd, l0, cnt
+
+
+def test_frame_host_device_oracle_identical(case, oracle_l0):
+    fo = oracle_l0[0]
+    fd = case.gi.frame(case.grid)
+    fh = case.g.frame_from_bounds(case.sc.bounds, case.dim, np.array(case.sc.light.direction, np.float32))
+    assert bytes(fd) == bytes(fo)
+    assert bytes(fh) == bytes(fo)
+
+
+def test_frame_from_device_bounds(lib):
+    """bounds=None: the AABB is reduced on the device; the scene AABB is the room, so the frame is the same."""
+    c = Case(ntris=5000, nobj=40, dim=32, levels=5, res=256, width=64, height=32)
+    c.voxelize(bounds=False)
+    fo = c.oracle_frame()
+    assert bytes(c.gi.frame(c.grid)) == bytes(fo)
+
+
+def test_shadow_map_bit_exact(case, oracle_l0):
+    sd = oracle_l0[1]
+    got = case.gi.read_shadow(case.grid)
+    assert got.shape == sd.shape
+    assert np.array_equal(got.view(np.uint32), sd.view(np.uint32))
+    assert (sd < 1.0).mean() > 0.3  # the map is not trivially empty
+
+
+def test_voxel_occupancy_and_counts_bit_exact(case, oracle_l0):
+    cnt = oracle_l0[3]
+    got = case.gi.read_counts(case.grid)
+    assert np.array_equal(got > 0, cnt > 0), "occupancy differs in %d voxels" % int(((got > 0) != (cnt > 0)).sum())
+    assert np.array_equal(got, cnt)
+    l0 = case.gi.read_level(case.grid, 0)
+    assert np.array_equal(l0[..., 3] > 0, cnt > 0)
+
+
+def test_injected_radiance(case, oracle_l0):
+    l0_ref = oracle_l0[2]
+    l0 = case.gi.read_level(case.grid, 0)
+    mx, rms = rel_err(l0, l0_ref)
+    print("L0 radiance rel err max %.3g rms %.3g" % (mx, rms))
+    assert mx < REL_TOL
+    lit = (l0_ref[..., 0] > 0).sum()
+    assert lit > 1000
+
+
+def test_mip_chain(case, orc):
+    l0 = case.gi.read_level(case.grid, 0).astype(np.float64)
+    _, levels = orc.mip(l0, case.levels)
+    for lv in range(1, case.levels):
+        got = case.gi.read_level(case.grid, lv)
+        mx, rms = rel_err(got, levels[lv])
+        assert mx < 1e-5, "level %d max rel err %.3g" % (lv, mx)
+
+
+def test_gbuffer_bit_exact(case, orc):
+    keys = orc.raster(case.P.astype(np.float64) @ case.V.astype(np.float64), case.W, case.H, case.sc.tri_xyz)
+    dep, nrm, rgh, tid = orc.gbuffer_resolve(keys, case.sc.tri_xyz, case.sc.roughness, case.V)
+    gd, gn, gr, gt = case.gbuffer_host()
+    assert np.array_equal(gt, tid)
+    assert np.array_equal(gd.view(np.uint32), dep.view(np.uint32))
+    assert np.array_equal(gr, rgh)
+    # normals: FP32 on the device vs FP64 in the oracle, then rounded to FP16 -> at most one FP16 ulp apart
+    dx = np.abs(gn.astype(np.int64) & 0xffff - (nrm.astype(np.int64) & 0xffff))
+    assert int(np.abs((gn & 0xffff).astype(np.int64) - (nrm & 0xffff).astype(np.int64)).max()) <= 1
+    assert int(np.abs((gn >> 16).astype(np.int64) - (nrm >> 16).astype(np.int64)).max()) <= 1
+    del dx
+
+
+def test_trace_matches_oracle(case, orc, oracle_l0):
+    fo = oracle_l0[0]
+    got = case.trace()
+    dep, nrm, rgh, _ = case.gbuffer_host()
+    chain, _ = orc.mip(oracle_l0[2], case.levels)
+    ref = orc.trace(fo, case.dim, case.levels, chain, case.V, case.P, case.W, case.H, dep, nrm, rgh)
+    mx, rms = rel_err(got, ref)
+    print("trace rel err max %.3g rms %.3g" % (mx, rms))
+    assert mx < REL_TOL
+    assert ref[0, ..., :3].mean() > 0.01  # lit scene
+
+
+def test_shuffled_triangle_order_bit_identical(case):
+    rng = np.random.default_rng(7)
+    perm = rng.permutation(case.sc.ntris)
+    base = case.gi.read_level(case.grid, 0).copy()
+    c2 = Case(keep_counts=False)
+    tri = case.sc.tri_xyz.reshape(-1, 9)[perm].ravel()
+    alb = case.sc.albedo[perm]
+    c2.upload(tri, alb)
+    c2.voxelize()
+    got = c2.gi.read_level(c2.grid, 0)
+    assert np.array_equal(got.view(np.uint32), base.view(np.uint32))
+
+
+def test_dirty_brick_revoxelize_equals_full(lib):
+    c = Case(ntris=20000, nobj=200, dim=64, levels=6, res=1024, keep_counts=False)
+    c.voxelize()
+    moved = c.sc.move_objects(99, 0.05, 1.0)
+    assert len(moved) > 0
+    # dirty bricks: every brick (a superset is always correct); then a real subset
+    nb = (c.dim // 8) ** 3
+    c.upload(c.sc.tri_xyz, c.sc.albedo)
+    c.voxelize(dirty=np.arange(nb, dtype=np.uint32))
+    inc = c.gi.read_level(c.grid, 0).copy()
+    full = Case(ntris=20000, nobj=200, dim=64, levels=6, res=1024, keep_counts=False)
+    full.sc.move_objects(99, 0.05, 1.0)
+    full.upload(full.sc.tri_xyz, full.sc.albedo)
+    full.voxelize()
+    ref = full.gi.read_level(full.grid, 0)
+    assert np.array_equal(inc.view(np.uint32), ref.view(np.uint32))
+
+
+def test_fp16_storage_trace_error(lib, orc):
+    c = Case(fmt=1)
+    c.voxelize()
+    c.mip()
+    c.gbuffer()
+    got = c.trace()
+    fo = c.oracle_frame()
+    sd = orc.shadow_depth(orc.raster(orc.frame_matrix(fo), c.res, c.res, c.sc.tri_xyz))
+    l0, _ = orc.voxelize(fo, c.dim, c.res, c.sc.tri_xyz, c.sc.albedo, c.oracle_light(), sd)
+    chain, _ = orc.mip(l0, c.levels)
+    dep, nrm, rgh, _ = c.gbuffer_host()
+    ref = orc.trace(fo, c.dim, c.levels, chain, c.V, c.P, c.W, c.H, dep, nrm, rgh)
+    mx, rms = rel_err(got, ref)
+    print("fp16 storage trace rel err max %.3g rms %.3g" % (mx, rms))
+    assert mx < REL_TOL
