@@ -1,0 +1,392 @@
+"""Benchmark of the voxel cone-tracing GI path on GB300.
+
+One step = one request of the plain per-request path on the large synthetic scene: shadow-map raster +
+conservative voxelization with light injection (f184gi_voxelize), the mip chain (f184gi_mip) and the cone trace of
+one 1920x1080 view (f184gi_trace).  The metric is cone-traced Mpix/s (pixels traced / time).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--small]
+
+With N > 1 (launched by torch.distributed.run) every rank runs an independent replica of the request on its own
+GPU (the path has no data exchange between requests); value = all ranks' pixels / the slowest rank's time.
+--impl reference times the CPU restatement of the path (FP32, all host threads) on a bounded sample of the same
+workload.  Prints one JSON line on rank 0.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "cone-traced Mpix/s, p50/p99 latency @<=1e-3 rel err, served vs plain, 1 GB300"
+PLAIN_LARGE = dict(name="plain-large", seed=1184, ntris=500000, nobjects=2000, dim=256, levels=8, shadow_res=2048,
+                   width=1920, height=1080)
+SMALL = dict(name="plain-small-gpu", seed=184, ntris=20000, nobjects=200, dim=64, levels=6, shadow_res=1024,
+             width=640, height=360)
+
+
+def workload_desc(cfg):
+    return ("%s: %dk-triangle seeded scene (%d objects), %d^3 FP32 RGBA radiance/opacity grid in 8^3 bricks, "
+            "%d-level mip chain, %d^2 shadow map, %dx%d G-buffer, 5 diffuse (60 deg) + 1 specular cone, "
+            "max distance = grid diagonal, step = 0.5 x diameter"
+            % (cfg["name"], cfg["ntris"] // 1000, cfg["nobjects"], cfg["dim"], cfg["levels"], cfg["shadow_res"],
+               cfg["width"], cfg["height"]))
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def traffic_record(kernel):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary (None when absent)."""
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        t = json.load(f)
+    return t.get(kernel)
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.QUERY,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    sm.append(float(parts[1]))
+                    mx = max(mx, float(parts[2]))
+                except ValueError:
+                    continue
+                for n, v in zip(names, parts[5:9]):
+                    if v.lower().startswith("active"):
+                        reasons.add(n)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+# ---------------------------------------------------------------- CPU restatement (baseline / reference arm)
+
+def cpu_request(cfg, row_stride, scene=None, f64_check=None):
+    """Time the FP32 CPU restatement of one request on a row sample; returns (seconds per full request, info)."""
+    import numpy as np
+
+    import final184_gb300 as g
+    import oracle as o
+
+    sc = scene or g.SyntheticScene(cfg["seed"], cfg["ntris"], cfg["nobjects"])
+    dim, levels, res, W, H = cfg["dim"], cfg["levels"], cfg["shadow_res"], cfg["width"], cfg["height"]
+    ld = np.array(sc.light.direction, np.float32)
+    b = sc.bounds
+    light = o.make_light(list(sc.light.luminance), list(sc.light.direction))
+    t0 = time.perf_counter()
+    fo = o.grid_frame(o.make_bounds((b.min.x, b.min.y, b.min.z), (b.max.x, b.max.y, b.max.z)), dim, ld)
+    sd = o.shadow_depth(o.raster(o.frame_matrix(fo), res, res, sc.tri_xyz))
+    l0, _ = o.voxelize(fo, dim, res, sc.tri_xyz, sc.albedo, light, sd, f64=False)
+    chain, _ = o.mip(l0, levels, f64=False)
+    t1 = time.perf_counter()
+    gb = cpu_gbuffer(sc, cfg)
+    V, P, dep, nrm, rgh = gb
+    rows = list(range(0, H, row_stride))
+    t2 = time.perf_counter()
+    outs = {}
+    for r in rows:
+        outs[r] = o.trace(fo, dim, levels, chain, V, P, W, H, dep, nrm, rgh, rows=(r, r + 1), f64=False)[:, r]
+    t3 = time.perf_counter()
+    per_request = (t1 - t0) + (t3 - t2) * H / len(rows)
+    info = {"voxelize_mip_s": t1 - t0, "trace_rows": len(rows), "trace_s": t3 - t2}
+    return per_request, info, (sc, fo, chain, gb, outs)
+
+
+def cpu_gbuffer(sc, cfg):
+    import numpy as np
+
+    import final184_gb300 as g
+    import oracle as o
+
+    W, H = cfg["width"], cfg["height"]
+    V = g.look_at(sc.eye, sc.target)
+    P = g.perspective(59.0, W / H, 0.1, 100.0)
+    keys = o.raster(P.astype(np.float64) @ V.astype(np.float64), W, H, sc.tri_xyz)
+    dep, nrm, rgh, _ = o.gbuffer_resolve(keys, sc.tri_xyz, sc.roughness, V)
+    return V, P, dep, nrm, rgh
+
+
+def run_reference(args, cfg):
+    """--impl reference: the CPU restatement, all host threads, each step a bounded row sample."""
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return None
+    import final184_gb300 as g
+
+    sc = g.SyntheticScene(cfg["seed"], cfg["ntris"], cfg["nobjects"])
+    stride = 64 if cfg is PLAIN_LARGE else 16
+    for _ in range(min(args.warmup, 1)):
+        cpu_request(cfg, stride * 4, scene=sc)
+    times = []
+    for _ in range(args.steps):
+        t, info, _ = cpu_request(cfg, stride, scene=sc)
+        times.append(t)
+    t = statistics.mean(times)
+    mpix = cfg["width"] * cfg["height"] / t / 1e6
+    cores = os.cpu_count() or 1
+    sample = ("per step: full shadow raster + voxelization + mip chain of the scene, cone trace of every %d-th of "
+              "the %d rows (%d rows), trace time scaled to the full image" % (stride, cfg["height"], info["trace_rows"]))
+    line = {"metric": METRIC, "impl": "reference", "value": round(mpix, 4), "unit": "Mpix/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(t * 1e3, 2), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": workload_desc(cfg), "implementation": "CPU restatement of the path (oracle.cpp) "
+                                                                        "in FP32, std::thread over all host cores"},
+            "cpu_baseline": {"value": round(mpix, 4), "unit": "Mpix/s", "cores": cores, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": round(mpix, 4), "unit": "Mpix/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    return line
+
+
+# ---------------------------------------------------------------- GPU arm
+
+def run_gpu(args, cfg):
+    import numpy as np
+    import torch
+
+    import final184_gb300 as g
+
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.current_stream(dev)
+    sc = g.SyntheticScene(cfg["seed"], cfg["ntris"], cfg["nobjects"])
+    gi = g.VoxelGI(local)
+    dim, levels, res, W, H = cfg["dim"], cfg["levels"], cfg["shadow_res"], cfg["width"], cfg["height"]
+    grid = gi.create_grid(dim, levels, g.FMT_F32, 0, res)
+    npix = W * H
+    # host inputs (pinned) and device copies
+    tri_h = torch.from_numpy(sc.tri_xyz).pin_memory()
+    alb_h = torch.from_numpy(sc.albedo.view(np.int32)).pin_memory()
+    tri = tri_h.to(dev)
+    alb = alb_h.to(dev)
+    rough = torch.from_numpy(sc.roughness).to(dev)
+    V = g.look_at(sc.eye, sc.target)
+    P = g.perspective(59.0, W / H, 0.1, 100.0)
+    depth = torch.empty(npix, dtype=torch.float32, device=dev)
+    normal = torch.empty(npix, dtype=torch.int32, device=dev)
+    rgh = torch.empty(npix, dtype=torch.int16, device=dev)
+    out = torch.empty(2 * npix * 4, dtype=torch.float32, device=dev)
+    view = g.make_view(V, P, W, H, depth.data_ptr(), normal.data_ptr(), rgh.data_ptr(), out.data_ptr())
+    # the G-buffer is the trace's input (the reference's G-buffer pass); rasterized once, outside the timing
+    gi.gbuffer(tri.data_ptr(), rough.data_ptr(), sc.ntris, view, stream=stream)
+    gi.sync(stream)
+    gbuf_h = [depth.cpu().pin_memory(), normal.cpu().pin_memory(), rgh.cpu().pin_memory()]
+    out_h = torch.empty(out.numel(), dtype=torch.float32).pin_memory()
+    light = sc.light
+
+    def step(ev=None):
+        if ev is not None:
+            ev[0].record(stream)
+        gi.voxelize(grid, tri.data_ptr(), alb.data_ptr(), sc.ntris, light, bounds=sc.bounds, stream=stream)
+        if ev is not None:
+            ev[1].record(stream)
+        gi.mip(grid, stream=stream)
+        if ev is not None:
+            ev[2].record(stream)
+        gi.trace(grid, [view], stream=stream)
+        if ev is not None:
+            ev[3].record(stream)
+
+    for _ in range(args.warmup):
+        step()
+    gi.sync(stream)
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize(dev)
+
+    # ---- device-resident timing ----
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(args.steps)]
+    clocks = ClockSampler(local)
+    clocks.start()
+    launches0 = g.load().f184gi_kernel_launches()
+    barrier()
+    t_start = torch.cuda.Event(enable_timing=True)
+    t_end = torch.cuda.Event(enable_timing=True)
+    t_start.record(stream)
+    for k in range(args.steps):
+        step(evs[k])
+    t_end.record(stream)
+    barrier()
+    launches = g.load().f184gi_kernel_launches() - launches0
+    clk = clocks.stop()
+    gi.sync(stream)
+    total_ms = t_start.elapsed_time(t_end)
+    if world > 1:
+        t = torch.tensor([total_ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    ms_per_step = total_ms / args.steps
+    step_ms = [evs[k][0].elapsed_time(evs[k][3]) for k in range(args.steps)]
+    stage = {"voxelize": [e[0].elapsed_time(e[1]) for e in evs], "mip": [e[1].elapsed_time(e[2]) for e in evs],
+             "trace": [e[2].elapsed_time(e[3]) for e in evs]}
+    value = world * npix / (ms_per_step * 1e-3) / 1e6
+
+    # ---- end to end through the API with host buffers ----
+    gbuf_d = [depth, normal, rgh]
+    h2d = tri_h.numel() * 4 + alb_h.numel() * 4 + sum(x.numel() * x.element_size() for x in gbuf_h)
+    d2h = out.numel() * 4
+    barrier()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        tri.copy_(tri_h, non_blocking=True)
+        alb.copy_(alb_h, non_blocking=True)
+        for d_, h_ in zip(gbuf_d, gbuf_h):
+            d_.copy_(h_, non_blocking=True)
+        step()
+        out_h.copy_(out, non_blocking=True)
+    e1.record(stream)
+    barrier()
+    e2e_ms = e0.elapsed_time(e1) / args.steps
+    if world > 1:
+        t = torch.tensor([e2e_ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+    e2e_value = world * npix / (e2e_ms * 1e-3) / 1e6
+
+    # ---- roofline of the dominant kernel (HBM: nothing here is a dense contraction) ----
+    means = {k: statistics.mean(v) for k, v in stage.items()}
+    top = max(means, key=means.get)
+    esz = 16
+    chain_bytes = sum((dim >> l) ** 3 for l in range(levels)) * esz
+    l0_bytes = dim ** 3 * esz
+    alg = {
+        # triangles + albedo read, L0 written once, shadow map written and read once (4 B/texel)
+        "voxelize": sc.ntris * 40 + l0_bytes + 2 * 4 * res * res,
+        # L0 read once, levels 1.. written once
+        "mip": chain_bytes,
+        # G-buffer 10 B + 2 x RGBA FP32 out per pixel; the chain counted once per launch (upper bound of touched)
+        "trace": npix * (10 + 32) + chain_bytes,
+    }
+    peak, peak_kind = peaks()
+    achieved = alg[top] / (means[top] * 1e-3) / 1e9
+    kernel_names = {"voxelize": "vox_bricks", "mip": "mip_pass", "trace": "trace_kernel"}
+    tr = traffic_record(kernel_names[top])
+    line = {
+        "metric": METRIC, "value": round(value, 4), "unit": "Mpix/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms_per_step, 4), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": workload_desc(cfg), "form": "plain per-request FP32 GPU path",
+                   "parallelism": "replicas" if world > 1 else "single GPU",
+                   "l2": "per-step working set > 129 MB L2 (the %d MB grid chain is rewritten and re-read every step)"
+                         % (chain_bytes // 2 ** 20)},
+        "latency_ms": {"p50": round(statistics.median(step_ms), 4),
+                       "p99": round(sorted(step_ms)[min(len(step_ms) - 1, int(0.99 * len(step_ms)))], 4)},
+        "stages_ms": {k: round(v, 4) for k, v in means.items()},
+        "roofline": {"bound": "hbm", "kernel": top, "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4), "peak_source": peak_kind,
+                     "algorithmic_bytes": alg[top],
+                     "traffic": (tr * 1.0 if isinstance(tr, (int, float)) else None)},
+        "e2e": {"value": round(e2e_value, 4), "unit": "Mpix/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h), "ms_per_step": round(e2e_ms, 4)},
+        "gpu_launches": int(launches),
+        "clocks": clk,
+    }
+    if world > 1:
+        torch.distributed.barrier()
+    gi.close()
+    return line, sc
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--small", action="store_true", help="the 20k-triangle 64^3 640x360 case (profiling)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    cfg = SMALL if args.small else PLAIN_LARGE
+    from final184_gb300 import build as b
+
+    b.build()
+    if args.impl == "reference":
+        line = run_reference(args, cfg)
+        if line is not None:
+            print(json.dumps(line), flush=True)
+        return
+    rank, world, _ = dist_env()
+    line, sc = run_gpu(args, cfg)
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        from oracle import build as ob
+
+        ob.build_oracle()
+        stride = 64 if cfg is PLAIN_LARGE else 16
+        t, info, _ = cpu_request(cfg, stride, scene=sc)
+        line["cpu_baseline"] = {
+            "value": round(cfg["width"] * cfg["height"] / t / 1e6, 4), "unit": "Mpix/s", "cores": os.cpu_count(),
+            "kind": "port",
+            "sample": "full shadow raster + voxelization + mip chain on the CPU (%.1f s), cone trace of %d of %d rows "
+                      "(%.1f s) scaled to the full image; FP32 restatement, std::thread over all cores"
+                      % (info["voxelize_mip_s"], info["trace_rows"], cfg["height"], info["trace_s"])}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

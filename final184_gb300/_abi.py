@@ -80,6 +80,7 @@ PF = C.POINTER(C.c_float)
 PROTOTYPES = {
     "f184gi_last_error": (C.c_char_p, []),
     "f184gi_abi_version": (C.c_int, []),
+    "f184gi_kernel_launches": (C.c_uint64, []),
     "f184gi_create": (C.c_int, [C.POINTER(Config), C.POINTER(P)]),
     "f184gi_destroy": (C.c_int, [P]),
     "f184gi_memory_used": (C.c_int, [P, C.POINTER(U64)]),

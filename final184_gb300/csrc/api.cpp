@@ -3,6 +3,7 @@
 // A context owns device memory under an optional HBM budget: resident grids (mip chain + shadow map + frame)
 // and per-pass scratch that grows on demand and is reused.  Calls are stream-ordered on the caller's stream;
 // kernels report overflow/timeout through a device status word that f184gi_sync and the inspection calls read.
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <map>
@@ -18,7 +19,10 @@ namespace f184 {
 
 namespace {
 thread_local std::string g_last_error;
-}
+std::atomic<uint64_t> g_launches{0};
+}  // namespace
+
+void note_launches(uint32_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 
 int fail(int code, const std::string& msg) {
     g_last_error = msg;
@@ -188,6 +192,7 @@ int read_status(f184gi_ctx* c) {
 extern "C" {
 
 const char* f184gi_last_error(void) { return g_last_error.c_str(); }
+uint64_t f184gi_kernel_launches(void) { return g_launches.load(std::memory_order_relaxed); }
 int f184gi_abi_version(void) { return F184GI_ABI_VERSION; }
 
 int f184gi_create(const f184gi_config* cfg, f184gi_ctx** out) {

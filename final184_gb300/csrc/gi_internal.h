@@ -13,12 +13,15 @@ namespace f184 {
 constexpr int kMaxLevels = 11;
 constexpr int kBrickEdge = 8;
 constexpr int kBrickVox = 512;
-constexpr uint32_t kFixedFrac = 16;  // per-contribution injection weights are 16.16 fixed point
+constexpr uint32_t kFixedFrac = 31;  // per-contribution injection weights are 1.31 fixed point (64-bit sums)
 
 // device status bits (set by kernels, read by f184gi_sync / inspection calls)
 constexpr uint32_t kStatusOverflow = 1u;
 constexpr uint32_t kStatusTimeout = 2u;
 constexpr uint32_t kStatusRange = 4u;  // geometry outside the fixed-point range was skipped
+
+// process-wide count of kernels this library has launched (f184gi_kernel_launches)
+void note_launches(uint32_t n);
 
 int fail(int code, const std::string& msg);
 int cuda_fail(cudaError_t e, const char* what);

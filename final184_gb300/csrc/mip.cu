@@ -119,6 +119,7 @@ int mip_launch(const ChainLayout& c, uint32_t levels, uint32_t* d_status, cudaSt
         uint32_t blocks = ds >= 16 ? (ds / 16) * (ds / 16) * (ds / 16) : 1u;
         size_t smem = size_t(S) * S * S * c.esz;
         mip_pass<<<blocks, 512, smem, s>>>(c, l, nout, d_status);
+        note_launches(1);
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return cuda_fail(e, "mip");
         l += nout;

@@ -295,14 +295,17 @@ int raster_launch(const RasterJob& job, void* scratch, size_t scratch_bytes, uin
     if (job.ntris) {
         uint32_t blocks = uint32_t((job.ntris + 127) / 128);
         raster_setup<<<blocks, 128, 0, s>>>(job.tri, job.ntris, job, sc, tiles_x, d_status);
+        note_launches(1);
     }
     int rc = exclusive_scan(sc.tile_count, ntiles, sc.tile_start, sc.total, sc.scan_tmp, s);
     if (rc) return rc;
     if (job.ntris) {
         uint64_t nrec = job.ntris + sc.ovf_cap;
         raster_emit<<<uint32_t((nrec + 127) / 128), 128, 0, s>>>(job.ntris, sc, tiles_x, d_status);
+        note_launches(1);
     }
     raster_tiles<<<ntiles, 256, 0, s>>>(sc, tiles_x, job.width, job.height, job.keys);
+    note_launches(1);
     return cuda_fail(cudaGetLastError(), "raster");
 }
 
@@ -366,6 +369,7 @@ int gbuffer_resolve_launch(const unsigned long long* keys, uint32_t W, uint32_t 
     gbuffer_resolve<<<uint32_t((n + 255) / 256), 256, 0, s>>>(keys, W, H, tri, rough, V,
                                                               make_float3(eye[0], eye[1], eye[2]), depth, normal,
                                                               rough_out, tri_out);
+    note_launches(1);
     return cuda_fail(cudaGetLastError(), "gbuffer_resolve");
 }
 

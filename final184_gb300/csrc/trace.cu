@@ -259,6 +259,7 @@ int trace_launch(const ChainLayout& c, const TraceConsts& tc, const f184gi_grid_
     const TraceView* dv = static_cast<const TraceView*>(scratch);
     const uint32_t* db = reinterpret_cast<const uint32_t*>(static_cast<const unsigned char*>(scratch) + size_t(nviews) * sizeof(TraceView));
     trace_kernel<<<tiles, 128, 0, s>>>(c, tc, d_frame, dv, db, nviews);
+    note_launches(1);
     return cuda_fail(cudaGetLastError(), "trace");
 }
 

@@ -94,6 +94,7 @@ int exclusive_scan(const uint32_t* in, uint32_t n, uint32_t* out, uint32_t* tota
     scan_block_sums<<<nblocks, kScanThreads, 0, s>>>(in, n, bs);
     scan_top<<<1, kScanThreads, 0, s>>>(bs, nblocks, total);
     scan_apply<<<nblocks, kScanThreads, 0, s>>>(in, n, bs, out);
+    note_launches(3);
     return cuda_fail(cudaGetLastError(), "scan");
 }
 
@@ -159,10 +160,12 @@ int frame_launch(const float* tri, uint64_t ntris, const f184gi_bounds* bounds, 
         uint32_t blocks = uint32_t(std::min<uint64_t>((nthreads + 255) / 256, 152 * 8));
         if (blocks == 0) blocks = 1;
         bounds_reduce<<<blocks, 256, 0, s>>>(tri, ntris * 9, mm);
+        note_launches(2);
     } else {
         b = *bounds;
     }
     frame_kernel<<<1, 32, 0, s>>>(mm, b, bounds ? 0 : 1, dim, light_dir[0], light_dir[1], light_dir[2], d_frame);
+    note_launches(1);
     return cuda_fail(cudaGetLastError(), "frame");
 }
 
@@ -183,6 +186,7 @@ int read_level_launch(const ChainLayout& c, uint32_t level, uint32_t dir, float*
     uint64_t d = c.ldim[level];
     uint64_t n = d * d * d;
     read_level_kernel<<<uint32_t((n + 255) / 256), 256, 0, s>>>(c, level, dir, reinterpret_cast<float4*>(d_out));
+    note_launches(1);
     return cuda_fail(cudaGetLastError(), "read_level");
 }
 

@@ -5,7 +5,7 @@
 // last-writer-wins imageStore.  Here a voxel is covered when the triangle and the closed voxel box overlap
 // (separating-axis test), decided exactly in integers on vertices snapped to 1/256 voxel (FP64 snap).  Each
 // covering triangle adds its Lambert weight |dot(-L, n)| * albedo (the term of Shader/Lighting/indirect.frag:60-62,
-// 167) as 16.16 fixed point with integer atomics, so sums and counts are independent of triangle order.  The
+// 167) as 1.31 fixed point with 64-bit integer atomics, so sums and counts are independent of triangle order.  The
 // voxel's radiance is luminance * shadow(voxel centre) * mean weight, the shadow test being indirect.frag:160-165's
 // compare with a two-voxel bias, evaluated in FP64 against the shadow map rasterized by raster.cu.
 //
@@ -27,7 +27,7 @@ __constant__ float c_albedo_lut[256];  // (i / 255)^2.2
 
 struct TriRec {
     int32_t q[9];    // snapped vertices (x0 y0 z0 x1 ...), 24.8 voxel fixed point
-    uint32_t wq[3];  // injection weight per channel, 16.16 fixed point; wq[0] = kInvalid marks skipped
+    uint32_t wq[3];  // injection weight per channel, 1.31 fixed point (<= 2^31); wq[0] = kInvalid marks skipped
 };
 
 struct VoxScratch {
@@ -170,7 +170,7 @@ __global__ void vox_setup(const float* __restrict__ tri, const uint32_t* __restr
     uint32_t al = albedo[t];
     for (int c = 0; c < 3; ++c) {
         float w = cosv * c_albedo_lut[(al >> (8 * c)) & 255u];
-        r.wq[c] = min(__float2uint_rn(w * 65536.0f), 65536u);
+        r.wq[c] = min(__float2uint_rn(w * 2147483648.0f), 0x80000000u);
     }
     sc.recs[t] = r;
     visit_bricks<false>(r, uint32_t(t), dim, sc, status);
@@ -200,7 +200,7 @@ __global__ void __launch_bounds__(256) vox_bricks(VoxScratch sc, const f184gi_gr
                                                   const unsigned long long* __restrict__ shadow, uint32_t res,
                                                   uint32_t* counts, const uint32_t* __restrict__ dirty,
                                                   uint32_t* status) {
-    __shared__ uint32_t s_sum[3][512];
+    __shared__ unsigned long long s_sum[3][512];  // 33.31 fixed point: exact, order-independent sums
     __shared__ uint32_t s_cnt[512];
     const uint32_t m = dirty ? dirty[blockIdx.x] : blockIdx.x;
     const uint32_t nb = dim >> 3;
@@ -290,9 +290,9 @@ __global__ void __launch_bounds__(256) vox_bricks(VoxScratch sc, const f184gi_gr
             }
             if (hit) {
                 int li = lz * 64 + ly * 8 + lx;
-                atomicAdd(&s_sum[0][li], r.wq[0]);
-                atomicAdd(&s_sum[1][li], r.wq[1]);
-                atomicAdd(&s_sum[2][li], r.wq[2]);
+                atomicAdd(&s_sum[0][li], (unsigned long long)r.wq[0]);
+                atomicAdd(&s_sum[1][li], (unsigned long long)r.wq[1]);
+                atomicAdd(&s_sum[2][li], (unsigned long long)r.wq[2]);
                 atomicAdd(&s_cnt[li], 1u);
             }
         }
@@ -306,7 +306,6 @@ __global__ void __launch_bounds__(256) vox_bricks(VoxScratch sc, const f184gi_gr
         uint32_t cnt = s_cnt[li];
         float4 out = make_float4(0.f, 0.f, 0.f, 0.f);
         if (cnt) {
-            if (cnt >= 65536u) set_status(status, kStatusOverflow);
             int64_t ijk[3] = {bx * 8 + lx, by * 8 + ly, bz * 8 + lz};
             double cw[3];
             for (int a = 0; a < 3; ++a) cw[a] = dadd(fr->origin[a], dmul(dadd(double(ijk[a]), 0.5), fr->voxel_size));
@@ -320,7 +319,7 @@ __global__ void __launch_bounds__(256) vox_bricks(VoxScratch sc, const f184gi_gr
                 double sd = k == ~0ull ? 1.0 : double(__uint_as_float(uint32_t(k >> 32)));
                 lit = dsub(z, fr->shadow_bias) <= sd;
             }
-            float scale = lit ? (1.0f / 65536.0f) / float(cnt) : 0.0f;
+            float scale = lit ? (1.0f / 2147483648.0f) / float(cnt) : 0.0f;
             out.x = light.luminance[0] * (float(s_sum[0][li]) * scale);
             out.y = light.luminance[1] * (float(s_sum[1][li]) * scale);
             out.z = light.luminance[2] * (float(s_sum[2][li]) * scale);
@@ -385,14 +384,23 @@ int voxelize_launch(const VoxelizeJob& job, void* scratch, size_t scratch_bytes,
         sc.dirty_mask = mask;
         cudaMemsetAsync(mask, 0, size_t(nbricks / 32 + 1) * 4, s);
         vox_dirty_mask<<<(job.ndirty + 255) / 256, 256, 0, s>>>(job.dirty_bricks, job.ndirty, nbricks, mask);
+        note_launches(1);
     }
-    if (job.ntris) vox_setup<<<uint32_t((job.ntris + 127) / 128), 128, 0, s>>>(job.tri, job.albedo, job.ntris, job.d_frame, dim, sc, d_status);
+    if (job.ntris) {
+        vox_setup<<<uint32_t((job.ntris + 127) / 128), 128, 0, s>>>(job.tri, job.albedo, job.ntris, job.d_frame, dim,
+                                                                     sc, d_status);
+        note_launches(1);
+    }
     int rc = exclusive_scan(sc.brick_count, nbricks, sc.brick_start, sc.total, sc.scan_tmp, s);
     if (rc) return rc;
-    if (job.ntris) vox_emit<<<uint32_t((job.ntris + 127) / 128), 128, 0, s>>>(job.ntris, dim, sc, d_status);
+    if (job.ntris) {
+        vox_emit<<<uint32_t((job.ntris + 127) / 128), 128, 0, s>>>(job.ntris, dim, sc, d_status);
+        note_launches(1);
+    }
     uint32_t nblocks = job.ndirty ? job.ndirty : nbricks;
     vox_bricks<<<nblocks, 256, 0, s>>>(sc, job.d_frame, dim, job.chain, job.light, job.shadow_keys, job.shadow_res,
                                        job.counts, job.ndirty ? job.dirty_bricks : nullptr, d_status);
+    note_launches(1);
     return cuda_fail(cudaGetLastError(), "voxelize");
 }
 

@@ -141,6 +141,8 @@ typedef struct f184gi_ctx f184gi_ctx;
 /* ---- context and grids ---- */
 const char* f184gi_last_error(void);
 int f184gi_abi_version(void);
+/* number of kernels this library has launched in this process (diagnostics) */
+uint64_t f184gi_kernel_launches(void);
 int f184gi_create(const f184gi_config* cfg, f184gi_ctx** out);
 int f184gi_destroy(f184gi_ctx* ctx);
 /* bytes currently held on the device by the context */

@@ -713,10 +713,14 @@ int trace_impl(const f184gi_grid_frame* frame, uint32_t dim, uint32_t levels, ui
     const uint64_t npix = uint64_t(W) * H;
     (void)vs;
     Vec3<T> eye{iv[3], iv[7], iv[11]};
-    parallel_for(int64_t(row_begin), int64_t(std::min(row_end, H)), nthreads, [&](int64_t rb, int64_t re) {
-        for (int64_t py = rb; py < re; ++py)
-            for (uint32_t px = 0; px < W; ++px) {
-                uint64_t pi = uint64_t(py) * W + px;
+    // pixels of rows [row_begin, row_end), split evenly over the threads
+    const int64_t p_begin = int64_t(row_begin) * W, p_end = int64_t(std::min(row_end, H)) * W;
+    parallel_for(p_begin, p_end, nthreads, [&](int64_t pb, int64_t pe) {
+        for (int64_t pix = pb; pix < pe; ++pix) {
+            {
+                const int64_t py = pix / W;
+                const uint32_t px = uint32_t(pix % W);
+                uint64_t pi = uint64_t(pix);
                 T* od = out + pi * 4;
                 T* os = out + (npix + pi) * 4;
                 for (int k = 0; k < 4; ++k) od[k] = os[k] = T(0);
@@ -767,6 +771,7 @@ int trace_impl(const f184gi_grid_frame* frame, uint32_t dim, uint32_t levels, ui
                     for (int k = 0; k < 4; ++k) os[k] = sc[k];
                 }
             }
+        }
     });
     return 0;
 }

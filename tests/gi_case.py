@@ -9,6 +9,20 @@ REL_FLOOR = 1e-2
 REL_TOL = 1e-3
 
 
+def clip_matrix(proj, view):
+    """proj * view in FP64 in the operation order f184gi_gbuffer uses (products rounded, summed j = 0..3)."""
+    P = np.asarray(proj, dtype=np.float32).reshape(4, 4)
+    V = np.asarray(view, dtype=np.float32).reshape(4, 4)
+    M = np.zeros((4, 4), dtype=np.float64)
+    for r in range(4):
+        for k in range(4):
+            acc = 0.0
+            for j in range(4):
+                acc += float(P[r, j]) * float(V[j, k])
+            M[r, k] = acc
+    return M
+
+
 def rel_err(got, ref, floor=REL_FLOOR):
     got = np.asarray(got, dtype=np.float64)
     ref = np.asarray(ref, dtype=np.float64)

@@ -8,7 +8,7 @@ cone-traced pixels.
 import numpy as np
 import pytest
 
-from gi_case import REL_TOL, Case, rel_err
+from gi_case import REL_TOL, Case, clip_matrix, rel_err
 
 pytestmark = pytest.mark.gpu
 
@@ -83,7 +83,7 @@ def test_mip_chain(case, orc):
 
 
 def test_gbuffer_bit_exact(case, orc):
-    keys = orc.raster(case.P.astype(np.float64) @ case.V.astype(np.float64), case.W, case.H, case.sc.tri_xyz)
+    keys = orc.raster(clip_matrix(case.P, case.V), case.W, case.H, case.sc.tri_xyz)
     dep, nrm, rgh, tid = orc.gbuffer_resolve(keys, case.sc.tri_xyz, case.sc.roughness, case.V)
     gd, gn, gr, gt = case.gbuffer_host()
     assert np.array_equal(gt, tid)
