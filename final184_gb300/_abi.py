@@ -42,7 +42,8 @@ class GridDesc(C.Structure):
 
 class GridFrame(C.Structure):
     _fields_ = [("origin", C.c_double * 3), ("voxel_size", C.c_double), ("inv_voxel_fixed", C.c_double),
-                ("light_clip", C.c_double * 16), ("shadow_bias", C.c_double), ("light_dir", C.c_double * 3)]
+                ("light_clip", C.c_double * 16), ("shadow_bias", C.c_double), ("light_dir", C.c_double * 3),
+                ("light_vox", C.c_float * 12), ("shadow_bias_f", C.c_float), ("pad_f", C.c_float * 3)]
 
 
 class View(C.Structure):

@@ -114,6 +114,17 @@ F184_HD void frame_from_bounds(const float mn[3], const float mx[3], uint32_t di
     M[15] = 1.0;
     out->shadow_bias = hdiv(vs, R);
     for (int a = 0; a < 3; ++a) out->light_dir[a] = w[a];
+    // voxel centre (i, j, k) -> light clip row r = base_r + i s_r0 + j s_r1 + k s_r2 (rounded to FP32)
+    double hv = hmul(vs, 0.5);
+    double c0[3] = {hadd(out->origin[0], hv), hadd(out->origin[1], hv), hadd(out->origin[2], hv)};
+    for (int r = 0; r < 3; ++r) {
+        const double* Mr = M + 4 * r;
+        double base = hadd(hadd(hadd(hmul(Mr[0], c0[0]), hmul(Mr[1], c0[1])), hmul(Mr[2], c0[2])), Mr[3]);
+        out->light_vox[4 * r] = float(base);
+        for (int a = 0; a < 3; ++a) out->light_vox[4 * r + 1 + a] = float(hmul(Mr[a], vs));
+    }
+    out->shadow_bias_f = float(out->shadow_bias);
+    out->pad_f[0] = out->pad_f[1] = out->pad_f[2] = 0.0f;
 }
 
 }  // namespace f184

@@ -5,9 +5,11 @@
 // G-buffer pass (GBufferRenderer.cpp:79-116).  Coverage and depth are exact functions of the input:
 //   clip = M * (x, y, z, 1) in FP64, clipped to 0 <= z <= w and |x|,|y| <= 16 w (Sutherland-Hodgman, FP64),
 //   vertices snapped to 1/16 pixel, coverage by inclusive int64 edge functions at pixel centres,
-//   depth = (e0 z0 + e1 z1 + e2 z2) * (1 / area) in FP64, rounded to FP32;
-//   per pixel the minimum of key = (depth bits << 32 | triangle index) wins.
-// Work is binned into 16x16 pixel tiles; one CTA rasterizes a tile in shared memory.
+//   depth plane z0 + a (X - X0) + b (Y - Y0) solved in FP64 per triangle, rounded to FP32 and evaluated in FP32
+//   in that operation order; per pixel the minimum of key = (depth bits << 32 | triangle index) wins.
+// Per-fragment work is FP32/int only (the FP64 pipe of GB300 is narrow); FP64 is per vertex.
+// Work is binned into 16x16 pixel tiles (one CTA per tile, keys in shared memory).  Triangles spanning many
+// tiles are walked by a whole warp, so no thread serialises over a screen-sized triangle.
 #include "gi_device.cuh"
 #include "util.cuh"
 
@@ -17,11 +19,11 @@ namespace {
 constexpr int kTile = 16;
 constexpr double kGuard = 16.0;
 constexpr uint32_t kNone = 0xffffffffu;
+constexpr int kWarpCells = 8;  // triangles touching more tiles than this are binned by a whole warp
 
 struct SubTri {
     int32_t X[3], Y[3];
-    double Z[3];
-    double inv_area;
+    float z0, a, b;
     uint32_t tri;
     uint16_t x0, x1, y0, y1;
 };
@@ -68,13 +70,16 @@ __device__ int clip_polygon(V4* poly, int n) {
     return n;
 }
 
+// x / w with the division skipped when w is exactly 1 (orthographic frames): x / 1 == x in IEEE arithmetic
+__device__ __forceinline__ double persp_div(double x, double w) { return w == 1.0 ? x : __ddiv_rn(x, w); }
+
 __device__ bool snap(const V4& a, const V4& b, const V4& c, uint32_t W, uint32_t H, uint32_t tri, SubTri& s) {
     const V4* v[3] = {&a, &b, &c};
     int64_t X[3], Y[3];
     double Z[3];
     for (int i = 0; i < 3; ++i) {
         if (!(v[i]->w > 0.0)) return false;
-        double nx = __ddiv_rn(v[i]->x, v[i]->w), ny = __ddiv_rn(v[i]->y, v[i]->w), nz = __ddiv_rn(v[i]->z, v[i]->w);
+        double nx = persp_div(v[i]->x, v[i]->w), ny = persp_div(v[i]->y, v[i]->w), nz = persp_div(v[i]->z, v[i]->w);
         X[i] = __double2ll_rn(dmul(dadd(nx, 1.0), 8.0 * double(W)));
         Y[i] = __double2ll_rn(dmul(dadd(ny, 1.0), 8.0 * double(H)));
         Z[i] = nz;
@@ -96,12 +101,20 @@ __device__ bool snap(const V4& a, const V4& b, const V4& c, uint32_t W, uint32_t
     int64_t y0 = max(int64_t(0), -floor_div64(-(mny - 8), 16));
     int64_t y1 = min(int64_t(H) - 1, floor_div64(mxy - 8, 16));
     if (x0 > x1 || y0 > y1) return false;
+    // depth plane through the three snapped vertices (FP64 solve, FP32 result)
+    double dx1 = double(X[1] - X[0]), dy1 = double(Y[1] - Y[0]);
+    double dx2 = double(X[2] - X[0]), dy2 = double(Y[2] - Y[0]);
+    double dz1 = dsub(Z[1], Z[0]), dz2 = dsub(Z[2], Z[0]);
+    double D = double(area2);
+    double na = dsub(dmul(dz1, dy2), dmul(dz2, dy1));
+    double nb = dsub(dmul(dz2, dx1), dmul(dz1, dx2));
+    s.z0 = __double2float_rn(Z[0]);
+    s.a = __double2float_rn(__ddiv_rn(na, D));
+    s.b = __double2float_rn(__ddiv_rn(nb, D));
     for (int i = 0; i < 3; ++i) {
         s.X[i] = int32_t(X[i]);
         s.Y[i] = int32_t(Y[i]);
-        s.Z[i] = Z[i];
     }
-    s.inv_area = __ddiv_rn(1.0, double(area2));
     s.tri = tri;
     s.x0 = uint16_t(x0), s.x1 = uint16_t(x1), s.y0 = uint16_t(y0), s.y1 = uint16_t(y1);
     return true;
@@ -140,29 +153,8 @@ struct RasterScratch {
     uint64_t ovf_cap;
 };
 
-__device__ __forceinline__ void visit_tiles(const SubTri& s, uint32_t rec, uint32_t tiles_x, uint32_t* tile_count,
-                                            const uint32_t* tile_start, uint32_t* tile_fill, uint32_t* list,
-                                            uint64_t list_cap, uint32_t* status, bool emit) {
-    int tx0 = s.x0 / kTile, tx1 = s.x1 / kTile, ty0 = s.y0 / kTile, ty1 = s.y1 / kTile;
-    bool small = (tx1 - tx0) <= 1 && (ty1 - ty0) <= 1;
-    for (int ty = ty0; ty <= ty1; ++ty)
-        for (int tx = tx0; tx <= tx1; ++tx) {
-            if (!small && !tile_may_overlap(s, tx, ty)) continue;
-            uint32_t t = uint32_t(ty) * tiles_x + uint32_t(tx);
-            if (!emit) {
-                atomicAdd(&tile_count[t], 1u);
-            } else {
-                uint64_t slot = uint64_t(tile_start[t]) + atomicAdd(&tile_fill[t], 1u);
-                if (slot < list_cap)
-                    list[slot] = rec;
-                else
-                    set_status(status, kStatusOverflow);
-            }
-        }
-}
-
 __global__ void raster_setup(const float* __restrict__ tri, uint64_t ntris, RasterJob job, RasterScratch sc,
-                             uint32_t tiles_x, uint32_t* status) {
+                             uint32_t* status) {
     uint64_t t = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (t >= ntris) return;
     const double* M = job.d_M ? job.d_M : job.M;
@@ -196,18 +188,74 @@ __global__ void raster_setup(const float* __restrict__ tri, uint64_t ntris, Rast
             rec = ntris + k;
         }
         sc.recs[rec] = s;
-        visit_tiles(s, uint32_t(rec), tiles_x, sc.tile_count, nullptr, nullptr, nullptr, 0, status, false);
     }
     if (!primary_done) sc.recs[t].tri = kNone;
 }
 
-__global__ void raster_emit(uint64_t ntris, RasterScratch sc, uint32_t tiles_x, uint32_t* status) {
-    uint64_t r = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    uint64_t nrec = ntris + min(uint64_t(*sc.ovf_count), sc.ovf_cap);
-    if (r >= nrec) return;
-    SubTri s = sc.recs[r];
-    if (s.tri == kNone) return;
-    visit_tiles(s, uint32_t(r), tiles_x, nullptr, sc.tile_start, sc.tile_fill, sc.list, sc.list_cap, status, true);
+__device__ __forceinline__ void bin_cell(const SubTri& s, uint32_t rec, int tx, int ty, bool test, uint32_t tiles_x,
+                                         const RasterScratch& sc, uint32_t* status, bool emit) {
+    if (test && !tile_may_overlap(s, tx, ty)) return;
+    uint32_t t = uint32_t(ty) * tiles_x + uint32_t(tx);
+    if (!emit) {
+        atomicAdd(&sc.tile_count[t], 1u);
+    } else {
+        uint64_t slot = uint64_t(sc.tile_start[t]) + atomicAdd(&sc.tile_fill[t], 1u);
+        if (slot < sc.list_cap)
+            sc.list[slot] = rec;
+        else
+            set_status(status, kStatusOverflow);
+    }
+}
+
+__device__ __forceinline__ SubTri shfl_subtri(const SubTri& s, int src) {
+    SubTri r;
+    for (int i = 0; i < 3; ++i) {
+        r.X[i] = __shfl_sync(0xffffffffu, s.X[i], src);
+        r.Y[i] = __shfl_sync(0xffffffffu, s.Y[i], src);
+    }
+    r.z0 = __shfl_sync(0xffffffffu, s.z0, src);
+    r.a = __shfl_sync(0xffffffffu, s.a, src);
+    r.b = __shfl_sync(0xffffffffu, s.b, src);
+    r.tri = __shfl_sync(0xffffffffu, s.tri, src);
+    uint32_t p0 = __shfl_sync(0xffffffffu, uint32_t(s.x0) | (uint32_t(s.x1) << 16), src);
+    uint32_t p1 = __shfl_sync(0xffffffffu, uint32_t(s.y0) | (uint32_t(s.y1) << 16), src);
+    r.x0 = uint16_t(p0 & 0xffff), r.x1 = uint16_t(p0 >> 16), r.y0 = uint16_t(p1 & 0xffff), r.y1 = uint16_t(p1 >> 16);
+    return r;
+}
+
+// Count (emit = false) or list (emit = true) the tiles of every record.  Blocks are whole warps; a record that
+// touches more than kWarpCells tiles is walked by all 32 lanes of its warp.
+__global__ void __launch_bounds__(128) raster_bin(uint64_t ntris, RasterScratch sc, uint32_t tiles_x, uint32_t* status,
+                                                  int emit) {
+    const uint64_t r = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    const uint64_t nrec = ntris + min(uint64_t(*sc.ovf_count), sc.ovf_cap);
+    const uint32_t lane = threadIdx.x & 31;
+    SubTri s;
+    bool valid = r < nrec;
+    if (valid) {
+        s = sc.recs[r];
+        valid = s.tri != kNone;
+    }
+    int tx0 = 0, ty0 = 0, ntx = 0, nty = 0;
+    if (valid) {
+        tx0 = s.x0 / kTile, ty0 = s.y0 / kTile;
+        ntx = s.x1 / kTile - tx0 + 1, nty = s.y1 / kTile - ty0 + 1;
+    }
+    const int ncell = ntx * nty;
+    const bool big = valid && ncell > kWarpCells;
+    if (valid && !big)
+        for (int c = 0; c < ncell; ++c)
+            bin_cell(s, uint32_t(r), tx0 + c % ntx, ty0 + c / ntx, ncell > 2, tiles_x, sc, status, emit != 0);
+    uint32_t m = __ballot_sync(0xffffffffu, big);
+    while (m) {
+        const int src = __ffs(m) - 1;
+        m &= m - 1;
+        const SubTri b = shfl_subtri(s, src);
+        const uint32_t rb = __shfl_sync(0xffffffffu, uint32_t(r), src);
+        const int bx0 = b.x0 / kTile, by0 = b.y0 / kTile;
+        const int bnx = b.x1 / kTile - bx0 + 1, bn = bnx * (b.y1 / kTile - by0 + 1);
+        for (int c = int(lane); c < bn; c += 32) bin_cell(b, rb, bx0 + c % bnx, by0 + c / bnx, true, tiles_x, sc, status, emit != 0);
+    }
 }
 
 __global__ void __launch_bounds__(256) raster_tiles(RasterScratch sc, uint32_t tiles_x, uint32_t W, uint32_t H,
@@ -233,14 +281,10 @@ __global__ void __launch_bounds__(256) raster_tiles(RasterScratch sc, uint32_t t
             int64_t e1 = edge(s, 2, 0, Px, Py);
             int64_t e2 = edge(s, 0, 1, Px, Py);
             if (e0 < 0 || e1 < 0 || e2 < 0) continue;
-            double z = dmul(double(e0), s.Z[0]);
-            z = dadd(z, dmul(double(e1), s.Z[1]));
-            z = dadd(z, dmul(double(e2), s.Z[2]));
-            z = dmul(z, s.inv_area);
-            float zf = __double2float_rn(z);
-            if (!(zf >= 0.0f)) zf = 0.0f;
-            if (zf > 1.0f) zf = 1.0f;
-            unsigned long long key = (uint64_t(__float_as_uint(zf)) << 32) | s.tri;
+            float z = __fadd_rn(__fadd_rn(s.z0, __fmul_rn(s.a, float(Px - s.X[0]))), __fmul_rn(s.b, float(Py - s.Y[0])));
+            if (!(z > 0.0f)) z = 0.0f;  // also maps -0 and NaN to +0
+            if (z > 1.0f) z = 1.0f;
+            unsigned long long key = (uint64_t(__float_as_uint(z)) << 32) | s.tri;
             atomicMin(&sk[(py - ty * kTile) * kTile + (px - tx * kTile)], key);
         }
     }
@@ -292,16 +336,17 @@ int raster_launch(const RasterJob& job, void* scratch, size_t scratch_bytes, uin
     cudaMemsetAsync(sc.ovf_count, 0, 4, s);
     cudaMemsetAsync(sc.tile_count, 0, size_t(ntiles) * 4, s);
     cudaMemsetAsync(sc.tile_fill, 0, size_t(ntiles) * 4, s);
+    const uint64_t nrec = job.ntris + sc.ovf_cap;
+    const uint32_t bin_blocks = uint32_t((nrec + 127) / 128);
     if (job.ntris) {
-        uint32_t blocks = uint32_t((job.ntris + 127) / 128);
-        raster_setup<<<blocks, 128, 0, s>>>(job.tri, job.ntris, job, sc, tiles_x, d_status);
-        note_launches(1);
+        raster_setup<<<uint32_t((job.ntris + 127) / 128), 128, 0, s>>>(job.tri, job.ntris, job, sc, d_status);
+        raster_bin<<<bin_blocks, 128, 0, s>>>(job.ntris, sc, tiles_x, d_status, 0);
+        note_launches(2);
     }
     int rc = exclusive_scan(sc.tile_count, ntiles, sc.tile_start, sc.total, sc.scan_tmp, s);
     if (rc) return rc;
     if (job.ntris) {
-        uint64_t nrec = job.ntris + sc.ovf_cap;
-        raster_emit<<<uint32_t((nrec + 127) / 128), 128, 0, s>>>(job.ntris, sc, tiles_x, d_status);
+        raster_bin<<<bin_blocks, 128, 0, s>>>(job.ntris, sc, tiles_x, d_status, 1);
         note_launches(1);
     }
     raster_tiles<<<ntiles, 256, 0, s>>>(sc, tiles_x, job.width, job.height, job.keys);

@@ -55,34 +55,60 @@ __device__ __forceinline__ float3 oct_decode(uint32_t p) {
     return norm3(v);
 }
 
-__device__ __forceinline__ float4 tri_sample(const ChainLayout& c, uint32_t l, uint64_t vol_off, float3 x) {
-    const int d = int(c.ldim[l]);
+// Level table staged in shared memory: lanes index it with their own (divergent) level, which the constant
+// bank would serialise.
+struct LevelTab {
+    uint64_t off[kMaxLevels];
+    uint64_t vol[kMaxLevels];
+};
+
+// 8-tap trilinear sample of one volume of level l (d voxels per axis) at x (L0 voxel units); taps outside the
+// volume read zero.  Brick addresses are built per axis: the Morton bits of the two brick coordinates and the
+// in-brick offsets of the two tap coordinates are computed once and OR-ed per tap.
+__device__ __forceinline__ float4 tri_sample(const void* base, uint32_t format, int d, uint32_t l, uint64_t vol_off,
+                                             float3 x) {
     const float s = __int_as_float((127 - int(l)) << 23);  // 2^-l
-    float u[3] = {x.x * s - 0.5f, x.y * s - 0.5f, x.z * s - 0.5f};
-    int i0[3];
+    const float u[3] = {x.x * s - 0.5f, x.y * s - 0.5f, x.z * s - 0.5f};
+    int c0[3];
     float f[3];
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
         float fl = floorf(u[a]);
-        i0[a] = int(fl);
+        c0[a] = int(fl);
         f[a] = u[a] - fl;
     }
+    // per axis and tap (0, 1): validity, high (Morton) part, low (in-brick / linear) part
+    bool ok[3][2];
+    uint32_t hi[3][2], lo[3][2];
+    const bool bricked = d >= 8;
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int t = 0; t < 2; ++t) {
+            int c = c0[a] + t;
+            ok[a][t] = unsigned(c) < unsigned(d);
+            uint32_t cu = uint32_t(c) & 1023u;
+            if (bricked) {
+                hi[a][t] = part1by2(cu >> 3) << a;
+                lo[a][t] = (cu & 7u) << (3 * a);
+            } else {
+                hi[a][t] = 0;
+                lo[a][t] = a == 0 ? cu : (a == 1 ? cu * uint32_t(d) : cu * uint32_t(d * d));
+            }
+        }
+    const float wx[2] = {1.0f - f[0], f[0]}, wy[2] = {1.0f - f[1], f[1]}, wz[2] = {1.0f - f[2], f[2]};
     float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
-    for (int dz = 0; dz < 2; ++dz) {
-        int z = i0[2] + dz;
-        float wz = dz ? f[2] : 1.0f - f[2];
+    for (int tz = 0; tz < 2; ++tz)
 #pragma unroll
-        for (int dy = 0; dy < 2; ++dy) {
-            int y = i0[1] + dy;
-            float wy = dy ? f[1] : 1.0f - f[1];
+        for (int ty = 0; ty < 2; ++ty) {
+            const float wyz = wy[ty] * wz[tz];
 #pragma unroll
-            for (int dx = 0; dx < 2; ++dx) {
-                int xx = i0[0] + dx;
-                float wx = dx ? f[0] : 1.0f - f[0];
-                if (unsigned(z) < unsigned(d) && unsigned(y) < unsigned(d) && unsigned(xx) < unsigned(d)) {
-                    float w = wx * wy * wz;
-                    float4 v = load_vox(c.base, c.format, vol_off + vox_index(d, xx, y, z));
+            for (int tx = 0; tx < 2; ++tx) {
+                if (ok[0][tx] && ok[1][ty] && ok[2][tz]) {
+                    uint64_t idx = (uint64_t(hi[0][tx] | hi[1][ty] | hi[2][tz]) << 9) | (lo[0][tx] | lo[1][ty] | lo[2][tz]);
+                    float4 v = load_vox(base, format, vol_off + idx);
+                    float w = wx[tx] * wyz;
                     acc.x += w * v.x;
                     acc.y += w * v.y;
                     acc.z += w * v.z;
@@ -90,18 +116,19 @@ __device__ __forceinline__ float4 tri_sample(const ChainLayout& c, uint32_t l, u
                 }
             }
         }
-    }
     return acc;
 }
 
-__device__ __forceinline__ float4 level_sample(const ChainLayout& c, uint32_t l, float3 x, float3 dir) {
-    if (!c.aniso || l == 0) return tri_sample(c, l, c.off[l], x);
+__device__ __forceinline__ float4 level_sample(const ChainLayout& c, const LevelTab& lt, uint32_t l, float3 x,
+                                               float3 dir) {
+    const int d = int(c.dim >> l);
+    if (!c.aniso || l == 0) return tri_sample(c.base, c.format, d, l, lt.off[l], x);
     float w[3] = {dir.x * dir.x, dir.y * dir.y, dir.z * dir.z};
     int sel[3] = {dir.x >= 0.0f ? 0 : 1, dir.y >= 0.0f ? 2 : 3, dir.z >= 0.0f ? 4 : 5};
     float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
-        float4 s = tri_sample(c, l, c.off[l] + uint64_t(sel[a]) * c.vol[l], x);
+        float4 s = tri_sample(c.base, c.format, d, l, lt.off[l] + uint64_t(sel[a]) * lt.vol[l], x);
         acc.x += w[a] * s.x;
         acc.y += w[a] * s.y;
         acc.z += w[a] * s.z;
@@ -110,7 +137,8 @@ __device__ __forceinline__ float4 level_sample(const ChainLayout& c, uint32_t l,
     return acc;
 }
 
-__device__ float4 cone(const ChainLayout& c, const TraceConsts& tc, float3 o, float3 dir, float tan_half) {
+__device__ float4 cone(const ChainLayout& c, const LevelTab& lt, const TraceConsts& tc, float3 o, float3 dir,
+                       float tan_half) {
     float cr = 0.f, cg = 0.f, cb = 0.f, alpha = 0.f;
     float t = tc.p.start_offset;
     const float dimf = float(c.dim);
@@ -124,9 +152,9 @@ __device__ float4 cone(const ChainLayout& c, const TraceConsts& tc, float3 o, fl
         float fl = floorf(lvl);
         uint32_t l0 = uint32_t(fl);
         float f = lvl - fl;
-        float4 s = level_sample(c, l0, x, dir);
+        float4 s = level_sample(c, lt, l0, x, dir);
         if (f > 0.0f && l0 + 1 < c.levels) {
-            float4 s1 = level_sample(c, l0 + 1, x, dir);
+            float4 s1 = level_sample(c, lt, l0 + 1, x, dir);
             s.x = s.x + f * (s1.x - s.x);
             s.y = s.y + f * (s1.y - s.y);
             s.z = s.z + f * (s1.z - s.z);
@@ -155,8 +183,8 @@ __device__ __forceinline__ void store_out(void* out, uint32_t fmt, uint64_t i, f
     }
 }
 
-__device__ void trace_pixel(const ChainLayout& c, const TraceConsts& tc, const TraceView& v, float3 org, float inv_vs,
-                            uint32_t px, uint32_t py) {
+__device__ void trace_pixel(const ChainLayout& c, const LevelTab& lt, const TraceConsts& tc, const TraceView& v,
+                            float3 org, float inv_vs, uint32_t px, uint32_t py) {
     const uint64_t npix = uint64_t(v.width) * v.height;
     const uint64_t pi = uint64_t(py) * v.width + px;
     float d = v.depth[pi];
@@ -185,21 +213,21 @@ __device__ void trace_pixel(const ChainLayout& c, const TraceConsts& tc, const T
     coord_space(nw, bx, by, bz);
     float4 acc;
     if (tc.p.diffuse_cones >= 5) {
-        float4 c0 = cone(c, tc, o, bz, tc.p.diffuse_tan_half);
+        float4 c0 = cone(c, lt, tc, o, bz, tc.p.diffuse_tan_half);
         acc = make_float4(0.25f * c0.x, 0.25f * c0.y, 0.25f * c0.z, 0.25f * c0.w);
         const float cphi[4] = {1.f, 0.f, -1.f, 0.f}, sphi[4] = {0.f, 1.f, 0.f, -1.f};
 #pragma unroll 1
         for (int k = 0; k < 4; ++k) {
             float3 side = add3(mul3(bx, cphi[k]), mul3(by, sphi[k]));
             float3 dir = norm3(add3(mul3(bz, tc.cos_tilt), mul3(side, tc.sin_tilt)));
-            float4 ck = cone(c, tc, o, dir, tc.p.diffuse_tan_half);
+            float4 ck = cone(c, lt, tc, o, dir, tc.p.diffuse_tan_half);
             acc.x += 0.1875f * ck.x;
             acc.y += 0.1875f * ck.y;
             acc.z += 0.1875f * ck.z;
             acc.w += 0.1875f * ck.w;
         }
     } else {
-        acc = cone(c, tc, o, bz, tc.p.diffuse_tan_half);
+        acc = cone(c, lt, tc, o, bz, tc.p.diffuse_tan_half);
     }
     store_out(v.out, v.out_format, pi, acc);
     float4 sp = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -208,15 +236,21 @@ __device__ void trace_pixel(const ChainLayout& c, const TraceConsts& tc, const T
         float dn = dot3(vd, nw);
         float3 rd = norm3(sub3(vd, mul3(nw, 2.0f * dn)));
         float th = fmaxf(rough, tc.p.min_spec_tan_half);
-        sp = cone(c, tc, o, rd, th);
+        sp = cone(c, lt, tc, o, rd, th);
     }
     store_out(v.out, v.out_format, npix + pi, sp);
 }
 
 // One CTA = one 16x8 pixel tile of one view; tiles of all views are enumerated in view order.
-__global__ void __launch_bounds__(128) trace_kernel(ChainLayout c, TraceConsts tc, const f184gi_grid_frame* __restrict__ fr,
+__global__ void __launch_bounds__(128, 4) trace_kernel(ChainLayout c, TraceConsts tc, const f184gi_grid_frame* __restrict__ fr,
                                                     const TraceView* __restrict__ views,
                                                     const uint32_t* __restrict__ tile_base, uint32_t nviews) {
+    __shared__ LevelTab lt;
+    if (threadIdx.x < kMaxLevels) {
+        lt.off[threadIdx.x] = c.off[threadIdx.x];
+        lt.vol[threadIdx.x] = c.vol[threadIdx.x];
+    }
+    __syncthreads();
     uint32_t tile = blockIdx.x;
     uint32_t vi = 0;
     while (vi + 1 < nviews && tile >= tile_base[vi + 1]) ++vi;
@@ -229,7 +263,7 @@ __global__ void __launch_bounds__(128) trace_kernel(ChainLayout c, TraceConsts t
     // world -> L0 voxel units: (p - origin) * (inv_voxel_fixed / 256), all scalings exact
     float3 org = f3(float(fr->origin[0]), float(fr->origin[1]), float(fr->origin[2]));
     float inv_vs = float(fr->inv_voxel_fixed * (1.0 / 256.0));
-    trace_pixel(c, tc, v, org, inv_vs, px, py);
+    trace_pixel(c, lt, tc, v, org, inv_vs, px, py);
 }
 
 }  // namespace

@@ -7,7 +7,8 @@
 // covering triangle adds its Lambert weight |dot(-L, n)| * albedo (the term of Shader/Lighting/indirect.frag:60-62,
 // 167) as 1.31 fixed point with 64-bit integer atomics, so sums and counts are independent of triangle order.  The
 // voxel's radiance is luminance * shadow(voxel centre) * mean weight, the shadow test being indirect.frag:160-165's
-// compare with a two-voxel bias, evaluated in FP64 against the shadow map rasterized by raster.cu.
+// compare with a two-voxel bias, evaluated as a fixed FP32 operation sequence (the same decision on any IEEE
+// machine) against the shadow map rasterized by raster.cu.  FP64 is used per vertex only (the snap).
 //
 // Pipeline: setup (snap, weight, count overlapped bricks) -> scan -> emit (triangle lists per brick) ->
 // one CTA per brick accumulates in shared memory, resolves and writes the brick once.
@@ -94,54 +95,88 @@ __device__ __forceinline__ void voxel_range(const int32_t* q, uint32_t dim, int3
     }
 }
 
-template <bool kEmit>
-__device__ void visit_bricks(const TriRec& r, uint32_t t, uint32_t dim, const VoxScratch& sc, uint32_t* status) {
-    int32_t lo[3], hi[3];
-    voxel_range(r.q, dim, lo, hi);
-    int32_t b0[3], b1[3];
-    for (int a = 0; a < 3; ++a) b0[a] = lo[a] >> 3, b1[a] = hi[a] >> 3;
-    bool single = b0[0] == b1[0] && b0[1] == b1[1] && b0[2] == b1[2];
-    for (int bz = b0[2]; bz <= b1[2]; ++bz)
-        for (int by = b0[1]; by <= b1[1]; ++by)
-            for (int bx = b0[0]; bx <= b1[0]; ++bx) {
-                uint32_t m = morton3(bx, by, bz);
-                if (sc.dirty_mask && !((sc.dirty_mask[m >> 5] >> (m & 31)) & 1u)) continue;
-                if (!single) {
-                    const int64_t c[3] = {bx * kBrickFix + kBrickFix / 2, by * kBrickFix + kBrickFix / 2,
-                                          bz * kBrickFix + kBrickFix / 2};
-                    if (!tri_box_sat(r.q, c, kBrickFix / 2)) continue;
-                }
-                if (!kEmit) {
-                    atomicAdd(&sc.brick_count[m], 1u);
-                } else {
-                    uint64_t slot = uint64_t(sc.brick_start[m]) + atomicAdd(&sc.brick_fill[m], 1u);
-                    if (slot < sc.list_cap)
-                        sc.list[slot] = t;
-                    else
-                        set_status(status, kStatusOverflow);
-                }
-            }
+constexpr int kWarpCells = 8;  // triangles overlapping more bricks than this are binned by a whole warp
+
+__device__ __forceinline__ void bin_brick(const int32_t* q, uint32_t t, int bx, int by, int bz, bool test,
+                                          const VoxScratch& sc, uint32_t* status, bool emit) {
+    uint32_t m = morton3(bx, by, bz);
+    if (sc.dirty_mask && !((sc.dirty_mask[m >> 5] >> (m & 31)) & 1u)) return;
+    if (test) {
+        const int64_t c[3] = {bx * kBrickFix + kBrickFix / 2, by * kBrickFix + kBrickFix / 2,
+                              bz * kBrickFix + kBrickFix / 2};
+        if (!tri_box_sat(q, c, kBrickFix / 2)) return;
+    }
+    if (!emit) {
+        atomicAdd(&sc.brick_count[m], 1u);
+    } else {
+        uint64_t slot = uint64_t(sc.brick_start[m]) + atomicAdd(&sc.brick_fill[m], 1u);
+        if (slot < sc.list_cap)
+            sc.list[slot] = t;
+        else
+            set_status(status, kStatusOverflow);
+    }
 }
 
-__global__ void vox_setup(const float* __restrict__ tri, const uint32_t* __restrict__ albedo, uint64_t ntris,
-                          const f184gi_grid_frame* __restrict__ fr, uint32_t dim, VoxScratch sc, uint32_t* status) {
-    uint64_t t = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (t >= ntris) return;
+// Count (emit = false) or list (emit = true) the bricks a triangle overlaps.  Every lane of the warp must call
+// this; a triangle whose brick box holds more than kWarpCells bricks is walked by all 32 lanes.
+__device__ void bin_bricks_warp(const TriRec& r, bool valid, uint32_t t, uint32_t dim, const VoxScratch& sc,
+                                uint32_t* status, bool emit) {
+    int32_t b0[3] = {0, 0, 0}, nb[3] = {0, 0, 0};
+    if (valid) {
+        int32_t lo[3], hi[3];
+        voxel_range(r.q, dim, lo, hi);
+        for (int a = 0; a < 3; ++a) b0[a] = lo[a] >> 3, nb[a] = (hi[a] >> 3) - b0[a] + 1;
+    }
+    const int ncell = nb[0] * nb[1] * nb[2];
+    const bool big = valid && ncell > kWarpCells;
+    if (valid && !big)
+        for (int c = 0; c < ncell; ++c)
+            bin_brick(r.q, t, b0[0] + c % nb[0], b0[1] + (c / nb[0]) % nb[1], b0[2] + c / (nb[0] * nb[1]), ncell > 1,
+                      sc, status, emit);
+    uint32_t m = __ballot_sync(0xffffffffu, big);
+    const int lane = int(threadIdx.x & 31);
+    while (m) {
+        const int src = __ffs(m) - 1;
+        m &= m - 1;
+        int32_t q[9];
+#pragma unroll
+        for (int i = 0; i < 9; ++i) q[i] = __shfl_sync(0xffffffffu, r.q[i], src);
+        const uint32_t tb = __shfl_sync(0xffffffffu, t, src);
+        int32_t c0[3], cn[3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            c0[a] = __shfl_sync(0xffffffffu, b0[a], src);
+            cn[a] = __shfl_sync(0xffffffffu, nb[a], src);
+        }
+        const int n = cn[0] * cn[1] * cn[2];
+        for (int c = lane; c < n; c += 32)
+            bin_brick(q, tb, c0[0] + c % cn[0], c0[1] + (c / cn[0]) % cn[1], c0[2] + c / (cn[0] * cn[1]), true, sc,
+                      status, emit);
+    }
+}
+
+__global__ void __launch_bounds__(128) vox_setup(const float* __restrict__ tri, const uint32_t* __restrict__ albedo,
+                                                 uint64_t ntris, const f184gi_grid_frame* __restrict__ fr, uint32_t dim,
+                                                 VoxScratch sc, uint32_t* status) {
+    const uint64_t t = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     TriRec r;
-    bool ok = true;
-    const float* p = tri + t * 9;
+    bool ok = t < ntris;  // no early return: bin_bricks_warp needs the whole warp
+    const float* p = tri + (ok ? t : 0) * 9;
     for (int i = 0; i < 9; ++i) {
         int a = i % 3;
-        double d = dsub(double(p[i]), fr->origin[a]);
-        double s = dmul(d, fr->inv_voxel_fixed);
-        int64_t q = __double2ll_rn(s);
+        int64_t q = 0;
+        if (ok) {
+            double d = dsub(double(p[i]), fr->origin[a]);
+            double s = dmul(d, fr->inv_voxel_fixed);
+            q = __double2ll_rn(s);
+        }
         if (q >= kMaxQ || q <= -kMaxQ) {
+            set_status(status, kStatusRange);
             ok = false;
             q = 0;
         }
         r.q[i] = int32_t(q);
     }
-    if (!ok) set_status(status, kStatusRange);
     if (ok) {
         int64_t e0[3], e1[3];
         for (int a = 0; a < 3; ++a) {
@@ -155,33 +190,34 @@ __global__ void vox_setup(const float* __restrict__ tri, const uint32_t* __restr
         voxel_range(r.q, dim, lo, hi);
         if (lo[0] > hi[0] || lo[1] > hi[1] || lo[2] > hi[2]) ok = false;
     }
-    if (!ok) {
-        r.wq[0] = r.wq[1] = r.wq[2] = kInvalid;
-        sc.recs[t] = r;
-        return;
+    r.wq[0] = r.wq[1] = r.wq[2] = kInvalid;
+    if (ok) {
+        // injection weight |dot(-L, n)| * albedo, FP32
+        float3 a = make_float3(p[3] - p[0], p[4] - p[1], p[5] - p[2]);
+        float3 b = make_float3(p[6] - p[0], p[7] - p[1], p[8] - p[2]);
+        float3 n = make_float3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+        float len = sqrtf(n.x * n.x + n.y * n.y + n.z * n.z);
+        float wi0 = -float(fr->light_dir[0]), wi1 = -float(fr->light_dir[1]), wi2 = -float(fr->light_dir[2]);
+        float cosv = len > 0.0f ? fabsf(wi0 * n.x + wi1 * n.y + wi2 * n.z) / len : 0.0f;
+        uint32_t al = albedo[t];
+        for (int c = 0; c < 3; ++c) {
+            float w = cosv * c_albedo_lut[(al >> (8 * c)) & 255u];
+            r.wq[c] = min(__float2uint_rn(w * 2147483648.0f), 0x80000000u);
+        }
     }
-    // injection weight |dot(-L, n)| * albedo, FP32
-    float3 a = make_float3(p[3] - p[0], p[4] - p[1], p[5] - p[2]);
-    float3 b = make_float3(p[6] - p[0], p[7] - p[1], p[8] - p[2]);
-    float3 n = make_float3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
-    float len = sqrtf(n.x * n.x + n.y * n.y + n.z * n.z);
-    float wi0 = -float(fr->light_dir[0]), wi1 = -float(fr->light_dir[1]), wi2 = -float(fr->light_dir[2]);
-    float cosv = len > 0.0f ? fabsf(wi0 * n.x + wi1 * n.y + wi2 * n.z) / len : 0.0f;
-    uint32_t al = albedo[t];
-    for (int c = 0; c < 3; ++c) {
-        float w = cosv * c_albedo_lut[(al >> (8 * c)) & 255u];
-        r.wq[c] = min(__float2uint_rn(w * 2147483648.0f), 0x80000000u);
-    }
-    sc.recs[t] = r;
-    visit_bricks<false>(r, uint32_t(t), dim, sc, status);
+    if (t < ntris) sc.recs[t] = r;
+    bin_bricks_warp(r, ok, uint32_t(t), dim, sc, status, false);
 }
 
-__global__ void vox_emit(uint64_t ntris, uint32_t dim, VoxScratch sc, uint32_t* status) {
-    uint64_t t = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (t >= ntris) return;
-    TriRec r = sc.recs[t];
-    if (r.wq[0] == kInvalid) return;
-    visit_bricks<true>(r, uint32_t(t), dim, sc, status);
+__global__ void __launch_bounds__(128) vox_emit(uint64_t ntris, uint32_t dim, VoxScratch sc, uint32_t* status) {
+    const uint64_t t = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    TriRec r;
+    bool ok = false;
+    if (t < ntris) {
+        r = sc.recs[t];
+        ok = r.wq[0] != kInvalid;
+    }
+    bin_bricks_warp(r, ok, uint32_t(t), dim, sc, status, true);
 }
 
 __global__ void vox_dirty_mask(const uint32_t* dirty, uint32_t ndirty, uint32_t nbricks, uint32_t* mask) {
@@ -299,25 +335,31 @@ __global__ void __launch_bounds__(256) vox_bricks(VoxScratch sc, const f184gi_gr
     }
     __syncthreads();
     // resolve: radiance = luminance * shadow * mean weight, opacity 1 where covered
-    const double* M = fr->light_clip;
-    const double half_res = 0.5 * double(res);
+    const float* lv = fr->light_vox;
+    const float half_res = 0.5f * float(res);
+    const float bias = fr->shadow_bias_f;
     for (int li = threadIdx.x; li < 512; li += 256) {
         int lx = li & 7, ly = (li >> 3) & 7, lz = li >> 6;
         uint32_t cnt = s_cnt[li];
         float4 out = make_float4(0.f, 0.f, 0.f, 0.f);
         if (cnt) {
-            int64_t ijk[3] = {bx * 8 + lx, by * 8 + ly, bz * 8 + lz};
-            double cw[3];
-            for (int a = 0; a < 3; ++a) cw[a] = dadd(fr->origin[a], dmul(dadd(double(ijk[a]), 0.5), fr->voxel_size));
-            double x = drow(M + 0, cw[0], cw[1], cw[2]);
-            double y = drow(M + 4, cw[0], cw[1], cw[2]);
-            double z = drow(M + 8, cw[0], cw[1], cw[2]);
-            double tx = floor(dmul(dadd(x, 1.0), half_res)), ty = floor(dmul(dadd(y, 1.0), half_res));
+            // shadow test of the voxel centre: exact FP32 operation sequence (see frame.h)
+            float fi = float(bx * 8 + lx), fj = float(by * 8 + ly), fk = float(bz * 8 + lz);
+            float v[3];
+#pragma unroll
+            for (int rr = 0; rr < 3; ++rr) {
+                const float* c = lv + 4 * rr;
+                float s = __fadd_rn(c[0], __fmul_rn(fi, c[1]));
+                s = __fadd_rn(s, __fmul_rn(fj, c[2]));
+                v[rr] = __fadd_rn(s, __fmul_rn(fk, c[3]));
+            }
+            float tx = floorf(__fmul_rn(__fadd_rn(v[0], 1.0f), half_res));
+            float ty = floorf(__fmul_rn(__fadd_rn(v[1], 1.0f), half_res));
             bool lit = true;
-            if (tx >= 0.0 && ty >= 0.0 && tx < double(res) && ty < double(res)) {
+            if (tx >= 0.0f && ty >= 0.0f && tx < float(res) && ty < float(res)) {
                 unsigned long long k = shadow[uint64_t(ty) * res + uint64_t(tx)];
-                double sd = k == ~0ull ? 1.0 : double(__uint_as_float(uint32_t(k >> 32)));
-                lit = dsub(z, fr->shadow_bias) <= sd;
+                float sd = k == ~0ull ? 1.0f : __uint_as_float(uint32_t(k >> 32));
+                lit = __fsub_rn(v[2], bias) <= sd;
             }
             float scale = lit ? (1.0f / 2147483648.0f) / float(cnt) : 0.0f;
             out.x = light.luminance[0] * (float(s_sum[0][li]) * scale);

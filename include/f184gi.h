@@ -95,6 +95,11 @@ typedef struct f184gi_grid_frame {
     double light_clip[16];  /* world -> shadow clip space (row-major), z in [0,1] */
     double shadow_bias;     /* clip-z bias of the shadow compare (two voxels along the light) */
     double light_dir[3];    /* normalised direction of travel */
+    /* shadow clip coordinates of voxel centres as FP32 affine functions of the voxel index:
+     * row r in (x, y, z): light_vox[4r] + i light_vox[4r+1] + j light_vox[4r+2] + k light_vox[4r+3] */
+    float light_vox[12];
+    float shadow_bias_f;
+    float pad_f[3];
 } f184gi_grid_frame;
 
 /* One view over one G-buffer (the trace's inputs).  The G-buffer layout:

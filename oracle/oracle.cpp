@@ -120,11 +120,13 @@ int clip_polygon(V4* poly, int n) {
     return n;
 }
 
+// Snapped triangle: vertices in 1/16 pixel, depth plane z(X, Y) = z0 + a (X - X0) + b (Y - Y0) with
+// z0, a, b rounded to FP32 from an FP64 plane solve.
 struct SnapTri {
     int64_t X[3], Y[3];
     double Z[3];
     int64_t area2;
-    double inv_area;         // 1 / area2, rounded once
+    float z0, a, b;
     int64_t x0, x1, y0, y1;  // pixel range, inclusive
 };
 
@@ -146,7 +148,19 @@ bool snap_tri(const V4& a, const V4& b, const V4& c, uint32_t W, uint32_t H, Sna
         area2 = -area2;
     }
     s.area2 = area2;
-    s.inv_area = 1.0 / double(area2);
+    {
+        double dx1 = double(s.X[1] - s.X[0]), dy1 = double(s.Y[1] - s.Y[0]);
+        double dx2 = double(s.X[2] - s.X[0]), dy2 = double(s.Y[2] - s.Y[0]);
+        double dz1 = s.Z[1] - s.Z[0], dz2 = s.Z[2] - s.Z[0];
+        double D = double(area2);
+        double na = dz1 * dy2;
+        na = na - dz2 * dy1;
+        double nb = dz2 * dx1;
+        nb = nb - dz1 * dx2;
+        s.z0 = float(s.Z[0]);
+        s.a = float(na / D);
+        s.b = float(nb / D);
+    }
     int64_t mnx = std::min({s.X[0], s.X[1], s.X[2]}), mxx = std::max({s.X[0], s.X[1], s.X[2]});
     int64_t mny = std::min({s.Y[0], s.Y[1], s.Y[2]}), mxy = std::max({s.Y[0], s.Y[1], s.Y[2]});
     // pixel centres at 16 p + 8
@@ -167,12 +181,11 @@ void raster_tri(const SnapTri& s, uint32_t tri, uint32_t W, int64_t row_lo, int6
             int64_t e1 = (s.X[0] - s.X[2]) * (Py - s.Y[2]) - (s.Y[0] - s.Y[2]) * (Px - s.X[2]);
             int64_t e2 = (s.X[1] - s.X[0]) * (Py - s.Y[0]) - (s.Y[1] - s.Y[0]) * (Px - s.X[0]);
             if (e0 < 0 || e1 < 0 || e2 < 0) continue;
-            double z = double(e0) * s.Z[0];
-            z = z + double(e1) * s.Z[1];
-            z = z + double(e2) * s.Z[2];
-            z = z * s.inv_area;
-            float zf = float(z);
-            if (!(zf >= 0.0f)) zf = 0.0f;
+            float ta = s.a * float(Px - s.X[0]);
+            float zf = s.z0 + ta;
+            float tb = s.b * float(Py - s.Y[0]);
+            zf = zf + tb;
+            if (!(zf > 0.0f)) zf = 0.0f;  // also maps -0 and NaN to +0
             if (zf > 1.0f) zf = 1.0f;
             uint64_t key = (uint64_t(float_bits(zf)) << 32) | tri;
             uint64_t& k = keys[uint64_t(py) * W + uint64_t(px)];
@@ -381,24 +394,28 @@ bool tri_box_overlap(const FixTri& t, int64_t i, int64_t j, int64_t k) {
     return true;
 }
 
+// Shadow visibility of the centre of voxel (i, j, k), FP32 in this exact operation order (the decision must
+// not depend on the arithmetic precision of the caller):
+//   v_r = ((base_r + i s_r0) + j s_r1) + k s_r2,  texel = floor((v + 1) * res/2),  lit = z - bias <= depth
+inline float vox_light(const float* lv, float fi, float fj, float fk) {
+    float a = fi * lv[1];
+    float s = lv[0] + a;
+    float b = fj * lv[2];
+    s = s + b;
+    float c = fk * lv[3];
+    return s + c;
+}
+
 bool shade_voxel(const f184gi_grid_frame& fr, uint32_t res, const float* shadow, int64_t i, int64_t j, int64_t k) {
-    double cw[3];
-    const int64_t ijk[3] = {i, j, k};
-    for (int a = 0; a < 3; ++a) {
-        double t = double(ijk[a]) + 0.5;
-        t = t * fr.voxel_size;
-        cw[a] = fr.origin[a] + t;
-    }
-    const double* M = fr.light_clip;
-    double x = mrow(M + 0, cw[0], cw[1], cw[2]);
-    double y = mrow(M + 4, cw[0], cw[1], cw[2]);
-    double z = mrow(M + 8, cw[0], cw[1], cw[2]);
-    double half = 0.5 * double(res);
-    double fx = (x + 1.0) * half, fy = (y + 1.0) * half;
-    double tx = std::floor(fx), ty = std::floor(fy);
-    if (tx < 0.0 || ty < 0.0 || tx >= double(res) || ty >= double(res)) return true;
-    double sd = double(shadow[uint64_t(ty) * res + uint64_t(tx)]);
-    double zb = z - fr.shadow_bias;
+    float fi = float(i), fj = float(j), fk = float(k);
+    float x = vox_light(fr.light_vox + 0, fi, fj, fk);
+    float y = vox_light(fr.light_vox + 4, fi, fj, fk);
+    float z = vox_light(fr.light_vox + 8, fi, fj, fk);
+    float half = 0.5f * float(res);
+    float tx = std::floor((x + 1.0f) * half), ty = std::floor((y + 1.0f) * half);
+    if (!(tx >= 0.0f && ty >= 0.0f && tx < float(res) && ty < float(res))) return true;
+    float sd = shadow[uint64_t(ty) * res + uint64_t(tx)];
+    float zb = z - fr.shadow_bias_f;
     return zb <= sd;
 }
 
@@ -841,6 +858,14 @@ int orc_grid_frame(const f184gi_bounds* b, uint32_t dim, const float light_dir[3
     M[15] = 1.0;
     out->shadow_bias = vs / R;
     for (int a = 0; a < 3; ++a) out->light_dir[a] = w[a];
+    // FP32 affine map voxel index -> light clip (centre of voxel (0,0,0) plus one-voxel steps)
+    double hv = vs * 0.5;
+    double c0[3] = {out->origin[0] + hv, out->origin[1] + hv, out->origin[2] + hv};
+    for (int r = 0; r < 3; ++r) {
+        out->light_vox[4 * r] = float(mrow(M + 4 * r, c0[0], c0[1], c0[2]));
+        for (int a = 0; a < 3; ++a) out->light_vox[4 * r + 1 + a] = float(M[4 * r + a] * vs);
+    }
+    out->shadow_bias_f = float(out->shadow_bias);
     return 0;
 }
 
@@ -849,7 +874,6 @@ int orc_raster(const double M[16], uint32_t W, uint32_t H, const float* tri, uin
     if (!M || !tri || !keys || W == 0 || H == 0) return -1;
     std::fill(keys, keys + uint64_t(W) * H, ~uint64_t(0));
     // snap every triangle once, then rasterize row slabs in parallel
-    std::vector<std::vector<SnapTri>> snaps(ntris);
     std::vector<uint32_t> owner;
     std::vector<SnapTri> all;
     for (uint64_t t = 0; t < ntris; ++t) {

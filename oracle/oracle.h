@@ -28,7 +28,9 @@ extern "C" {
 int orc_grid_frame(const f184gi_bounds* bounds, uint32_t dim, const float light_dir[3], f184gi_grid_frame* out);
 
 /* Exact triangle raster: u64 key = (float bits of depth) << 32 | triangle index, min per pixel
- * (~0 = empty).  clip = M * (x,y,z,1) in FP64; clipped to 0<=z<=w, |x|,|y| <= 16 w. */
+ * (~0 = empty).  clip = M * (x,y,z,1) in FP64; clipped to 0<=z<=w, |x|,|y| <= 16 w; vertices snapped to
+ * 1/16 pixel; inclusive int64 edge functions at pixel centres; depth from the FP32-rounded plane
+ * z0 + a dX + b dY evaluated in FP32 in that order. */
 int orc_raster(const double M[16], uint32_t width, uint32_t height, const float* tri_xyz, uint64_t ntris,
                uint64_t* keys, int nthreads);
 
