@@ -93,6 +93,7 @@ PROTOTYPES = {
     "f184gi_trace": (C.c_int, [P, U32, C.POINTER(View), U32, C.POINTER(ConeParams), P]),
     "f184gi_cone_params_default": (None, [C.POINTER(ConeParams)]),
     "f184gi_gbuffer": (C.c_int, [P, P, P, U64, C.POINTER(View), P, P]),
+    "f184gi_transform": (C.c_int, [P, P, U64, PF, P, P]),
     "f184gi_sync": (C.c_int, [P, P]),
     "f184gi_grid_get_frame": (C.c_int, [P, U32, C.POINTER(GridFrame)]),
     "f184gi_frame_from_bounds": (C.c_int, [C.POINTER(Bounds), U32, PF, C.POINTER(GridFrame)]),

@@ -456,6 +456,12 @@ int f184gi_gbuffer(f184gi_ctx* c, const float* tri, const float* rough, uint64_t
                                   const_cast<uint16_t*>(view->roughness), tri_id_out, s);
 }
 
+int f184gi_transform(f184gi_ctx* c, const float* obj_xyz, uint64_t ntris, const float model[12], float* world_xyz,
+                     void* stream) {
+    if (!c || !model || (ntris && (!obj_xyz || !world_xyz))) return fail(F184GI_ERR_INVALID, "transform: null argument");
+    return transform_launch(obj_xyz, ntris, model, world_xyz, static_cast<cudaStream_t>(stream));
+}
+
 int f184gi_sync(f184gi_ctx* c, void* stream) {
     if (!c) return fail(F184GI_ERR_INVALID, "sync: null context");
     cudaError_t e = cudaStreamSynchronize(static_cast<cudaStream_t>(stream));

@@ -111,4 +111,7 @@ int gbuffer_resolve_launch(const unsigned long long* keys, uint32_t width, uint3
 
 int read_level_launch(const ChainLayout& chain, uint32_t level, uint32_t dir, float* d_out, cudaStream_t s);
 
+// dst = model (row-major 3x4) * src, per vertex; products and sums rounded in order (no FMA)
+int transform_launch(const float* src, uint64_t ntris, const float model[12], float* dst, cudaStream_t s);
+
 }  // namespace f184

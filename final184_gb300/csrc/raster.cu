@@ -19,7 +19,7 @@ namespace {
 constexpr int kTile = 16;
 constexpr double kGuard = 16.0;
 constexpr uint32_t kNone = 0xffffffffu;
-constexpr int kWarpCells = 8;  // triangles touching more tiles than this are binned by a whole warp
+constexpr int kBigCells = 8;  // records touching more tiles than this are binned by a whole CTA
 
 struct SubTri {
     int32_t X[3], Y[3];
@@ -149,6 +149,8 @@ struct RasterScratch {
     uint32_t* total;       // [1]
     uint32_t* scan_tmp;
     uint32_t* list;
+    uint32_t* big;         // records with more than kBigCells tiles (binned by bin_big)
+    uint32_t* big_count;   // [1]
     uint64_t list_cap;
     uint64_t ovf_cap;
 };
@@ -207,54 +209,37 @@ __device__ __forceinline__ void bin_cell(const SubTri& s, uint32_t rec, int tx, 
     }
 }
 
-__device__ __forceinline__ SubTri shfl_subtri(const SubTri& s, int src) {
-    SubTri r;
-    for (int i = 0; i < 3; ++i) {
-        r.X[i] = __shfl_sync(0xffffffffu, s.X[i], src);
-        r.Y[i] = __shfl_sync(0xffffffffu, s.Y[i], src);
-    }
-    r.z0 = __shfl_sync(0xffffffffu, s.z0, src);
-    r.a = __shfl_sync(0xffffffffu, s.a, src);
-    r.b = __shfl_sync(0xffffffffu, s.b, src);
-    r.tri = __shfl_sync(0xffffffffu, s.tri, src);
-    uint32_t p0 = __shfl_sync(0xffffffffu, uint32_t(s.x0) | (uint32_t(s.x1) << 16), src);
-    uint32_t p1 = __shfl_sync(0xffffffffu, uint32_t(s.y0) | (uint32_t(s.y1) << 16), src);
-    r.x0 = uint16_t(p0 & 0xffff), r.x1 = uint16_t(p0 >> 16), r.y0 = uint16_t(p1 & 0xffff), r.y1 = uint16_t(p1 >> 16);
-    return r;
-}
-
-// Count (emit = false) or list (emit = true) the tiles of every record.  Blocks are whole warps; a record that
-// touches more than kWarpCells tiles is walked by all 32 lanes of its warp.
+// Count (emit = 0) or list (emit = 1) the tiles of every record with at most kBigCells tiles; larger records are
+// queued (count pass) for raster_bin_big, which gives each its own CTA.
 __global__ void __launch_bounds__(128) raster_bin(uint64_t ntris, RasterScratch sc, uint32_t tiles_x, uint32_t* status,
                                                   int emit) {
     const uint64_t r = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     const uint64_t nrec = ntris + min(uint64_t(*sc.ovf_count), sc.ovf_cap);
-    const uint32_t lane = threadIdx.x & 31;
-    SubTri s;
-    bool valid = r < nrec;
-    if (valid) {
-        s = sc.recs[r];
-        valid = s.tri != kNone;
+    if (r >= nrec) return;
+    const SubTri s = sc.recs[r];
+    if (s.tri == kNone) return;
+    const int tx0 = s.x0 / kTile, ty0 = s.y0 / kTile;
+    const int ntx = s.x1 / kTile - tx0 + 1, ncell = ntx * (s.y1 / kTile - ty0 + 1);
+    if (ncell > kBigCells) {
+        if (!emit) {
+            uint32_t k = atomicAdd(sc.big_count, 1u);
+            if (k < uint32_t(nrec)) sc.big[k] = uint32_t(r);
+        }
+        return;
     }
-    int tx0 = 0, ty0 = 0, ntx = 0, nty = 0;
-    if (valid) {
-        tx0 = s.x0 / kTile, ty0 = s.y0 / kTile;
-        ntx = s.x1 / kTile - tx0 + 1, nty = s.y1 / kTile - ty0 + 1;
-    }
-    const int ncell = ntx * nty;
-    const bool big = valid && ncell > kWarpCells;
-    if (valid && !big)
-        for (int c = 0; c < ncell; ++c)
-            bin_cell(s, uint32_t(r), tx0 + c % ntx, ty0 + c / ntx, ncell > 2, tiles_x, sc, status, emit != 0);
-    uint32_t m = __ballot_sync(0xffffffffu, big);
-    while (m) {
-        const int src = __ffs(m) - 1;
-        m &= m - 1;
-        const SubTri b = shfl_subtri(s, src);
-        const uint32_t rb = __shfl_sync(0xffffffffu, uint32_t(r), src);
-        const int bx0 = b.x0 / kTile, by0 = b.y0 / kTile;
-        const int bnx = b.x1 / kTile - bx0 + 1, bn = bnx * (b.y1 / kTile - by0 + 1);
-        for (int c = int(lane); c < bn; c += 32) bin_cell(b, rb, bx0 + c % bnx, by0 + c / bnx, true, tiles_x, sc, status, emit != 0);
+    for (int c = 0; c < ncell; ++c)
+        bin_cell(s, uint32_t(r), tx0 + c % ntx, ty0 + c / ntx, ncell > 2, tiles_x, sc, status, emit != 0);
+}
+
+__global__ void __launch_bounds__(256) raster_bin_big(RasterScratch sc, uint32_t tiles_x, uint32_t* status, int emit) {
+    const uint32_t nbig = *sc.big_count;
+    for (uint32_t i = blockIdx.x; i < nbig; i += gridDim.x) {
+        const uint32_t r = sc.big[i];
+        const SubTri s = sc.recs[r];
+        const int tx0 = s.x0 / kTile, ty0 = s.y0 / kTile;
+        const int ntx = s.x1 / kTile - tx0 + 1, ncell = ntx * (s.y1 / kTile - ty0 + 1);
+        for (int c = int(threadIdx.x); c < ncell; c += int(blockDim.x))
+            bin_cell(s, r, tx0 + c % ntx, ty0 + c / ntx, true, tiles_x, sc, status, emit != 0);
     }
 }
 
@@ -281,7 +266,9 @@ __global__ void __launch_bounds__(256) raster_tiles(RasterScratch sc, uint32_t t
             int64_t e1 = edge(s, 2, 0, Px, Py);
             int64_t e2 = edge(s, 0, 1, Px, Py);
             if (e0 < 0 || e1 < 0 || e2 < 0) continue;
-            float z = __fadd_rn(__fadd_rn(s.z0, __fmul_rn(s.a, float(Px - s.X[0]))), __fmul_rn(s.b, float(Py - s.Y[0])));
+            // |P - X0| < 2^21: the int32 -> float conversion is exact (an int64 conversion would use the FP64 pipe)
+            const int32_t dX = int32_t(Px) - s.X[0], dY = int32_t(Py) - s.Y[0];
+            float z = __fadd_rn(__fadd_rn(s.z0, __fmul_rn(s.a, float(dX))), __fmul_rn(s.b, float(dY)));
             if (!(z > 0.0f)) z = 0.0f;  // also maps -0 and NaN to +0
             if (z > 1.0f) z = 1.0f;
             unsigned long long key = (uint64_t(__float_as_uint(z)) << 32) | s.tri;
@@ -304,13 +291,14 @@ T* carve(char*& p, uint64_t n) {
 }  // namespace
 
 static uint64_t ovf_capacity(uint64_t ntris) { return ntris / 2 + 4096; }
+static constexpr uint32_t kBigBlocks = 2 * 152;
 static uint64_t list_capacity(uint64_t ntris, uint32_t ntiles) { return ntris * 8 + uint64_t(ntiles) * 16 + 65536; }
 
 size_t raster_scratch_bytes(uint64_t ntris, uint32_t W, uint32_t H) {
     uint32_t tiles = ((W + kTile - 1) / kTile) * ((H + kTile - 1) / kTile);
     uint64_t recs = ntris + ovf_capacity(ntris);
     return recs * sizeof(SubTri) + uint64_t(tiles) * 12 + scan_scratch_bytes(tiles) + list_capacity(ntris, tiles) * 4 +
-           16 * 256;
+           recs * 4 + 20 * 256;
 }
 
 int raster_launch(const RasterJob& job, void* scratch, size_t scratch_bytes, uint32_t* d_status, cudaStream_t s) {
@@ -333,6 +321,9 @@ int raster_launch(const RasterJob& job, void* scratch, size_t scratch_bytes, uin
     sc.scan_tmp = carve<uint32_t>(p, scan_scratch_bytes(ntiles) / 4);
     sc.list_cap = list_capacity(job.ntris, ntiles);
     sc.list = carve<uint32_t>(p, sc.list_cap);
+    sc.big = carve<uint32_t>(p, job.ntris + sc.ovf_cap);
+    sc.big_count = carve<uint32_t>(p, 1);
+    cudaMemsetAsync(sc.big_count, 0, 4, s);
     cudaMemsetAsync(sc.ovf_count, 0, 4, s);
     cudaMemsetAsync(sc.tile_count, 0, size_t(ntiles) * 4, s);
     cudaMemsetAsync(sc.tile_fill, 0, size_t(ntiles) * 4, s);
@@ -341,13 +332,15 @@ int raster_launch(const RasterJob& job, void* scratch, size_t scratch_bytes, uin
     if (job.ntris) {
         raster_setup<<<uint32_t((job.ntris + 127) / 128), 128, 0, s>>>(job.tri, job.ntris, job, sc, d_status);
         raster_bin<<<bin_blocks, 128, 0, s>>>(job.ntris, sc, tiles_x, d_status, 0);
-        note_launches(2);
+        raster_bin_big<<<kBigBlocks, 256, 0, s>>>(sc, tiles_x, d_status, 0);
+        note_launches(3);
     }
     int rc = exclusive_scan(sc.tile_count, ntiles, sc.tile_start, sc.total, sc.scan_tmp, s);
     if (rc) return rc;
     if (job.ntris) {
         raster_bin<<<bin_blocks, 128, 0, s>>>(job.ntris, sc, tiles_x, d_status, 1);
-        note_launches(1);
+        raster_bin_big<<<kBigBlocks, 256, 0, s>>>(sc, tiles_x, d_status, 1);
+        note_launches(2);
     }
     raster_tiles<<<ntiles, 256, 0, s>>>(sc, tiles_x, job.width, job.height, job.keys);
     note_launches(1);

@@ -63,10 +63,11 @@ struct LevelTab {
 };
 
 // 8-tap trilinear sample of one volume of level l (d voxels per axis) at x (L0 voxel units); taps outside the
-// volume read zero.  Brick addresses are built per axis: the Morton bits of the two brick coordinates and the
-// in-brick offsets of the two tap coordinates are computed once and OR-ed per tap.
-__device__ __forceinline__ float4 tri_sample(const void* base, uint32_t format, int d, uint32_t l, uint64_t vol_off,
-                                             float3 x) {
+// volume read zero.  Interior samples (all taps inside) address the seven other taps from the first one with
+// one delta per axis: +1 / +8 / +64 inside a brick, or the Morton step to the next brick when the tap crosses a
+// brick face.  Samples touching the border take the general path with a validity test per tap.
+template <int FMT>
+__device__ __forceinline__ float4 tri_sample(const void* base, int d, uint32_t l, uint64_t vol_off, float3 x) {
     const float s = __int_as_float((127 - int(l)) << 23);  // 2^-l
     const float u[3] = {x.x * s - 0.5f, x.y * s - 0.5f, x.z * s - 0.5f};
     int c0[3];
@@ -77,7 +78,50 @@ __device__ __forceinline__ float4 tri_sample(const void* base, uint32_t format, 
         c0[a] = int(fl);
         f[a] = u[a] - fl;
     }
-    // per axis and tap (0, 1): validity, high (Morton) part, low (in-brick / linear) part
+    const float wx[2] = {1.0f - f[0], f[0]}, wy[2] = {1.0f - f[1], f[1]}, wz[2] = {1.0f - f[2], f[2]};
+    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+    const unsigned lim = unsigned(d - 1);
+    if (unsigned(c0[0]) < lim && unsigned(c0[1]) < lim && unsigned(c0[2]) < lim) {
+        int64_t i0, dx, dy, dz;
+        if (d >= 8) {
+            uint32_t hs[3];
+            int64_t del[3];
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                uint32_t b = uint32_t(c0[a]) >> 3;
+                hs[a] = part1by2(b);
+                const int64_t step_in = int64_t(1) << (3 * a);
+                // crossing the brick face: local coordinate 7 -> 0 and the Morton code steps along axis a
+                const int64_t cross = (int64_t(part1by2(b + 1) - hs[a]) << (9 + a)) - 7 * step_in;
+                del[a] = (c0[a] & 7) != 7 ? step_in : cross;
+            }
+            i0 = (int64_t(hs[0] | (hs[1] << 1) | (hs[2] << 2)) << 9) |
+                 ((c0[2] & 7) << 6) | ((c0[1] & 7) << 3) | (c0[0] & 7);
+            dx = del[0], dy = del[1], dz = del[2];
+        } else {
+            i0 = (int64_t(c0[2]) * d + c0[1]) * d + c0[0];
+            dx = 1, dy = d, dz = int64_t(d) * d;
+        }
+        const int64_t ib = int64_t(vol_off) + i0;
+#pragma unroll
+        for (int tz = 0; tz < 2; ++tz)
+#pragma unroll
+            for (int ty = 0; ty < 2; ++ty) {
+                const float wyz = wy[ty] * wz[tz];
+                const int64_t row = ib + (tz ? dz : 0) + (ty ? dy : 0);
+#pragma unroll
+                for (int tx = 0; tx < 2; ++tx) {
+                    float4 v = load_vox(base, FMT, uint64_t(row + (tx ? dx : 0)));
+                    float w = wx[tx] * wyz;
+                    acc.x += w * v.x;
+                    acc.y += w * v.y;
+                    acc.z += w * v.z;
+                    acc.w += w * v.w;
+                }
+            }
+        return acc;
+    }
+    // border: per-axis validity, high (Morton) and low (in-brick / linear) address parts
     bool ok[3][2];
     uint32_t hi[3][2], lo[3][2];
     const bool bricked = d >= 8;
@@ -96,8 +140,6 @@ __device__ __forceinline__ float4 tri_sample(const void* base, uint32_t format, 
                 lo[a][t] = a == 0 ? cu : (a == 1 ? cu * uint32_t(d) : cu * uint32_t(d * d));
             }
         }
-    const float wx[2] = {1.0f - f[0], f[0]}, wy[2] = {1.0f - f[1], f[1]}, wz[2] = {1.0f - f[2], f[2]};
-    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
     for (int tz = 0; tz < 2; ++tz)
 #pragma unroll
@@ -107,7 +149,7 @@ __device__ __forceinline__ float4 tri_sample(const void* base, uint32_t format, 
             for (int tx = 0; tx < 2; ++tx) {
                 if (ok[0][tx] && ok[1][ty] && ok[2][tz]) {
                     uint64_t idx = (uint64_t(hi[0][tx] | hi[1][ty] | hi[2][tz]) << 9) | (lo[0][tx] | lo[1][ty] | lo[2][tz]);
-                    float4 v = load_vox(base, format, vol_off + idx);
+                    float4 v = load_vox(base, FMT, vol_off + idx);
                     float w = wx[tx] * wyz;
                     acc.x += w * v.x;
                     acc.y += w * v.y;
@@ -119,16 +161,17 @@ __device__ __forceinline__ float4 tri_sample(const void* base, uint32_t format, 
     return acc;
 }
 
+template <int FMT, bool ANISO>
 __device__ __forceinline__ float4 level_sample(const ChainLayout& c, const LevelTab& lt, uint32_t l, float3 x,
                                                float3 dir) {
     const int d = int(c.dim >> l);
-    if (!c.aniso || l == 0) return tri_sample(c.base, c.format, d, l, lt.off[l], x);
+    if (!ANISO || l == 0) return tri_sample<FMT>(c.base, d, l, lt.off[l], x);
     float w[3] = {dir.x * dir.x, dir.y * dir.y, dir.z * dir.z};
     int sel[3] = {dir.x >= 0.0f ? 0 : 1, dir.y >= 0.0f ? 2 : 3, dir.z >= 0.0f ? 4 : 5};
     float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
-        float4 s = tri_sample(c.base, c.format, d, l, lt.off[l] + uint64_t(sel[a]) * lt.vol[l], x);
+        float4 s = tri_sample<FMT>(c.base, d, l, lt.off[l] + uint64_t(sel[a]) * lt.vol[l], x);
         acc.x += w[a] * s.x;
         acc.y += w[a] * s.y;
         acc.z += w[a] * s.z;
@@ -137,6 +180,7 @@ __device__ __forceinline__ float4 level_sample(const ChainLayout& c, const Level
     return acc;
 }
 
+template <int FMT, bool ANISO>
 __device__ float4 cone(const ChainLayout& c, const LevelTab& lt, const TraceConsts& tc, float3 o, float3 dir,
                        float tan_half) {
     float cr = 0.f, cg = 0.f, cb = 0.f, alpha = 0.f;
@@ -152,9 +196,9 @@ __device__ float4 cone(const ChainLayout& c, const LevelTab& lt, const TraceCons
         float fl = floorf(lvl);
         uint32_t l0 = uint32_t(fl);
         float f = lvl - fl;
-        float4 s = level_sample(c, lt, l0, x, dir);
+        float4 s = level_sample<FMT, ANISO>(c, lt, l0, x, dir);
         if (f > 0.0f && l0 + 1 < c.levels) {
-            float4 s1 = level_sample(c, lt, l0 + 1, x, dir);
+            float4 s1 = level_sample<FMT, ANISO>(c, lt, l0 + 1, x, dir);
             s.x = s.x + f * (s1.x - s.x);
             s.y = s.y + f * (s1.y - s.y);
             s.z = s.z + f * (s1.z - s.z);
@@ -183,6 +227,7 @@ __device__ __forceinline__ void store_out(void* out, uint32_t fmt, uint64_t i, f
     }
 }
 
+template <int FMT, bool ANISO>
 __device__ void trace_pixel(const ChainLayout& c, const LevelTab& lt, const TraceConsts& tc, const TraceView& v,
                             float3 org, float inv_vs, uint32_t px, uint32_t py) {
     const uint64_t npix = uint64_t(v.width) * v.height;
@@ -213,21 +258,21 @@ __device__ void trace_pixel(const ChainLayout& c, const LevelTab& lt, const Trac
     coord_space(nw, bx, by, bz);
     float4 acc;
     if (tc.p.diffuse_cones >= 5) {
-        float4 c0 = cone(c, lt, tc, o, bz, tc.p.diffuse_tan_half);
+        float4 c0 = cone<FMT, ANISO>(c, lt, tc, o, bz, tc.p.diffuse_tan_half);
         acc = make_float4(0.25f * c0.x, 0.25f * c0.y, 0.25f * c0.z, 0.25f * c0.w);
         const float cphi[4] = {1.f, 0.f, -1.f, 0.f}, sphi[4] = {0.f, 1.f, 0.f, -1.f};
 #pragma unroll 1
         for (int k = 0; k < 4; ++k) {
             float3 side = add3(mul3(bx, cphi[k]), mul3(by, sphi[k]));
             float3 dir = norm3(add3(mul3(bz, tc.cos_tilt), mul3(side, tc.sin_tilt)));
-            float4 ck = cone(c, lt, tc, o, dir, tc.p.diffuse_tan_half);
+            float4 ck = cone<FMT, ANISO>(c, lt, tc, o, dir, tc.p.diffuse_tan_half);
             acc.x += 0.1875f * ck.x;
             acc.y += 0.1875f * ck.y;
             acc.z += 0.1875f * ck.z;
             acc.w += 0.1875f * ck.w;
         }
     } else {
-        acc = cone(c, lt, tc, o, bz, tc.p.diffuse_tan_half);
+        acc = cone<FMT, ANISO>(c, lt, tc, o, bz, tc.p.diffuse_tan_half);
     }
     store_out(v.out, v.out_format, pi, acc);
     float4 sp = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -236,12 +281,13 @@ __device__ void trace_pixel(const ChainLayout& c, const LevelTab& lt, const Trac
         float dn = dot3(vd, nw);
         float3 rd = norm3(sub3(vd, mul3(nw, 2.0f * dn)));
         float th = fmaxf(rough, tc.p.min_spec_tan_half);
-        sp = cone(c, lt, tc, o, rd, th);
+        sp = cone<FMT, ANISO>(c, lt, tc, o, rd, th);
     }
     store_out(v.out, v.out_format, npix + pi, sp);
 }
 
 // One CTA = one 16x8 pixel tile of one view; tiles of all views are enumerated in view order.
+template <int FMT, bool ANISO>
 __global__ void __launch_bounds__(128, 4) trace_kernel(ChainLayout c, TraceConsts tc, const f184gi_grid_frame* __restrict__ fr,
                                                     const TraceView* __restrict__ views,
                                                     const uint32_t* __restrict__ tile_base, uint32_t nviews) {
@@ -263,7 +309,7 @@ __global__ void __launch_bounds__(128, 4) trace_kernel(ChainLayout c, TraceConst
     // world -> L0 voxel units: (p - origin) * (inv_voxel_fixed / 256), all scalings exact
     float3 org = f3(float(fr->origin[0]), float(fr->origin[1]), float(fr->origin[2]));
     float inv_vs = float(fr->inv_voxel_fixed * (1.0 / 256.0));
-    trace_pixel(c, lt, tc, v, org, inv_vs, px, py);
+    trace_pixel<FMT, ANISO>(c, lt, tc, v, org, inv_vs, px, py);
 }
 
 }  // namespace
@@ -292,7 +338,15 @@ int trace_launch(const ChainLayout& c, const TraceConsts& tc, const f184gi_grid_
     if (e != cudaSuccess) return cuda_fail(e, "trace: view table sync");
     const TraceView* dv = static_cast<const TraceView*>(scratch);
     const uint32_t* db = reinterpret_cast<const uint32_t*>(static_cast<const unsigned char*>(scratch) + size_t(nviews) * sizeof(TraceView));
-    trace_kernel<<<tiles, 128, 0, s>>>(c, tc, d_frame, dv, db, nviews);
+    // one instantiation per storage format and mip kind keeps each kernel's code small (instruction cache)
+    if (c.format == F184GI_FMT_F32 && !c.aniso)
+        trace_kernel<F184GI_FMT_F32, false><<<tiles, 128, 0, s>>>(c, tc, d_frame, dv, db, nviews);
+    else if (c.format == F184GI_FMT_F32)
+        trace_kernel<F184GI_FMT_F32, true><<<tiles, 128, 0, s>>>(c, tc, d_frame, dv, db, nviews);
+    else if (!c.aniso)
+        trace_kernel<F184GI_FMT_F16, false><<<tiles, 128, 0, s>>>(c, tc, d_frame, dv, db, nviews);
+    else
+        trace_kernel<F184GI_FMT_F16, true><<<tiles, 128, 0, s>>>(c, tc, d_frame, dv, db, nviews);
     note_launches(1);
     return cuda_fail(cudaGetLastError(), "trace");
 }

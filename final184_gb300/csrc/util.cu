@@ -191,3 +191,31 @@ int read_level_launch(const ChainLayout& c, uint32_t level, uint32_t dir, float*
 }
 
 }  // namespace f184
+
+// ---------------- instance transform (tc::Matrix3x4 applied to object-space triangles) ----------------
+namespace f184 {
+namespace {
+struct Mat34 {
+    float m[12];
+};
+__global__ void transform_kernel(const float* __restrict__ src, uint64_t nverts, Mat34 M, float* __restrict__ dst) {
+    uint64_t v = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (v >= nverts) return;
+    float x = src[v * 3], y = src[v * 3 + 1], z = src[v * 3 + 2];
+    for (int r = 0; r < 3; ++r)
+        dst[v * 3 + r] = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(M.m[r * 4], x), __fmul_rn(M.m[r * 4 + 1], y)),
+                                             __fmul_rn(M.m[r * 4 + 2], z)),
+                                   M.m[r * 4 + 3]);
+}
+}  // namespace
+
+int transform_launch(const float* src, uint64_t ntris, const float model[12], float* dst, cudaStream_t s) {
+    Mat34 M;
+    for (int i = 0; i < 12; ++i) M.m[i] = model[i];
+    uint64_t nv = ntris * 3;
+    if (nv == 0) return F184GI_OK;
+    transform_kernel<<<uint32_t((nv + 255) / 256), 256, 0, s>>>(src, nv, M, dst);
+    note_launches(1);
+    return cuda_fail(cudaGetLastError(), "transform");
+}
+}  // namespace f184

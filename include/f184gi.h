@@ -181,6 +181,12 @@ void f184gi_cone_params_default(f184gi_cone_params* p);
 
 /* ---- supporting passes ---- */
 
+/* world_xyz = model * obj_xyz for ntris triangles (9 floats each, device buffers), model = a row-major 3x4
+ * matrix in the layout of tc::Matrix3x4 (Math/Matrix3x4.h).  This is the per-primitive ModelMat transform the
+ * reference applies in its voxelization geometry stage (Pipelang/Internal/main.lua:94-98, 130-131). */
+int f184gi_transform(f184gi_ctx* ctx, const float* obj_xyz, uint64_t ntris, const float model[12], float* world_xyz,
+                     void* stream);
+
 /* Rasterize a G-buffer for one camera (the reference's GBufferRenderer pass,
  * Foreground/Renderer/GBufferRenderer.cpp:79-116 with main.lua:32-58,227-240): flat face normals facing the
  * camera, per-triangle roughness (device FP32), depth of view->proj.  Writes view->depth/normal/roughness
