@@ -351,6 +351,138 @@ def run_gpu(args, cfg):
     return line, sc
 
 
+SERVED = dict(scenes=[(128, 7, 100000, 400), (128, 7, 200000, 800), (256, 8, 300000, 1200), (256, 8, 500000, 2000)],
+              requests=120, rate=200.0, max_moved=0.05, views=(1, 16), sizes=((512, 512), (1920, 1080)),
+              shadow_res=2048, seed=4242, budget=120 << 30)
+
+
+def run_served(args, cfg=SERVED):
+    """Served form vs the plain per-request path on the same seeded request stream (one GPU)."""
+    import threading
+
+    import numpy as np
+    import torch
+
+    import final184_gb300 as g
+
+    rng = np.random.default_rng(cfg["seed"])
+    dev = torch.device("cuda", 0)
+    scenes, pools = [], []
+    gi = g.VoxelGI(0)
+    for k, (dim, levels, ntris, nobj) in enumerate(cfg["scenes"]):
+        sc = g.SyntheticScene(cfg["seed"] + 100 * k, ntris, nobj)
+        scenes.append((sc, dim, levels))
+        tri = torch.from_numpy(sc.tri_xyz).to(dev)
+        rough = torch.from_numpy(sc.roughness).to(dev)
+        pool = []
+        for v in range(8):  # G-buffers of 8 cameras per scene (inputs of the trace)
+            (w0, h0), (w1, h1) = cfg["sizes"]
+            t = rng.uniform(0, 1)
+            W, H = int(w0 + t * (w1 - w0)) // 8 * 8, int(h0 + t * (h1 - h0)) // 8 * 8
+            eye, tgt = sc.camera(v)
+            V, P = g.look_at(eye, tgt), g.perspective(59.0, W / H, 0.1, 100.0)
+            n = W * H
+            bufs = (torch.empty(n, dtype=torch.float32, device=dev), torch.empty(n, dtype=torch.int32, device=dev),
+                    torch.empty(n, dtype=torch.int16, device=dev))
+            view = g.make_view(V, P, W, H, bufs[0].data_ptr(), bufs[1].data_ptr(), bufs[2].data_ptr(), 0)
+            gi.gbuffer(tri.data_ptr(), rough.data_ptr(), sc.ntris, view)
+            pool.append((V, P, W, H, bufs))
+        pools.append(pool)
+    gi.sync()
+    # the request stream: Poisson arrivals, 0..5% of a scene's objects moved, 1..16 views
+    reqs, t = [], 0.0
+    for i in range(cfg["requests"]):
+        t += rng.exponential(1.0 / cfg["rate"])
+        si = int(rng.integers(0, len(scenes)))
+        sc = scenes[si][0]
+        nmov = int(rng.integers(0, int(cfg["max_moved"] * (sc.nobjects - 1)) + 1))
+        moves = []
+        for o in rng.choice(np.arange(1, sc.nobjects), nmov, replace=False):
+            moves.append((int(sc.object_first[o]), int(sc.object_count[o]),
+                          [float(x) for x in rng.uniform(-0.2, 0.2, 3).astype(np.float32)]))
+        nv = int(rng.integers(cfg["views"][0], cfg["views"][1] + 1))
+        vids = [int(x) for x in rng.integers(0, 8, nv)]
+        reqs.append((t, si, moves, vids))
+    pixels = sum(pools[si][v][2] * pools[si][v][3] for _, si, _, vids in reqs for v in vids)
+    max_px = max(p[2] * p[3] for pool in pools for p in pool)
+    outs = [torch.empty(2 * max_px * 4, dtype=torch.float16, device=dev) for _ in range(16)]
+
+    def views_for(si, vids, fmt):
+        vs = []
+        for j, v in enumerate(vids):
+            V, P, W, H, b = pools[si][v]
+            vs.append(g.make_view(V, P, W, H, b[0].data_ptr(), b[1].data_ptr(), b[2].data_ptr(), outs[j].data_ptr(),
+                                  fmt))
+        return vs
+
+    # ---- served: FP16 grids with resident weights, continuous batching, arrivals in real time ----
+    srv = g.Server(0, slots=2, max_batch_views=64, hbm_budget=cfg["budget"])
+    for k, (sc, dim, levels) in enumerate(scenes):
+        srv.add_scene(k, g.GridDesc(dim, levels, g.FMT_F16, 0, cfg["shadow_res"], 0), sc.tri_xyz, sc.albedo,
+                      sc.bounds, sc.light)
+    tickets = [None] * len(reqs)
+
+    def submitter():
+        t0 = time.perf_counter()
+        for i, (ta, si, moves, vids) in enumerate(reqs):
+            d = ta - (time.perf_counter() - t0)
+            if d > 0:
+                time.sleep(d)
+            tickets[i] = srv.submit(si, views_for(si, vids, g.FMT_F16), moves)
+
+    w0 = time.perf_counter()
+    th = threading.Thread(target=submitter)
+    th.start()
+    th.join()
+    for tk in tickets:
+        srv.wait(tk)
+    served_s = time.perf_counter() - w0
+    st = srv.stats()
+    srv.close()
+    # ---- plain: the same stream back to back, one request at a time, FP32 grids, full voxelization ----
+    plain_lat = []
+    geo = [sc.tri_xyz.copy() for sc, _, _ in scenes]
+    grids = [gi.create_grid(dim, levels, g.FMT_F32, 0, cfg["shadow_res"]) for _, dim, levels in scenes]
+    dtri = [torch.from_numpy(x).to(dev) for x in geo]
+    dalb = [torch.from_numpy(sc.albedo.view(np.int32)).to(dev) for sc, _, _ in scenes]
+    outs = [torch.empty(2 * max_px * 4, dtype=torch.float32, device=dev) for _ in range(16)]
+    torch.cuda.synchronize()
+    p0 = time.perf_counter()
+    for ta, si, moves, vids in reqs:
+        r0 = time.perf_counter()
+        sc = scenes[si][0]
+        for f, c, off in moves:  # the caller moves its geometry and re-uploads it
+            seg = geo[si][f * 9:(f + c) * 9].reshape(-1, 3)
+            seg += np.asarray(off, dtype=np.float32)
+        dtri[si].copy_(torch.from_numpy(geo[si]))
+        gi.voxelize(grids[si], dtri[si].data_ptr(), dalb[si].data_ptr(), sc.ntris, sc.light, bounds=sc.bounds)
+        gi.mip(grids[si])
+        for v in views_for(si, vids, g.FMT_F32):
+            gi.trace(grids[si], [v])
+        gi.sync()
+        plain_lat.append((time.perf_counter() - r0) * 1e3)
+    plain_s = time.perf_counter() - p0
+    gi.close()
+    plain_lat.sort()
+    served_mpix = pixels / served_s / 1e6
+    plain_mpix = pixels / plain_s / 1e6
+    return {
+        "workload": "%d requests, Poisson arrivals at %.0f req/s, 0-5%% of a scene's objects moved, 1-16 views of "
+                    "512x512..1920x1080 on resident grids %s, %.0f GB admission budget"
+                    % (len(reqs), cfg["rate"], "/".join("%d^3:%dk" % (d, n // 1000) for d, _, n, _ in cfg["scenes"]),
+                       cfg["budget"] / 2 ** 30),
+        "pixels": int(pixels),
+        "served": {"value": round(served_mpix, 2), "unit": "Mpix/s", "p50_ms": round(st.p50_ms, 2),
+                   "p99_ms": round(st.p99_ms, 2), "batches": int(st.batches),
+                   "mean_batch_views": round(st.mean_batch_views, 2), "wall_s": round(served_s, 3),
+                   "storage": "fp16, resident weights + dirty-brick re-voxelization"},
+        "plain": {"value": round(plain_mpix, 2), "unit": "Mpix/s", "p50_ms": round(plain_lat[len(plain_lat) // 2], 2),
+                  "p99_ms": round(plain_lat[min(len(plain_lat) - 1, int(0.99 * len(plain_lat)))], 2),
+                  "wall_s": round(plain_s, 3), "storage": "fp32, full voxelization per request, one launch per view"},
+        "served_over_plain": round(served_mpix / plain_mpix, 3),
+    }
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -359,6 +491,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--small", action="store_true", help="the 20k-triangle 64^3 640x360 case (profiling)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-served", action="store_true", help="skip the served-vs-plain request stream")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     cfg = SMALL if args.small else PLAIN_LARGE
@@ -384,6 +517,8 @@ def main():
             "sample": "full shadow raster + voxelization + mip chain on the CPU (%.1f s), cone trace of %d of %d rows "
                       "(%.1f s) scaled to the full image; FP32 restatement, std::thread over all cores"
                       % (info["voxelize_mip_s"], info["trace_rows"], cfg["height"], info["trace_s"])}
+    if rank == 0 and world == 1 and not args.no_served and not args.small:
+        line["served"] = run_served(args)
     if rank == 0:
         print(json.dumps(line), flush=True)
 

@@ -236,3 +236,56 @@ def make_view(view_m, proj_m, width, height, depth_ptr, normal_ptr, rough_ptr, o
     v.depth, v.normal, v.roughness, v.out = depth_ptr, normal_ptr, rough_ptr, out_ptr
     v.out_format = out_format
     return v
+
+
+class Server:
+    """Continuous-batching request server over device-resident scenes (f184gi_server_*)."""
+
+    def __init__(self, device=0, slots=2, max_batch_views=64, blocks_per_sm=0, hbm_budget=0, cone=None):
+        self.lib = load()
+        cfg = _abi.ServerConfig(device, slots, max_batch_views, blocks_per_sm, hbm_budget,
+                                cone if cone is not None else _abi.ConeParams())
+        h = C.c_void_p()
+        check(self.lib.f184gi_server_create(C.byref(cfg), C.byref(h)))
+        self.h = h
+        self._keep = {}
+
+    def add_scene(self, scene_id, desc, tri_xyz, albedo, bounds, light):
+        tri = np.ascontiguousarray(tri_xyz, dtype=np.float32)
+        alb = np.ascontiguousarray(albedo, dtype=np.uint32)
+        check(self.lib.f184gi_server_add_scene(self.h, scene_id, C.byref(desc), tri.ctypes.data, alb.ctypes.data,
+                                               tri.size // 9, C.byref(bounds), C.byref(light)))
+
+    def submit(self, scene_id, views, moves=(), host_buffers=False):
+        mv = (_abi.Move * max(1, len(moves)))(*[_abi.Move(int(f), int(c), (C.c_float * 3)(*o)) for f, c, o in moves])
+        vw = (View * len(views))(*views)
+        req = _abi.Request(scene_id, _abi.REQ_HOST_BUFFERS if host_buffers else 0, mv, len(moves), len(views), vw)
+        t = C.c_uint64()
+        check(self.lib.f184gi_server_submit(self.h, C.byref(req), C.byref(t)))
+        return t.value
+
+    def wait(self, ticket, timeout_ms=0):
+        r = _abi.RequestResult()
+        rc = self.lib.f184gi_server_wait(self.h, ticket, timeout_ms, C.byref(r))
+        if rc != _abi.OK:
+            raise F184Error(rc, self.lib.f184gi_last_error().decode())
+        return r
+
+    def cancel(self, ticket):
+        check(self.lib.f184gi_server_cancel(self.h, ticket))
+
+    def stats(self):
+        st = _abi.ServerStats()
+        check(self.lib.f184gi_server_get_stats(self.h, C.byref(st)))
+        return st
+
+    def close(self):
+        if self.h:
+            check(self.lib.f184gi_server_destroy(self.h))
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

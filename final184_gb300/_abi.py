@@ -11,6 +11,7 @@ LIB_PATH = os.path.join(HERE, "libf184gi.so")
 FMT_F32 = 0
 FMT_F16 = 1
 GRID_KEEP_COUNTS = 1
+GRID_RESIDENT_WEIGHTS = 2
 
 OK = 0
 ERR_INVALID = -1
@@ -21,6 +22,7 @@ ERR_OVERFLOW = -5
 ERR_TIMEOUT = -6
 ERR_NOTFOUND = -7
 ERR_CANCELLED = -8
+REQ_HOST_BUFFERS = 1
 
 
 class Vec3(C.Structure):
@@ -59,6 +61,32 @@ class ConeParams(C.Structure):
                 ("pad", C.c_uint32)]
 
 
+class Move(C.Structure):
+    _fields_ = [("first", C.c_uint32), ("count", C.c_uint32), ("offset", C.c_float * 3)]
+
+
+class ServerConfig(C.Structure):
+    _fields_ = [("device", C.c_int), ("slots", C.c_uint32), ("max_batch_views", C.c_uint32),
+                ("blocks_per_sm", C.c_uint32), ("hbm_budget", C.c_uint64), ("cone", ConeParams)]
+
+
+class Request(C.Structure):
+    _fields_ = [("scene_id", C.c_uint32), ("flags", C.c_uint32), ("moves", C.POINTER(Move)), ("nmoves", C.c_uint32),
+                ("nviews", C.c_uint32), ("views", C.POINTER(View))]
+
+
+class RequestResult(C.Structure):
+    _fields_ = [("status", C.c_int), ("batch", C.c_uint32), ("queued_ms", C.c_double), ("latency_ms", C.c_double),
+                ("pixels", C.c_uint64)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("requests_done", C.c_uint64), ("requests_cancelled", C.c_uint64), ("batches", C.c_uint64),
+                ("pixels", C.c_uint64), ("p50_ms", C.c_double), ("p99_ms", C.c_double), ("mean_ms", C.c_double),
+                ("mean_batch_views", C.c_double), ("hbm_used", C.c_uint64), ("hbm_budget", C.c_uint64),
+                ("pending", C.c_uint32), ("inflight", C.c_uint32)]
+
+
 class Config(C.Structure):
     _fields_ = [("device", C.c_int), ("flags", C.c_uint32), ("hbm_budget", C.c_uint64)]
 
@@ -94,6 +122,7 @@ PROTOTYPES = {
     "f184gi_cone_params_default": (None, [C.POINTER(ConeParams)]),
     "f184gi_gbuffer": (C.c_int, [P, P, P, U64, C.POINTER(View), P, P]),
     "f184gi_transform": (C.c_int, [P, P, U64, PF, P, P]),
+    "f184gi_apply_moves": (C.c_int, [P, P, C.POINTER(Move), U32, U64, P]),
     "f184gi_sync": (C.c_int, [P, P]),
     "f184gi_grid_get_frame": (C.c_int, [P, U32, C.POINTER(GridFrame)]),
     "f184gi_frame_from_bounds": (C.c_int, [C.POINTER(Bounds), U32, PF, C.POINTER(GridFrame)]),
@@ -105,6 +134,13 @@ PROTOTYPES = {
     "f184gi_camera_ortho": (None, [F32, F32, F32, F32, PF]),
     "f184gi_camera_look_at": (None, [PF, PF, PF]),
     "f184gi_mat4_inverse": (C.c_int, [PF, PF]),
+    "f184gi_server_create": (C.c_int, [C.POINTER(ServerConfig), C.POINTER(P)]),
+    "f184gi_server_destroy": (C.c_int, [P]),
+    "f184gi_server_add_scene": (C.c_int, [P, U32, C.POINTER(GridDesc), P, P, U64, C.POINTER(Bounds), C.POINTER(Light)]),
+    "f184gi_server_submit": (C.c_int, [P, C.POINTER(Request), C.POINTER(U64)]),
+    "f184gi_server_wait": (C.c_int, [P, U64, U32, C.POINTER(RequestResult)]),
+    "f184gi_server_cancel": (C.c_int, [P, U64]),
+    "f184gi_server_get_stats": (C.c_int, [P, C.POINTER(ServerStats)]),
     "f184gi_scene_generate": (C.c_int, [U64, U64, U32, C.POINTER(C.POINTER(Scene))]),
     "f184gi_scene_free": (None, [C.POINTER(Scene)]),
     "f184gi_scene_move_objects": (C.c_int, [C.POINTER(Scene), U64, F32, F32, C.POINTER(U32), C.POINTER(U32)]),

@@ -17,7 +17,7 @@ NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_SOURCES = ["util.cu", "raster.cu", "voxelize.cu", "mip.cu", "trace.cu"]
-CPP_SOURCES = ["api.cpp", "scene.cpp"]
+CPP_SOURCES = ["api.cpp", "scene.cpp", "serve.cpp"]
 
 
 def _run(cmd):

@@ -78,6 +78,8 @@ struct GridObj {
     size_t shadow_bytes = 0;
     uint32_t* counts = nullptr;
     size_t counts_bytes = 0;
+    float4* weights = nullptr;  // resident mean injection weights (F184GI_GRID_RESIDENT_WEIGHTS)
+    size_t weights_bytes = 0;
     f184gi_grid_frame* d_frame = nullptr;
     bool voxelized = false;
 };
@@ -225,6 +227,7 @@ int f184gi_destroy(f184gi_ctx* c) {
         dev_free(c, g.chain.base, g.chain_bytes);
         dev_free(c, g.shadow, g.shadow_bytes);
         dev_free(c, g.counts, g.counts_bytes);
+        dev_free(c, g.weights, g.weights_bytes);
         dev_free(c, g.d_frame, sizeof(f184gi_grid_frame));
     }
     for (Scratch* s : {&c->raster, &c->vox, &c->trace, &c->misc, &c->keys}) dev_free(c, s->ptr, s->bytes);
@@ -246,6 +249,7 @@ int f184gi_grid_bytes(const f184gi_grid_desc* d, uint64_t* bytes) {
     uint64_t esz = d->format == F184GI_FMT_F32 ? 16 : 8;
     uint64_t b = chain_elems(*d) * esz + uint64_t(d->shadow_res) * d->shadow_res * 8 + sizeof(f184gi_grid_frame);
     if (d->flags & F184GI_GRID_KEEP_COUNTS) b += uint64_t(d->dim) * d->dim * d->dim * 4;
+    if (d->flags & F184GI_GRID_RESIDENT_WEIGHTS) b += uint64_t(d->dim) * d->dim * d->dim * 16;
     *bytes = b;
     return F184GI_OK;
 }
@@ -287,6 +291,19 @@ int f184gi_grid_create(f184gi_ctx* c, const f184gi_grid_desc* d, uint32_t* grid)
         g.counts = static_cast<uint32_t*>(cp);
         cudaMemset(g.counts, 0, g.counts_bytes);
     }
+    if (d->flags & F184GI_GRID_RESIDENT_WEIGHTS) {
+        g.weights_bytes = size_t(d->dim) * d->dim * d->dim * 16;
+        void* wp = nullptr;
+        if ((rc = dev_alloc(c, &wp, g.weights_bytes))) {
+            dev_free(c, base, g.chain_bytes);
+            dev_free(c, sh, g.shadow_bytes);
+            dev_free(c, fr, sizeof(f184gi_grid_frame));
+            dev_free(c, g.counts, g.counts_bytes);
+            return rc;
+        }
+        g.weights = static_cast<float4*>(wp);
+        cudaMemset(g.weights, 0, g.weights_bytes);
+    }
     cudaMemset(base, 0, g.chain_bytes);
     cudaMemset(fr, 0, sizeof(f184gi_grid_frame));
     uint32_t id = c->next_id++;
@@ -303,6 +320,7 @@ int f184gi_grid_destroy(f184gi_ctx* c, uint32_t grid) {
     dev_free(c, g->chain.base, g->chain_bytes);
     dev_free(c, g->shadow, g->shadow_bytes);
     dev_free(c, g->counts, g->counts_bytes);
+    dev_free(c, g->weights, g->weights_bytes);
     dev_free(c, g->d_frame, sizeof(f184gi_grid_frame));
     c->grids.erase(grid);
     return F184GI_OK;
@@ -346,10 +364,24 @@ int f184gi_voxelize(f184gi_ctx* c, uint32_t grid, const float* tri, const uint32
     vj.counts = g->counts;
     vj.dirty_bricks = dirty;
     vj.ndirty = ndirty;
+    if (g->weights && ndirty && !g->voxelized)
+        return fail(F184GI_ERR_INVALID, "voxelize: a dirty-brick update needs one full voxelization first");
+    vj.weights = g->weights;
     if ((rc = scratch_get(c, c->vox, voxelize_scratch_bytes(ntris, d.dim)))) return rc;
     if ((rc = voxelize_launch(vj, c->vox.ptr, c->vox.bytes, c->d_status, s))) return rc;
+    if (g->weights && (rc = relight_launch(g->weights, g->d_frame, g->chain, *light, g->shadow, d.shadow_res, s)))
+        return rc;
     g->voxelized = true;
     return F184GI_OK;
+}
+
+int f184gi_apply_moves(f184gi_ctx* c, float* tri_xyz, const f184gi_move* moves, uint32_t nmoves, uint64_t ntris,
+                       void* stream) {
+    if (!c || (nmoves && (!moves || !tri_xyz))) return fail(F184GI_ERR_INVALID, "apply_moves: null argument");
+    for (uint32_t i = 0; i < nmoves; ++i)
+        if (uint64_t(moves[i].first) + moves[i].count > ntris)
+            return fail(F184GI_ERR_INVALID, "apply_moves: triangle range out of bounds");
+    return moves_launch(tri_xyz, moves, nmoves, static_cast<cudaStream_t>(stream));
 }
 
 int f184gi_mip(f184gi_ctx* c, uint32_t grid, uint32_t levels, uint32_t anisotropic, void* stream) {
@@ -543,3 +575,15 @@ int f184gi_grid_level_ptr(f184gi_ctx* c, uint32_t grid, uint32_t level, void** p
 }
 
 }  // extern "C"
+
+namespace f184 {
+// Device description of a grid for batched tracing (used by the request server).
+int grid_internal(f184gi_ctx* c, uint32_t grid, ChainLayout* chain, const f184gi_grid_frame** d_frame) {
+    if (!c || !chain || !d_frame) return fail(F184GI_ERR_INVALID, "grid_internal: null argument");
+    GridObj* g = find_grid(c, grid);
+    if (!g) return fail(F184GI_ERR_NOTFOUND, "grid_internal: unknown grid");
+    *chain = g->chain;
+    *d_frame = g->d_frame;
+    return F184GI_OK;
+}
+}  // namespace f184

@@ -75,7 +75,11 @@ struct VoxelizeJob {
     uint32_t* counts;                   // optional (dim^3, linear)
     const uint32_t* dirty_bricks;       // optional list (Morton brick indices of L0)
     uint32_t ndirty;
+    float4* weights;                    // optional: write the mean-weight grid W instead of L0 radiance
 };
+// L0 = luminance * (lit ? W : 0) over the whole grid (after a shadow-map change); W as written by voxelize
+int relight_launch(const float4* weights, const f184gi_grid_frame* d_frame, const ChainLayout& chain,
+                   const f184gi_light& light, const unsigned long long* shadow, uint32_t res, cudaStream_t s);
 size_t voxelize_scratch_bytes(uint64_t ntris, uint32_t dim);
 int voxelize_launch(const VoxelizeJob& job, void* scratch, size_t scratch_bytes, uint32_t* d_status,
                     cudaStream_t s);
@@ -95,6 +99,12 @@ struct TraceView {
     const uint16_t* rough;
     void* out;
     uint32_t out_format;
+    // the grid this view traces (batched launches mix grids)
+    const void* grid_base;
+    uint32_t grid_dim, grid_levels;
+    const f184gi_grid_frame* frame;
+    float tmax;
+    uint64_t off[kMaxLevels], vol[kMaxLevels];
 };
 struct TraceConsts {
     float tmax;
@@ -104,12 +114,32 @@ struct TraceConsts {
 int trace_launch(const ChainLayout& chain, const TraceConsts& tc, const f184gi_grid_frame* d_frame,
                  const TraceView* views, uint32_t nviews, void* scratch, size_t scratch_bytes, cudaStream_t s);
 size_t trace_scratch_bytes(uint32_t nviews);
+// batched tracing: fill a view table on the host (returns the tile count), copy it to the device, launch
+void trace_view_set_grid(TraceView& v, const ChainLayout& c, const f184gi_grid_frame* d_frame, float tmax);
+size_t trace_table_bytes(uint32_t nviews);
+uint32_t trace_fill_table(const TraceView* views, uint32_t nviews, void* host_table);
+int trace_launch_table(uint32_t fmt, bool aniso, const TraceConsts& tc, const void* dev_table, uint32_t nviews,
+                       uint32_t ntiles, uint32_t* work, uint32_t persistent_blocks, cudaStream_t s);
+
+// Batched persistent trace replayed from a CUDA graph: [view table H2D] -> [work counter = 0] -> [kernel].
+struct TraceGraph;
+uint32_t trace_persistent_blocks(uint32_t fmt, bool aniso, uint32_t per_sm);  // per_sm 0 = occupancy maximum
+int trace_graph_create(TraceGraph** out, uint32_t fmt, bool aniso, uint32_t max_views, uint32_t blocks,
+                       const TraceConsts& tc);
+int trace_graph_launch(TraceGraph* g, const TraceView* views, uint32_t nviews, cudaStream_t s);
+void trace_graph_destroy(TraceGraph* g);
+
+// grid of a context as the kernels see it (chain layout and device frame)
+int grid_internal(f184gi_ctx* c, uint32_t grid, ChainLayout* chain, const f184gi_grid_frame** d_frame);
 
 int gbuffer_resolve_launch(const unsigned long long* keys, uint32_t width, uint32_t height, const float* tri,
                            const float* rough, const float view[16], const float eye[3], float* depth,
                            uint32_t* normal, uint16_t* rough_out, uint32_t* tri_out, cudaStream_t s);
 
 int read_level_launch(const ChainLayout& chain, uint32_t level, uint32_t dir, float* d_out, cudaStream_t s);
+
+// translate triangle ranges (FP32 adds, the same rounding as a host-side mirror)
+int moves_launch(float* tri, const f184gi_move* moves, uint32_t nmoves, cudaStream_t s);
 
 // dst = model (row-major 3x4) * src, per vertex; products and sums rounded in order (no FMA)
 int transform_launch(const float* src, uint64_t ntris, const float model[12], float* dst, cudaStream_t s);

@@ -1,0 +1,631 @@
+// serve.cpp -- the served form: continuous batching of GI requests over device-resident scenes.
+//
+// The reference renders one frame at a time from one render thread (App/Game.cpp:248-345, CMegaPipeline::Render);
+// this host runtime instead serves a stream of requests (object moves + view sets) against scenes kept on the
+// device.  A scheduler thread forms batches whenever one of `slots` in-flight batches is free:
+//   - admission: one request per scene per batch (a scene's requests apply in submission order), the HBM budget
+//     for staging of host-buffer requests, at most max_batch_views views;
+//   - per touched scene: rigid moves on the device, dirty bricks from the moved objects' old and new boxes
+//     (computed on a host mirror of the geometry), geometry re-voxelization of those bricks, relight of the grid
+//     from the new shadow map, mip rebuild;
+//   - one persistent trace launch over all views of the batch, replayed from the slot's CUDA graph.
+// A completer thread retires batches in launch order and records per-request latency.  Batches on different
+// slots overlap on the device; requests that arrive meanwhile join the next batch.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <mutex>
+#include <set>
+#include <thread>
+#include <vector>
+
+#include "gi_internal.h"
+
+using namespace f184;
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+double ms_between(Clock::time_point a, Clock::time_point b) {
+    return std::chrono::duration<double, std::milli>(b - a).count();
+}
+
+struct Scene {
+    uint32_t id = 0;
+    f184gi_ctx* ctx = nullptr;
+    uint32_t grid = 0;
+    f184gi_grid_desc desc{};
+    float* d_tri = nullptr;
+    uint32_t* d_alb = nullptr;
+    uint64_t ntris = 0;
+    std::vector<float> h_tri;  // host mirror of the device geometry (same FP32 adds)
+    f184gi_bounds bounds{};
+    f184gi_light light{};
+    f184gi_grid_frame frame{};
+    ChainLayout chain{};
+    const f184gi_grid_frame* d_frame = nullptr;
+    uint32_t* d_dirty = nullptr;
+    uint32_t* h_dirty = nullptr;  // pinned staging of the dirty list
+    uint32_t nbricks = 0;
+    std::vector<uint8_t> flag;
+    bool busy = false;
+    uint64_t bytes = 0;
+};
+
+struct Request {
+    uint64_t ticket = 0;
+    uint32_t scene = 0, flags = 0;
+    std::vector<f184gi_move> moves;
+    std::vector<f184gi_view> views;   // as submitted
+    Clock::time_point t_submit, t_admit, t_done;
+    int status = 0;
+    bool done = false, admitted = false;
+    uint32_t batch = 0;
+    uint64_t pixels = 0, staging = 0;
+    void* d_stage = nullptr;
+};
+
+struct Slot {
+    cudaStream_t stream = nullptr;
+    cudaEvent_t done = nullptr;
+    TraceGraph* graph = nullptr;
+    std::vector<Request*> reqs;
+    std::vector<Scene*> scenes;  // scene of each request, resolved under the server lock
+    std::vector<TraceView> tv;
+    uint32_t batch = 0;
+    bool busy = false;
+};
+
+uint64_t staging_bytes(const f184gi_request& r) {
+    if (!(r.flags & F184GI_REQ_HOST_BUFFERS)) return 0;
+    uint64_t b = 0;
+    for (uint32_t i = 0; i < r.nviews; ++i) {
+        uint64_t n = uint64_t(r.views[i].width) * r.views[i].height;
+        uint64_t out = r.views[i].out_format == F184GI_FMT_F32 ? 32 : 16;
+        b += ((n * (4 + 4 + 2 + out)) + 1023) / 1024 * 1024;
+    }
+    return b;
+}
+
+}  // namespace
+
+struct f184gi_server {
+    f184gi_server_config cfg{};
+    std::mutex mu;
+    std::condition_variable cv_sched, cv_done;
+    std::deque<Request*> pending;
+    std::map<uint64_t, Request*> reqs;
+    std::map<uint32_t, Scene*> scenes;
+    std::vector<Slot> slots;
+    std::deque<int> launched;
+    std::thread sched, completer;
+    bool stop = false;
+    uint64_t next_ticket = 1, generation = 0;
+    uint32_t next_batch = 1;
+    uint64_t hbm_used = 0;
+    int fmt = -1, aniso = -1;
+    TraceConsts tc{};
+    std::vector<double> lat;
+    uint64_t done_n = 0, cancelled = 0, batches = 0, pixels = 0, batch_views = 0;
+};
+
+namespace {
+
+void mark_box(Scene* sc, const float mn[3], const float mx[3]) {
+    const double vs = sc->frame.voxel_size;
+    const int dim = int(sc->desc.dim);
+    int b0[3], b1[3];
+    for (int a = 0; a < 3; ++a) {
+        // conservative: one voxel of margin around the closed box
+        double lo = std::floor((double(mn[a]) - sc->frame.origin[a]) / vs) - 1.0;
+        double hi = std::floor((double(mx[a]) - sc->frame.origin[a]) / vs) + 1.0;
+        int i0 = int(std::max(0.0, std::min(double(dim - 1), lo)));
+        int i1 = int(std::max(0.0, std::min(double(dim - 1), hi)));
+        b0[a] = i0 >> 3, b1[a] = i1 >> 3;
+    }
+    for (int z = b0[2]; z <= b1[2]; ++z)
+        for (int y = b0[1]; y <= b1[1]; ++y)
+            for (int x = b0[0]; x <= b1[0]; ++x) {
+                uint32_t m = 0;
+                for (int bit = 0; bit < 10; ++bit)
+                    m |= (((uint32_t(x) >> bit) & 1u) << (3 * bit)) | (((uint32_t(y) >> bit) & 1u) << (3 * bit + 1)) |
+                         (((uint32_t(z) >> bit) & 1u) << (3 * bit + 2));
+                sc->flag[m] = 1;
+            }
+}
+
+void range_box(const Scene* sc, uint32_t first, uint32_t count, float mn[3], float mx[3]) {
+    for (int a = 0; a < 3; ++a) mn[a] = 1e30f, mx[a] = -1e30f;
+    const float* p = sc->h_tri.data() + uint64_t(first) * 9;
+    for (uint64_t v = 0; v < uint64_t(count) * 3; ++v)
+        for (int a = 0; a < 3; ++a) {
+            mn[a] = std::min(mn[a], p[v * 3 + a]);
+            mx[a] = std::max(mx[a], p[v * 3 + a]);
+        }
+}
+
+// Scene work of one request on `s`: moves, dirty-brick re-voxelization, relight, mips.
+int scene_update(Scene* sc, const Request* r, cudaStream_t s) {
+    if (r->moves.empty()) return F184GI_OK;
+    std::fill(sc->flag.begin(), sc->flag.end(), 0);
+    for (const f184gi_move& m : r->moves) {
+        float mn[3], mx[3];
+        range_box(sc, m.first, m.count, mn, mx);
+        mark_box(sc, mn, mx);
+        float* p = sc->h_tri.data() + uint64_t(m.first) * 9;
+        for (uint64_t v = 0; v < uint64_t(m.count) * 3; ++v)
+            for (int a = 0; a < 3; ++a) p[v * 3 + a] = p[v * 3 + a] + m.offset[a];
+        range_box(sc, m.first, m.count, mn, mx);
+        mark_box(sc, mn, mx);
+    }
+    uint32_t nd = 0;
+    for (uint32_t m = 0; m < sc->nbricks; ++m)
+        if (sc->flag[m]) sc->h_dirty[nd++] = m;
+    int rc = f184gi_apply_moves(sc->ctx, sc->d_tri, r->moves.data(), uint32_t(r->moves.size()), sc->ntris, s);
+    if (rc) return rc;
+    if (nd == 0) return F184GI_OK;
+    cudaError_t e = cudaMemcpyAsync(sc->d_dirty, sc->h_dirty, size_t(nd) * 4, cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) return cuda_fail(e, "server: dirty list");
+    rc = f184gi_voxelize(sc->ctx, sc->grid, sc->d_tri, sc->d_alb, sc->ntris, &sc->bounds, &sc->light, sc->d_dirty, nd, s);
+    if (rc) return rc;
+    return f184gi_mip(sc->ctx, sc->grid, 0, sc->desc.anisotropic, s);
+}
+
+int prepare_view(f184gi_server* S, const Scene* sc, const f184gi_view& v, TraceView& t) {
+    double V[16], P[16], IV[16], IP[16];
+    for (int k = 0; k < 16; ++k) V[k] = v.view[k], P[k] = v.proj[k];
+    if (!invert4(V, IV) || !invert4(P, IP)) return fail(F184GI_ERR_INVALID, "server: singular view or projection");
+    t = TraceView{};
+    for (int k = 0; k < 16; ++k) t.iview[k] = float(IV[k]), t.iproj[k] = float(IP[k]);
+    t.eye[0] = float(IV[3]), t.eye[1] = float(IV[7]), t.eye[2] = float(IV[11]);
+    t.width = v.width, t.height = v.height;
+    t.depth = v.depth, t.normal = v.normal, t.rough = v.roughness, t.out = v.out, t.out_format = v.out_format;
+    float tmax = S->tc.p.max_distance > 0.0f ? S->tc.p.max_distance : float(double(sc->desc.dim) * std::sqrt(3.0));
+    trace_view_set_grid(t, sc->chain, sc->d_frame, tmax);
+    return F184GI_OK;
+}
+
+// Stage host-buffer request inputs on the device (allocation from the stream-ordered pool).
+int stage_in(Request* r, cudaStream_t s) {
+    if (!(r->flags & F184GI_REQ_HOST_BUFFERS)) return F184GI_OK;
+    cudaError_t e = cudaMallocAsync(&r->d_stage, r->staging, s);
+    if (e != cudaSuccess) return cuda_fail(e, "server: staging allocation");
+    unsigned char* p = static_cast<unsigned char*>(r->d_stage);
+    for (f184gi_view& v : r->views) {
+        const uint64_t n = uint64_t(v.width) * v.height;
+        const uint64_t out = v.out_format == F184GI_FMT_F32 ? 32 : 16;
+        unsigned char* d_depth = p;
+        unsigned char* d_norm = d_depth + n * 4;
+        unsigned char* d_rough = d_norm + n * 4;
+        unsigned char* d_out = d_rough + n * 2;
+        p += ((n * (10 + out)) + 1023) / 1024 * 1024;
+        if ((e = cudaMemcpyAsync(d_depth, v.depth, n * 4, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
+            (e = cudaMemcpyAsync(d_norm, v.normal, n * 4, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
+            (e = cudaMemcpyAsync(d_rough, v.roughness, n * 2, cudaMemcpyHostToDevice, s)) != cudaSuccess)
+            return cuda_fail(e, "server: staging copy");
+        v.depth = reinterpret_cast<const float*>(d_depth);
+        v.normal = reinterpret_cast<const uint32_t*>(d_norm);
+        v.roughness = reinterpret_cast<const uint16_t*>(d_rough);
+        (void)out;
+        // keep the caller's host output pointer in `pad`-sized side storage: swap after the trace
+        v.out = d_out;
+    }
+    return F184GI_OK;
+}
+
+int stage_out(Request* r, const std::vector<void*>& host_out, cudaStream_t s) {
+    if (!(r->flags & F184GI_REQ_HOST_BUFFERS)) return F184GI_OK;
+    for (size_t i = 0; i < r->views.size(); ++i) {
+        const f184gi_view& v = r->views[i];
+        const uint64_t n = uint64_t(v.width) * v.height * (v.out_format == F184GI_FMT_F32 ? 32 : 16);
+        cudaError_t e = cudaMemcpyAsync(host_out[i], v.out, n, cudaMemcpyDeviceToHost, s);
+        if (e != cudaSuccess) return cuda_fail(e, "server: result copy");
+    }
+    cudaError_t e = cudaFreeAsync(r->d_stage, s);
+    r->d_stage = nullptr;
+    return cuda_fail(e, "server: staging free");
+}
+
+int issue_batch(f184gi_server* S, Slot& slot) {
+    cudaStream_t s = slot.stream;
+    slot.tv.clear();
+    std::vector<std::vector<void*>> host_out(slot.reqs.size());
+    for (size_t k = 0; k < slot.reqs.size(); ++k) {
+        Request* r = slot.reqs[k];
+        Scene* sc = slot.scenes[k];
+        for (const f184gi_view& v : r->views) host_out[k].push_back(v.out);
+        int rc = stage_in(r, s);
+        if (!rc) rc = scene_update(sc, r, s);
+        if (rc) return rc;
+        for (const f184gi_view& v : r->views) {
+            TraceView t;
+            if ((rc = prepare_view(S, sc, v, t))) return rc;
+            slot.tv.push_back(t);
+        }
+    }
+    if (!slot.graph) {
+        uint32_t blocks = trace_persistent_blocks(uint32_t(S->fmt), S->aniso != 0, S->cfg.blocks_per_sm);
+        int rc = trace_graph_create(&slot.graph, uint32_t(S->fmt), S->aniso != 0, S->cfg.max_batch_views, blocks, S->tc);
+        if (rc) return rc;
+    }
+    int rc = trace_graph_launch(slot.graph, slot.tv.data(), uint32_t(slot.tv.size()), s);
+    if (rc) return rc;
+    for (size_t k = 0; k < slot.reqs.size(); ++k)
+        if ((rc = stage_out(slot.reqs[k], host_out[k], s))) return rc;
+    return cuda_fail(cudaEventRecord(slot.done, s), "server: batch event");
+}
+
+int free_slot(f184gi_server* S) {
+    for (size_t i = 0; i < S->slots.size(); ++i)
+        if (!S->slots[i].busy) return int(i);
+    return -1;
+}
+
+void finish_request(f184gi_server* S, Request* r, int status, Clock::time_point now) {
+    r->status = status;
+    r->done = true;
+    r->t_done = now;
+    if (status == F184GI_OK) {
+        S->lat.push_back(ms_between(r->t_submit, now));
+        S->done_n += 1;
+        S->pixels += r->pixels;
+    }
+    S->hbm_used -= r->staging;
+}
+
+void scheduler(f184gi_server* S) {
+    cudaSetDevice(S->cfg.device);
+    std::unique_lock<std::mutex> lk(S->mu);
+    uint64_t seen = S->generation;
+    while (true) {
+        S->cv_sched.wait(lk, [&] { return S->stop || (!S->pending.empty() && free_slot(S) >= 0); });
+        if (S->stop) break;
+        const int si = free_slot(S);
+        Slot& slot = S->slots[si];
+        std::vector<Request*> batch;
+        std::set<uint32_t> blocked;  // scenes whose next request cannot run in this batch
+        uint32_t nviews = 0;
+        for (auto it = S->pending.begin(); it != S->pending.end();) {
+            Request* r = *it;
+            Scene* sc = S->scenes.at(r->scene);
+            if (sc->busy || blocked.count(r->scene)) {
+                blocked.insert(r->scene);
+                ++it;
+                continue;
+            }
+            if (nviews + r->views.size() > S->cfg.max_batch_views) break;
+            if (S->cfg.hbm_budget && S->hbm_used + r->staging > S->cfg.hbm_budget) {
+                blocked.insert(r->scene);  // waits for memory; later requests of the scene wait behind it
+                ++it;
+                continue;
+            }
+            batch.push_back(r);
+            blocked.insert(r->scene);
+            sc->busy = true;
+            nviews += uint32_t(r->views.size());
+            S->hbm_used += r->staging;
+            it = S->pending.erase(it);
+        }
+        if (batch.empty()) {  // nothing admissible until a batch completes
+            S->cv_sched.wait_for(lk, std::chrono::milliseconds(50), [&] { return S->stop || S->generation != seen; });
+            seen = S->generation;
+            continue;
+        }
+        const Clock::time_point now = Clock::now();
+        slot.busy = true;
+        slot.reqs = batch;
+        slot.scenes.clear();
+        for (Request* r : batch) slot.scenes.push_back(S->scenes.at(r->scene));
+        slot.batch = S->next_batch++;
+        for (Request* r : batch) r->admitted = true, r->t_admit = now, r->batch = slot.batch;
+        lk.unlock();
+        int rc = issue_batch(S, slot);
+        lk.lock();
+        if (rc) {
+            const Clock::time_point t = Clock::now();
+            cudaStreamSynchronize(slot.stream);
+            for (size_t k = 0; k < slot.reqs.size(); ++k) {
+                Request* r = slot.reqs[k];
+                if (r->d_stage) cudaFree(r->d_stage), r->d_stage = nullptr;
+                finish_request(S, r, rc, t);
+                slot.scenes[k]->busy = false;
+            }
+            slot.reqs.clear();
+            slot.busy = false;
+            S->generation++;
+            S->cv_done.notify_all();
+            continue;
+        }
+        S->launched.push_back(si);
+        S->cv_done.notify_all();
+    }
+}
+
+void completer(f184gi_server* S) {
+    cudaSetDevice(S->cfg.device);
+    std::unique_lock<std::mutex> lk(S->mu);
+    while (true) {
+        S->cv_done.wait(lk, [&] { return !S->launched.empty() || S->stop; });
+        if (S->launched.empty()) {
+            if (S->stop) break;
+            continue;
+        }
+        const int si = S->launched.front();
+        Slot& slot = S->slots[si];
+        lk.unlock();
+        cudaError_t e = cudaEventSynchronize(slot.done);
+        int st = e == cudaSuccess ? F184GI_OK : cuda_fail(e, "server: batch");
+        if (st == F184GI_OK) {
+            // kernels flag overflow / timeout on each touched scene's context
+            for (Scene* sc : slot.scenes) {
+                int rs = f184gi_sync(sc->ctx, slot.stream);
+                if (rs) st = rs;
+            }
+        }
+        lk.lock();
+        S->launched.pop_front();
+        const Clock::time_point now = Clock::now();
+        for (size_t k = 0; k < slot.reqs.size(); ++k) {
+            finish_request(S, slot.reqs[k], st, now);
+            slot.scenes[k]->busy = false;
+        }
+        S->batches += 1;
+        S->batch_views += slot.tv.size();
+        slot.reqs.clear();
+        slot.busy = false;
+        S->generation++;
+        S->cv_sched.notify_all();
+        S->cv_done.notify_all();
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+int f184gi_server_create(const f184gi_server_config* cfg, f184gi_server** out) {
+    if (!out) return fail(F184GI_ERR_INVALID, "server_create: out is null");
+    *out = nullptr;
+    f184gi_server_config c = cfg ? *cfg : f184gi_server_config{};
+    if (c.slots == 0) c.slots = 2;
+    if (c.slots > 4) return fail(F184GI_ERR_INVALID, "server_create: slots must be 1..4");
+    if (c.max_batch_views == 0) c.max_batch_views = 64;
+    if (c.max_batch_views > 4096) return fail(F184GI_ERR_INVALID, "server_create: max_batch_views too large");
+    if (c.cone.diffuse_cones == 0) f184gi_cone_params_default(&c.cone);
+    cudaError_t e = cudaSetDevice(c.device);
+    if (e != cudaSuccess) return cuda_fail(e, "server_create: device");
+    f184gi_server* S = new f184gi_server();
+    S->cfg = c;
+    S->tc.p = c.cone;
+    const double tilt = double(c.cone.diffuse_tilt_deg) * M_PI / 180.0;
+    S->tc.cos_tilt = float(std::cos(tilt));
+    S->tc.sin_tilt = float(std::sin(tilt));
+    S->tc.tmax = 0.0f;  // per view
+    S->slots.resize(c.slots);
+    for (Slot& sl : S->slots) {
+        if ((e = cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking)) != cudaSuccess ||
+            (e = cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming)) != cudaSuccess) {
+            f184gi_server_destroy(S);
+            return cuda_fail(e, "server_create: streams");
+        }
+    }
+    S->sched = std::thread(scheduler, S);
+    S->completer = std::thread(completer, S);
+    *out = S;
+    return F184GI_OK;
+}
+
+int f184gi_server_destroy(f184gi_server* S) {
+    if (!S) return fail(F184GI_ERR_INVALID, "server_destroy: null server");
+    {
+        std::lock_guard<std::mutex> lk(S->mu);
+        S->stop = true;
+    }
+    S->cv_sched.notify_all();
+    S->cv_done.notify_all();
+    if (S->sched.joinable()) S->sched.join();
+    if (S->completer.joinable()) S->completer.join();
+    cudaDeviceSynchronize();
+    for (Slot& sl : S->slots) {
+        trace_graph_destroy(sl.graph);
+        if (sl.stream) cudaStreamDestroy(sl.stream);
+        if (sl.done) cudaEventDestroy(sl.done);
+    }
+    for (auto& kv : S->scenes) {
+        Scene* sc = kv.second;
+        cudaFree(sc->d_tri);
+        cudaFree(sc->d_alb);
+        cudaFree(sc->d_dirty);
+        cudaFreeHost(sc->h_dirty);
+        if (sc->ctx) f184gi_destroy(sc->ctx);
+        delete sc;
+    }
+    for (auto& kv : S->reqs) delete kv.second;
+    delete S;
+    return F184GI_OK;
+}
+
+int f184gi_server_add_scene(f184gi_server* S, uint32_t id, const f184gi_grid_desc* desc, const float* tri,
+                            const uint32_t* albedo, uint64_t ntris, const f184gi_bounds* bounds,
+                            const f184gi_light* light) {
+    if (!S || !desc || !tri || !albedo || !bounds || !light || ntris == 0)
+        return fail(F184GI_ERR_INVALID, "server_add_scene: null argument");
+    {
+        std::lock_guard<std::mutex> lk(S->mu);
+        if (S->scenes.count(id)) return fail(F184GI_ERR_INVALID, "server_add_scene: scene id already registered");
+        if ((S->fmt >= 0 && S->fmt != int(desc->format)) || (S->aniso >= 0 && S->aniso != int(desc->anisotropic)))
+            return fail(F184GI_ERR_INVALID, "server_add_scene: all scenes of a server share format and anisotropy");
+    }
+    f184gi_grid_desc d = *desc;
+    d.flags |= F184GI_GRID_RESIDENT_WEIGHTS;
+    uint64_t need = 0;
+    int rc = f184gi_grid_bytes(&d, &need);
+    if (rc) return rc;
+    need += ntris * 40 + voxelize_scratch_bytes(ntris, d.dim) + raster_scratch_bytes(ntris, d.shadow_res, d.shadow_res);
+    {
+        std::lock_guard<std::mutex> lk(S->mu);
+        if (S->cfg.hbm_budget && S->hbm_used + need > S->cfg.hbm_budget)
+            return fail(F184GI_ERR_BUDGET, "server_add_scene: the scene does not fit the HBM budget");
+        S->hbm_used += need;  // reserved while building
+    }
+    Scene* sc = new Scene();
+    sc->id = id;
+    sc->desc = d;
+    sc->ntris = ntris;
+    sc->bounds = *bounds;
+    sc->light = *light;
+    f184gi_config cc{S->cfg.device, 0u, 0u};
+    cudaError_t e = cudaSuccess;
+    if (!(rc = f184gi_create(&cc, &sc->ctx))) rc = f184gi_grid_create(sc->ctx, &d, &sc->grid);
+    sc->nbricks = (d.dim / 8) * (d.dim / 8) * (d.dim / 8);
+    if (!rc && ((e = cudaMalloc(&sc->d_tri, ntris * 36)) != cudaSuccess || (e = cudaMalloc(&sc->d_alb, ntris * 4)) != cudaSuccess ||
+                (e = cudaMalloc(&sc->d_dirty, size_t(sc->nbricks) * 4)) != cudaSuccess ||
+                (e = cudaHostAlloc(&sc->h_dirty, size_t(sc->nbricks) * 4, cudaHostAllocDefault)) != cudaSuccess))
+        rc = cuda_fail(e, "server_add_scene: allocation");
+    if (!rc) {
+        sc->h_tri.assign(tri, tri + ntris * 9);
+        sc->flag.assign(sc->nbricks, 0);
+        cudaMemcpy(sc->d_tri, tri, ntris * 36, cudaMemcpyHostToDevice);
+        cudaMemcpy(sc->d_alb, albedo, ntris * 4, cudaMemcpyHostToDevice);
+        rc = f184gi_voxelize(sc->ctx, sc->grid, sc->d_tri, sc->d_alb, ntris, bounds, light, nullptr, 0, nullptr);
+    }
+    if (!rc) rc = f184gi_mip(sc->ctx, sc->grid, 0, d.anisotropic, nullptr);
+    if (!rc) rc = f184gi_sync(sc->ctx, nullptr);
+    if (!rc) rc = compute_frame(*bounds, d.dim, light->direction, &sc->frame);
+    if (!rc) rc = grid_internal(sc->ctx, sc->grid, &sc->chain, &sc->d_frame);
+    std::lock_guard<std::mutex> lk(S->mu);
+    if (rc) {
+        S->hbm_used -= need;
+        cudaFree(sc->d_tri);
+        cudaFree(sc->d_alb);
+        cudaFree(sc->d_dirty);
+        cudaFreeHost(sc->h_dirty);
+        if (sc->ctx) f184gi_destroy(sc->ctx);
+        delete sc;
+        return rc;
+    }
+    sc->bytes = need;
+    S->fmt = int(d.format);
+    S->aniso = int(d.anisotropic);
+    S->scenes[id] = sc;
+    return F184GI_OK;
+}
+
+int f184gi_server_submit(f184gi_server* S, const f184gi_request* req, uint64_t* ticket) {
+    if (!S || !req || !ticket) return fail(F184GI_ERR_INVALID, "server_submit: null argument");
+    if (req->nviews == 0 || !req->views) return fail(F184GI_ERR_INVALID, "server_submit: a request needs views");
+    if (req->nmoves && !req->moves) return fail(F184GI_ERR_INVALID, "server_submit: null moves");
+    for (uint32_t i = 0; i < req->nviews; ++i) {
+        const f184gi_view& v = req->views[i];
+        if (!v.depth || !v.normal || !v.roughness || !v.out || v.width == 0 || v.height == 0 ||
+            (v.out_format != F184GI_FMT_F32 && v.out_format != F184GI_FMT_F16))
+            return fail(F184GI_ERR_INVALID, "server_submit: malformed view " + std::to_string(i));
+    }
+    Request* r = new Request();
+    r->scene = req->scene_id;
+    r->flags = req->flags;
+    r->moves.assign(req->moves, req->moves + req->nmoves);
+    r->views.assign(req->views, req->views + req->nviews);
+    for (const f184gi_view& v : r->views) r->pixels += uint64_t(v.width) * v.height;
+    r->staging = staging_bytes(*req);
+    std::lock_guard<std::mutex> lk(S->mu);
+    auto it = S->scenes.find(req->scene_id);
+    if (it == S->scenes.end()) {
+        delete r;
+        return fail(F184GI_ERR_NOTFOUND, "server_submit: unknown scene");
+    }
+    for (const f184gi_move& m : r->moves)
+        if (uint64_t(m.first) + m.count > it->second->ntris) {
+            delete r;
+            return fail(F184GI_ERR_INVALID, "server_submit: move range out of bounds");
+        }
+    if (req->nviews > S->cfg.max_batch_views) {
+        delete r;
+        return fail(F184GI_ERR_INVALID, "server_submit: more views than max_batch_views");
+    }
+    if (S->cfg.hbm_budget && r->staging > S->cfg.hbm_budget) {
+        delete r;
+        return fail(F184GI_ERR_BUDGET, "server_submit: the request's staging exceeds the HBM budget");
+    }
+    r->ticket = S->next_ticket++;
+    r->t_submit = Clock::now();
+    S->reqs[r->ticket] = r;
+    S->pending.push_back(r);
+    *ticket = r->ticket;
+    S->cv_sched.notify_all();
+    return F184GI_OK;
+}
+
+int f184gi_server_wait(f184gi_server* S, uint64_t ticket, uint32_t timeout_ms, f184gi_request_result* out) {
+    if (!S) return fail(F184GI_ERR_INVALID, "server_wait: null server");
+    std::unique_lock<std::mutex> lk(S->mu);
+    auto it = S->reqs.find(ticket);
+    if (it == S->reqs.end()) return fail(F184GI_ERR_NOTFOUND, "server_wait: unknown ticket");
+    Request* r = it->second;
+    if (timeout_ms) {
+        if (!S->cv_done.wait_for(lk, std::chrono::milliseconds(timeout_ms), [&] { return r->done; }))
+            return fail(F184GI_ERR_TIMEOUT, "server_wait: timed out");
+    } else {
+        S->cv_done.wait(lk, [&] { return r->done; });
+    }
+    if (out) {
+        out->status = r->status;
+        out->batch = r->batch;
+        out->queued_ms = r->admitted ? ms_between(r->t_submit, r->t_admit) : 0.0;
+        out->latency_ms = ms_between(r->t_submit, r->t_done);
+        out->pixels = r->pixels;
+    }
+    return r->status == F184GI_ERR_CANCELLED ? F184GI_OK : (r->status ? fail(r->status, "server: request failed") : F184GI_OK);
+}
+
+int f184gi_server_cancel(f184gi_server* S, uint64_t ticket) {
+    if (!S) return fail(F184GI_ERR_INVALID, "server_cancel: null server");
+    std::lock_guard<std::mutex> lk(S->mu);
+    auto it = S->reqs.find(ticket);
+    if (it == S->reqs.end()) return fail(F184GI_ERR_NOTFOUND, "server_cancel: unknown ticket");
+    Request* r = it->second;
+    auto p = std::find(S->pending.begin(), S->pending.end(), r);
+    if (p == S->pending.end()) return fail(F184GI_ERR_INVALID, "server_cancel: the request is running or done");
+    S->pending.erase(p);
+    r->status = F184GI_ERR_CANCELLED;
+    r->done = true;
+    r->t_done = Clock::now();
+    S->cancelled += 1;
+    S->cv_done.notify_all();
+    S->cv_sched.notify_all();
+    return F184GI_OK;
+}
+
+int f184gi_server_get_stats(f184gi_server* S, f184gi_server_stats* out) {
+    if (!S || !out) return fail(F184GI_ERR_INVALID, "server_stats: null argument");
+    std::lock_guard<std::mutex> lk(S->mu);
+    *out = f184gi_server_stats{};
+    out->requests_done = S->done_n;
+    out->requests_cancelled = S->cancelled;
+    out->batches = S->batches;
+    out->pixels = S->pixels;
+    if (!S->lat.empty()) {
+        std::vector<double> l = S->lat;
+        std::sort(l.begin(), l.end());
+        auto pct = [&](double q) { return l[std::min(l.size() - 1, size_t(q * double(l.size() - 1) + 0.5))]; };
+        out->p50_ms = pct(0.50);
+        out->p99_ms = pct(0.99);
+        double s = 0.0;
+        for (double x : l) s += x;
+        out->mean_ms = s / double(l.size());
+    }
+    out->mean_batch_views = S->batches ? double(S->batch_views) / double(S->batches) : 0.0;
+    out->hbm_used = S->hbm_used;
+    out->hbm_budget = S->cfg.hbm_budget;
+    out->pending = uint32_t(S->pending.size());
+    uint32_t inflight = 0;
+    for (const Slot& sl : S->slots) inflight += sl.busy ? 1u : 0u;
+    out->inflight = inflight;
+    return F184GI_OK;
+}
+
+}  // extern "C"

@@ -55,11 +55,16 @@ __device__ __forceinline__ float3 oct_decode(uint32_t p) {
     return norm3(v);
 }
 
-// Level table staged in shared memory: lanes index it with their own (divergent) level, which the constant
-// bank would serialise.
-struct LevelTab {
+// The grid a tile traces against, staged in shared memory per CTA: lanes index the level table with their own
+// (divergent) level, which the constant bank would serialise, and batched launches trace many grids.
+struct GridRef {
     uint64_t off[kMaxLevels];
     uint64_t vol[kMaxLevels];
+    const void* base;
+    uint32_t dim, levels;
+    float tmax;
+    float org[3];
+    float inv_vs;
 };
 
 // 8-tap trilinear sample of one volume of level l (d voxels per axis) at x (L0 voxel units); taps outside the
@@ -162,16 +167,15 @@ __device__ __forceinline__ float4 tri_sample(const void* base, int d, uint32_t l
 }
 
 template <int FMT, bool ANISO>
-__device__ __forceinline__ float4 level_sample(const ChainLayout& c, const LevelTab& lt, uint32_t l, float3 x,
-                                               float3 dir) {
-    const int d = int(c.dim >> l);
-    if (!ANISO || l == 0) return tri_sample<FMT>(c.base, d, l, lt.off[l], x);
+__device__ __forceinline__ float4 level_sample(const GridRef& g, uint32_t l, float3 x, float3 dir) {
+    const int d = int(g.dim >> l);
+    if (!ANISO || l == 0) return tri_sample<FMT>(g.base, d, l, g.off[l], x);
     float w[3] = {dir.x * dir.x, dir.y * dir.y, dir.z * dir.z};
     int sel[3] = {dir.x >= 0.0f ? 0 : 1, dir.y >= 0.0f ? 2 : 3, dir.z >= 0.0f ? 4 : 5};
     float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
-        float4 s = tri_sample<FMT>(c.base, d, l, lt.off[l] + uint64_t(sel[a]) * lt.vol[l], x);
+        float4 s = tri_sample<FMT>(g.base, d, l, g.off[l] + uint64_t(sel[a]) * g.vol[l], x);
         acc.x += w[a] * s.x;
         acc.y += w[a] * s.y;
         acc.z += w[a] * s.z;
@@ -181,13 +185,12 @@ __device__ __forceinline__ float4 level_sample(const ChainLayout& c, const Level
 }
 
 template <int FMT, bool ANISO>
-__device__ float4 cone(const ChainLayout& c, const LevelTab& lt, const TraceConsts& tc, float3 o, float3 dir,
-                       float tan_half) {
+__device__ float4 cone(const GridRef& g, const TraceConsts& tc, float3 o, float3 dir, float tan_half) {
     float cr = 0.f, cg = 0.f, cb = 0.f, alpha = 0.f;
     float t = tc.p.start_offset;
-    const float dimf = float(c.dim);
-    const float maxl = float(c.levels - 1);
-    while (t <= tc.tmax) {
+    const float dimf = float(g.dim);
+    const float maxl = float(g.levels - 1);
+    while (t <= g.tmax) {
         float diam = fmaxf(1.0f, 2.0f * t * tan_half);
         float lvl = fminf(fmaxf(log2f(diam), 0.0f), maxl);
         float3 x = add3(o, mul3(dir, t));
@@ -196,9 +199,9 @@ __device__ float4 cone(const ChainLayout& c, const LevelTab& lt, const TraceCons
         float fl = floorf(lvl);
         uint32_t l0 = uint32_t(fl);
         float f = lvl - fl;
-        float4 s = level_sample<FMT, ANISO>(c, lt, l0, x, dir);
-        if (f > 0.0f && l0 + 1 < c.levels) {
-            float4 s1 = level_sample<FMT, ANISO>(c, lt, l0 + 1, x, dir);
+        float4 s = level_sample<FMT, ANISO>(g, l0, x, dir);
+        if (f > 0.0f && l0 + 1 < g.levels) {
+            float4 s1 = level_sample<FMT, ANISO>(g, l0 + 1, x, dir);
             s.x = s.x + f * (s1.x - s.x);
             s.y = s.y + f * (s1.y - s.y);
             s.z = s.z + f * (s1.z - s.z);
@@ -228,8 +231,7 @@ __device__ __forceinline__ void store_out(void* out, uint32_t fmt, uint64_t i, f
 }
 
 template <int FMT, bool ANISO>
-__device__ void trace_pixel(const ChainLayout& c, const LevelTab& lt, const TraceConsts& tc, const TraceView& v,
-                            float3 org, float inv_vs, uint32_t px, uint32_t py) {
+__device__ void trace_pixel(const GridRef& g, const TraceConsts& tc, const TraceView& v, uint32_t px, uint32_t py) {
     const uint64_t npix = uint64_t(v.width) * v.height;
     const uint64_t pi = uint64_t(py) * v.width + px;
     float d = v.depth[pi];
@@ -252,27 +254,27 @@ __device__ void trace_pixel(const ChainLayout& c, const LevelTab& lt, const Trac
     float3 nw = norm3(f3(iv[0] * nv.x + iv[1] * nv.y + iv[2] * nv.z, iv[4] * nv.x + iv[5] * nv.y + iv[6] * nv.z,
                          iv[8] * nv.x + iv[9] * nv.y + iv[10] * nv.z));
     float rough = __half2float(__ushort_as_half(v.rough[pi]));
-    float3 pv = f3((wp.x - org.x) * inv_vs, (wp.y - org.y) * inv_vs, (wp.z - org.z) * inv_vs);
+    float3 pv = f3((wp.x - g.org[0]) * g.inv_vs, (wp.y - g.org[1]) * g.inv_vs, (wp.z - g.org[2]) * g.inv_vs);
     float3 o = add3(pv, mul3(nw, tc.p.start_offset));
     float3 bx, by, bz;
     coord_space(nw, bx, by, bz);
     float4 acc;
     if (tc.p.diffuse_cones >= 5) {
-        float4 c0 = cone<FMT, ANISO>(c, lt, tc, o, bz, tc.p.diffuse_tan_half);
+        float4 c0 = cone<FMT, ANISO>(g, tc, o, bz, tc.p.diffuse_tan_half);
         acc = make_float4(0.25f * c0.x, 0.25f * c0.y, 0.25f * c0.z, 0.25f * c0.w);
         const float cphi[4] = {1.f, 0.f, -1.f, 0.f}, sphi[4] = {0.f, 1.f, 0.f, -1.f};
 #pragma unroll 1
         for (int k = 0; k < 4; ++k) {
             float3 side = add3(mul3(bx, cphi[k]), mul3(by, sphi[k]));
             float3 dir = norm3(add3(mul3(bz, tc.cos_tilt), mul3(side, tc.sin_tilt)));
-            float4 ck = cone<FMT, ANISO>(c, lt, tc, o, dir, tc.p.diffuse_tan_half);
+            float4 ck = cone<FMT, ANISO>(g, tc, o, dir, tc.p.diffuse_tan_half);
             acc.x += 0.1875f * ck.x;
             acc.y += 0.1875f * ck.y;
             acc.z += 0.1875f * ck.z;
             acc.w += 0.1875f * ck.w;
         }
     } else {
-        acc = cone<FMT, ANISO>(c, lt, tc, o, bz, tc.p.diffuse_tan_half);
+        acc = cone<FMT, ANISO>(g, tc, o, bz, tc.p.diffuse_tan_half);
     }
     store_out(v.out, v.out_format, pi, acc);
     float4 sp = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -281,49 +283,100 @@ __device__ void trace_pixel(const ChainLayout& c, const LevelTab& lt, const Trac
         float dn = dot3(vd, nw);
         float3 rd = norm3(sub3(vd, mul3(nw, 2.0f * dn)));
         float th = fmaxf(rough, tc.p.min_spec_tan_half);
-        sp = cone<FMT, ANISO>(c, lt, tc, o, rd, th);
+        sp = cone<FMT, ANISO>(g, tc, o, rd, th);
     }
     store_out(v.out, v.out_format, npix + pi, sp);
 }
 
-// One CTA = one 16x8 pixel tile of one view; tiles of all views are enumerated in view order.
-template <int FMT, bool ANISO>
-__global__ void __launch_bounds__(128, 4) trace_kernel(ChainLayout c, TraceConsts tc, const f184gi_grid_frame* __restrict__ fr,
-                                                    const TraceView* __restrict__ views,
-                                                    const uint32_t* __restrict__ tile_base, uint32_t nviews) {
-    __shared__ LevelTab lt;
-    if (threadIdx.x < kMaxLevels) {
-        lt.off[threadIdx.x] = c.off[threadIdx.x];
-        lt.vol[threadIdx.x] = c.vol[threadIdx.x];
+// Tiles of 16x8 pixels of all views are numbered in view order (tile_base = per-view prefix).  A CTA traces one
+// tile at a time: blockIdx.x in the one-shot launch, or tiles taken from a device work counter in the persistent
+// launch (one resident wave of CTAs that drains the whole batch, so views of different size balance).
+template <int FMT, bool ANISO, bool PERSISTENT>
+__global__ void __launch_bounds__(128, 4) trace_kernel(TraceConsts tc, const TraceView* __restrict__ views,
+                                                    const uint32_t* __restrict__ tile_base, uint32_t nviews,
+                                                    uint32_t* work) {
+    __shared__ GridRef g;
+    __shared__ uint32_t s_tile, s_view;
+    const uint32_t ntiles = tile_base[nviews];
+    uint32_t cur_view = 0xffffffffu;
+    for (uint32_t it = 0;; ++it) {
+        if (threadIdx.x == 0) {
+            uint32_t tile = PERSISTENT ? atomicAdd(work, 1u) : (it == 0 ? blockIdx.x : ntiles);
+            uint32_t lo = 0, hi = nviews;  // last view with tile_base[v] <= tile
+            while (hi - lo > 1) {
+                uint32_t mid = (lo + hi) / 2;
+                if (tile_base[mid] <= tile) lo = mid; else hi = mid;
+            }
+            s_tile = tile;
+            s_view = lo;
+        }
+        __syncthreads();
+        const uint32_t tile = s_tile, vi = s_view;
+        if (tile >= ntiles) return;
+        const TraceView& v = views[vi];
+        if (vi != cur_view) {  // stage the view's grid description
+            if (threadIdx.x < kMaxLevels) {
+                g.off[threadIdx.x] = v.off[threadIdx.x];
+                g.vol[threadIdx.x] = v.vol[threadIdx.x];
+            }
+            if (threadIdx.x == 0) {
+                g.base = v.grid_base;
+                g.dim = v.grid_dim;
+                g.levels = v.grid_levels;
+                g.tmax = v.tmax;
+                // world -> L0 voxel units: (p - origin) * (inv_voxel_fixed / 256), all scalings exact
+                for (int a = 0; a < 3; ++a) g.org[a] = float(v.frame->origin[a]);
+                g.inv_vs = float(v.frame->inv_voxel_fixed * (1.0 / 256.0));
+            }
+            cur_view = vi;
+            __syncthreads();
+        }
+        const uint32_t local = tile - tile_base[vi];
+        const uint32_t tiles_x = (v.width + 15) / 16;
+        const uint32_t px = (local % tiles_x) * 16 + (threadIdx.x & 15);
+        const uint32_t py = (local / tiles_x) * 8 + (threadIdx.x >> 4);
+        if (px < v.width && py < v.height) trace_pixel<FMT, ANISO>(g, tc, v, px, py);
+        __syncthreads();  // s_tile / g are rewritten for the next tile
     }
-    __syncthreads();
-    uint32_t tile = blockIdx.x;
-    uint32_t vi = 0;
-    while (vi + 1 < nviews && tile >= tile_base[vi + 1]) ++vi;
-    const TraceView& v = views[vi];
-    uint32_t local = tile - tile_base[vi];
-    uint32_t tiles_x = (v.width + 15) / 16;
-    uint32_t px = (local % tiles_x) * 16 + (threadIdx.x & 15);
-    uint32_t py = (local / tiles_x) * 8 + (threadIdx.x >> 4);
-    if (px >= v.width || py >= v.height) return;
-    // world -> L0 voxel units: (p - origin) * (inv_voxel_fixed / 256), all scalings exact
-    float3 org = f3(float(fr->origin[0]), float(fr->origin[1]), float(fr->origin[2]));
-    float inv_vs = float(fr->inv_voxel_fixed * (1.0 / 256.0));
-    trace_pixel<FMT, ANISO>(c, lt, tc, v, org, inv_vs, px, py);
+}
+
+template <bool PERSISTENT>
+void launch_variant(uint32_t fmt, bool aniso, uint32_t blocks, cudaStream_t s, const TraceConsts& tc,
+                    const TraceView* dv, const uint32_t* db, uint32_t nviews, uint32_t* work) {
+    // one instantiation per storage format and mip kind keeps each kernel's code small (instruction cache)
+    if (fmt == F184GI_FMT_F32 && !aniso)
+        trace_kernel<F184GI_FMT_F32, false, PERSISTENT><<<blocks, 128, 0, s>>>(tc, dv, db, nviews, work);
+    else if (fmt == F184GI_FMT_F32)
+        trace_kernel<F184GI_FMT_F32, true, PERSISTENT><<<blocks, 128, 0, s>>>(tc, dv, db, nviews, work);
+    else if (!aniso)
+        trace_kernel<F184GI_FMT_F16, false, PERSISTENT><<<blocks, 128, 0, s>>>(tc, dv, db, nviews, work);
+    else
+        trace_kernel<F184GI_FMT_F16, true, PERSISTENT><<<blocks, 128, 0, s>>>(tc, dv, db, nviews, work);
+    note_launches(1);
 }
 
 }  // namespace
 
-size_t trace_scratch_bytes(uint32_t nviews) { return size_t(nviews) * sizeof(TraceView) + size_t(nviews + 1) * 4 + 512; }
+void trace_view_set_grid(TraceView& v, const ChainLayout& c, const f184gi_grid_frame* d_frame, float tmax) {
+    v.grid_base = c.base;
+    v.grid_dim = c.dim;
+    v.grid_levels = c.levels;
+    v.frame = d_frame;
+    v.tmax = tmax;
+    for (int l = 0; l < kMaxLevels; ++l) {
+        v.off[l] = l < int(c.levels) ? c.off[l] : 0;
+        v.vol[l] = l < int(c.levels) ? c.vol[l] : 0;
+    }
+}
 
-int trace_launch(const ChainLayout& c, const TraceConsts& tc, const f184gi_grid_frame* d_frame, const TraceView* views,
-                 uint32_t nviews, void* scratch, size_t scratch_bytes, cudaStream_t s) {
-    if (nviews == 0) return F184GI_OK;
-    if (scratch_bytes < trace_scratch_bytes(nviews)) return fail(F184GI_ERR_INVALID, "trace: scratch too small");
-    // host staging of the view table (views + tile prefix), copied once per call
-    std::vector<unsigned char> host(trace_scratch_bytes(nviews));
-    TraceView* hv = reinterpret_cast<TraceView*>(host.data());
-    uint32_t* hb = reinterpret_cast<uint32_t*>(host.data() + size_t(nviews) * sizeof(TraceView));
+size_t trace_table_bytes(uint32_t nviews) {
+    return (size_t(nviews) * sizeof(TraceView) + size_t(nviews + 1) * 4 + 255) / 256 * 256 + 256;
+}
+
+uint32_t trace_fill_table(const TraceView* views, uint32_t nviews, void* host_table) {
+    unsigned char* h = static_cast<unsigned char*>(host_table);
+    TraceView* hv = reinterpret_cast<TraceView*>(h);
+    uint32_t* hb = reinterpret_cast<uint32_t*>(h + size_t(nviews) * sizeof(TraceView));
     uint32_t tiles = 0;
     for (uint32_t i = 0; i < nviews; ++i) {
         hv[i] = views[i];
@@ -331,24 +384,175 @@ int trace_launch(const ChainLayout& c, const TraceConsts& tc, const f184gi_grid_
         tiles += ((views[i].width + 15) / 16) * ((views[i].height + 7) / 8);
     }
     hb[nviews] = tiles;
+    return tiles;
+}
+
+int trace_launch_table(uint32_t fmt, bool aniso, const TraceConsts& tc, const void* dev_table, uint32_t nviews,
+                       uint32_t ntiles, uint32_t* work, uint32_t persistent_blocks, cudaStream_t s) {
+    const TraceView* dv = static_cast<const TraceView*>(dev_table);
+    const uint32_t* db = reinterpret_cast<const uint32_t*>(static_cast<const unsigned char*>(dev_table) +
+                                                           size_t(nviews) * sizeof(TraceView));
+    if (persistent_blocks && work)
+        launch_variant<true>(fmt, aniso, persistent_blocks, s, tc, dv, db, nviews, work);
+    else
+        launch_variant<false>(fmt, aniso, ntiles, s, tc, dv, db, nviews, nullptr);
+    return cuda_fail(cudaGetLastError(), "trace");
+}
+
+size_t trace_scratch_bytes(uint32_t nviews) { return trace_table_bytes(nviews); }
+
+int trace_launch(const ChainLayout& c, const TraceConsts& tc, const f184gi_grid_frame* d_frame, const TraceView* views,
+                 uint32_t nviews, void* scratch, size_t scratch_bytes, cudaStream_t s) {
+    if (nviews == 0) return F184GI_OK;
+    if (scratch_bytes < trace_scratch_bytes(nviews)) return fail(F184GI_ERR_INVALID, "trace: scratch too small");
+    std::vector<TraceView> vv(views, views + nviews);
+    for (auto& v : vv) trace_view_set_grid(v, c, d_frame, tc.tmax);
+    std::vector<unsigned char> host(trace_table_bytes(nviews));
+    uint32_t tiles = trace_fill_table(vv.data(), nviews, host.data());
     cudaError_t e = cudaMemcpyAsync(scratch, host.data(), host.size(), cudaMemcpyHostToDevice, s);
     if (e != cudaSuccess) return cuda_fail(e, "trace: view table");
     // the staging buffer must outlive the async copy
     e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) return cuda_fail(e, "trace: view table sync");
-    const TraceView* dv = static_cast<const TraceView*>(scratch);
-    const uint32_t* db = reinterpret_cast<const uint32_t*>(static_cast<const unsigned char*>(scratch) + size_t(nviews) * sizeof(TraceView));
-    // one instantiation per storage format and mip kind keeps each kernel's code small (instruction cache)
-    if (c.format == F184GI_FMT_F32 && !c.aniso)
-        trace_kernel<F184GI_FMT_F32, false><<<tiles, 128, 0, s>>>(c, tc, d_frame, dv, db, nviews);
-    else if (c.format == F184GI_FMT_F32)
-        trace_kernel<F184GI_FMT_F32, true><<<tiles, 128, 0, s>>>(c, tc, d_frame, dv, db, nviews);
-    else if (!c.aniso)
-        trace_kernel<F184GI_FMT_F16, false><<<tiles, 128, 0, s>>>(c, tc, d_frame, dv, db, nviews);
-    else
-        trace_kernel<F184GI_FMT_F16, true><<<tiles, 128, 0, s>>>(c, tc, d_frame, dv, db, nviews);
-    note_launches(1);
-    return cuda_fail(cudaGetLastError(), "trace");
+    return trace_launch_table(c.format, c.aniso != 0, tc, scratch, nviews, tiles, nullptr, 0, s);
+}
+
+}  // namespace f184
+
+// ---------------- batched trace under a CUDA graph ----------------
+namespace f184 {
+namespace {
+
+template <int FMT, bool ANISO>
+void* persistent_kernel_ptr() {
+    return reinterpret_cast<void*>(&trace_kernel<FMT, ANISO, true>);
+}
+
+void* persistent_kernel(uint32_t fmt, bool aniso) {
+    if (fmt == F184GI_FMT_F32) return aniso ? persistent_kernel_ptr<F184GI_FMT_F32, true>() : persistent_kernel_ptr<F184GI_FMT_F32, false>();
+    return aniso ? persistent_kernel_ptr<F184GI_FMT_F16, true>() : persistent_kernel_ptr<F184GI_FMT_F16, false>();
+}
+
+}  // namespace
+
+// Table layout (host pinned and device): [tile_base: max_views + 1 u32, padded to 256 B][views: max_views]
+struct TraceGraph {
+    uint32_t fmt = 0;
+    bool aniso = false;
+    uint32_t max_views = 0, blocks = 0;
+    size_t header = 0, bytes = 0;
+    unsigned char* h_table = nullptr;
+    unsigned char* d_table = nullptr;
+    uint32_t* d_work = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    cudaGraphNode_t copy = nullptr, reset = nullptr, kernel = nullptr;
+    TraceConsts tc{};
+    uint32_t nviews = 0;
+    const TraceView* kviews = nullptr;
+    const uint32_t* kbase = nullptr;
+};
+
+uint32_t trace_persistent_blocks(uint32_t fmt, bool aniso, uint32_t per_sm) {
+    int dev = 0, sms = 0, maxb = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&maxb, persistent_kernel(fmt, aniso), 128, 0);
+    if (maxb <= 0) maxb = 1;
+    uint32_t b = per_sm ? std::min<uint32_t>(per_sm, uint32_t(maxb)) : uint32_t(maxb);
+    return b * uint32_t(sms > 0 ? sms : 1);
+}
+
+static void graph_params(TraceGraph* g, cudaKernelNodeParams& kp, void** args) {
+    args[0] = &g->tc;
+    args[1] = &g->kviews;
+    args[2] = &g->kbase;
+    args[3] = &g->nviews;
+    args[4] = &g->d_work;
+    kp = cudaKernelNodeParams{};
+    kp.func = persistent_kernel(g->fmt, g->aniso);
+    kp.gridDim = dim3(g->blocks);
+    kp.blockDim = dim3(128);
+    kp.sharedMemBytes = 0;
+    kp.kernelParams = args;
+}
+
+int trace_graph_create(TraceGraph** out, uint32_t fmt, bool aniso, uint32_t max_views, uint32_t blocks,
+                       const TraceConsts& tc) {
+    *out = nullptr;
+    TraceGraph* g = new TraceGraph();
+    g->fmt = fmt, g->aniso = aniso, g->max_views = max_views, g->blocks = blocks, g->tc = tc;
+    g->header = (size_t(max_views + 1) * 4 + 255) / 256 * 256;
+    g->bytes = g->header + size_t(max_views) * sizeof(TraceView);
+    cudaError_t e = cudaHostAlloc(&g->h_table, g->bytes, cudaHostAllocDefault);
+    if (e == cudaSuccess) e = cudaMalloc(&g->d_table, g->bytes + 256);
+    if (e == cudaSuccess) e = cudaMalloc(&g->d_work, 256);
+    if (e == cudaSuccess) e = cudaGraphCreate(&g->graph, 0);
+    if (e == cudaSuccess)
+        e = cudaGraphAddMemcpyNode1D(&g->copy, g->graph, nullptr, 0, g->d_table, g->h_table, g->bytes,
+                                     cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        cudaMemsetParams mp{};
+        mp.dst = g->d_work;
+        mp.value = 0;
+        mp.elementSize = 4;
+        mp.width = 1;
+        mp.height = 1;
+        mp.pitch = 4;
+        e = cudaGraphAddMemsetNode(&g->reset, g->graph, &g->copy, 1, &mp);
+    }
+    g->kbase = reinterpret_cast<const uint32_t*>(g->d_table);
+    g->kviews = reinterpret_cast<const TraceView*>(g->d_table + g->header);
+    if (e == cudaSuccess) {
+        cudaKernelNodeParams kp;
+        void* args[5];
+        graph_params(g, kp, args);
+        e = cudaGraphAddKernelNode(&g->kernel, g->graph, &g->reset, 1, &kp);
+    }
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&g->exec, g->graph, 0);
+    if (e != cudaSuccess) {
+        trace_graph_destroy(g);
+        return cuda_fail(e, "trace graph");
+    }
+    *out = g;
+    return F184GI_OK;
+}
+
+int trace_graph_launch(TraceGraph* g, const TraceView* views, uint32_t nviews, cudaStream_t s) {
+    if (nviews == 0) return F184GI_OK;
+    if (nviews > g->max_views) return fail(F184GI_ERR_INVALID, "trace graph: batch exceeds max_views");
+    uint32_t* hb = reinterpret_cast<uint32_t*>(g->h_table);
+    TraceView* hv = reinterpret_cast<TraceView*>(g->h_table + g->header);
+    uint32_t tiles = 0;
+    for (uint32_t i = 0; i < nviews; ++i) {
+        hv[i] = views[i];
+        hb[i] = tiles;
+        tiles += ((views[i].width + 15) / 16) * ((views[i].height + 7) / 8);
+    }
+    hb[nviews] = tiles;
+    g->nviews = nviews;
+    const size_t used = g->header + size_t(nviews) * sizeof(TraceView);
+    cudaError_t e = cudaGraphExecMemcpyNodeSetParams1D(g->exec, g->copy, g->d_table, g->h_table, used,
+                                                       cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        cudaKernelNodeParams kp;
+        void* args[5];
+        graph_params(g, kp, args);
+        e = cudaGraphExecKernelNodeSetParams(g->exec, g->kernel, &kp);
+    }
+    if (e == cudaSuccess) e = cudaGraphLaunch(g->exec, s);
+    if (e == cudaSuccess) note_launches(1);
+    return cuda_fail(e, "trace graph launch");
+}
+
+void trace_graph_destroy(TraceGraph* g) {
+    if (!g) return;
+    if (g->exec) cudaGraphExecDestroy(g->exec);
+    if (g->graph) cudaGraphDestroy(g->graph);
+    cudaFreeHost(g->h_table);
+    cudaFree(g->d_table);
+    cudaFree(g->d_work);
+    delete g;
 }
 
 }  // namespace f184

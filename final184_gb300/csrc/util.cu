@@ -219,3 +219,44 @@ int transform_launch(const float* src, uint64_t ntris, const float model[12], fl
     return cuda_fail(cudaGetLastError(), "transform");
 }
 }  // namespace f184
+
+// ---------------- rigid moves of triangle ranges ----------------
+namespace f184 {
+namespace {
+constexpr int kMovesPerLaunch = 64;
+struct MoveTable {
+    f184gi_move m[kMovesPerLaunch];
+    uint32_t start[kMovesPerLaunch + 1];  // prefix of vertex counts
+    uint32_t n;
+};
+__global__ void moves_kernel(float* __restrict__ tri, MoveTable t) {
+    const uint32_t total = t.start[t.n];
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < total; v += gridDim.x * blockDim.x) {
+        uint32_t lo = 0, hi = t.n;
+        while (hi - lo > 1) {
+            uint32_t mid = (lo + hi) / 2;
+            if (t.start[mid] <= v) lo = mid; else hi = mid;
+        }
+        const f184gi_move& m = t.m[lo];
+        const uint64_t vert = uint64_t(m.first) * 3 + (v - t.start[lo]);
+        for (int a = 0; a < 3; ++a) tri[vert * 3 + a] = __fadd_rn(tri[vert * 3 + a], m.offset[a]);
+    }
+}
+}  // namespace
+
+int moves_launch(float* tri, const f184gi_move* moves, uint32_t nmoves, cudaStream_t s) {
+    for (uint32_t b = 0; b < nmoves; b += kMovesPerLaunch) {
+        MoveTable t{};
+        t.n = std::min<uint32_t>(kMovesPerLaunch, nmoves - b);
+        t.start[0] = 0;
+        for (uint32_t i = 0; i < t.n; ++i) {
+            t.m[i] = moves[b + i];
+            t.start[i + 1] = t.start[i] + moves[b + i].count * 3;
+        }
+        if (t.start[t.n] == 0) continue;
+        moves_kernel<<<std::min<uint32_t>((t.start[t.n] + 255) / 256, 152 * 4), 256, 0, s>>>(tri, t);
+        note_launches(1);
+    }
+    return cuda_fail(cudaGetLastError(), "apply_moves");
+}
+}  // namespace f184

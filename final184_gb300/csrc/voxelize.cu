@@ -224,43 +224,110 @@ __global__ void vox_dirty_mask(const uint32_t* dirty, uint32_t ndirty, uint32_t 
     if (i < ndirty && dirty[i] < nbricks) atomicOr(&mask[dirty[i] >> 5], 1u << (dirty[i] & 31));
 }
 
-constexpr int kSmallVox = 64;       // items with at most this many candidate voxels run on one thread
-constexpr uint32_t kLargeCap = 512;  // per-brick queue of warp-shared items (overflow runs on one thread)
+// Shadow visibility of the centre of voxel (i, j, k): the exact FP32 operation sequence of the frame's affine
+// voxel -> light-clip map, nearest texel, lit iff z - bias <= stored depth (empty texels hold depth 1).
+__device__ __forceinline__ bool voxel_lit(const f184gi_grid_frame* __restrict__ fr,
+                                          const unsigned long long* __restrict__ shadow, uint32_t res, int i, int j,
+                                          int k) {
+    const float* lv = fr->light_vox;
+    const float fi = float(i), fj = float(j), fk = float(k);
+    float v[3];
+#pragma unroll
+    for (int rr = 0; rr < 3; ++rr) {
+        const float* c = lv + 4 * rr;
+        float s = __fadd_rn(c[0], __fmul_rn(fi, c[1]));
+        s = __fadd_rn(s, __fmul_rn(fj, c[2]));
+        v[rr] = __fadd_rn(s, __fmul_rn(fk, c[3]));
+    }
+    const float half_res = 0.5f * float(res);
+    const float tx = floorf(__fmul_rn(__fadd_rn(v[0], 1.0f), half_res));
+    const float ty = floorf(__fmul_rn(__fadd_rn(v[1], 1.0f), half_res));
+    if (!(tx >= 0.0f && ty >= 0.0f && tx < float(res) && ty < float(res))) return true;
+    const unsigned long long key = shadow[uint64_t(ty) * res + uint64_t(tx)];
+    const float sd = key == ~0ull ? 1.0f : __uint_as_float(uint32_t(key >> 32));
+    return __fsub_rn(v[2], fr->shadow_bias_f) <= sd;
+}
 
-// One thread tests every candidate voxel of a (triangle, brick) item; l0..l1 is the item's voxel box in brick
-// coordinates.  The same exact tests as the warp path: edge axes crossed with x depend only on (y, z), so they
-// are hoisted out of the x loop.
-__device__ __forceinline__ void item_thread(const TriRec& r, const int64_t base[3], const int32_t l0[3],
-                                            const int32_t l1[3], unsigned long long (*s_sum)[512], uint32_t* s_cnt) {
+// Relight: L0 radiance = luminance * (lit ? weight : 0) for every voxel of the mean-weight grid W (same brick
+// layout as L0).  With vox_bricks writing W, this gives the same bytes as the fused pass; the served path runs it
+// after every shadow-map change without re-voxelizing.
+__global__ void __launch_bounds__(256) relight_bricks(const float4* __restrict__ W, const f184gi_grid_frame* __restrict__ fr,
+                                                      uint32_t dim, ChainLayout chain, f184gi_light light,
+                                                      const unsigned long long* __restrict__ shadow, uint32_t res) {
+    const uint32_t nb = dim >> 3;
+    const uint64_t nvox = uint64_t(nb) * nb * nb * 512;
+    for (uint64_t e = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; e < nvox; e += uint64_t(gridDim.x) * blockDim.x) {
+        const uint32_t m = uint32_t(e >> 9), li = uint32_t(e & 511);
+        const float4 w = W[e];
+        float4 out = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (w.w != 0.0f) {
+            const int i = int(compact1by2(m)) * 8 + int(li & 7), j = int(compact1by2(m >> 1)) * 8 + int((li >> 3) & 7),
+                      k = int(compact1by2(m >> 2)) * 8 + int(li >> 6);
+            const bool lit = voxel_lit(fr, shadow, res, i, j, k);
+            out = make_float4(light.luminance[0] * (lit ? w.x : 0.0f), light.luminance[1] * (lit ? w.y : 0.0f),
+                              light.luminance[2] * (lit ? w.z : 0.0f), 1.0f);
+        }
+        store_vox(chain.base, chain.format, chain.off[0] + e, out);
+    }
+}
+
+// Exact tests of one (triangle, brick) item, prepared by one thread and shared through shared memory.  With
+// m = 2 (voxel - brick origin) + 1 (odd, 1..15) the voxel centre is 128 m + brick offset and every separating-axis
+// test reads lo <= a . m <= hi in integers.  The nine edge x unit-axis tests each ignore one coordinate, so they
+// are evaluated once per cell of the three 8x8 projections of the item's voxel box into bit masks; a voxel is
+// covered when its three projection bits are set and the plane test passes.
+struct ItemSetup {
+    unsigned long long mask[3];  // P = 0: bit y + 8z; P = 1: bit z + 8x; P = 2: bit x + 8y
+    long long n[3];              // triangle normal (relative to the brick)
+    long long plo, phi;          // plane test bounds on n . m
+    uint32_t wq[3];
+    uint8_t l0[3], ext[3];       // voxel box inside the brick: first voxel and extent per axis
+};
+
+__device__ void item_setup(const TriRec& r, const int64_t base[3], const int32_t l0[3], const int32_t l1[3],
+                           ItemSetup& out) {
     int64_t v[3][3];
 #pragma unroll
     for (int a = 0; a < 3; ++a)
 #pragma unroll
         for (int b = 0; b < 3; ++b) v[a][b] = int64_t(r.q[a * 3 + b]) - base[b];
-    // nine edge axes: a = edge x unit(ax); keep its two non-zero components (|a| < 2^21) and the bounds
-    int32_t c1[9], c2[9], alo[9], ahi[9];
+    unsigned long long mk[3] = {0ull, 0ull, 0ull};
 #pragma unroll
-    for (int e = 0; e < 3; ++e) {
-        int64_t ed[3];
+    for (int P = 0; P < 3; ++P) {
+        // the three edge axes of projection P: a = edge x unit(P); components on the two kept axes
+        const int ku = (P + 1) % 3, kw = (P + 2) % 3;  // kept axes: u first, w second
+        int32_t cu[3], cw[3], lo[3], hi[3];
 #pragma unroll
-        for (int b = 0; b < 3; ++b) ed[b] = v[(e + 1) % 3][b] - v[e][b];
+        for (int e = 0; e < 3; ++e) {
+            int64_t ed[3];
 #pragma unroll
-        for (int ax = 0; ax < 3; ++ax) {
-            int64_t a0 = 0, a1 = 0, a2 = 0;
-            if (ax == 0) a1 = ed[2], a2 = -ed[1];
-            if (ax == 1) a0 = -ed[2], a2 = ed[0];
-            if (ax == 2) a0 = ed[1], a1 = -ed[0];
-            int64_t p0 = a0 * v[0][0] + a1 * v[0][1] + a2 * v[0][2];
-            int64_t p1 = a0 * v[1][0] + a1 * v[1][1] + a2 * v[1][2];
-            int64_t p2 = a0 * v[2][0] + a1 * v[2][1] + a2 * v[2][2];
-            int64_t rr = kHalf * (iabs64(a0) + iabs64(a1) + iabs64(a2));
+            for (int b = 0; b < 3; ++b) ed[b] = v[(e + 1) % 3][b] - v[e][b];
+            int64_t a[3] = {0, 0, 0};
+            if (P == 0) a[1] = ed[2], a[2] = -ed[1];
+            if (P == 1) a[0] = -ed[2], a[2] = ed[0];
+            if (P == 2) a[0] = ed[1], a[1] = -ed[0];
+            int64_t p0 = a[0] * v[0][0] + a[1] * v[0][1] + a[2] * v[0][2];
+            int64_t p1 = a[0] * v[1][0] + a[1] * v[1][1] + a[2] * v[1][2];
+            int64_t p2 = a[0] * v[2][0] + a[1] * v[2][1] + a[2] * v[2][2];
+            int64_t rr = kHalf * (iabs64(a[0]) + iabs64(a[1]) + iabs64(a[2]));
             int64_t pmin = min(p0, min(p1, p2)), pmax = max(p0, max(p1, p2));
-            const int k = e * 3 + ax;
-            // ax 0: (y, z) components; ax 1: (x, z); ax 2: (x, y)
-            c1[k] = int32_t(ax == 0 ? a1 : a0);
-            c2[k] = int32_t(ax == 2 ? a1 : a2);
-            alo[k] = clamp32(sar7_ceil(pmin - rr));
-            ahi[k] = clamp32(sar7_floor(pmax + rr));
+            cu[e] = int32_t(a[ku]);
+            cw[e] = int32_t(a[kw]);
+            lo[e] = clamp32(sar7_ceil(pmin - rr));
+            hi[e] = clamp32(sar7_floor(pmax + rr));
+        }
+        for (int w = l0[kw]; w <= l1[kw]; ++w) {
+            const int32_t mw = 2 * w + 1;
+            for (int u = l0[ku]; u <= l1[ku]; ++u) {
+                const int32_t mu = 2 * u + 1;
+                bool pass = true;
+#pragma unroll
+                for (int e = 0; e < 3; ++e) {
+                    int32_t d = cu[e] * mu + cw[e] * mw;
+                    pass = pass && d >= lo[e] && d <= hi[e];
+                }
+                if (pass) mk[P] |= 1ull << (u + 8 * w);
+            }
         }
     }
     int64_t e0[3], e1[3];
@@ -268,236 +335,121 @@ __device__ __forceinline__ void item_thread(const TriRec& r, const int64_t base[
     for (int b = 0; b < 3; ++b) e0[b] = v[1][b] - v[0][b], e1[b] = v[2][b] - v[0][b];
     const int64_t n0 = e0[1] * e1[2] - e0[2] * e1[1], n1 = e0[2] * e1[0] - e0[0] * e1[2],
                   n2 = e0[0] * e1[1] - e0[1] * e1[0];
-    const int64_t s = n0 * v[0][0] + n1 * v[0][1] + n2 * v[0][2];
+    const int64_t sp = n0 * v[0][0] + n1 * v[0][1] + n2 * v[0][2];
     const int64_t rr = kHalf * (iabs64(n0) + iabs64(n1) + iabs64(n2));
-    const int64_t plo = sar7_ceil(s - rr), phi = sar7_floor(s + rr);
-    const uint32_t w0 = r.wq[0], w1 = r.wq[1], w2 = r.wq[2];
-    for (int lz = l0[2]; lz <= l1[2]; ++lz) {
-        const int32_t mz = 2 * lz + 1;
-        for (int ly = l0[1]; ly <= l1[1]; ++ly) {
-            const int32_t my = 2 * ly + 1;
-            bool row = true;
+    out.mask[0] = mk[0], out.mask[1] = mk[1], out.mask[2] = mk[2];
+    out.n[0] = n0, out.n[1] = n1, out.n[2] = n2;
+    out.plo = sar7_ceil(sp - rr);  // overlap iff sp - rr <= 128 (n . m) <= sp + rr
+    out.phi = sar7_floor(sp + rr);
+    out.wq[0] = r.wq[0], out.wq[1] = r.wq[1], out.wq[2] = r.wq[2];
 #pragma unroll
-            for (int e = 0; e < 3; ++e) {  // x-crossed axes: independent of x
-                const int k = e * 3;
-                int32_t d = c1[k] * my + c2[k] * mz;
-                row = row && d >= alo[k] && d <= ahi[k];
-            }
-            if (!row) continue;
-            const int64_t pyz = n1 * my + n2 * mz;
-            for (int lx = l0[0]; lx <= l1[0]; ++lx) {
-                const int32_t mx = 2 * lx + 1;
-                bool hit = true;
-#pragma unroll
-                for (int e = 0; e < 3; ++e) {
-                    const int k1 = e * 3 + 1, k2 = e * 3 + 2;
-                    int32_t d1 = c1[k1] * mx + c2[k1] * mz;  // (x, z)
-                    int32_t d2 = c1[k2] * mx + c2[k2] * my;  // (x, y)
-                    hit = hit && d1 >= alo[k1] && d1 <= ahi[k1] && d2 >= alo[k2] && d2 <= ahi[k2];
-                }
-                if (!hit) continue;
-                const int64_t pd = pyz + n0 * mx;
-                if (pd < plo || pd > phi) continue;
-                const int li = lz * 64 + ly * 8 + lx;
-                atomicAdd(&s_sum[0][li], (unsigned long long)w0);
-                atomicAdd(&s_sum[1][li], (unsigned long long)w1);
-                atomicAdd(&s_sum[2][li], (unsigned long long)w2);
-                atomicAdd(&s_cnt[li], 1u);
-            }
-        }
-    }
+    for (int a = 0; a < 3; ++a) out.l0[a] = uint8_t(l0[a]), out.ext[a] = uint8_t(l1[a] - l0[a] + 1);
 }
 
-// Separating-axis tests of one (triangle, brick) item.  With m = 2 (voxel - brick origin) + 1 (odd, 1..15) the
-// voxel centre is 128 m + brick offset, and each test reads lo <= a . m <= hi (exact integers).  The nine
-// edge x unit-axis tests each ignore one coordinate, so they are evaluated once per cell of three 8x8
-// projections into bit masks; a voxel is covered when its three projection bits and the plane test pass.
+constexpr int kChunk = 128;  // items prepared per round (one per thread; = threads per CTA)
 
-__global__ void __launch_bounds__(256, 2) vox_bricks(VoxScratch sc, const f184gi_grid_frame* __restrict__ fr,
+__global__ void __launch_bounds__(kChunk, 4) vox_bricks(VoxScratch sc, const f184gi_grid_frame* __restrict__ fr,
                                                   uint32_t dim, ChainLayout chain, f184gi_light light,
                                                   const unsigned long long* __restrict__ shadow, uint32_t res,
                                                   uint32_t* counts, const uint32_t* __restrict__ dirty,
-                                                  uint32_t* status) {
+                                                  float4* __restrict__ weights, uint32_t* status) {
     __shared__ unsigned long long s_sum[3][512];  // 33.31 fixed point: exact, order-independent sums
     __shared__ uint32_t s_cnt[512];
-    __shared__ int32_t s_ax[8][9][5];                // per warp: the nine edge-axis tests of its current item
-    __shared__ unsigned long long s_mask[8][3];      // per warp: projection masks of its current item
-    __shared__ uint32_t s_large[kLargeCap];          // list positions of items handled by whole warps
-    __shared__ uint32_t s_nlarge;
-    if (threadIdx.x == 0) s_nlarge = 0;
+    __shared__ ItemSetup s_item[kChunk];
+    __shared__ uint32_t s_start[kChunk + 1];       // prefix of candidate voxels per prepared item
     const uint32_t m = dirty ? dirty[blockIdx.x] : blockIdx.x;
     const uint32_t nb = dim >> 3;
     if (m >= nb * nb * nb) return;
     const int32_t bx = int32_t(compact1by2(m)), by = int32_t(compact1by2(m >> 1)), bz = int32_t(compact1by2(m >> 2));
-    for (int i = threadIdx.x; i < 512; i += 256) {
+    for (int i = threadIdx.x; i < 512; i += kChunk) {
         s_sum[0][i] = s_sum[1][i] = s_sum[2][i] = 0;
         s_cnt[i] = 0;
     }
-    __syncthreads();
     const uint32_t beg = sc.brick_start[m];
     const uint32_t end = uint32_t(min(uint64_t(beg) + sc.brick_count[m], sc.list_cap));
-    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int64_t base[3] = {int64_t(bx) * kBrickFix, int64_t(by) * kBrickFix, int64_t(bz) * kBrickFix};
-    // Phase A: one thread per item whose box inside the brick has at most kSmallVox voxels (most items);
-    // larger items are queued for Phase B, where a whole warp shares one item.
-    for (uint32_t it = beg + threadIdx.x; it < end; it += blockDim.x) {
-        const TriRec r = sc.recs[sc.list[it]];
-        int32_t lo[3], hi[3];
-        voxel_range(r.q, dim, lo, hi);
-        lo[0] = max(lo[0], bx * 8), hi[0] = min(hi[0], bx * 8 + 7);
-        lo[1] = max(lo[1], by * 8), hi[1] = min(hi[1], by * 8 + 7);
-        lo[2] = max(lo[2], bz * 8), hi[2] = min(hi[2], bz * 8 + 7);
-        if (lo[0] > hi[0] || lo[1] > hi[1] || lo[2] > hi[2]) continue;
-        const int vol = (hi[0] - lo[0] + 1) * (hi[1] - lo[1] + 1) * (hi[2] - lo[2] + 1);
-        if (vol > kSmallVox) {
-            uint32_t k = atomicAdd(&s_nlarge, 1u);
-            if (k < kLargeCap) {
-                s_large[k] = it;
-                continue;
+    for (uint32_t c0 = beg; c0 < end; c0 += kChunk) {
+        // phase 1: one thread prepares one item
+        const uint32_t it = c0 + threadIdx.x;
+        uint32_t nvox = 0;
+        if (it < end) {
+            const TriRec r = sc.recs[sc.list[it]];
+            int32_t lo[3], hi[3];
+            voxel_range(r.q, dim, lo, hi);
+            const int32_t l0[3] = {max(lo[0], bx * 8) - bx * 8, max(lo[1], by * 8) - by * 8, max(lo[2], bz * 8) - bz * 8};
+            const int32_t l1[3] = {min(hi[0], bx * 8 + 7) - bx * 8, min(hi[1], by * 8 + 7) - by * 8,
+                                   min(hi[2], bz * 8 + 7) - bz * 8};
+            if (l0[0] <= l1[0] && l0[1] <= l1[1] && l0[2] <= l1[2]) {
+                item_setup(r, base, l0, l1, s_item[threadIdx.x]);
+                nvox = uint32_t((l1[0] - l0[0] + 1) * (l1[1] - l0[1] + 1) * (l1[2] - l0[2] + 1));
             }
         }
-        const int32_t l0[3] = {lo[0] - bx * 8, lo[1] - by * 8, lo[2] - bz * 8};
-        const int32_t l1[3] = {hi[0] - bx * 8, hi[1] - by * 8, hi[2] - bz * 8};
-        item_thread(r, base, l0, l1, s_sum, s_cnt);
-    }
-    __syncthreads();
-    const uint32_t nlarge = min(s_nlarge, kLargeCap);
-    // Phase B: warp-shared large items
-    for (uint32_t k = warp; k < nlarge; k += 8) {
-        const TriRec r = sc.recs[sc.list[s_large[k]]];
-        int32_t lo[3], hi[3];
-        voxel_range(r.q, dim, lo, hi);
-        lo[0] = max(lo[0], bx * 8), hi[0] = min(hi[0], bx * 8 + 7);
-        lo[1] = max(lo[1], by * 8), hi[1] = min(hi[1], by * 8 + 7);
-        lo[2] = max(lo[2], bz * 8), hi[2] = min(hi[2], bz * 8 + 7);
-        // vertices relative to the brick origin (|v| < 2^20)
-        int64_t v[3][3];
-        for (int a = 0; a < 3; ++a)
-            for (int b = 0; b < 3; ++b) v[a][b] = int64_t(r.q[a * 3 + b]) - base[b];
-        // lanes 0..8: edge e = lane / 3 crossed with unit axis P = lane % 3 (the projection it belongs to)
-        if (lane < 9) {
-            const int e = int(lane) / 3, ax = int(lane) % 3;
-            int64_t ed[3];
-#pragma unroll
-            for (int b = 0; b < 3; ++b)  // edge e: v[e] -> v[(e + 1) % 3], selected without local-memory indexing
-                ed[b] = e == 0 ? v[1][b] - v[0][b] : (e == 1 ? v[2][b] - v[1][b] : v[0][b] - v[2][b]);
-            int64_t a0 = 0, a1 = 0, a2 = 0;
-            if (ax == 0) a1 = ed[2], a2 = -ed[1];
-            if (ax == 1) a0 = -ed[2], a2 = ed[0];
-            if (ax == 2) a0 = ed[1], a1 = -ed[0];
-            int64_t p0 = a0 * v[0][0] + a1 * v[0][1] + a2 * v[0][2];
-            int64_t p1 = a0 * v[1][0] + a1 * v[1][1] + a2 * v[1][2];
-            int64_t p2 = a0 * v[2][0] + a1 * v[2][1] + a2 * v[2][2];
-            int64_t rr = kHalf * (iabs64(a0) + iabs64(a1) + iabs64(a2));
-            int64_t pmin = min(p0, min(p1, p2)), pmax = max(p0, max(p1, p2));
-            // overlap iff pmin - rr <= 128 (a . m) <= pmax + rr
-            int32_t* sa = s_ax[warp][lane];
-            sa[0] = int32_t(a0), sa[1] = int32_t(a1), sa[2] = int32_t(a2);
-            sa[3] = clamp32(sar7_ceil(pmin - rr));
-            sa[4] = clamp32(sar7_floor(pmax + rr));
-        }
-        if (lane < 3) s_mask[warp][lane] = 0ull;
-        int64_t pn[3], plo, phi;
+        // exclusive scan of the candidate counts (warp shuffles + one pass over the 8 warp totals)
         {
-            int64_t e0[3], e1[3];
-            for (int b = 0; b < 3; ++b) {
-                e0[b] = v[1][b] - v[0][b];
-                e1[b] = v[2][b] - v[0][b];
-            }
-            pn[0] = e0[1] * e1[2] - e0[2] * e1[1];
-            pn[1] = e0[2] * e1[0] - e0[0] * e1[2];
-            pn[2] = e0[0] * e1[1] - e0[1] * e1[0];
-            int64_t s = pn[0] * v[0][0] + pn[1] * v[0][1] + pn[2] * v[0][2];
-            int64_t rr = kHalf * (iabs64(pn[0]) + iabs64(pn[1]) + iabs64(pn[2]));
-            // overlap iff s - rr <= 128 (n . m) <= s + rr
-            plo = sar7_ceil(s - rr);
-            phi = sar7_floor(s + rr);
-        }
-        __syncwarp();
-        const int l0x = lo[0] - bx * 8, l0y = lo[1] - by * 8, l0z = lo[2] - bz * 8;
-        const int nx = hi[0] - lo[0] + 1, ny = hi[1] - lo[1] + 1, nz = hi[2] - lo[2] + 1;
-        // projection cells: P = 0 -> (y, z), P = 1 -> (z, x), P = 2 -> (x, y)
-        const int n0 = ny * nz, n1 = nz * nx, n2 = nx * ny;
-        for (int e = int(lane); e < n0 + n1 + n2; e += 32) {
-            int P, u, w;  // u, w: local coordinates of the two kept axes, bit = u + 8 w
-            if (e < n0) {
-                P = 0, u = l0y + e % ny, w = l0z + e / ny;
-            } else if (e < n0 + n1) {
-                int c = e - n0;
-                P = 1, u = l0z + c % nz, w = l0x + c / nz;
-            } else {
-                int c = e - n0 - n1;
-                P = 2, u = l0x + c % nx, w = l0y + c / nx;
-            }
-            // m along the two kept axes (the dropped axis has a zero coefficient in these tests)
-            const int32_t mu = 2 * u + 1, mw = 2 * w + 1;
-            const int32_t mx = P == 0 ? 0 : (P == 1 ? mw : mu);
-            const int32_t my = P == 0 ? mu : (P == 1 ? 0 : mw);
-            const int32_t mz = P == 0 ? mw : (P == 1 ? mu : 0);
-            bool pass = true;
+            const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+            uint32_t x = nvox;
 #pragma unroll
-            for (int edge = 0; edge < 3; ++edge) {
-                const int32_t* sa = s_ax[warp][edge * 3 + P];
-                int32_t d = sa[0] * mx + sa[1] * my + sa[2] * mz;
-                pass = pass && d >= sa[3] && d <= sa[4];
+            for (int o = 1; o < 32; o <<= 1) {
+                uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+                if (lane >= uint32_t(o)) x += y;
             }
-            if (pass) atomicOr(&s_mask[warp][P], 1ull << (u + 8 * w));
+            __shared__ uint32_t s_wsum[kChunk / 32];
+            if (lane == 31) s_wsum[wid] = x;
+            __syncthreads();
+            uint32_t pre = 0;
+            for (uint32_t w = 0; w < wid; ++w) pre += s_wsum[w];
+            s_start[threadIdx.x] = pre + x - nvox;
+            if (threadIdx.x == kChunk - 1) s_start[kChunk] = pre + x;
+            __syncthreads();
         }
-        __syncwarp();
-        const unsigned long long mk0 = s_mask[warp][0], mk1 = s_mask[warp][1], mk2 = s_mask[warp][2];
-        const int nvox = nx * ny * nz;
-        for (int p = int(lane); p < nvox; p += 32) {
-            int lx = l0x + p % nx, ly = l0y + (p / nx) % ny, lz = l0z + p / (nx * ny);
-            bool hit = ((mk0 >> (ly + 8 * lz)) & (mk1 >> (lz + 8 * lx)) & (mk2 >> (lx + 8 * ly)) & 1ull) != 0;
-            if (hit) {
-                int64_t d = pn[0] * (2 * lx + 1) + pn[1] * (2 * ly + 1) + pn[2] * (2 * lz + 1);
-                hit = d >= plo && d <= phi;
+        const uint32_t total = s_start[kChunk];
+        // phase 2: all threads share the candidate voxels of the chunk evenly
+        for (uint32_t vv = threadIdx.x; vv < total; vv += blockDim.x) {
+            uint32_t lo = 0, hi = kChunk;  // the item k with s_start[k] <= vv < s_start[k + 1]
+            while (hi - lo > 1) {
+                uint32_t mid = (lo + hi) >> 1;
+                if (s_start[mid] <= vv) lo = mid; else hi = mid;
             }
-            if (hit) {
-                int li = lz * 64 + ly * 8 + lx;
-                atomicAdd(&s_sum[0][li], (unsigned long long)r.wq[0]);
-                atomicAdd(&s_sum[1][li], (unsigned long long)r.wq[1]);
-                atomicAdd(&s_sum[2][li], (unsigned long long)r.wq[2]);
-                atomicAdd(&s_cnt[li], 1u);
-            }
+            const ItemSetup& is = s_item[lo];
+            const uint32_t local = vv - s_start[lo];
+            const uint32_t ex = is.ext[0], ey = is.ext[1];
+            const int lx = is.l0[0] + int(local % ex), ly = is.l0[1] + int((local / ex) % ey),
+                      lz = is.l0[2] + int(local / (ex * ey));
+            const bool proj = ((is.mask[0] >> (ly + 8 * lz)) & (is.mask[1] >> (lz + 8 * lx)) &
+                               (is.mask[2] >> (lx + 8 * ly)) & 1ull) != 0;
+            if (!proj) continue;
+            const long long d = is.n[0] * (2 * lx + 1) + is.n[1] * (2 * ly + 1) + is.n[2] * (2 * lz + 1);
+            if (d < is.plo || d > is.phi) continue;
+            const int li = lz * 64 + ly * 8 + lx;
+            atomicAdd(&s_sum[0][li], (unsigned long long)is.wq[0]);
+            atomicAdd(&s_sum[1][li], (unsigned long long)is.wq[1]);
+            atomicAdd(&s_sum[2][li], (unsigned long long)is.wq[2]);
+            atomicAdd(&s_cnt[li], 1u);
         }
-        __syncwarp();  // the next item rewrites this warp's axis table and masks
+        __syncthreads();  // the next chunk rewrites the item table
     }
     __syncthreads();
     // resolve: radiance = luminance * shadow * mean weight, opacity 1 where covered
-    const float* lv = fr->light_vox;
-    const float half_res = 0.5f * float(res);
-    const float bias = fr->shadow_bias_f;
-    for (int li = threadIdx.x; li < 512; li += 256) {
+    for (int li = threadIdx.x; li < 512; li += kChunk) {
         int lx = li & 7, ly = (li >> 3) & 7, lz = li >> 6;
         uint32_t cnt = s_cnt[li];
         float4 out = make_float4(0.f, 0.f, 0.f, 0.f);
         if (cnt) {
-            // shadow test of the voxel centre: exact FP32 operation sequence (see frame.h)
-            float fi = float(bx * 8 + lx), fj = float(by * 8 + ly), fk = float(bz * 8 + lz);
-            float v[3];
-#pragma unroll
-            for (int rr = 0; rr < 3; ++rr) {
-                const float* c = lv + 4 * rr;
-                float s = __fadd_rn(c[0], __fmul_rn(fi, c[1]));
-                s = __fadd_rn(s, __fmul_rn(fj, c[2]));
-                v[rr] = __fadd_rn(s, __fmul_rn(fk, c[3]));
+            // mean injection weight (FP32), then radiance = luminance * (lit ? weight : 0)
+            const float q = (1.0f / 2147483648.0f) / float(cnt);
+            const float4 w = make_float4(float(s_sum[0][li]) * q, float(s_sum[1][li]) * q, float(s_sum[2][li]) * q, 1.0f);
+            if (weights) {
+                out = w;  // geometry only: relight_bricks applies the shadow test and the luminance
+            } else {
+                const bool lit = voxel_lit(fr, shadow, res, bx * 8 + lx, by * 8 + ly, bz * 8 + lz);
+                out = make_float4(light.luminance[0] * (lit ? w.x : 0.0f), light.luminance[1] * (lit ? w.y : 0.0f),
+                                  light.luminance[2] * (lit ? w.z : 0.0f), 1.0f);
             }
-            float tx = floorf(__fmul_rn(__fadd_rn(v[0], 1.0f), half_res));
-            float ty = floorf(__fmul_rn(__fadd_rn(v[1], 1.0f), half_res));
-            bool lit = true;
-            if (tx >= 0.0f && ty >= 0.0f && tx < float(res) && ty < float(res)) {
-                unsigned long long k = shadow[uint64_t(ty) * res + uint64_t(tx)];
-                float sd = k == ~0ull ? 1.0f : __uint_as_float(uint32_t(k >> 32));
-                lit = __fsub_rn(v[2], bias) <= sd;
-            }
-            float scale = lit ? (1.0f / 2147483648.0f) / float(cnt) : 0.0f;
-            out.x = light.luminance[0] * (float(s_sum[0][li]) * scale);
-            out.y = light.luminance[1] * (float(s_sum[1][li]) * scale);
-            out.z = light.luminance[2] * (float(s_sum[2][li]) * scale);
-            out.w = 1.0f;
         }
-        store_vox(chain.base, chain.format, chain.off[0] + (uint64_t(m) << 9) + li, out);
+        if (weights)
+            weights[(uint64_t(m) << 9) + li] = out;
+        else
+            store_vox(chain.base, chain.format, chain.off[0] + (uint64_t(m) << 9) + li, out);
         if (counts) {
             uint64_t lin = (uint64_t(bz * 8 + lz) * dim + uint64_t(by * 8 + ly)) * dim + uint64_t(bx * 8 + lx);
             counts[lin] = cnt;
@@ -575,10 +527,19 @@ int voxelize_launch(const VoxelizeJob& job, void* scratch, size_t scratch_bytes,
         note_launches(2);
     }
     uint32_t nblocks = job.ndirty ? job.ndirty : nbricks;
-    vox_bricks<<<nblocks, 256, 0, s>>>(sc, job.d_frame, dim, job.chain, job.light, job.shadow_keys, job.shadow_res,
-                                       job.counts, job.ndirty ? job.dirty_bricks : nullptr, d_status);
+    vox_bricks<<<nblocks, kChunk, 0, s>>>(sc, job.d_frame, dim, job.chain, job.light, job.shadow_keys, job.shadow_res,
+                                       job.counts, job.ndirty ? job.dirty_bricks : nullptr, job.weights, d_status);
     note_launches(1);
     return cuda_fail(cudaGetLastError(), "voxelize");
 }
 
+}  // namespace f184
+
+namespace f184 {
+int relight_launch(const float4* weights, const f184gi_grid_frame* d_frame, const ChainLayout& chain,
+                   const f184gi_light& light, const unsigned long long* shadow, uint32_t res, cudaStream_t s) {
+    relight_bricks<<<152 * 8, 256, 0, s>>>(weights, d_frame, chain.dim, chain, light, shadow, res);
+    note_launches(1);
+    return cuda_fail(cudaGetLastError(), "relight");
+}
 }  // namespace f184

@@ -76,6 +76,11 @@ typedef struct f184gi_light {
 
 /* grid flags */
 #define F184GI_GRID_KEEP_COUNTS 1u /* also keep the per-voxel contribution count (u32, L0) for inspection */
+/* Keep the unshadowed mean injection weight of every voxel (FP32 RGBA, 16 B/voxel) resident.  f184gi_voxelize
+ * then re-voxelizes only the dirty bricks' geometry and relights the whole grid from the new shadow map, so a
+ * moved object's shadow changes propagate without re-voxelizing the bricks it shadows.  L0 is byte-identical to
+ * a full voxelization. */
+#define F184GI_GRID_RESIDENT_WEIGHTS 2u
 
 typedef struct f184gi_grid_desc {
     uint32_t dim;         /* voxels per axis at L0: power of two, 16..512 */
@@ -181,6 +186,16 @@ void f184gi_cone_params_default(f184gi_cone_params* p);
 
 /* ---- supporting passes ---- */
 
+/* A rigid move of one object: triangles [first, first + count) translated by offset (FP32 adds per vertex). */
+typedef struct f184gi_move {
+    uint32_t first, count;
+    float offset[3];
+} f184gi_move;
+
+/* Apply moves to a device triangle buffer of ntris triangles (moves: host array). */
+int f184gi_apply_moves(f184gi_ctx* ctx, float* tri_xyz, const f184gi_move* moves, uint32_t nmoves, uint64_t ntris,
+                       void* stream);
+
 /* world_xyz = model * obj_xyz for ntris triangles (9 floats each, device buffers), model = a row-major 3x4
  * matrix in the layout of tc::Matrix3x4 (Math/Matrix3x4.h).  This is the per-primitive ModelMat transform the
  * reference applies in its voxelization geometry stage (Pipelang/Internal/main.lua:94-98, 130-131). */
@@ -197,6 +212,67 @@ int f184gi_gbuffer(f184gi_ctx* ctx, const float* tri_xyz, const float* roughness
 /* Wait for the stream, then report (and clear) errors that kernels flagged on the device since the last
  * check: F184GI_ERR_OVERFLOW (a bounded structure overflowed), F184GI_ERR_TIMEOUT (a bounded wait expired). */
 int f184gi_sync(f184gi_ctx* ctx, void* stream);
+
+/* ---- served form: continuous batching over device-resident grids ----
+ *
+ * A server owns resident scenes (triangles on the device + a grid with resident weights) and runs a request loop:
+ * requests (rigid object moves + a set of views) queue on the host; whenever one of `slots` in-flight batches
+ * is free, the scheduler admits pending requests (one per scene per batch, HBM budget for their staging
+ * buffers, at most max_batch_views views), re-voxelizes the moved objects' bricks, relights and rebuilds the
+ * mips of each touched scene, and traces every view of the batch in one persistent launch replayed from a CUDA
+ * graph.  Requests that arrive while batches run join the next batch; batches on different slots overlap.
+ * Results are the same as running each request alone (per scene, requests apply in submission order). */
+typedef struct f184gi_server f184gi_server;
+
+typedef struct f184gi_server_config {
+    int device;
+    uint32_t slots;           /* batches in flight (1..4, 0 = 2) */
+    uint32_t max_batch_views; /* views per batched launch (0 = 64) */
+    uint32_t blocks_per_sm;   /* persistent trace CTAs per SM (0 = occupancy maximum) */
+    uint64_t hbm_budget;      /* bytes for resident scenes + request staging (0 = no limit) */
+    f184gi_cone_params cone;  /* cone parameters for every request (diffuse_cones == 0: defaults) */
+} f184gi_server_config;
+
+#define F184GI_REQ_HOST_BUFFERS 1u /* view G-buffers / outputs are host pointers: staged through the budget */
+
+typedef struct f184gi_request {
+    uint32_t scene_id;
+    uint32_t flags;
+    const f184gi_move* moves; /* applied before the views are traced */
+    uint32_t nmoves;
+    uint32_t nviews;
+    const f184gi_view* views;
+} f184gi_request;
+
+typedef struct f184gi_request_result {
+    int status;         /* 0, F184GI_ERR_CANCELLED, or the failing call's status */
+    uint32_t batch;     /* batch sequence number it ran in */
+    double queued_ms;   /* submit -> admission */
+    double latency_ms;  /* submit -> results complete on the device */
+    uint64_t pixels;
+} f184gi_request_result;
+
+typedef struct f184gi_server_stats {
+    uint64_t requests_done, requests_cancelled, batches, pixels;
+    double p50_ms, p99_ms, mean_ms;  /* request latency over completed requests */
+    double mean_batch_views;
+    uint64_t hbm_used, hbm_budget;
+    uint32_t pending, inflight;
+} f184gi_server_stats;
+
+int f184gi_server_create(const f184gi_server_config* cfg, f184gi_server** out);
+int f184gi_server_destroy(f184gi_server* s);
+/* Register a scene: host triangles/albedo are copied to the device, voxelized and mip-mapped (synchronously). */
+int f184gi_server_add_scene(f184gi_server* s, uint32_t scene_id, const f184gi_grid_desc* desc, const float* tri_xyz,
+                            const uint32_t* albedo, uint64_t ntris, const f184gi_bounds* bounds,
+                            const f184gi_light* light);
+/* Queue a request (moves and views are copied); returns a ticket.  F184GI_ERR_BUDGET if its staging can never fit. */
+int f184gi_server_submit(f184gi_server* s, const f184gi_request* req, uint64_t* ticket);
+/* Wait until the ticket completes (timeout_ms 0 = no limit): F184GI_ERR_TIMEOUT when the wait expires. */
+int f184gi_server_wait(f184gi_server* s, uint64_t ticket, uint32_t timeout_ms, f184gi_request_result* out);
+/* Cancel a request that has not been admitted yet (F184GI_ERR_INVALID once it is running or done). */
+int f184gi_server_cancel(f184gi_server* s, uint64_t ticket);
+int f184gi_server_get_stats(f184gi_server* s, f184gi_server_stats* out);
 
 /* ---- inspection (host copies; synchronise the stream) ---- */
 int f184gi_grid_get_frame(f184gi_ctx* ctx, uint32_t grid, f184gi_grid_frame* out);

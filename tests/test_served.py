@@ -1,0 +1,222 @@
+"""The served form (f184gi_server_*): continuous batching over device-resident scenes.
+
+GPU: every request's traced output is byte-identical whether it ran alone or batched with others; dirty-brick
+re-voxelization after moves equals a full voxelization of the moved scene; host-buffer requests equal device-buffer
+requests; admission against the HBM budget, cancellation and bounded waits.  CPU: creating a server without a
+GPU fails with a status code (no fallback).
+"""
+import numpy as np
+import pytest
+
+SEEDS = [11, 12, 13]
+
+
+def test_server_needs_a_gpu(lib):
+    import torch
+
+    import final184_gb300 as g
+
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    with pytest.raises(g.F184Error):
+        g.Server(0)
+
+
+class Fixture:
+    """Three seeded scenes, device G-buffers for a few views each, and a reproducible request list."""
+
+    def __init__(self, dim=64, levels=6, res=1024, fmt=1):
+        import torch
+
+        import final184_gb300 as g
+
+        self.g, self.torch = g, torch
+        self.dev = torch.device("cuda:0")
+        self.scenes = [g.SyntheticScene(s, 20000, 200) for s in SEEDS]
+        self.desc = g.GridDesc(dim, levels, fmt, 0, res, 0)
+        gi = g.VoxelGI(0)
+        self.views = {}  # (scene, view) -> (V, P, W, H, depth, normal, rough)
+        sizes = [(160, 90), (128, 128), (200, 120), (96, 64)]
+        for si, sc in enumerate(self.scenes):
+            tri = torch.from_numpy(sc.tri_xyz).to(self.dev)
+            rough = torch.from_numpy(sc.roughness).to(self.dev)
+            for vi, (W, H) in enumerate(sizes):
+                eye, tgt = sc.camera(vi)
+                V = g.look_at(eye, tgt)
+                P = g.perspective(59.0, W / H, 0.1, 100.0)
+                n = W * H
+                d = torch.empty(n, dtype=torch.float32, device=self.dev)
+                nr = torch.empty(n, dtype=torch.int32, device=self.dev)
+                rg = torch.empty(n, dtype=torch.int16, device=self.dev)
+                out = torch.empty(2 * n * 4, dtype=torch.float32, device=self.dev)
+                view = g.make_view(V, P, W, H, d.data_ptr(), nr.data_ptr(), rg.data_ptr(), out.data_ptr())
+                gi.gbuffer(tri.data_ptr(), rough.data_ptr(), sc.ntris, view)
+                self.views[(si, vi)] = (V, P, W, H, d, nr, rg)
+        gi.sync()
+        gi.close()
+        rng = np.random.default_rng(5)
+        self.requests = []  # (scene, [view ids], [moves])
+        for k in range(12):
+            si = int(rng.integers(0, 3))
+            nv = int(rng.integers(1, 5))
+            vids = [int(x) for x in rng.choice(4, nv, replace=False)]
+            sc = self.scenes[si]
+            moves = []
+            for o in rng.choice(np.arange(1, sc.nobjects), 3, replace=False):
+                off = rng.uniform(-0.3, 0.3, 3).astype(np.float32)
+                moves.append((int(sc.object_first[o]), int(sc.object_count[o]), [float(x) for x in off]))
+            self.requests.append((si, vids, moves))
+
+    def server(self, **kw):
+        srv = self.g.Server(0, **kw)
+        for si, sc in enumerate(self.scenes):
+            srv.add_scene(si, self.desc, sc.tri_xyz, sc.albedo, sc.bounds, sc.light)
+        return srv
+
+    def make_views(self, si, vids, out_dtype=np.float32):
+        outs, views = [], []
+        for vi in vids:
+            V, P, W, H, d, nr, rg = self.views[(si, vi)]
+            out = self.torch.zeros(2 * W * H * 4, dtype=self.torch.float32, device=self.dev)
+            outs.append(out)
+            views.append(self.g.make_view(V, P, W, H, d.data_ptr(), nr.data_ptr(), rg.data_ptr(), out.data_ptr()))
+        return views, outs
+
+
+@pytest.fixture(scope="module")
+def fx(lib):
+    return Fixture()
+
+
+def run_all(fx, srv, one_at_a_time):
+    results, keep = [], []
+    tickets = []
+    for si, vids, moves in fx.requests:
+        views, outs = fx.make_views(si, vids)
+        keep.append(outs)
+        t = srv.submit(si, views, moves)
+        tickets.append(t)
+        if one_at_a_time:
+            srv.wait(t)
+    res = [srv.wait(t) for t in tickets]
+    fx.torch.cuda.synchronize()
+    for outs in keep:
+        results.append([o.cpu().numpy().copy() for o in outs])
+    return results, res
+
+
+@pytest.mark.gpu
+def test_each_request_same_alone_and_in_the_mix(fx):
+    srv = fx.server(slots=2, max_batch_views=32)
+    alone, _ = run_all(fx, srv, one_at_a_time=True)
+    srv.close()
+    srv = fx.server(slots=2, max_batch_views=32)
+    mixed, res = run_all(fx, srv, one_at_a_time=False)
+    st = srv.stats()
+    srv.close()
+    assert st.requests_done == len(fx.requests)
+    assert max(r.batch for r in res) < len(fx.requests)  # some requests really shared a batch
+    for a, b in zip(alone, mixed):
+        for x, y in zip(a, b):
+            assert np.array_equal(x.view(np.uint32), y.view(np.uint32))
+    assert any(float(np.abs(x).sum()) > 0 for a in mixed for x in a)
+
+
+@pytest.mark.gpu
+def test_dirty_updates_equal_full_voxelization(fx):
+    g, torch = fx.g, fx.torch
+    srv = fx.server(slots=1)
+    # apply every request's moves of scene 0 in order, then trace view 0
+    moved = g.SyntheticScene(SEEDS[0], 20000, 200)
+    tri = moved.tri_xyz.copy()
+    for si, vids, moves in fx.requests:
+        if si != 0:
+            continue
+        views, outs = fx.make_views(0, [0])
+        srv.wait(srv.submit(0, views, moves))
+        for f, c, off in moves:
+            seg = tri[f * 9:(f + c) * 9].reshape(-1, 3)
+            seg += np.asarray(off, dtype=np.float32)
+            tri[f * 9:(f + c) * 9] = seg.ravel()
+    views, served_out = fx.make_views(0, [0])
+    srv.wait(srv.submit(0, views, []))
+    srv.close()
+    # the same geometry voxelized from scratch through the plain API
+    gi = g.VoxelGI(0)
+    grid = gi.create_grid(fx.desc.dim, fx.desc.levels, fx.desc.format, 0, fx.desc.shadow_res)
+    td = torch.from_numpy(tri).to(fx.dev)
+    ad = torch.from_numpy(moved.albedo.view(np.int32)).to(fx.dev)
+    gi.voxelize(grid, td.data_ptr(), ad.data_ptr(), moved.ntris, moved.light, bounds=moved.bounds)
+    gi.mip(grid)
+    views2, plain_out = fx.make_views(0, [0])
+    gi.trace(grid, views2)
+    gi.sync()
+    a = served_out[0].cpu().numpy()
+    b = plain_out[0].cpu().numpy()
+    assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+    gi.close()
+
+
+@pytest.mark.gpu
+def test_host_buffer_requests_match_device_requests(fx):
+    g = fx.g
+    srv = fx.server(slots=2)
+    si, vids = 1, [0, 2]
+    views, outs = fx.make_views(si, vids)
+    srv.wait(srv.submit(si, views, []))
+    dev = [o.cpu().numpy() for o in outs]
+    hviews, host_out, keep = [], [], []
+    for vi in vids:
+        V, P, W, H, d, nr, rg = fx.views[(si, vi)]
+        hd, hn, hr = d.cpu().numpy(), nr.cpu().numpy(), rg.cpu().numpy()
+        ho = np.zeros(2 * W * H * 4, np.float32)
+        keep += [hd, hn, hr]
+        host_out.append(ho)
+        hviews.append(g.make_view(V, P, W, H, hd.ctypes.data, hn.ctypes.data, hr.ctypes.data, ho.ctypes.data))
+    srv.wait(srv.submit(si, hviews, [], host_buffers=True))
+    srv.close()
+    for a, b in zip(dev, host_out):
+        assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+
+
+@pytest.mark.gpu
+def test_admission_budget_cancel_and_timeout(fx):
+    g = fx.g
+    # a budget too small for the scene is refused at registration
+    srv = g.Server(0, hbm_budget=64 << 20)
+    with pytest.raises(g.F184Error) as e:
+        sc = fx.scenes[0]
+        srv.add_scene(0, fx.desc, sc.tri_xyz, sc.albedo, sc.bounds, sc.light)
+    assert e.value.code == g._abi.ERR_BUDGET
+    srv.close()
+    # a host-buffer request whose staging can never fit is refused at submission
+    srv = fx.server(slots=1, hbm_budget=2 << 30)
+    big = 1 << 15
+    bogus = np.zeros(16, np.float32)
+    v = g.make_view(np.eye(4), g.perspective(59.0, 1.0, 0.1, 100.0), big, big, bogus.ctypes.data, bogus.ctypes.data,
+                    bogus.ctypes.data, bogus.ctypes.data)
+    with pytest.raises(g.F184Error) as e:
+        srv.submit(0, [v], [], host_buffers=True)
+    assert e.value.code == g._abi.ERR_BUDGET
+    # queue several requests on one slot: the last is still pending and can be cancelled
+    tickets = []
+    keep = []
+    for k in range(6):
+        views, outs = fx.make_views(k % 3, [0, 1, 2, 3])
+        keep.append(outs)
+        tickets.append(srv.submit(k % 3, views, fx.requests[k][2]))
+    srv.cancel(tickets[-1])
+    r = srv.wait(tickets[-1])
+    assert r.status == g._abi.ERR_CANCELLED
+    # a bounded wait can expire (1 ms on a request queued behind others) without disturbing the request
+    try:
+        srv.wait(tickets[-2], timeout_ms=1)
+    except g.F184Error as ex:
+        assert ex.code == g._abi.ERR_TIMEOUT
+    for t in tickets[:-1]:
+        assert srv.wait(t).status == 0
+    with pytest.raises(g.F184Error):
+        srv.cancel(tickets[0])  # already done
+    st = srv.stats()
+    assert st.requests_done == 5 and st.requests_cancelled == 1
+    srv.close()
