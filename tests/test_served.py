@@ -182,8 +182,8 @@ def test_host_buffer_requests_match_device_requests(fx):
 @pytest.mark.gpu
 def test_admission_budget_cancel_and_timeout(fx):
     g = fx.g
-    # a budget too small for the scene is refused at registration
-    srv = g.Server(0, hbm_budget=64 << 20)
+    # a budget too small for the scene (a 64^3 FP16 chain with resident weights takes ~15 MB) is refused
+    srv = g.Server(0, hbm_budget=4 << 20)
     with pytest.raises(g.F184Error) as e:
         sc = fx.scenes[0]
         srv.add_scene(0, fx.desc, sc.tri_xyz, sc.albedo, sc.bounds, sc.light)
@@ -204,7 +204,9 @@ def test_admission_budget_cancel_and_timeout(fx):
     for k in range(6):
         views, outs = fx.make_views(k % 3, [0, 1, 2, 3])
         keep.append(outs)
-        tickets.append(srv.submit(k % 3, views, fx.requests[k][2]))
+        nt = fx.scenes[k % 3].ntris
+        moves = [m for m in fx.requests[k][2] if m[0] + m[1] <= nt]
+        tickets.append(srv.submit(k % 3, views, moves))
     srv.cancel(tickets[-1])
     r = srv.wait(tickets[-1])
     assert r.status == g._abi.ERR_CANCELLED
