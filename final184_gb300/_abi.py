@@ -121,6 +121,7 @@ PROTOTYPES = {
     "f184gi_trace": (C.c_int, [P, U32, C.POINTER(View), U32, C.POINTER(ConeParams), P]),
     "f184gi_cone_params_default": (None, [C.POINTER(ConeParams)]),
     "f184gi_gbuffer": (C.c_int, [P, P, P, U64, C.POINTER(View), P, P]),
+    "f184gi_gbuffer_static": (C.c_int, [P, P, P, U64, C.POINTER(View), P, P]),
     "f184gi_transform": (C.c_int, [P, P, U64, PF, P, P]),
     "f184gi_apply_moves": (C.c_int, [P, P, C.POINTER(Move), U32, U64, P]),
     "f184gi_sync": (C.c_int, [P, P]),

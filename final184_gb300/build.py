@@ -16,7 +16,7 @@ CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-CU_SOURCES = ["util.cu", "raster.cu", "voxelize.cu", "mip.cu", "trace.cu"]
+CU_SOURCES = ["util.cu", "raster.cu", "voxelize.cu", "mip.cu", "trace.cu", "noalloc.cu"]
 CPP_SOURCES = ["api.cpp", "scene.cpp", "serve.cpp"]
 
 

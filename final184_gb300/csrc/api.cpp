@@ -586,4 +586,20 @@ int grid_internal(f184gi_ctx* c, uint32_t grid, ChainLayout* chain, const f184gi
     *d_frame = g->d_frame;
     return F184GI_OK;
 }
+
+int ctx_internal(f184gi_ctx* c, int* device, uint32_t** d_status) {
+    if (!c || !device || !d_status) return fail(F184GI_ERR_INVALID, "ctx_internal: null argument");
+    *device = c->device;
+    *d_status = c->d_status;
+    return F184GI_OK;
+}
+
+void view_clip_matrix(const f184gi_view* v, double M[16]) {
+    for (int r = 0; r < 4; ++r)
+        for (int k = 0; k < 4; ++k) {
+            double acc = 0.0;
+            for (int j = 0; j < 4; ++j) acc += double(v->proj[r * 4 + j]) * double(v->view[j * 4 + k]);
+            M[r * 4 + k] = acc;
+        }
+}
 }  // namespace f184

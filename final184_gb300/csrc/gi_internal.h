@@ -131,6 +131,10 @@ void trace_graph_destroy(TraceGraph* g);
 
 // grid of a context as the kernels see it (chain layout and device frame)
 int grid_internal(f184gi_ctx* c, uint32_t grid, ChainLayout* chain, const f184gi_grid_frame** d_frame);
+// the context's device ordinal and device status word
+int ctx_internal(f184gi_ctx* c, int* device, uint32_t** d_status);
+// clip = proj * view of a view in FP64, summed in index order without FMA contraction
+void view_clip_matrix(const f184gi_view* v, double M[16]);
 
 int gbuffer_resolve_launch(const unsigned long long* keys, uint32_t width, uint32_t height, const float* tri,
                            const float* rough, const float view[16], const float eye[3], float* depth,

@@ -209,6 +209,18 @@ int f184gi_transform(f184gi_ctx* ctx, const float* obj_xyz, uint64_t ntris, cons
 int f184gi_gbuffer(f184gi_ctx* ctx, const float* tri_xyz, const float* roughness, uint64_t ntris,
                    const f184gi_view* view, uint32_t* tri_id_out, void* stream);
 
+/* f184gi_gbuffer without any device allocation; no counterpart in the reference.  For callers that cannot
+ * allocate device memory while they draw: a render loop that must not stall on the device-wide synchronisation
+ * of cudaMalloc/cudaFree, or a process whose device memory is all handed out (to a caching allocator, or to a
+ * context at its HBM budget).  Same arguments and results as f184gi_gbuffer; the scratch is one fixed 48 MiB
+ * device array in the library, shared by every call on a device.  Limits: ntris <= 262144 and
+ * width*height <= 2097152 (1920x1080 fits); larger calls return F184GI_ERR_INVALID and name the limit.  The
+ * first call on a device looks up the array's address (and can load its module): make it before any stream
+ * capture.  Calls that overlap on the GPU race on the array; calls in order on one stream do not.  Errors that
+ * kernels flag are reported by f184gi_sync(ctx, stream) as for f184gi_gbuffer. */
+int f184gi_gbuffer_static(f184gi_ctx* ctx, const float* tri_xyz, const float* roughness, uint64_t ntris,
+                          const f184gi_view* view, uint32_t* tri_id_out, void* stream);
+
 /* Wait for the stream, then report (and clear) errors that kernels flagged on the device since the last
  * check: F184GI_ERR_OVERFLOW (a bounded structure overflowed), F184GI_ERR_TIMEOUT (a bounded wait expired). */
 int f184gi_sync(f184gi_ctx* ctx, void* stream);
