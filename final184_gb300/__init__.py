@@ -241,10 +241,13 @@ def make_view(view_m, proj_m, width, height, depth_ptr, normal_ptr, rough_ptr, o
 class Server:
     """Continuous-batching request server over device-resident scenes (f184gi_server_*)."""
 
-    def __init__(self, device=0, slots=2, max_batch_views=64, blocks_per_sm=0, hbm_budget=0, cone=None):
+    def __init__(self, device=0, slots=2, max_batch_views=64, blocks_per_sm=0, hbm_budget=0, cone=None,
+                 trace_variant=None):
+        """trace_variant None: tune the cone-trace kernel variant on the first batch; k: use variant k."""
         self.lib = load()
         cfg = _abi.ServerConfig(device, slots, max_batch_views, blocks_per_sm, hbm_budget,
-                                cone if cone is not None else _abi.ConeParams())
+                                cone if cone is not None else _abi.ConeParams(),
+                                0 if trace_variant is None else trace_variant + 1, 0)
         h = C.c_void_p()
         check(self.lib.f184gi_server_create(C.byref(cfg), C.byref(h)))
         self.h = h

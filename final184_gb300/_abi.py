@@ -67,7 +67,8 @@ class Move(C.Structure):
 
 class ServerConfig(C.Structure):
     _fields_ = [("device", C.c_int), ("slots", C.c_uint32), ("max_batch_views", C.c_uint32),
-                ("blocks_per_sm", C.c_uint32), ("hbm_budget", C.c_uint64), ("cone", ConeParams)]
+                ("blocks_per_sm", C.c_uint32), ("hbm_budget", C.c_uint64), ("cone", ConeParams),
+                ("trace_variant", C.c_uint32), ("pad", C.c_uint32)]
 
 
 class Request(C.Structure):
@@ -84,7 +85,9 @@ class ServerStats(C.Structure):
     _fields_ = [("requests_done", C.c_uint64), ("requests_cancelled", C.c_uint64), ("batches", C.c_uint64),
                 ("pixels", C.c_uint64), ("p50_ms", C.c_double), ("p99_ms", C.c_double), ("mean_ms", C.c_double),
                 ("mean_batch_views", C.c_double), ("hbm_used", C.c_uint64), ("hbm_budget", C.c_uint64),
-                ("pending", C.c_uint32), ("inflight", C.c_uint32)]
+                ("pending", C.c_uint32), ("inflight", C.c_uint32), ("trace_variant", C.c_uint32),
+                ("trace_variants", C.c_uint32), ("trace_tile", C.c_uint32 * 2), ("trace_ctas_per_sm", C.c_uint32),
+                ("pad", C.c_uint32), ("tune_ms", C.c_float * 8)]
 
 
 class Config(C.Structure):

@@ -92,6 +92,8 @@ struct f184gi_ctx {
     uint32_t next_id = 1;
     Scratch raster, vox, trace, misc, keys;
     uint32_t* d_status = nullptr;
+    TraceStaging* trace_stage = nullptr;
+    uint32_t trace_variant = kTraceDefaultVariant;
 };
 
 namespace {
@@ -231,6 +233,7 @@ int f184gi_destroy(f184gi_ctx* c) {
         dev_free(c, g.d_frame, sizeof(f184gi_grid_frame));
     }
     for (Scratch* s : {&c->raster, &c->vox, &c->trace, &c->misc, &c->keys}) dev_free(c, s->ptr, s->bytes);
+    trace_staging_destroy(c->trace_stage);
     dev_free(c, c->d_status, 256);
     delete c;
     return F184GI_OK;
@@ -452,8 +455,8 @@ int f184gi_trace(f184gi_ctx* c, uint32_t grid, const f184gi_view* views, uint32_
     }
     int rc = scratch_get(c, c->trace, trace_scratch_bytes(nviews));
     if (rc) return rc;
-    return trace_launch(g->chain, tc, g->d_frame, tv.data(), nviews, c->trace.ptr, c->trace.bytes,
-                        static_cast<cudaStream_t>(stream));
+    return trace_launch(g->chain, tc, g->d_frame, tv.data(), nviews, c->trace.ptr, c->trace.bytes, c->trace_variant,
+                        &c->trace_stage, static_cast<cudaStream_t>(stream));
 }
 
 int f184gi_gbuffer(f184gi_ctx* c, const float* tri, const float* rough, uint64_t ntris, const f184gi_view* view,

@@ -111,22 +111,37 @@ struct TraceConsts {
     float cos_tilt, sin_tilt;
     f184gi_cone_params p;
 };
-int trace_launch(const ChainLayout& chain, const TraceConsts& tc, const f184gi_grid_frame* d_frame,
-                 const TraceView* views, uint32_t nviews, void* scratch, size_t scratch_bytes, cudaStream_t s);
-size_t trace_scratch_bytes(uint32_t nviews);
-// batched tracing: fill a view table on the host (returns the tile count), copy it to the device, launch
+// Cone-trace kernel variants: the tile shape (tw x th pixels, one thread each) and the CTAs kept resident per SM
+// (the register budget).  Every variant computes each pixel with the same arithmetic, so results are identical;
+// the batched launch picks the fastest by timing them on the work it serves.
+struct TraceVariant {
+    uint32_t tw, th, minb;
+};
+constexpr uint32_t kTraceVariantCount = 5;
+constexpr TraceVariant kTraceVariants[kTraceVariantCount] = {
+    {16, 8, 4}, {16, 8, 6}, {8, 8, 12}, {32, 4, 6}, {8, 16, 6}};
+constexpr uint32_t kTraceDefaultVariant = 0;
+const void* trace_kernel_fn(uint32_t fmt, bool aniso, uint32_t variant);
+uint32_t trace_view_tiles(uint32_t width, uint32_t height, uint32_t variant);
 void trace_view_set_grid(TraceView& v, const ChainLayout& c, const f184gi_grid_frame* d_frame, float tmax);
-size_t trace_table_bytes(uint32_t nviews);
-uint32_t trace_fill_table(const TraceView* views, uint32_t nviews, void* host_table);
-int trace_launch_table(uint32_t fmt, bool aniso, const TraceConsts& tc, const void* dev_table, uint32_t nviews,
-                       uint32_t ntiles, uint32_t* work, uint32_t persistent_blocks, cudaStream_t s);
 
-// Batched persistent trace replayed from a CUDA graph: [view table H2D] -> [work counter = 0] -> [kernel].
+// One-shot launch of one or more views of one grid (the view table goes through pinned staging).
+struct TraceStaging;
+void trace_staging_destroy(TraceStaging* st);
+size_t trace_scratch_bytes(uint32_t nviews);
+int trace_launch(const ChainLayout& chain, const TraceConsts& tc, const f184gi_grid_frame* d_frame,
+                 const TraceView* views, uint32_t nviews, void* scratch, size_t scratch_bytes, uint32_t variant,
+                 TraceStaging** staging, cudaStream_t s);
+
+// Batched persistent trace replayed from CUDA graphs: [view table H2D] -> [work counter = 0] -> [kernel].
 struct TraceGraph;
-uint32_t trace_persistent_blocks(uint32_t fmt, bool aniso, uint32_t per_sm);  // per_sm 0 = occupancy maximum
-int trace_graph_create(TraceGraph** out, uint32_t fmt, bool aniso, uint32_t max_views, uint32_t blocks,
+uint32_t trace_persistent_blocks(uint32_t fmt, bool aniso, uint32_t variant, uint32_t per_sm);  // per_sm 0 = max
+int trace_graph_create(TraceGraph** out, uint32_t fmt, bool aniso, uint32_t max_views, uint32_t per_sm,
                        const TraceConsts& tc);
-int trace_graph_launch(TraceGraph* g, const TraceView* views, uint32_t nviews, cudaStream_t s);
+int trace_graph_launch(TraceGraph* g, const TraceView* views, uint32_t nviews, uint32_t variant, cudaStream_t s);
+// time every variant on this batch (outputs are written each time, identically); the fastest goes to *best
+int trace_graph_tune(TraceGraph* g, const TraceView* views, uint32_t nviews, cudaStream_t s, uint32_t* best,
+                     float* ms);
 void trace_graph_destroy(TraceGraph* g);
 
 // grid of a context as the kernels see it (chain layout and device frame)

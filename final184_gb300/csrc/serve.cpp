@@ -109,11 +109,20 @@ struct f184gi_server {
     uint64_t hbm_used = 0;
     int fmt = -1, aniso = -1;
     TraceConsts tc{};
+    int variant = -1;  // trace kernel variant, tuned on the first batch
+    float tune_ms[kTraceVariantCount] = {};
     std::vector<double> lat;
     uint64_t done_n = 0, cancelled = 0, batches = 0, pixels = 0, batch_views = 0;
 };
 
 namespace {
+
+uint32_t sm_count() {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    return uint32_t(sms > 0 ? sms : 1);
+}
 
 void mark_box(Scene* sc, const float mn[3], const float mx[3]) {
     const double vs = sc->frame.voxel_size;
@@ -248,12 +257,22 @@ int issue_batch(f184gi_server* S, Slot& slot) {
         }
     }
     if (!slot.graph) {
-        uint32_t blocks = trace_persistent_blocks(uint32_t(S->fmt), S->aniso != 0, S->cfg.blocks_per_sm);
-        int rc = trace_graph_create(&slot.graph, uint32_t(S->fmt), S->aniso != 0, S->cfg.max_batch_views, blocks, S->tc);
+        int rc = trace_graph_create(&slot.graph, uint32_t(S->fmt), S->aniso != 0, S->cfg.max_batch_views,
+                                    S->cfg.blocks_per_sm, S->tc);
         if (rc) return rc;
     }
-    int rc = trace_graph_launch(slot.graph, slot.tv.data(), uint32_t(slot.tv.size()), s);
-    if (rc) return rc;
+    int rc = F184GI_OK;
+    if (S->variant < 0) {  // first batch: it runs alone (the scheduler issues nothing else meanwhile)
+        uint32_t best = kTraceDefaultVariant;
+        float ms[kTraceVariantCount];
+        if ((rc = trace_graph_tune(slot.graph, slot.tv.data(), uint32_t(slot.tv.size()), s, &best, ms))) return rc;
+        std::lock_guard<std::mutex> lk(S->mu);
+        for (uint32_t v = 0; v < kTraceVariantCount; ++v) S->tune_ms[v] = ms[v];
+        S->variant = int(best);
+    } else {
+        rc = trace_graph_launch(slot.graph, slot.tv.data(), uint32_t(slot.tv.size()), uint32_t(S->variant), s);
+        if (rc) return rc;
+    }
     for (size_t k = 0; k < slot.reqs.size(); ++k)
         if ((rc = stage_out(slot.reqs[k], host_out[k], s))) return rc;
     return cuda_fail(cudaEventRecord(slot.done, s), "server: batch event");
@@ -396,6 +415,9 @@ int f184gi_server_create(const f184gi_server_config* cfg, f184gi_server** out) {
     if (c.max_batch_views == 0) c.max_batch_views = 64;
     if (c.max_batch_views > 4096) return fail(F184GI_ERR_INVALID, "server_create: max_batch_views too large");
     if (c.cone.diffuse_cones == 0) f184gi_cone_params_default(&c.cone);
+    if (c.trace_variant > kTraceVariantCount)
+        return fail(F184GI_ERR_INVALID, "server_create: trace_variant must be 0 (tune) or 1.." +
+                                            std::to_string(kTraceVariantCount));
     cudaError_t e = cudaSetDevice(c.device);
     if (e != cudaSuccess) return cuda_fail(e, "server_create: device");
     f184gi_server* S = new f184gi_server();
@@ -405,6 +427,7 @@ int f184gi_server_create(const f184gi_server_config* cfg, f184gi_server** out) {
     S->tc.cos_tilt = float(std::cos(tilt));
     S->tc.sin_tilt = float(std::sin(tilt));
     S->tc.tmax = 0.0f;  // per view
+    if (c.trace_variant) S->variant = int(c.trace_variant) - 1;
     S->slots.resize(c.slots);
     for (Slot& sl : S->slots) {
         if ((e = cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking)) != cudaSuccess ||
@@ -625,6 +648,17 @@ int f184gi_server_get_stats(f184gi_server* S, f184gi_server_stats* out) {
     uint32_t inflight = 0;
     for (const Slot& sl : S->slots) inflight += sl.busy ? 1u : 0u;
     out->inflight = inflight;
+    out->trace_variants = kTraceVariantCount;
+    if (S->variant >= 0 && S->fmt >= 0) {
+        const TraceVariant& v = kTraceVariants[S->variant];
+        out->trace_variant = uint32_t(S->variant);
+        out->trace_tile[0] = v.tw;
+        out->trace_tile[1] = v.th;
+        out->trace_ctas_per_sm = trace_persistent_blocks(uint32_t(S->fmt), S->aniso != 0, uint32_t(S->variant),
+                                                         S->cfg.blocks_per_sm) /
+                                 std::max(1u, sm_count());
+        for (uint32_t k = 0; k < kTraceVariantCount && k < 8; ++k) out->tune_ms[k] = S->tune_ms[k];
+    }
     return F184GI_OK;
 }
 

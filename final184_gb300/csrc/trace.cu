@@ -1,361 +1,28 @@
-// trace.cu -- per-pixel diffuse + specular cone trace over a G-buffer.
-//
-// Replaces the reference's indirect pass (Shader/Lighting/indirect.frag:104-243), which marches four
-// stochastic single rays per pixel through a one-level RG16UI volume.  Here each pixel traces five diffuse cones
-// (60-degree aperture: one along the normal, four tilted 60 degrees, in the frame of the reference's
-// make_coord_space, indirect.frag:71-86) and one specular cone whose tan(half aperture) is the G-buffer
-// roughness.  A cone steps by half its diameter, samples the mip chain quadrilinearly (trilinear inside a
-// level, linear between log2(diameter) levels, zero outside the grid) and composites front to back in FP32.
-// The G-buffer decode follows indirect.frag:44-58 and 189-196 (InvProj, then InvModelView).
+// trace.cu -- host side of the cone trace: view tables, launches of the kernel variants (trace_kernel.cuh, one
+// translation unit per storage format and mip kind), the batched persistent launch under CUDA graphs, and the
+// variant tuner.
+#include <algorithm>
 #include <vector>
 
-#include "gi_device.cuh"
+#include "gi_internal.h"
 
 namespace f184 {
-namespace {
 
-__device__ __forceinline__ float3 f3(float x, float y, float z) { return make_float3(x, y, z); }
-__device__ __forceinline__ float3 add3(float3 a, float3 b) { return f3(a.x + b.x, a.y + b.y, a.z + b.z); }
-__device__ __forceinline__ float3 sub3(float3 a, float3 b) { return f3(a.x - b.x, a.y - b.y, a.z - b.z); }
-__device__ __forceinline__ float3 mul3(float3 a, float s) { return f3(a.x * s, a.y * s, a.z * s); }
-__device__ __forceinline__ float dot3(float3 a, float3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
-__device__ __forceinline__ float3 cross3(float3 a, float3 b) {
-    return f3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
-}
-__device__ __forceinline__ float3 norm3(float3 a) {
-    float l = sqrtf(dot3(a, a));
-    return l > 0.0f ? mul3(a, 1.0f / l) : a;
+const void* trace_kernel_f32_iso(uint32_t variant);
+const void* trace_kernel_f32_aniso(uint32_t variant);
+const void* trace_kernel_f16_iso(uint32_t variant);
+const void* trace_kernel_f16_aniso(uint32_t variant);
+
+const void* trace_kernel_fn(uint32_t fmt, bool aniso, uint32_t variant) {
+    if (variant >= kTraceVariantCount) return nullptr;
+    if (fmt == F184GI_FMT_F32) return aniso ? trace_kernel_f32_aniso(variant) : trace_kernel_f32_iso(variant);
+    return aniso ? trace_kernel_f16_aniso(variant) : trace_kernel_f16_iso(variant);
 }
 
-// make_coord_space, indirect.frag:71-86
-__device__ __forceinline__ void coord_space(float3 n, float3& x, float3& y, float3& z) {
-    z = n;
-    float3 h = z;
-    float ax = fabsf(h.x), ay = fabsf(h.y), az = fabsf(h.z);
-    if (ax <= ay && ax <= az)
-        h.x = 1.0f;
-    else if (ay <= ax && ay <= az)
-        h.y = 1.0f;
-    else
-        h.z = 1.0f;
-    z = norm3(z);
-    y = norm3(cross3(h, z));
-    x = norm3(cross3(z, y));
+uint32_t trace_view_tiles(uint32_t width, uint32_t height, uint32_t variant) {
+    const TraceVariant& v = kTraceVariants[variant];
+    return ((width + v.tw - 1) / v.tw) * ((height + v.th - 1) / v.th);
 }
-
-__device__ __forceinline__ float3 oct_decode(uint32_t p) {
-    float x = __half2float(__ushort_as_half(uint16_t(p & 0xffffu)));
-    float y = __half2float(__ushort_as_half(uint16_t(p >> 16)));
-    float3 v = f3(x, y, 1.0f - fabsf(x) - fabsf(y));
-    if (v.z < 0.0f) {
-        float ox = v.x, oy = v.y;
-        v.x = (1.0f - fabsf(oy)) * (ox >= 0.0f ? 1.0f : -1.0f);
-        v.y = (1.0f - fabsf(ox)) * (oy >= 0.0f ? 1.0f : -1.0f);
-    }
-    return norm3(v);
-}
-
-// The grid a tile traces against, staged in shared memory per CTA: lanes index the level table with their own
-// (divergent) level, which the constant bank would serialise, and batched launches trace many grids.
-struct GridRef {
-    uint64_t off[kMaxLevels];
-    uint64_t vol[kMaxLevels];
-    const void* base;
-    uint32_t dim, levels;
-    float tmax;
-    float org[3];
-    float inv_vs;
-};
-
-// 8-tap trilinear sample of one volume of level l (d voxels per axis) at x (L0 voxel units); taps outside the
-// volume read zero.  Interior samples (all taps inside) address the seven other taps from the first one with
-// one delta per axis: +1 / +8 / +64 inside a brick, or the Morton step to the next brick when the tap crosses a
-// brick face.  Samples touching the border take the general path with a validity test per tap.
-template <int FMT>
-__device__ __forceinline__ float4 tri_sample(const void* base, int d, uint32_t l, uint64_t vol_off, float3 x) {
-    const float s = __int_as_float((127 - int(l)) << 23);  // 2^-l
-    const float u[3] = {x.x * s - 0.5f, x.y * s - 0.5f, x.z * s - 0.5f};
-    int c0[3];
-    float f[3];
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-        float fl = floorf(u[a]);
-        c0[a] = int(fl);
-        f[a] = u[a] - fl;
-    }
-    const float wx[2] = {1.0f - f[0], f[0]}, wy[2] = {1.0f - f[1], f[1]}, wz[2] = {1.0f - f[2], f[2]};
-    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
-    const unsigned lim = unsigned(d - 1);
-    if (unsigned(c0[0]) < lim && unsigned(c0[1]) < lim && unsigned(c0[2]) < lim) {
-        int64_t i0, dx, dy, dz;
-        if (d >= 8) {
-            uint32_t hs[3];
-            int64_t del[3];
-#pragma unroll
-            for (int a = 0; a < 3; ++a) {
-                uint32_t b = uint32_t(c0[a]) >> 3;
-                hs[a] = part1by2(b);
-                const int64_t step_in = int64_t(1) << (3 * a);
-                // crossing the brick face: local coordinate 7 -> 0 and the Morton code steps along axis a
-                const int64_t cross = (int64_t(part1by2(b + 1) - hs[a]) << (9 + a)) - 7 * step_in;
-                del[a] = (c0[a] & 7) != 7 ? step_in : cross;
-            }
-            i0 = (int64_t(hs[0] | (hs[1] << 1) | (hs[2] << 2)) << 9) |
-                 ((c0[2] & 7) << 6) | ((c0[1] & 7) << 3) | (c0[0] & 7);
-            dx = del[0], dy = del[1], dz = del[2];
-        } else {
-            i0 = (int64_t(c0[2]) * d + c0[1]) * d + c0[0];
-            dx = 1, dy = d, dz = int64_t(d) * d;
-        }
-        const int64_t ib = int64_t(vol_off) + i0;
-#pragma unroll
-        for (int tz = 0; tz < 2; ++tz)
-#pragma unroll
-            for (int ty = 0; ty < 2; ++ty) {
-                const float wyz = wy[ty] * wz[tz];
-                const int64_t row = ib + (tz ? dz : 0) + (ty ? dy : 0);
-#pragma unroll
-                for (int tx = 0; tx < 2; ++tx) {
-                    float4 v = load_vox(base, FMT, uint64_t(row + (tx ? dx : 0)));
-                    float w = wx[tx] * wyz;
-                    acc.x += w * v.x;
-                    acc.y += w * v.y;
-                    acc.z += w * v.z;
-                    acc.w += w * v.w;
-                }
-            }
-        return acc;
-    }
-    // border: per-axis validity, high (Morton) and low (in-brick / linear) address parts
-    bool ok[3][2];
-    uint32_t hi[3][2], lo[3][2];
-    const bool bricked = d >= 8;
-#pragma unroll
-    for (int a = 0; a < 3; ++a)
-#pragma unroll
-        for (int t = 0; t < 2; ++t) {
-            int c = c0[a] + t;
-            ok[a][t] = unsigned(c) < unsigned(d);
-            uint32_t cu = uint32_t(c) & 1023u;
-            if (bricked) {
-                hi[a][t] = part1by2(cu >> 3) << a;
-                lo[a][t] = (cu & 7u) << (3 * a);
-            } else {
-                hi[a][t] = 0;
-                lo[a][t] = a == 0 ? cu : (a == 1 ? cu * uint32_t(d) : cu * uint32_t(d * d));
-            }
-        }
-#pragma unroll
-    for (int tz = 0; tz < 2; ++tz)
-#pragma unroll
-        for (int ty = 0; ty < 2; ++ty) {
-            const float wyz = wy[ty] * wz[tz];
-#pragma unroll
-            for (int tx = 0; tx < 2; ++tx) {
-                if (ok[0][tx] && ok[1][ty] && ok[2][tz]) {
-                    uint64_t idx = (uint64_t(hi[0][tx] | hi[1][ty] | hi[2][tz]) << 9) | (lo[0][tx] | lo[1][ty] | lo[2][tz]);
-                    float4 v = load_vox(base, FMT, vol_off + idx);
-                    float w = wx[tx] * wyz;
-                    acc.x += w * v.x;
-                    acc.y += w * v.y;
-                    acc.z += w * v.z;
-                    acc.w += w * v.w;
-                }
-            }
-        }
-    return acc;
-}
-
-template <int FMT, bool ANISO>
-__device__ __forceinline__ float4 level_sample(const GridRef& g, uint32_t l, float3 x, float3 dir) {
-    const int d = int(g.dim >> l);
-    if (!ANISO || l == 0) return tri_sample<FMT>(g.base, d, l, g.off[l], x);
-    float w[3] = {dir.x * dir.x, dir.y * dir.y, dir.z * dir.z};
-    int sel[3] = {dir.x >= 0.0f ? 0 : 1, dir.y >= 0.0f ? 2 : 3, dir.z >= 0.0f ? 4 : 5};
-    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-        float4 s = tri_sample<FMT>(g.base, d, l, g.off[l] + uint64_t(sel[a]) * g.vol[l], x);
-        acc.x += w[a] * s.x;
-        acc.y += w[a] * s.y;
-        acc.z += w[a] * s.z;
-        acc.w += w[a] * s.w;
-    }
-    return acc;
-}
-
-template <int FMT, bool ANISO>
-__device__ float4 cone(const GridRef& g, const TraceConsts& tc, float3 o, float3 dir, float tan_half) {
-    float cr = 0.f, cg = 0.f, cb = 0.f, alpha = 0.f;
-    float t = tc.p.start_offset;
-    const float dimf = float(g.dim);
-    const float maxl = float(g.levels - 1);
-    while (t <= g.tmax) {
-        float diam = fmaxf(1.0f, 2.0f * t * tan_half);
-        float lvl = fminf(fmaxf(log2f(diam), 0.0f), maxl);
-        float3 x = add3(o, mul3(dir, t));
-        float m = 2.0f * diam;
-        if (x.x < -m || x.y < -m || x.z < -m || x.x > dimf + m || x.y > dimf + m || x.z > dimf + m) break;
-        float fl = floorf(lvl);
-        uint32_t l0 = uint32_t(fl);
-        float f = lvl - fl;
-        float4 s = level_sample<FMT, ANISO>(g, l0, x, dir);
-        if (f > 0.0f && l0 + 1 < g.levels) {
-            float4 s1 = level_sample<FMT, ANISO>(g, l0 + 1, x, dir);
-            s.x = s.x + f * (s1.x - s.x);
-            s.y = s.y + f * (s1.y - s.y);
-            s.z = s.z + f * (s1.z - s.z);
-            s.w = s.w + f * (s1.w - s.w);
-        }
-        float tr = 1.0f - alpha;
-        cr += tr * s.x;
-        cg += tr * s.y;
-        cb += tr * s.z;
-        alpha += tr * s.w;
-        if (alpha >= tc.p.alpha_stop) break;
-        t += tc.p.step_factor * diam;
-    }
-    return make_float4(cr, cg, cb, alpha);
-}
-
-__device__ __forceinline__ void store_out(void* out, uint32_t fmt, uint64_t i, float4 v) {
-    if (fmt == F184GI_FMT_F32) {
-        reinterpret_cast<float4*>(out)[i] = v;
-    } else {
-        __half2 a = __floats2half2_rn(v.x, v.y), b = __floats2half2_rn(v.z, v.w);
-        uint2 raw;
-        raw.x = *reinterpret_cast<uint32_t*>(&a);
-        raw.y = *reinterpret_cast<uint32_t*>(&b);
-        reinterpret_cast<uint2*>(out)[i] = raw;
-    }
-}
-
-template <int FMT, bool ANISO>
-__device__ void trace_pixel(const GridRef& g, const TraceConsts& tc, const TraceView& v, uint32_t px, uint32_t py) {
-    const uint64_t npix = uint64_t(v.width) * v.height;
-    const uint64_t pi = uint64_t(py) * v.width + px;
-    float d = v.depth[pi];
-    if (!(d < 1.0f)) {
-        store_out(v.out, v.out_format, pi, make_float4(0.f, 0.f, 0.f, 0.f));
-        store_out(v.out, v.out_format, npix + pi, make_float4(0.f, 0.f, 0.f, 0.f));
-        return;
-    }
-    const float* ip = v.iproj;
-    const float* iv = v.iview;
-    float nx = (float(px) + 0.5f) / float(v.width) * 2.0f - 1.0f;
-    float ny = (float(py) + 0.5f) / float(v.height) * 2.0f - 1.0f;
-    float vp[4];
-#pragma unroll
-    for (int r = 0; r < 4; ++r) vp[r] = ip[r * 4 + 0] * nx + ip[r * 4 + 1] * ny + ip[r * 4 + 2] * d + ip[r * 4 + 3];
-    float3 cs = f3(vp[0] / vp[3], vp[1] / vp[3], vp[2] / vp[3]);
-    float3 wp = f3(iv[0] * cs.x + iv[1] * cs.y + iv[2] * cs.z + iv[3], iv[4] * cs.x + iv[5] * cs.y + iv[6] * cs.z + iv[7],
-                   iv[8] * cs.x + iv[9] * cs.y + iv[10] * cs.z + iv[11]);
-    float3 nv = oct_decode(v.normal[pi]);
-    float3 nw = norm3(f3(iv[0] * nv.x + iv[1] * nv.y + iv[2] * nv.z, iv[4] * nv.x + iv[5] * nv.y + iv[6] * nv.z,
-                         iv[8] * nv.x + iv[9] * nv.y + iv[10] * nv.z));
-    float rough = __half2float(__ushort_as_half(v.rough[pi]));
-    float3 pv = f3((wp.x - g.org[0]) * g.inv_vs, (wp.y - g.org[1]) * g.inv_vs, (wp.z - g.org[2]) * g.inv_vs);
-    float3 o = add3(pv, mul3(nw, tc.p.start_offset));
-    float3 bx, by, bz;
-    coord_space(nw, bx, by, bz);
-    float4 acc;
-    if (tc.p.diffuse_cones >= 5) {
-        float4 c0 = cone<FMT, ANISO>(g, tc, o, bz, tc.p.diffuse_tan_half);
-        acc = make_float4(0.25f * c0.x, 0.25f * c0.y, 0.25f * c0.z, 0.25f * c0.w);
-        const float cphi[4] = {1.f, 0.f, -1.f, 0.f}, sphi[4] = {0.f, 1.f, 0.f, -1.f};
-#pragma unroll 1
-        for (int k = 0; k < 4; ++k) {
-            float3 side = add3(mul3(bx, cphi[k]), mul3(by, sphi[k]));
-            float3 dir = norm3(add3(mul3(bz, tc.cos_tilt), mul3(side, tc.sin_tilt)));
-            float4 ck = cone<FMT, ANISO>(g, tc, o, dir, tc.p.diffuse_tan_half);
-            acc.x += 0.1875f * ck.x;
-            acc.y += 0.1875f * ck.y;
-            acc.z += 0.1875f * ck.z;
-            acc.w += 0.1875f * ck.w;
-        }
-    } else {
-        acc = cone<FMT, ANISO>(g, tc, o, bz, tc.p.diffuse_tan_half);
-    }
-    store_out(v.out, v.out_format, pi, acc);
-    float4 sp = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (tc.p.specular) {
-        float3 vd = norm3(sub3(wp, f3(v.eye[0], v.eye[1], v.eye[2])));
-        float dn = dot3(vd, nw);
-        float3 rd = norm3(sub3(vd, mul3(nw, 2.0f * dn)));
-        float th = fmaxf(rough, tc.p.min_spec_tan_half);
-        sp = cone<FMT, ANISO>(g, tc, o, rd, th);
-    }
-    store_out(v.out, v.out_format, npix + pi, sp);
-}
-
-// Tiles of 16x8 pixels of all views are numbered in view order (tile_base = per-view prefix).  A CTA traces one
-// tile at a time: blockIdx.x in the one-shot launch, or tiles taken from a device work counter in the persistent
-// launch (one resident wave of CTAs that drains the whole batch, so views of different size balance).
-template <int FMT, bool ANISO, bool PERSISTENT>
-__global__ void __launch_bounds__(128, 4) trace_kernel(TraceConsts tc, const TraceView* __restrict__ views,
-                                                    const uint32_t* __restrict__ tile_base, uint32_t nviews,
-                                                    uint32_t* work) {
-    __shared__ GridRef g;
-    __shared__ uint32_t s_tile, s_view;
-    const uint32_t ntiles = tile_base[nviews];
-    uint32_t cur_view = 0xffffffffu;
-    for (uint32_t it = 0;; ++it) {
-        if (threadIdx.x == 0) {
-            uint32_t tile = PERSISTENT ? atomicAdd(work, 1u) : (it == 0 ? blockIdx.x : ntiles);
-            uint32_t lo = 0, hi = nviews;  // last view with tile_base[v] <= tile
-            while (hi - lo > 1) {
-                uint32_t mid = (lo + hi) / 2;
-                if (tile_base[mid] <= tile) lo = mid; else hi = mid;
-            }
-            s_tile = tile;
-            s_view = lo;
-        }
-        __syncthreads();
-        const uint32_t tile = s_tile, vi = s_view;
-        if (tile >= ntiles) return;
-        const TraceView& v = views[vi];
-        if (vi != cur_view) {  // stage the view's grid description
-            if (threadIdx.x < kMaxLevels) {
-                g.off[threadIdx.x] = v.off[threadIdx.x];
-                g.vol[threadIdx.x] = v.vol[threadIdx.x];
-            }
-            if (threadIdx.x == 0) {
-                g.base = v.grid_base;
-                g.dim = v.grid_dim;
-                g.levels = v.grid_levels;
-                g.tmax = v.tmax;
-                // world -> L0 voxel units: (p - origin) * (inv_voxel_fixed / 256), all scalings exact
-                for (int a = 0; a < 3; ++a) g.org[a] = float(v.frame->origin[a]);
-                g.inv_vs = float(v.frame->inv_voxel_fixed * (1.0 / 256.0));
-            }
-            cur_view = vi;
-            __syncthreads();
-        }
-        const uint32_t local = tile - tile_base[vi];
-        const uint32_t tiles_x = (v.width + 15) / 16;
-        const uint32_t px = (local % tiles_x) * 16 + (threadIdx.x & 15);
-        const uint32_t py = (local / tiles_x) * 8 + (threadIdx.x >> 4);
-        if (px < v.width && py < v.height) trace_pixel<FMT, ANISO>(g, tc, v, px, py);
-        __syncthreads();  // s_tile / g are rewritten for the next tile
-    }
-}
-
-template <bool PERSISTENT>
-void launch_variant(uint32_t fmt, bool aniso, uint32_t blocks, cudaStream_t s, const TraceConsts& tc,
-                    const TraceView* dv, const uint32_t* db, uint32_t nviews, uint32_t* work) {
-    // one instantiation per storage format and mip kind keeps each kernel's code small (instruction cache)
-    if (fmt == F184GI_FMT_F32 && !aniso)
-        trace_kernel<F184GI_FMT_F32, false, PERSISTENT><<<blocks, 128, 0, s>>>(tc, dv, db, nviews, work);
-    else if (fmt == F184GI_FMT_F32)
-        trace_kernel<F184GI_FMT_F32, true, PERSISTENT><<<blocks, 128, 0, s>>>(tc, dv, db, nviews, work);
-    else if (!aniso)
-        trace_kernel<F184GI_FMT_F16, false, PERSISTENT><<<blocks, 128, 0, s>>>(tc, dv, db, nviews, work);
-    else
-        trace_kernel<F184GI_FMT_F16, true, PERSISTENT><<<blocks, 128, 0, s>>>(tc, dv, db, nviews, work);
-    note_launches(1);
-}
-
-}  // namespace
 
 void trace_view_set_grid(TraceView& v, const ChainLayout& c, const f184gi_grid_frame* d_frame, float tmax) {
     v.grid_base = c.base;
@@ -369,127 +36,153 @@ void trace_view_set_grid(TraceView& v, const ChainLayout& c, const f184gi_grid_f
     }
 }
 
-size_t trace_table_bytes(uint32_t nviews) {
-    return (size_t(nviews) * sizeof(TraceView) + size_t(nviews + 1) * 4 + 255) / 256 * 256 + 256;
-}
+namespace {
 
-uint32_t trace_fill_table(const TraceView* views, uint32_t nviews, void* host_table) {
-    unsigned char* h = static_cast<unsigned char*>(host_table);
-    TraceView* hv = reinterpret_cast<TraceView*>(h);
-    uint32_t* hb = reinterpret_cast<uint32_t*>(h + size_t(nviews) * sizeof(TraceView));
+// Table layout (host and device): [tile_base: nviews + 1 u32, padded to 256 B][views: nviews]
+size_t table_header(uint32_t nviews) { return (size_t(nviews + 1) * 4 + 255) / 256 * 256; }
+size_t table_bytes(uint32_t nviews) { return table_header(nviews) + size_t(nviews) * sizeof(TraceView); }
+
+uint32_t fill_table(const TraceView* views, uint32_t nviews, uint32_t variant, unsigned char* h) {
+    uint32_t* hb = reinterpret_cast<uint32_t*>(h);
+    TraceView* hv = reinterpret_cast<TraceView*>(h + table_header(nviews));
     uint32_t tiles = 0;
     for (uint32_t i = 0; i < nviews; ++i) {
         hv[i] = views[i];
         hb[i] = tiles;
-        tiles += ((views[i].width + 15) / 16) * ((views[i].height + 7) / 8);
+        tiles += trace_view_tiles(views[i].width, views[i].height, variant);
     }
     hb[nviews] = tiles;
     return tiles;
 }
 
-int trace_launch_table(uint32_t fmt, bool aniso, const TraceConsts& tc, const void* dev_table, uint32_t nviews,
-                       uint32_t ntiles, uint32_t* work, uint32_t persistent_blocks, cudaStream_t s) {
-    const TraceView* dv = static_cast<const TraceView*>(dev_table);
-    const uint32_t* db = reinterpret_cast<const uint32_t*>(static_cast<const unsigned char*>(dev_table) +
-                                                           size_t(nviews) * sizeof(TraceView));
-    if (persistent_blocks && work)
-        launch_variant<true>(fmt, aniso, persistent_blocks, s, tc, dv, db, nviews, work);
-    else
-        launch_variant<false>(fmt, aniso, ntiles, s, tc, dv, db, nviews, nullptr);
-    return cuda_fail(cudaGetLastError(), "trace");
-}
-
-size_t trace_scratch_bytes(uint32_t nviews) { return trace_table_bytes(nviews); }
-
-int trace_launch(const ChainLayout& c, const TraceConsts& tc, const f184gi_grid_frame* d_frame, const TraceView* views,
-                 uint32_t nviews, void* scratch, size_t scratch_bytes, cudaStream_t s) {
-    if (nviews == 0) return F184GI_OK;
-    if (scratch_bytes < trace_scratch_bytes(nviews)) return fail(F184GI_ERR_INVALID, "trace: scratch too small");
-    std::vector<TraceView> vv(views, views + nviews);
-    for (auto& v : vv) trace_view_set_grid(v, c, d_frame, tc.tmax);
-    std::vector<unsigned char> host(trace_table_bytes(nviews));
-    uint32_t tiles = trace_fill_table(vv.data(), nviews, host.data());
-    cudaError_t e = cudaMemcpyAsync(scratch, host.data(), host.size(), cudaMemcpyHostToDevice, s);
-    if (e != cudaSuccess) return cuda_fail(e, "trace: view table");
-    // the staging buffer must outlive the async copy
-    e = cudaStreamSynchronize(s);
-    if (e != cudaSuccess) return cuda_fail(e, "trace: view table sync");
-    return trace_launch_table(c.format, c.aniso != 0, tc, scratch, nviews, tiles, nullptr, 0, s);
-}
-
-}  // namespace f184
-
-// ---------------- batched trace under a CUDA graph ----------------
-namespace f184 {
-namespace {
-
-template <int FMT, bool ANISO>
-void* persistent_kernel_ptr() {
-    return reinterpret_cast<void*>(&trace_kernel<FMT, ANISO, true>);
-}
-
-void* persistent_kernel(uint32_t fmt, bool aniso) {
-    if (fmt == F184GI_FMT_F32) return aniso ? persistent_kernel_ptr<F184GI_FMT_F32, true>() : persistent_kernel_ptr<F184GI_FMT_F32, false>();
-    return aniso ? persistent_kernel_ptr<F184GI_FMT_F16, true>() : persistent_kernel_ptr<F184GI_FMT_F16, false>();
+cudaError_t launch(const void* fn, uint32_t variant, uint32_t blocks, const TraceConsts& tc, const unsigned char* d_table,
+                   uint32_t nviews, uint32_t* work, cudaStream_t s) {
+    TraceConsts tcv = tc;
+    const TraceView* dv = reinterpret_cast<const TraceView*>(d_table + table_header(nviews));
+    const uint32_t* db = reinterpret_cast<const uint32_t*>(d_table);
+    void* args[5] = {&tcv, &dv, &db, &nviews, &work};
+    const TraceVariant& v = kTraceVariants[variant];
+    return cudaLaunchKernel(fn, dim3(blocks), dim3(v.tw * v.th), args, 0, s);
 }
 
 }  // namespace
 
-// Table layout (host pinned and device): [tile_base: max_views + 1 u32, padded to 256 B][views: max_views]
-struct TraceGraph {
-    uint32_t fmt = 0;
-    bool aniso = false;
-    uint32_t max_views = 0, blocks = 0;
-    size_t header = 0, bytes = 0;
-    unsigned char* h_table = nullptr;
-    unsigned char* d_table = nullptr;
-    uint32_t* d_work = nullptr;
+// Pinned host staging of the view table of the one-shot launch: reused once the event of its last copy has
+// passed, so a launch never waits for the stream.
+struct TraceStaging {
+    unsigned char* host = nullptr;
+    size_t bytes = 0;
+    cudaEvent_t copied = nullptr;
+};
+
+void trace_staging_destroy(TraceStaging* st) {
+    if (!st) return;
+    if (st->copied) {
+        cudaEventSynchronize(st->copied);
+        cudaEventDestroy(st->copied);
+    }
+    cudaFreeHost(st->host);
+    delete st;
+}
+
+size_t trace_scratch_bytes(uint32_t nviews) { return table_bytes(nviews) + 256; }
+
+int trace_launch(const ChainLayout& c, const TraceConsts& tc, const f184gi_grid_frame* d_frame, const TraceView* views,
+                 uint32_t nviews, void* scratch, size_t scratch_bytes, uint32_t variant, TraceStaging** staging,
+                 cudaStream_t s) {
+    if (nviews == 0) return F184GI_OK;
+    if (scratch_bytes < trace_scratch_bytes(nviews)) return fail(F184GI_ERR_INVALID, "trace: scratch too small");
+    const void* fn = trace_kernel_fn(c.format, c.aniso != 0, variant);
+    if (!fn) return fail(F184GI_ERR_INVALID, "trace: unknown kernel variant");
+    const size_t need = table_bytes(nviews);
+    TraceStaging* st = *staging;
+    cudaError_t e = cudaSuccess;
+    if (!st) {
+        st = *staging = new TraceStaging();
+        if ((e = cudaEventCreateWithFlags(&st->copied, cudaEventDisableTiming)) != cudaSuccess)
+            return cuda_fail(e, "trace: staging event");
+    }
+    if ((e = cudaEventSynchronize(st->copied)) != cudaSuccess) return cuda_fail(e, "trace: staging wait");
+    if (st->bytes < need) {
+        cudaFreeHost(st->host);
+        st->host = nullptr;
+        st->bytes = 0;
+        if ((e = cudaHostAlloc(&st->host, need, cudaHostAllocDefault)) != cudaSuccess)
+            return cuda_fail(e, "trace: staging allocation");
+        st->bytes = need;
+    }
+    std::vector<TraceView> vv(views, views + nviews);
+    for (auto& v : vv) trace_view_set_grid(v, c, d_frame, tc.tmax);
+    const uint32_t tiles = fill_table(vv.data(), nviews, variant, st->host);
+    unsigned char* d_table = static_cast<unsigned char*>(scratch);
+    if ((e = cudaMemcpyAsync(d_table, st->host, need, cudaMemcpyHostToDevice, s)) != cudaSuccess)
+        return cuda_fail(e, "trace: view table");
+    if ((e = cudaEventRecord(st->copied, s)) != cudaSuccess) return cuda_fail(e, "trace: staging event");
+    if (tiles == 0) return F184GI_OK;
+    e = launch(fn, variant, tiles, tc, d_table, nviews, nullptr, s);
+    note_launches(1);
+    return cuda_fail(e, "trace");
+}
+
+// ---------------- batched trace under CUDA graphs ----------------
+
+// One graph per kernel variant, instantiated on first use:
+//   [view table H2D] -> [work counter = 0] -> [persistent kernel: one resident wave of CTAs]
+struct TraceGraphVariant {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     cudaGraphNode_t copy = nullptr, reset = nullptr, kernel = nullptr;
+    uint32_t blocks = 0;
+};
+
+struct TraceGraph {
+    uint32_t fmt = 0;
+    bool aniso = false;
+    uint32_t max_views = 0, per_sm = 0;
+    size_t bytes = 0;
+    unsigned char* h_table = nullptr;
+    unsigned char* d_table = nullptr;
+    uint32_t* d_work = nullptr;
     TraceConsts tc{};
     uint32_t nviews = 0;
     const TraceView* kviews = nullptr;
     const uint32_t* kbase = nullptr;
+    TraceGraphVariant var[kTraceVariantCount];
 };
 
-uint32_t trace_persistent_blocks(uint32_t fmt, bool aniso, uint32_t per_sm) {
+uint32_t trace_persistent_blocks(uint32_t fmt, bool aniso, uint32_t variant, uint32_t per_sm) {
     int dev = 0, sms = 0, maxb = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&maxb, persistent_kernel(fmt, aniso), 128, 0);
+    const TraceVariant& v = kTraceVariants[variant];
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&maxb, trace_kernel_fn(fmt, aniso, variant), int(v.tw * v.th), 0);
     if (maxb <= 0) maxb = 1;
     uint32_t b = per_sm ? std::min<uint32_t>(per_sm, uint32_t(maxb)) : uint32_t(maxb);
     return b * uint32_t(sms > 0 ? sms : 1);
 }
 
-static void graph_params(TraceGraph* g, cudaKernelNodeParams& kp, void** args) {
+static void graph_params(TraceGraph* g, uint32_t variant, cudaKernelNodeParams& kp, void** args) {
     args[0] = &g->tc;
     args[1] = &g->kviews;
     args[2] = &g->kbase;
     args[3] = &g->nviews;
     args[4] = &g->d_work;
+    const TraceVariant& v = kTraceVariants[variant];
     kp = cudaKernelNodeParams{};
-    kp.func = persistent_kernel(g->fmt, g->aniso);
-    kp.gridDim = dim3(g->blocks);
-    kp.blockDim = dim3(128);
+    kp.func = const_cast<void*>(trace_kernel_fn(g->fmt, g->aniso, variant));
+    kp.gridDim = dim3(g->var[variant].blocks);
+    kp.blockDim = dim3(v.tw * v.th);
     kp.sharedMemBytes = 0;
     kp.kernelParams = args;
 }
 
-int trace_graph_create(TraceGraph** out, uint32_t fmt, bool aniso, uint32_t max_views, uint32_t blocks,
-                       const TraceConsts& tc) {
-    *out = nullptr;
-    TraceGraph* g = new TraceGraph();
-    g->fmt = fmt, g->aniso = aniso, g->max_views = max_views, g->blocks = blocks, g->tc = tc;
-    g->header = (size_t(max_views + 1) * 4 + 255) / 256 * 256;
-    g->bytes = g->header + size_t(max_views) * sizeof(TraceView);
-    cudaError_t e = cudaHostAlloc(&g->h_table, g->bytes, cudaHostAllocDefault);
-    if (e == cudaSuccess) e = cudaMalloc(&g->d_table, g->bytes + 256);
-    if (e == cudaSuccess) e = cudaMalloc(&g->d_work, 256);
-    if (e == cudaSuccess) e = cudaGraphCreate(&g->graph, 0);
+static cudaError_t graph_variant(TraceGraph* g, uint32_t variant) {
+    TraceGraphVariant& gv = g->var[variant];
+    if (gv.exec) return cudaSuccess;
+    gv.blocks = trace_persistent_blocks(g->fmt, g->aniso, variant, g->per_sm);
+    cudaError_t e = cudaGraphCreate(&gv.graph, 0);
     if (e == cudaSuccess)
-        e = cudaGraphAddMemcpyNode1D(&g->copy, g->graph, nullptr, 0, g->d_table, g->h_table, g->bytes,
+        e = cudaGraphAddMemcpyNode1D(&gv.copy, gv.graph, nullptr, 0, g->d_table, g->h_table, g->bytes,
                                      cudaMemcpyHostToDevice);
     if (e == cudaSuccess) {
         cudaMemsetParams mp{};
@@ -499,17 +192,30 @@ int trace_graph_create(TraceGraph** out, uint32_t fmt, bool aniso, uint32_t max_
         mp.width = 1;
         mp.height = 1;
         mp.pitch = 4;
-        e = cudaGraphAddMemsetNode(&g->reset, g->graph, &g->copy, 1, &mp);
+        e = cudaGraphAddMemsetNode(&gv.reset, gv.graph, &gv.copy, 1, &mp);
     }
-    g->kbase = reinterpret_cast<const uint32_t*>(g->d_table);
-    g->kviews = reinterpret_cast<const TraceView*>(g->d_table + g->header);
     if (e == cudaSuccess) {
         cudaKernelNodeParams kp;
         void* args[5];
-        graph_params(g, kp, args);
-        e = cudaGraphAddKernelNode(&g->kernel, g->graph, &g->reset, 1, &kp);
+        g->nviews = g->max_views;
+        g->kbase = reinterpret_cast<const uint32_t*>(g->d_table);
+        g->kviews = reinterpret_cast<const TraceView*>(g->d_table + table_header(g->max_views));
+        graph_params(g, variant, kp, args);
+        e = cudaGraphAddKernelNode(&gv.kernel, gv.graph, &gv.reset, 1, &kp);
     }
-    if (e == cudaSuccess) e = cudaGraphInstantiate(&g->exec, g->graph, 0);
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&gv.exec, gv.graph, 0);
+    return e;
+}
+
+int trace_graph_create(TraceGraph** out, uint32_t fmt, bool aniso, uint32_t max_views, uint32_t per_sm,
+                       const TraceConsts& tc) {
+    *out = nullptr;
+    TraceGraph* g = new TraceGraph();
+    g->fmt = fmt, g->aniso = aniso, g->max_views = max_views, g->per_sm = per_sm, g->tc = tc;
+    g->bytes = table_bytes(max_views);
+    cudaError_t e = cudaHostAlloc(&g->h_table, g->bytes, cudaHostAllocDefault);
+    if (e == cudaSuccess) e = cudaMalloc(&g->d_table, g->bytes + 256);
+    if (e == cudaSuccess) e = cudaMalloc(&g->d_work, 256);
     if (e != cudaSuccess) {
         trace_graph_destroy(g);
         return cuda_fail(e, "trace graph");
@@ -518,37 +224,78 @@ int trace_graph_create(TraceGraph** out, uint32_t fmt, bool aniso, uint32_t max_
     return F184GI_OK;
 }
 
-int trace_graph_launch(TraceGraph* g, const TraceView* views, uint32_t nviews, cudaStream_t s) {
+// The table is laid out for this batch's view count; the kernel node gets pointers into it.
+int trace_graph_launch(TraceGraph* g, const TraceView* views, uint32_t nviews, uint32_t variant, cudaStream_t s) {
     if (nviews == 0) return F184GI_OK;
     if (nviews > g->max_views) return fail(F184GI_ERR_INVALID, "trace graph: batch exceeds max_views");
-    uint32_t* hb = reinterpret_cast<uint32_t*>(g->h_table);
-    TraceView* hv = reinterpret_cast<TraceView*>(g->h_table + g->header);
-    uint32_t tiles = 0;
-    for (uint32_t i = 0; i < nviews; ++i) {
-        hv[i] = views[i];
-        hb[i] = tiles;
-        tiles += ((views[i].width + 15) / 16) * ((views[i].height + 7) / 8);
-    }
-    hb[nviews] = tiles;
+    if (variant >= kTraceVariantCount) return fail(F184GI_ERR_INVALID, "trace graph: unknown variant");
+    cudaError_t e = graph_variant(g, variant);
+    if (e != cudaSuccess) return cuda_fail(e, "trace graph");
+    TraceGraphVariant& gv = g->var[variant];
+    fill_table(views, nviews, variant, g->h_table);
     g->nviews = nviews;
-    const size_t used = g->header + size_t(nviews) * sizeof(TraceView);
-    cudaError_t e = cudaGraphExecMemcpyNodeSetParams1D(g->exec, g->copy, g->d_table, g->h_table, used,
-                                                       cudaMemcpyHostToDevice);
+    g->kbase = reinterpret_cast<const uint32_t*>(g->d_table);
+    g->kviews = reinterpret_cast<const TraceView*>(g->d_table + table_header(nviews));
+    e = cudaGraphExecMemcpyNodeSetParams1D(gv.exec, gv.copy, g->d_table, g->h_table, table_bytes(nviews),
+                                           cudaMemcpyHostToDevice);
     if (e == cudaSuccess) {
         cudaKernelNodeParams kp;
         void* args[5];
-        graph_params(g, kp, args);
-        e = cudaGraphExecKernelNodeSetParams(g->exec, g->kernel, &kp);
+        graph_params(g, variant, kp, args);
+        e = cudaGraphExecKernelNodeSetParams(gv.exec, gv.kernel, &kp);
     }
-    if (e == cudaSuccess) e = cudaGraphLaunch(g->exec, s);
+    if (e == cudaSuccess) e = cudaGraphLaunch(gv.exec, s);
     if (e == cudaSuccess) note_launches(1);
     return cuda_fail(e, "trace graph launch");
 }
 
+// Self-tuning: trace this batch once with every variant (each run writes the same outputs), twice over, and
+// keep the variant with the shortest time.  The batch runs alone on the device while it is tuned.
+int trace_graph_tune(TraceGraph* g, const TraceView* views, uint32_t nviews, cudaStream_t s, uint32_t* best,
+                     float* ms_out) {
+    cudaEvent_t ev[2];
+    cudaError_t e = cudaEventCreate(&ev[0]);
+    if (e == cudaSuccess) e = cudaEventCreate(&ev[1]);
+    if (e != cudaSuccess) return cuda_fail(e, "trace tune: events");
+    float ms[kTraceVariantCount];
+    int rc = F184GI_OK;
+    for (uint32_t v = 0; v < kTraceVariantCount; ++v) ms[v] = 3.0e38f;
+    for (int round = 0; round < 2 && rc == F184GI_OK; ++round)
+        for (uint32_t v = 0; v < kTraceVariantCount && rc == F184GI_OK; ++v) {
+            // the host table is rewritten per variant: the previous run (and its copy) must be complete
+            if ((e = cudaStreamSynchronize(s)) != cudaSuccess) {
+                rc = cuda_fail(e, "trace tune");
+                break;
+            }
+            cudaEventRecord(ev[0], s);
+            if ((rc = trace_graph_launch(g, views, nviews, v, s))) break;
+            cudaEventRecord(ev[1], s);
+            if ((e = cudaEventSynchronize(ev[1])) != cudaSuccess) {
+                rc = cuda_fail(e, "trace tune");
+                break;
+            }
+            float t = 0.0f;
+            cudaEventElapsedTime(&t, ev[0], ev[1]);
+            ms[v] = std::min(ms[v], t);
+        }
+    cudaEventDestroy(ev[0]);
+    cudaEventDestroy(ev[1]);
+    if (rc) return rc;
+    uint32_t b = 0;
+    for (uint32_t v = 1; v < kTraceVariantCount; ++v)
+        if (ms[v] < ms[b]) b = v;
+    *best = b;
+    if (ms_out)
+        for (uint32_t v = 0; v < kTraceVariantCount; ++v) ms_out[v] = ms[v];
+    return F184GI_OK;
+}
+
 void trace_graph_destroy(TraceGraph* g) {
     if (!g) return;
-    if (g->exec) cudaGraphExecDestroy(g->exec);
-    if (g->graph) cudaGraphDestroy(g->graph);
+    for (TraceGraphVariant& gv : g->var) {
+        if (gv.exec) cudaGraphExecDestroy(gv.exec);
+        if (gv.graph) cudaGraphDestroy(gv.graph);
+    }
     cudaFreeHost(g->h_table);
     cudaFree(g->d_table);
     cudaFree(g->d_work);

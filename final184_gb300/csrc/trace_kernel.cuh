@@ -1,0 +1,369 @@
+#pragma once
+// trace_kernel.cuh -- the cone-trace kernel: per-pixel diffuse + specular cones over a G-buffer.
+//
+// Replaces the reference's indirect pass (Shader/Lighting/indirect.frag:104-243), which marches four
+// stochastic single rays per pixel through a one-level RG16UI volume.  Here each pixel traces five diffuse cones
+// (60-degree aperture: one along the normal, four tilted 60 degrees, in the frame of the reference's
+// make_coord_space, indirect.frag:71-86) and one specular cone whose tan(half aperture) is the G-buffer
+// roughness.  A cone steps by half its diameter, samples the mip chain quadrilinearly (trilinear inside a
+// level, linear between log2(diameter) levels, zero outside the grid) and composites front to back in FP32.
+// The G-buffer decode follows indirect.frag:44-58 and 189-196 (InvProj, then InvModelView).
+#include "gi_device.cuh"
+
+namespace f184 {
+namespace {
+
+__device__ __forceinline__ float3 f3(float x, float y, float z) { return make_float3(x, y, z); }
+__device__ __forceinline__ float3 add3(float3 a, float3 b) { return f3(a.x + b.x, a.y + b.y, a.z + b.z); }
+__device__ __forceinline__ float3 sub3(float3 a, float3 b) { return f3(a.x - b.x, a.y - b.y, a.z - b.z); }
+__device__ __forceinline__ float3 mul3(float3 a, float s) { return f3(a.x * s, a.y * s, a.z * s); }
+__device__ __forceinline__ float dot3(float3 a, float3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ float3 cross3(float3 a, float3 b) {
+    return f3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+__device__ __forceinline__ float3 norm3(float3 a) {
+    float l = sqrtf(dot3(a, a));
+    return l > 0.0f ? mul3(a, 1.0f / l) : a;
+}
+
+// make_coord_space, indirect.frag:71-86
+__device__ __forceinline__ void coord_space(float3 n, float3& x, float3& y, float3& z) {
+    z = n;
+    float3 h = z;
+    float ax = fabsf(h.x), ay = fabsf(h.y), az = fabsf(h.z);
+    if (ax <= ay && ax <= az)
+        h.x = 1.0f;
+    else if (ay <= ax && ay <= az)
+        h.y = 1.0f;
+    else
+        h.z = 1.0f;
+    z = norm3(z);
+    y = norm3(cross3(h, z));
+    x = norm3(cross3(z, y));
+}
+
+__device__ __forceinline__ float3 oct_decode(uint32_t p) {
+    float x = __half2float(__ushort_as_half(uint16_t(p & 0xffffu)));
+    float y = __half2float(__ushort_as_half(uint16_t(p >> 16)));
+    float3 v = f3(x, y, 1.0f - fabsf(x) - fabsf(y));
+    if (v.z < 0.0f) {
+        float ox = v.x, oy = v.y;
+        v.x = (1.0f - fabsf(oy)) * (ox >= 0.0f ? 1.0f : -1.0f);
+        v.y = (1.0f - fabsf(ox)) * (oy >= 0.0f ? 1.0f : -1.0f);
+    }
+    return norm3(v);
+}
+
+// The grid a tile traces against, staged in shared memory per CTA: lanes index the level table with their own
+// (divergent) level, which the constant bank would serialise, and batched launches trace many grids.
+struct GridRef {
+    uint32_t off[kMaxLevels];  // element offsets (a chain holds < 2^32 elements: dim <= 512)
+    uint32_t vol[kMaxLevels];
+    const void* base;
+    uint32_t dim, levels;
+    float tmax;
+    float org[3];
+    float inv_vs;
+};
+
+// Brick-offset table staged in shared memory: lut[a * kLut + b] = part1by2(b) << (9 + a), the element offset of
+// brick coordinate b along axis a (b <= 64 covers dim 512).  The brick offset of (bx, by, bz) is the sum of
+// three entries, and the step to the next brick along an axis is the difference of two.
+constexpr int kLut = 65;
+
+// 8-tap trilinear sample of one volume of level l (d voxels per axis) at x (L0 voxel units); taps outside the
+// volume read zero.  Interior samples (all taps inside) address the seven other taps from the first one with
+// one delta per axis: +1 / +8 / +64 inside a brick, or the Morton step to the next brick when the tap crosses a
+// brick face.  Samples touching the border take the general path with a validity test per tap.
+template <int FMT>
+__device__ __forceinline__ float4 tri_sample(const void* base, int d, uint32_t l, uint32_t vol_off, float3 x,
+                                             const uint32_t* lut) {
+    const float s = __int_as_float((127 - int(l)) << 23);  // 2^-l
+    const float u[3] = {x.x * s - 0.5f, x.y * s - 0.5f, x.z * s - 0.5f};
+    int c0[3];
+    float f[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        float fl = floorf(u[a]);
+        c0[a] = int(fl);
+        f[a] = u[a] - fl;
+    }
+    const float wx[2] = {1.0f - f[0], f[0]}, wy[2] = {1.0f - f[1], f[1]}, wz[2] = {1.0f - f[2], f[2]};
+    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+    const unsigned lim = unsigned(d - 1);
+    if (unsigned(c0[0]) < lim && unsigned(c0[1]) < lim && unsigned(c0[2]) < lim) {
+        uint32_t i0, dx, dy, dz;
+        if (d >= 8) {
+            const uint32_t bx = uint32_t(c0[0]) >> 3, by = uint32_t(c0[1]) >> 3, bz = uint32_t(c0[2]) >> 3;
+            const uint32_t hx = lut[bx], hy = lut[kLut + by], hz = lut[2 * kLut + bz];
+            i0 = hx + hy + hz + ((uint32_t(c0[2] & 7) << 6) | (uint32_t(c0[1] & 7) << 3) | uint32_t(c0[0] & 7));
+            // crossing the brick face: local coordinate 7 -> 0 and the brick offset steps along the axis
+            dx = (c0[0] & 7) != 7 ? 1u : lut[bx + 1] - hx - 7u;
+            dy = (c0[1] & 7) != 7 ? 8u : lut[kLut + by + 1] - hy - 56u;
+            dz = (c0[2] & 7) != 7 ? 64u : lut[2 * kLut + bz + 1] - hz - 448u;
+        } else {
+            i0 = (uint32_t(c0[2]) * uint32_t(d) + uint32_t(c0[1])) * uint32_t(d) + uint32_t(c0[0]);
+            dx = 1u, dy = uint32_t(d), dz = uint32_t(d) * uint32_t(d);
+        }
+        const uint32_t ib = vol_off + i0;
+#pragma unroll
+        for (int tz = 0; tz < 2; ++tz)
+#pragma unroll
+            for (int ty = 0; ty < 2; ++ty) {
+                const float wyz = wy[ty] * wz[tz];
+                const uint32_t row = ib + (tz ? dz : 0u) + (ty ? dy : 0u);
+#pragma unroll
+                for (int tx = 0; tx < 2; ++tx) {
+                    float4 v = load_vox(base, FMT, row + (tx ? dx : 0u));
+                    float w = wx[tx] * wyz;
+                    acc.x += w * v.x;
+                    acc.y += w * v.y;
+                    acc.z += w * v.z;
+                    acc.w += w * v.w;
+                }
+            }
+        return acc;
+    }
+    // border: per-axis validity, high (Morton) and low (in-brick / linear) address parts
+    bool ok[3][2];
+    uint32_t hi[3][2], lo[3][2];
+    const bool bricked = d >= 8;
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int t = 0; t < 2; ++t) {
+            int c = c0[a] + t;
+            ok[a][t] = unsigned(c) < unsigned(d);
+            uint32_t cu = uint32_t(c) & 1023u;
+            if (bricked) {
+                hi[a][t] = part1by2(cu >> 3) << a;
+                lo[a][t] = (cu & 7u) << (3 * a);
+            } else {
+                hi[a][t] = 0;
+                lo[a][t] = a == 0 ? cu : (a == 1 ? cu * uint32_t(d) : cu * uint32_t(d * d));
+            }
+        }
+#pragma unroll
+    for (int tz = 0; tz < 2; ++tz)
+#pragma unroll
+        for (int ty = 0; ty < 2; ++ty) {
+            const float wyz = wy[ty] * wz[tz];
+#pragma unroll
+            for (int tx = 0; tx < 2; ++tx) {
+                if (ok[0][tx] && ok[1][ty] && ok[2][tz]) {
+                    uint32_t idx = ((hi[0][tx] | hi[1][ty] | hi[2][tz]) << 9) | (lo[0][tx] | lo[1][ty] | lo[2][tz]);
+                    float4 v = load_vox(base, FMT, vol_off + idx);
+                    float w = wx[tx] * wyz;
+                    acc.x += w * v.x;
+                    acc.y += w * v.y;
+                    acc.z += w * v.z;
+                    acc.w += w * v.w;
+                }
+            }
+        }
+    return acc;
+}
+
+template <int FMT, bool ANISO>
+__device__ __forceinline__ float4 level_sample(const GridRef& g, const uint32_t* lut, uint32_t l, float3 x,
+                                               float3 dir) {
+    const int d = int(g.dim >> l);
+    if (!ANISO || l == 0) return tri_sample<FMT>(g.base, d, l, g.off[l], x, lut);
+    float w[3] = {dir.x * dir.x, dir.y * dir.y, dir.z * dir.z};
+    int sel[3] = {dir.x >= 0.0f ? 0 : 1, dir.y >= 0.0f ? 2 : 3, dir.z >= 0.0f ? 4 : 5};
+    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        float4 s = tri_sample<FMT>(g.base, d, l, g.off[l] + uint32_t(sel[a]) * g.vol[l], x, lut);
+        acc.x += w[a] * s.x;
+        acc.y += w[a] * s.y;
+        acc.z += w[a] * s.z;
+        acc.w += w[a] * s.w;
+    }
+    return acc;
+}
+
+template <int FMT, bool ANISO>
+__device__ float4 cone(const GridRef& g, const uint32_t* lut, const TraceConsts& tc, float3 o, float3 dir,
+                       float tan_half) {
+    float cr = 0.f, cg = 0.f, cb = 0.f, alpha = 0.f;
+    float t = tc.p.start_offset;
+    const float dimf = float(g.dim);
+    const float maxl = float(g.levels - 1);
+    while (t <= g.tmax) {
+        float diam = fmaxf(1.0f, 2.0f * t * tan_half);
+        float lvl = fminf(fmaxf(log2f(diam), 0.0f), maxl);
+        float3 x = add3(o, mul3(dir, t));
+        float m = 2.0f * diam;
+        if (x.x < -m || x.y < -m || x.z < -m || x.x > dimf + m || x.y > dimf + m || x.z > dimf + m) break;
+        float fl = floorf(lvl);
+        uint32_t l0 = uint32_t(fl);
+        float f = lvl - fl;
+        float4 s = level_sample<FMT, ANISO>(g, lut, l0, x, dir);
+        if (f > 0.0f && l0 + 1 < g.levels) {
+            float4 s1 = level_sample<FMT, ANISO>(g, lut, l0 + 1, x, dir);
+            s.x = s.x + f * (s1.x - s.x);
+            s.y = s.y + f * (s1.y - s.y);
+            s.z = s.z + f * (s1.z - s.z);
+            s.w = s.w + f * (s1.w - s.w);
+        }
+        float tr = 1.0f - alpha;
+        cr += tr * s.x;
+        cg += tr * s.y;
+        cb += tr * s.z;
+        alpha += tr * s.w;
+        if (alpha >= tc.p.alpha_stop) break;
+        t += tc.p.step_factor * diam;
+    }
+    return make_float4(cr, cg, cb, alpha);
+}
+
+__device__ __forceinline__ void store_out(void* out, uint32_t fmt, uint64_t i, float4 v) {
+    if (fmt == F184GI_FMT_F32) {
+        reinterpret_cast<float4*>(out)[i] = v;
+    } else {
+        __half2 a = __floats2half2_rn(v.x, v.y), b = __floats2half2_rn(v.z, v.w);
+        uint2 raw;
+        raw.x = *reinterpret_cast<uint32_t*>(&a);
+        raw.y = *reinterpret_cast<uint32_t*>(&b);
+        reinterpret_cast<uint2*>(out)[i] = raw;
+    }
+}
+
+template <int FMT, bool ANISO>
+__device__ void trace_pixel(const GridRef& g, const uint32_t* lut, const TraceConsts& tc, const TraceView& v,
+                            uint32_t px, uint32_t py) {
+    const uint64_t npix = uint64_t(v.width) * v.height;
+    const uint64_t pi = uint64_t(py) * v.width + px;
+    float d = v.depth[pi];
+    if (!(d < 1.0f)) {
+        store_out(v.out, v.out_format, pi, make_float4(0.f, 0.f, 0.f, 0.f));
+        store_out(v.out, v.out_format, npix + pi, make_float4(0.f, 0.f, 0.f, 0.f));
+        return;
+    }
+    const float* ip = v.iproj;
+    const float* iv = v.iview;
+    float nx = (float(px) + 0.5f) / float(v.width) * 2.0f - 1.0f;
+    float ny = (float(py) + 0.5f) / float(v.height) * 2.0f - 1.0f;
+    float vp[4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) vp[r] = ip[r * 4 + 0] * nx + ip[r * 4 + 1] * ny + ip[r * 4 + 2] * d + ip[r * 4 + 3];
+    float3 cs = f3(vp[0] / vp[3], vp[1] / vp[3], vp[2] / vp[3]);
+    float3 wp = f3(iv[0] * cs.x + iv[1] * cs.y + iv[2] * cs.z + iv[3], iv[4] * cs.x + iv[5] * cs.y + iv[6] * cs.z + iv[7],
+                   iv[8] * cs.x + iv[9] * cs.y + iv[10] * cs.z + iv[11]);
+    float3 nv = oct_decode(v.normal[pi]);
+    float3 nw = norm3(f3(iv[0] * nv.x + iv[1] * nv.y + iv[2] * nv.z, iv[4] * nv.x + iv[5] * nv.y + iv[6] * nv.z,
+                         iv[8] * nv.x + iv[9] * nv.y + iv[10] * nv.z));
+    float rough = __half2float(__ushort_as_half(v.rough[pi]));
+    float3 pv = f3((wp.x - g.org[0]) * g.inv_vs, (wp.y - g.org[1]) * g.inv_vs, (wp.z - g.org[2]) * g.inv_vs);
+    float3 o = add3(pv, mul3(nw, tc.p.start_offset));
+    float3 bx, by, bz;
+    coord_space(nw, bx, by, bz);
+    float4 acc;
+    if (tc.p.diffuse_cones >= 5) {
+        float4 c0 = cone<FMT, ANISO>(g, lut, tc, o, bz, tc.p.diffuse_tan_half);
+        acc = make_float4(0.25f * c0.x, 0.25f * c0.y, 0.25f * c0.z, 0.25f * c0.w);
+#pragma unroll 1
+        for (int k = 0; k < 4; ++k) {
+            // bx cos(phi) + by sin(phi) for phi = k * 90 degrees (the products by 0 and +-1 are exact)
+            float3 side = (k & 1) ? by : bx;
+            if (k & 2) side = f3(-side.x, -side.y, -side.z);
+            float3 dir = norm3(add3(mul3(bz, tc.cos_tilt), mul3(side, tc.sin_tilt)));
+            float4 ck = cone<FMT, ANISO>(g, lut, tc, o, dir, tc.p.diffuse_tan_half);
+            acc.x += 0.1875f * ck.x;
+            acc.y += 0.1875f * ck.y;
+            acc.z += 0.1875f * ck.z;
+            acc.w += 0.1875f * ck.w;
+        }
+    } else {
+        acc = cone<FMT, ANISO>(g, lut, tc, o, bz, tc.p.diffuse_tan_half);
+    }
+    store_out(v.out, v.out_format, pi, acc);
+    float4 sp = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (tc.p.specular) {
+        float3 vd = norm3(sub3(wp, f3(v.eye[0], v.eye[1], v.eye[2])));
+        float dn = dot3(vd, nw);
+        float3 rd = norm3(sub3(vd, mul3(nw, 2.0f * dn)));
+        float th = fmaxf(rough, tc.p.min_spec_tan_half);
+        sp = cone<FMT, ANISO>(g, lut, tc, o, rd, th);
+    }
+    store_out(v.out, v.out_format, npix + pi, sp);
+}
+
+// Tiles of TW x TH pixels of all views are numbered in view order (tile_base = per-view prefix).  A CTA traces
+// one tile at a time: blockIdx.x in the one-shot launch (work == nullptr), or tiles taken from a device work
+// counter in the persistent launch (one resident wave of CTAs that drains the whole batch, so views of different
+// size balance).  The tile shape and the CTAs resident per SM (MINB) are the variants the tuner picks from.
+template <int FMT, bool ANISO, int TW, int TH, int MINB>
+__global__ void __launch_bounds__(TW * TH, MINB) trace_kernel(TraceConsts tc, const TraceView* __restrict__ views,
+                                                             const uint32_t* __restrict__ tile_base, uint32_t nviews,
+                                                             uint32_t* work) {
+    __shared__ GridRef g;
+    __shared__ uint32_t s_lut[3 * kLut];
+    __shared__ uint32_t s_tile, s_view;
+    for (uint32_t i = threadIdx.x; i < 3 * kLut; i += TW * TH) s_lut[i] = part1by2(i % kLut) << (9 + i / kLut);
+    const uint32_t ntiles = tile_base[nviews];
+    uint32_t cur_view = 0xffffffffu;
+    for (uint32_t it = 0;; ++it) {
+        if (threadIdx.x == 0) {
+            uint32_t tile = work ? atomicAdd(work, 1u) : (it == 0 ? blockIdx.x : ntiles);
+            uint32_t lo = 0, hi = nviews;  // last view with tile_base[v] <= tile
+            while (hi - lo > 1) {
+                uint32_t mid = (lo + hi) / 2;
+                if (tile_base[mid] <= tile) lo = mid; else hi = mid;
+            }
+            s_tile = tile;
+            s_view = lo;
+        }
+        __syncthreads();
+        const uint32_t tile = s_tile, vi = s_view;
+        if (tile >= ntiles) return;
+        const TraceView& v = views[vi];
+        if (vi != cur_view) {  // stage the view's grid description
+            if (threadIdx.x < kMaxLevels) {
+                g.off[threadIdx.x] = uint32_t(v.off[threadIdx.x]);
+                g.vol[threadIdx.x] = uint32_t(v.vol[threadIdx.x]);
+            }
+            if (threadIdx.x == 0) {
+                g.base = v.grid_base;
+                g.dim = v.grid_dim;
+                g.levels = v.grid_levels;
+                g.tmax = v.tmax;
+                // world -> L0 voxel units: (p - origin) * (inv_voxel_fixed / 256), all scalings exact
+                for (int a = 0; a < 3; ++a) g.org[a] = float(v.frame->origin[a]);
+                g.inv_vs = float(v.frame->inv_voxel_fixed * (1.0 / 256.0));
+            }
+            cur_view = vi;
+            __syncthreads();
+        }
+        const uint32_t local = tile - tile_base[vi];
+        const uint32_t tiles_x = (v.width + TW - 1) / TW;
+        const uint32_t px = (local % tiles_x) * TW + (threadIdx.x % TW);
+        const uint32_t py = (local / tiles_x) * TH + (threadIdx.x / TW);
+        if (px < v.width && py < v.height) trace_pixel<FMT, ANISO>(g, s_lut, tc, v, px, py);
+        __syncthreads();  // s_tile / g are rewritten for the next tile
+    }
+}
+
+// Kernel of a variant (host stub address, for cudaLaunchKernel and graph kernel nodes).
+template <int FMT, bool ANISO, int V>
+const void* variant_fn() {
+    constexpr TraceVariant tv = kTraceVariants[V];
+    return reinterpret_cast<const void*>(&trace_kernel<FMT, ANISO, int(tv.tw), int(tv.th), int(tv.minb)>);
+}
+
+template <int FMT, bool ANISO>
+const void* kernel_for(uint32_t variant) {
+    static_assert(kTraceVariantCount == 5, "one case per variant");
+    switch (variant) {
+        case 0: return variant_fn<FMT, ANISO, 0>();
+        case 1: return variant_fn<FMT, ANISO, 1>();
+        case 2: return variant_fn<FMT, ANISO, 2>();
+        case 3: return variant_fn<FMT, ANISO, 3>();
+        case 4: return variant_fn<FMT, ANISO, 4>();
+        default: return nullptr;
+    }
+}
+
+}  // namespace
+}  // namespace f184

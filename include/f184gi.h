@@ -243,6 +243,8 @@ typedef struct f184gi_server_config {
     uint32_t blocks_per_sm;   /* persistent trace CTAs per SM (0 = occupancy maximum) */
     uint64_t hbm_budget;      /* bytes for resident scenes + request staging (0 = no limit) */
     f184gi_cone_params cone;  /* cone parameters for every request (diffuse_cones == 0: defaults) */
+    uint32_t trace_variant;   /* 0 = tune the cone-trace kernel variant on the first batch; k = use variant k-1 */
+    uint32_t pad;
 } f184gi_server_config;
 
 #define F184GI_REQ_HOST_BUFFERS 1u /* view G-buffers / outputs are host pointers: staged through the budget */
@@ -270,6 +272,11 @@ typedef struct f184gi_server_stats {
     double mean_batch_views;
     uint64_t hbm_used, hbm_budget;
     uint32_t pending, inflight;
+    /* the cone-trace kernel variant the server tuned on its first batch: tile of trace_tile[0] x trace_tile[1]
+     * pixels, trace_ctas_per_sm CTAs resident per SM; tune_ms = time of the first batch under each variant
+     * (trace_variants entries used, 0 before tuning) */
+    uint32_t trace_variant, trace_variants, trace_tile[2], trace_ctas_per_sm, pad;
+    float tune_ms[8];
 } f184gi_server_stats;
 
 int f184gi_server_create(const f184gi_server_config* cfg, f184gi_server** out);

@@ -158,6 +158,41 @@ def test_dirty_updates_equal_full_voxelization(fx):
 
 
 @pytest.mark.gpu
+def test_every_trace_variant_matches_the_plain_path(fx):
+    """Each cone-trace kernel variant (tile shape, CTAs per SM) gives the plain one-shot launch's bytes."""
+    g, torch = fx.g, fx.torch
+    si, vids = 2, [0, 1, 2, 3]
+    sc = fx.scenes[si]
+    gi = g.VoxelGI(0)
+    grid = gi.create_grid(fx.desc.dim, fx.desc.levels, fx.desc.format, 0, fx.desc.shadow_res, fx.desc.flags)
+    td = torch.from_numpy(sc.tri_xyz).to(fx.dev)
+    ad = torch.from_numpy(sc.albedo.view(np.int32)).to(fx.dev)
+    gi.voxelize(grid, td.data_ptr(), ad.data_ptr(), sc.ntris, sc.light, bounds=sc.bounds)
+    gi.mip(grid)
+    views, plain = fx.make_views(si, vids)
+    gi.trace(grid, views)
+    gi.sync()
+    ref = [o.cpu().numpy() for o in plain]
+    gi.close()
+    tuned = fx.server(slots=1)
+    views, outs = fx.make_views(si, vids)
+    tuned.wait(tuned.submit(si, views, []))
+    st = tuned.stats()
+    tuned.close()
+    assert st.trace_variant < st.trace_variants and all(st.tune_ms[k] > 0 for k in range(st.trace_variants))
+    for a, b in zip(ref, outs):
+        assert np.array_equal(a.view(np.uint32), b.cpu().numpy().view(np.uint32))
+    for k in range(st.trace_variants):
+        srv = fx.server(slots=1, trace_variant=k)
+        views, outs = fx.make_views(si, vids)
+        srv.wait(srv.submit(si, views, []))
+        assert srv.stats().trace_variant == k
+        srv.close()
+        for a, b in zip(ref, outs):
+            assert np.array_equal(a.view(np.uint32), b.cpu().numpy().view(np.uint32)), k
+
+
+@pytest.mark.gpu
 def test_host_buffer_requests_match_device_requests(fx):
     g = fx.g
     srv = fx.server(slots=2)
