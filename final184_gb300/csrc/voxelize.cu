@@ -356,7 +356,7 @@ __global__ void __launch_bounds__(kChunk, 4) vox_bricks(VoxScratch sc, const f18
     __shared__ unsigned long long s_sum[3][512];  // 33.31 fixed point: exact, order-independent sums
     __shared__ uint32_t s_cnt[512];
     __shared__ ItemSetup s_item[kChunk];
-    __shared__ uint32_t s_start[kChunk + 1];       // prefix of candidate voxels per prepared item
+    __shared__ uint32_t s_start[kChunk + 1];       // prefix of x-rows per prepared item
     const uint32_t m = dirty ? dirty[blockIdx.x] : blockIdx.x;
     const uint32_t nb = dim >> 3;
     if (m >= nb * nb * nb) return;
@@ -371,7 +371,7 @@ __global__ void __launch_bounds__(kChunk, 4) vox_bricks(VoxScratch sc, const f18
     for (uint32_t c0 = beg; c0 < end; c0 += kChunk) {
         // phase 1: one thread prepares one item
         const uint32_t it = c0 + threadIdx.x;
-        uint32_t nvox = 0;
+        uint32_t nrows = 0;
         if (it < end) {
             const TriRec r = sc.recs[sc.list[it]];
             int32_t lo[3], hi[3];
@@ -381,13 +381,13 @@ __global__ void __launch_bounds__(kChunk, 4) vox_bricks(VoxScratch sc, const f18
                                    min(hi[2], bz * 8 + 7) - bz * 8};
             if (l0[0] <= l1[0] && l0[1] <= l1[1] && l0[2] <= l1[2]) {
                 item_setup(r, base, l0, l1, s_item[threadIdx.x]);
-                nvox = uint32_t((l1[0] - l0[0] + 1) * (l1[1] - l0[1] + 1) * (l1[2] - l0[2] + 1));
+                nrows = uint32_t((l1[1] - l0[1] + 1) * (l1[2] - l0[2] + 1));
             }
         }
-        // exclusive scan of the candidate counts (warp shuffles + one pass over the 8 warp totals)
+        // exclusive scan of the row counts (warp shuffles + one pass over the 4 warp totals)
         {
             const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-            uint32_t x = nvox;
+            uint32_t x = nrows;
 #pragma unroll
             for (int o = 1; o < 32; o <<= 1) {
                 uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
@@ -398,33 +398,42 @@ __global__ void __launch_bounds__(kChunk, 4) vox_bricks(VoxScratch sc, const f18
             __syncthreads();
             uint32_t pre = 0;
             for (uint32_t w = 0; w < wid; ++w) pre += s_wsum[w];
-            s_start[threadIdx.x] = pre + x - nvox;
+            s_start[threadIdx.x] = pre + x - nrows;
             if (threadIdx.x == kChunk - 1) s_start[kChunk] = pre + x;
             __syncthreads();
         }
         const uint32_t total = s_start[kChunk];
-        // phase 2: all threads share the candidate voxels of the chunk evenly
-        for (uint32_t vv = threadIdx.x; vv < total; vv += blockDim.x) {
-            uint32_t lo = 0, hi = kChunk;  // the item k with s_start[k] <= vv < s_start[k + 1]
+        // phase 2: all threads share the x-rows (item, y, z) of the chunk's voxel boxes evenly.  A row's candidate
+        // voxels are the bits of one byte: projection 2 holds x + 8y (byte y), projection 1 holds z + 8x (the
+        // bits z, z + 8, .., z + 56, gathered into a byte by one multiply), projection 0 one bit y + 8z.
+        for (uint32_t rr = threadIdx.x; rr < total; rr += blockDim.x) {
+            uint32_t lo = 0, hi = kChunk;  // the item k with s_start[k] <= rr < s_start[k + 1]
             while (hi - lo > 1) {
                 uint32_t mid = (lo + hi) >> 1;
-                if (s_start[mid] <= vv) lo = mid; else hi = mid;
+                if (s_start[mid] <= rr) lo = mid; else hi = mid;
             }
             const ItemSetup& is = s_item[lo];
-            const uint32_t local = vv - s_start[lo];
-            const uint32_t ex = is.ext[0], ey = is.ext[1];
-            const int lx = is.l0[0] + int(local % ex), ly = is.l0[1] + int((local / ex) % ey),
-                      lz = is.l0[2] + int(local / (ex * ey));
-            const bool proj = ((is.mask[0] >> (ly + 8 * lz)) & (is.mask[1] >> (lz + 8 * lx)) &
-                               (is.mask[2] >> (lx + 8 * ly)) & 1ull) != 0;
-            if (!proj) continue;
-            const long long d = is.n[0] * (2 * lx + 1) + is.n[1] * (2 * ly + 1) + is.n[2] * (2 * lz + 1);
-            if (d < is.plo || d > is.phi) continue;
-            const int li = lz * 64 + ly * 8 + lx;
-            atomicAdd(&s_sum[0][li], (unsigned long long)is.wq[0]);
-            atomicAdd(&s_sum[1][li], (unsigned long long)is.wq[1]);
-            atomicAdd(&s_sum[2][li], (unsigned long long)is.wq[2]);
-            atomicAdd(&s_cnt[li], 1u);
+            const uint32_t local = rr - s_start[lo];
+            const uint32_t ey = is.ext[1];
+            // local / ey for local < 64, ey <= 8: the quotient's fraction stays >= 1/16 from an integer
+            const uint32_t qz = uint32_t((float(local) + 0.5f) * __frcp_rn(float(ey)));
+            const int ly = is.l0[1] + int(local - qz * ey), lz = is.l0[2] + int(qz);
+            if (!((is.mask[0] >> (ly + 8 * lz)) & 1ull)) continue;
+            const uint32_t col = uint32_t((((is.mask[1] >> lz) & 0x0101010101010101ull) * 0x0102040810204080ull) >> 56);
+            uint32_t xm = uint32_t(is.mask[2] >> (8 * ly)) & col & 0xffu;
+            if (!xm) continue;
+            const long long drow = is.n[1] * (2 * ly + 1) + is.n[2] * (2 * lz + 1);
+            while (xm) {
+                const int lx = __ffs(xm) - 1;
+                xm &= xm - 1;
+                const long long d = is.n[0] * (2 * lx + 1) + drow;
+                if (d < is.plo || d > is.phi) continue;
+                const int li = lz * 64 + ly * 8 + lx;
+                atomicAdd(&s_sum[0][li], (unsigned long long)is.wq[0]);
+                atomicAdd(&s_sum[1][li], (unsigned long long)is.wq[1]);
+                atomicAdd(&s_sum[2][li], (unsigned long long)is.wq[2]);
+                atomicAdd(&s_cnt[li], 1u);
+            }
         }
         __syncthreads();  // the next chunk rewrites the item table
     }
