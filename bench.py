@@ -348,6 +348,9 @@ def run_gpu(args, cfg):
                 "d2h_bytes_per_step": int(d2h), "ms_per_step": round(e2e_ms, 4)},
         "gpu_launches": int(launches),
         "clocks": clk,
+        # the traced image is lit (a black image would trace trivially short cones)
+        "image": {"mean_diffuse_rgb": round(float(out.view(2, -1, 4)[0, :, :3].mean()), 6),
+                  "mean_specular_rgb": round(float(out.view(2, -1, 4)[1, :, :3].mean()), 6)},
     }
     if world > 1:
         torch.distributed.barrier()
@@ -487,6 +490,176 @@ def run_served(args, cfg=SERVED):
     }
 
 
+PRECISION = dict(name="precision", seed=2184, ntris=2000000, nobjects=8000, dim=512, levels=9, shadow_res=4096,
+                 width=3840, height=2160)
+BATCHED = dict(seed=3184, scenes=64, dims=(64, 128, 256), tris=(10000, 1000000), views=(1, 8),
+               sizes=((256, 256), (1920, 1080)))
+
+
+def run_precision(args, cfg=PRECISION):
+    """Precision form: 512^3 FP16 chain with six-direction anisotropic mips (9 levels), 2M triangles, 3840x2160,
+    FP32 cone accumulation; optional error against the FP64 oracle on a row sample (--precision-check)."""
+    import numpy as np
+    import torch
+
+    import final184_gb300 as g
+
+    dev = torch.device("cuda", 0)
+    sc = g.SyntheticScene(cfg["seed"], cfg["ntris"], cfg["nobjects"])
+    gi = g.VoxelGI(0)
+    grid = gi.create_grid(cfg["dim"], cfg["levels"], g.FMT_F16, 1, cfg["shadow_res"])
+    tri = torch.from_numpy(sc.tri_xyz).to(dev)
+    alb = torch.from_numpy(sc.albedo.view(np.int32)).to(dev)
+    rough = torch.from_numpy(sc.roughness).to(dev)
+    W, H = cfg["width"], cfg["height"]
+    npix = W * H
+    V, P = g.look_at(sc.eye, sc.target), g.perspective(59.0, W / H, 0.1, 100.0)
+    depth = torch.empty(npix, dtype=torch.float32, device=dev)
+    normal = torch.empty(npix, dtype=torch.int32, device=dev)
+    rgh = torch.empty(npix, dtype=torch.int16, device=dev)
+    out = torch.empty(2 * npix * 4, dtype=torch.float32, device=dev)
+    view = g.make_view(V, P, W, H, depth.data_ptr(), normal.data_ptr(), rgh.data_ptr(), out.data_ptr())
+    stream = torch.cuda.Stream(dev)
+    gi.gbuffer(tri.data_ptr(), rough.data_ptr(), sc.ntris, view, stream=stream.cuda_stream)
+    gi.sync(stream.cuda_stream)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    stages = {"voxelize": [], "mip": [], "trace": []}
+    steps = max(2, min(args.steps, 5))
+    for k in range(2 + steps):
+        ev[0].record(stream)
+        gi.voxelize(grid, tri.data_ptr(), alb.data_ptr(), sc.ntris, sc.light, bounds=sc.bounds,
+                    stream=stream.cuda_stream)
+        ev[1].record(stream)
+        gi.mip(grid, stream=stream.cuda_stream)
+        ev[2].record(stream)
+        gi.trace(grid, [view], stream=stream.cuda_stream)
+        ev[3].record(stream)
+        gi.sync(stream.cuda_stream)
+        if k >= 2:
+            stages["voxelize"].append(ev[0].elapsed_time(ev[1]))
+            stages["mip"].append(ev[1].elapsed_time(ev[2]))
+            stages["trace"].append(ev[2].elapsed_time(ev[3]))
+    ms = {k: statistics.mean(v) for k, v in stages.items()}
+    step_ms = sum(ms.values())
+    res = {"workload": "%dk-triangle seeded scene (%d objects), %d^3 FP16 RGBA chain in 8^3 Morton bricks with "
+                       "6-direction anisotropic mips (%d levels), %d^2 shadow map, %dx%d G-buffer, FP32 cone "
+                       "accumulation" % (cfg["ntris"] // 1000, cfg["nobjects"], cfg["dim"], cfg["levels"],
+                                         cfg["shadow_res"], W, H),
+           "value": round(npix / (step_ms * 1e-3) / 1e6, 2), "unit": "Mpix/s", "steps": steps,
+           "ms_per_step": round(step_ms, 3), "stages_ms": {k: round(v, 3) for k, v in ms.items()},
+           "device_bytes": int(gi.memory_used()), "error_vs_fp64": None,
+           "image": {"mean_diffuse_rgb": round(float(out.view(2, -1, 4)[0, :, :3].mean()), 6),
+                     "mean_specular_rgb": round(float(out.view(2, -1, 4)[1, :, :3].mean()), 6)}}
+    if getattr(args, "precision_check", False):
+        res["error_vs_fp64"] = precision_error(g, sc, cfg, out.cpu().numpy().reshape(2, H, W, 4), depth, normal,
+                                               rgh, V, P)
+    gi.close()
+    return res
+
+
+def precision_error(g, sc, cfg, got, depth, normal, rgh, V, P, row_stride=64):
+    """Max / RMS relative error of the GPU output against the FP64 oracle (full voxelization and anisotropic mip
+    chain in FP64, cone trace of every row_stride-th row)."""
+    import numpy as np
+
+    import oracle as o
+
+    o.build.build_oracle()
+    W, H, dim, levels, res = cfg["width"], cfg["height"], cfg["dim"], cfg["levels"], cfg["shadow_res"]
+    b = sc.bounds
+    fo = o.grid_frame(o.make_bounds((b.min.x, b.min.y, b.min.z), (b.max.x, b.max.y, b.max.z)), dim,
+                      np.array(sc.light.direction, np.float32))
+    sd = o.shadow_depth(o.raster(o.frame_matrix(fo), res, res, sc.tri_xyz))
+    l0, _ = o.voxelize(fo, dim, res, sc.tri_xyz, sc.albedo,
+                       o.make_light(list(sc.light.luminance), list(sc.light.direction)), sd)
+    chain, _ = o.mip(l0, levels, aniso=True)
+    del l0
+    dep = depth.cpu().numpy().reshape(H, W)
+    nrm = normal.cpu().numpy().view(np.uint32).reshape(H, W)
+    rg = rgh.cpu().numpy().view(np.uint16).reshape(H, W)
+    emax, esq, n = 0.0, 0.0, 0
+    for r in range(0, H, row_stride):
+        ref = o.trace(fo, dim, levels, chain, V, P, W, H, dep, nrm, rg, rows=(r, r + 1), aniso=True)[:, r]
+        e = np.abs(got[:, r].astype(np.float64) - ref) / np.maximum(np.abs(ref), 1e-2)
+        emax = max(emax, float(e.max()))
+        esq += float((e ** 2).sum())
+        n += e.size
+    return {"max": emax, "rms": (esq / n) ** 0.5, "rows": len(range(0, H, row_stride)), "values": n,
+            "floor": 1e-2, "tolerance": 1e-3}
+
+
+def run_batched(args, cfg=BATCHED):
+    """Batched form: 64 resident scenes of mixed grid and triangle counts, 1-8 views each, all traces in one
+    persistent launch replayed from a CUDA graph (kernel variant tuned on the first batch)."""
+    import math
+
+    import numpy as np
+    import torch
+
+    import final184_gb300 as g
+
+    rng = np.random.default_rng(cfg["seed"])
+    dev = torch.device("cuda", 0)
+    srv = g.Server(0, slots=1, max_batch_views=1024)
+    gi = g.VoxelGI(0)
+    reqs, keep, pixels, tris_total = [], [], 0, 0
+    for k in range(cfg["scenes"]):
+        dim = int(rng.choice(cfg["dims"]))
+        ntris = int(math.exp(rng.uniform(math.log(cfg["tris"][0]), math.log(cfg["tris"][1]))))
+        sc = g.SyntheticScene(cfg["seed"] + 17 * k, ntris, max(20, ntris // 250))
+        tris_total += sc.ntris
+        levels = int(math.log2(dim))
+        srv.add_scene(k, g.GridDesc(dim, levels, g.FMT_F16, 0, min(2048, dim * 16), 0), sc.tri_xyz, sc.albedo,
+                      sc.bounds, sc.light)
+        tri = torch.from_numpy(sc.tri_xyz).to(dev)
+        rough = torch.from_numpy(sc.roughness).to(dev)
+        views = []
+        for v in range(int(rng.integers(cfg["views"][0], cfg["views"][1] + 1))):
+            (w0, h0), (w1, h1) = cfg["sizes"]
+            t = rng.uniform(0, 1)
+            W, H = int(w0 + t * (w1 - w0)), int(h0 + t * (h1 - h0))
+            eye, tgt = sc.camera(v)
+            Vm, Pm = g.look_at(eye, tgt), g.perspective(59.0, W / H, 0.1, 100.0)
+            n = W * H
+            bufs = (torch.empty(n, dtype=torch.float32, device=dev), torch.empty(n, dtype=torch.int32, device=dev),
+                    torch.empty(n, dtype=torch.int16, device=dev), torch.empty(n * 8, dtype=torch.float16, device=dev))
+            view = g.make_view(Vm, Pm, W, H, bufs[0].data_ptr(), bufs[1].data_ptr(), bufs[2].data_ptr(),
+                               bufs[3].data_ptr(), g.FMT_F16)
+            gi.gbuffer(tri.data_ptr(), rough.data_ptr(), sc.ntris, view)
+            keep.append(bufs)
+            views.append(view)
+            pixels += n
+        reqs.append((k, views, []))
+        del tri, rough
+    gi.sync()
+    gi.close()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    first = [srv.wait(t) for t in srv.submit_many(reqs)]  # first batch: tunes the kernel variant
+    first_s = time.perf_counter() - t0
+    runs = []
+    for _ in range(max(3, min(args.steps, 10))):
+        t0 = time.perf_counter()
+        res = [srv.wait(t) for t in srv.submit_many(reqs)]
+        runs.append(time.perf_counter() - t0)
+    st = srv.stats()
+    srv.close()
+    wall = statistics.median(runs)
+    nviews = sum(len(v) for _, v, _ in reqs)
+    lat = sorted(r.latency_ms for r in res)
+    return {"workload": "%d resident scenes (grids %s^3, %.1fM triangles in all), %d views of 256^2..1920x1080, "
+                        "FP16 storage, all traces in one persistent launch per batch under a CUDA graph"
+                        % (cfg["scenes"], "/".join(str(d) for d in cfg["dims"]), tris_total / 1e6, nviews),
+            "value": round(pixels / wall / 1e6, 2), "unit": "Mpix/s", "pixels": int(pixels), "views": nviews,
+            "batches_per_submit": len({r.batch for r in res}), "wall_ms": round(wall * 1e3, 3),
+            "p50_ms": round(lat[len(lat) // 2], 3), "p99_ms": round(lat[min(len(lat) - 1, int(0.99 * len(lat)))], 3),
+            "first_batch_ms_with_tuning": round(first_s * 1e3, 1),
+            "tuned": {"variant": int(st.trace_variant), "tile": [int(st.trace_tile[0]), int(st.trace_tile[1])],
+                      "ctas_per_sm": int(st.trace_ctas_per_sm),
+                      "tune_ms": [round(float(st.tune_ms[i]), 3) for i in range(st.trace_variants)]},
+            "first_batch_status": sorted({r.status for r in first})}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -496,6 +669,10 @@ def main():
     ap.add_argument("--small", action="store_true", help="the 20k-triangle 64^3 640x360 case (profiling)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-served", action="store_true", help="skip the served-vs-plain request stream")
+    ap.add_argument("--no-precision", action="store_true", help="skip the 512^3 anisotropic FP16 precision form")
+    ap.add_argument("--precision-check", action="store_true",
+                    help="also measure the precision form's error against the FP64 oracle (CPU heavy)")
+    ap.add_argument("--no-batched", action="store_true", help="skip the 64-scene batched form")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     cfg = SMALL if args.small else PLAIN_LARGE
@@ -523,6 +700,10 @@ def main():
                       % (info["voxelize_mip_s"], info["trace_rows"], cfg["height"], info["trace_s"])}
     if rank == 0 and world == 1 and not args.no_served and not args.small:
         line["served"] = run_served(args)
+    if rank == 0 and world == 1 and not args.no_batched and not args.small:
+        line["batched"] = run_batched(args)
+    if rank == 0 and world == 1 and not args.no_precision and not args.small:
+        line["precision"] = run_precision(args)
     if rank == 0:
         print(json.dumps(line), flush=True)
 

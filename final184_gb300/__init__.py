@@ -267,6 +267,21 @@ class Server:
         check(self.lib.f184gi_server_submit(self.h, C.byref(req), C.byref(t)))
         return t.value
 
+    def submit_many(self, requests, host_buffers=False):
+        """Queue [(scene_id, views, moves), ...] at once (one batch can take them all); returns the tickets."""
+        keep, reqs = [], []
+        for scene_id, views, moves in requests:
+            mv = (_abi.Move * max(1, len(moves)))(*[_abi.Move(int(f), int(c), (C.c_float * 3)(*o))
+                                                     for f, c, o in moves])
+            vw = (View * len(views))(*views)
+            keep += [mv, vw]
+            reqs.append(_abi.Request(scene_id, _abi.REQ_HOST_BUFFERS if host_buffers else 0, mv, len(moves),
+                                     len(views), vw))
+        arr = (_abi.Request * len(reqs))(*reqs)
+        t = (C.c_uint64 * len(reqs))()
+        check(self.lib.f184gi_server_submit_batch(self.h, arr, len(reqs), t))
+        return list(t)
+
     def wait(self, ticket, timeout_ms=0):
         r = _abi.RequestResult()
         rc = self.lib.f184gi_server_wait(self.h, ticket, timeout_ms, C.byref(r))

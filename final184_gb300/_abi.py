@@ -145,6 +145,7 @@ PROTOTYPES = {
     "f184gi_server_wait": (C.c_int, [P, U64, U32, C.POINTER(RequestResult)]),
     "f184gi_server_cancel": (C.c_int, [P, U64]),
     "f184gi_server_get_stats": (C.c_int, [P, C.POINTER(ServerStats)]),
+    "f184gi_server_submit_batch": (C.c_int, [P, C.POINTER(Request), U32, C.POINTER(U64)]),
     "f184gi_scene_generate": (C.c_int, [U64, U64, U32, C.POINTER(C.POINTER(Scene))]),
     "f184gi_scene_free": (None, [C.POINTER(Scene)]),
     "f184gi_scene_move_objects": (C.c_int, [C.POINTER(Scene), U64, F32, F32, C.POINTER(U32), C.POINTER(U32)]),

@@ -403,7 +403,7 @@ void f184gi_cone_params_default(f184gi_cone_params* p) {
     p->diffuse_tilt_deg = 60.0f;
     p->step_factor = 0.5f;
     p->max_distance = 0.0f;
-    p->alpha_stop = 0.999f;
+    p->alpha_stop = 1.0f;
     p->start_offset = 1.0f;
     p->min_spec_tan_half = 0.05f;
     p->specular = 1;
@@ -442,6 +442,7 @@ int f184gi_trace(f184gi_ctx* c, uint32_t grid, const f184gi_view* views, uint32_
         if (!invert4(V, IV) || !invert4(P, IP)) return fail(F184GI_ERR_INVALID, "trace: singular view or projection");
         TraceView& t = tv[i];
         for (int k = 0; k < 16; ++k) t.iview[k] = float(IV[k]), t.iproj[k] = float(IP[k]);
+        for (int k = 0; k < 8; ++k) t.iproj_zw[k] = IP[8 + k];
         t.eye[0] = float(IV[3]);
         t.eye[1] = float(IV[7]);
         t.eye[2] = float(IV[11]);

@@ -92,6 +92,7 @@ int mip_launch(const ChainLayout& chain, uint32_t levels, uint32_t* d_status, cu
 
 struct TraceView {
     float iview[16], iproj[16];     // inverses (FP32 of FP64 inverses)
+    double iproj_zw[8];             // rows 2 and 3 of the FP64 inverse projection (depth reconstruction)
     float eye[3];
     uint32_t width, height;
     const float* depth;

@@ -1,4 +1,5 @@
-// mip.cu -- 3D mip chain of the radiance/opacity grid (2x2x2 mean of premultiplied RGBA).
+// mip.cu -- 3D mip chain of the radiance/opacity grid: 2x2x2 mean of premultiplied RGBA (isotropic), or six
+// directional volumes per level (anisotropic).
 //
 // The reference volume has a single level (Foreground/Renderer/MegaPipeline.cpp:481, Range.Set(0,1,0,1)); this
 // pass follows the isotropic pre-filtering of voxel cone tracing (Crassin et al. 2011).  With bricks in Morton
@@ -23,16 +24,56 @@ __device__ __forceinline__ float4 raw_vox(const unsigned char* smem, uint32_t fo
 __device__ __forceinline__ float4 f4add(float4 a, float4 b) { return make_float4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w); }
 __device__ __forceinline__ float4 f4mul(float4 a, float s) { return make_float4(a.x * s, a.y * s, a.z * s, a.w * s); }
 
+// One output voxel from its 2x2x2 children, fetch(dx, dy, dz) returning child (dx, dy, dz).
+// Isotropic: the mean of the eight children.  Anisotropic direction d in (+x, -x, +y, -y, +z, -z): along the
+// axis of d the two children composite front to back (front = the child a cone travelling along d meets first:
+// f + (1 - f.alpha) b per channel) and the four columns across the axis are averaged.
+template <bool ANISO, class Fetch>
+__device__ __forceinline__ float4 reduce8(uint32_t dir, Fetch fetch) {
+    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (!ANISO) {
+        for (int dz = 0; dz < 2; ++dz)
+            for (int dy = 0; dy < 2; ++dy)
+                for (int dx = 0; dx < 2; ++dx) acc = f4add(acc, fetch(dx, dy, dz));
+        return f4mul(acc, 0.125f);
+    }
+    const int axis = int(dir >> 1);
+    const int neg = int(dir & 1u);
+    const int o1 = (axis + 1) % 3, o2 = (axis + 2) % 3;
+    for (int u = 0; u < 2; ++u)
+        for (int v = 0; v < 2; ++v) {
+            int of[3], ob[3];
+            of[axis] = neg, ob[axis] = 1 - neg;
+            of[o1] = ob[o1] = u;
+            of[o2] = ob[o2] = v;
+            const float4 f = fetch(of[0], of[1], of[2]);
+            const float4 b = fetch(ob[0], ob[1], ob[2]);
+            const float tr = 1.0f - f.w;
+            acc.x += f.x + tr * b.x;
+            acc.y += f.y + tr * b.y;
+            acc.z += f.z + tr * b.z;
+            acc.w += f.w + tr * b.w;
+        }
+    return f4mul(acc, 0.25f);
+}
+
 // Source block of S^3 voxels of level `src` (S = 16: eight bricks; S <= 8: the whole level) reduced into
 // levels src+1 .. src+nout.  Block b of the source level is the Morton-ordered group of 8 bricks 8b .. 8b+7.
+// Anisotropic chains: CTA x = block * 6 + direction (the six CTAs of one block run together, so a level-0
+// block read by all six comes from DRAM once); direction d of a level reduces direction d of the level below
+// (level 0 has one volume).
+template <bool ANISO>
 __global__ void __launch_bounds__(512) mip_pass(ChainLayout c, uint32_t src, uint32_t nout, uint32_t* status) {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ float4 lvl[2][512];
     __shared__ __align__(8) uint64_t bar;
+    const uint32_t dir = ANISO ? blockIdx.x % 6u : 0u;
+    const uint32_t blk = ANISO ? blockIdx.x / 6u : blockIdx.x;
     const uint32_t ds = c.ldim[src];
     const uint32_t S = ds >= 16 ? 16u : ds;
     const uint32_t nvox = S * S * S;
-    const uint64_t src_off = c.off[src] + (ds >= 16 ? uint64_t(blockIdx.x) * 4096u : 0u);
+    const uint64_t src_vol = (ANISO && src > 0) ? c.off[src] + uint64_t(dir) * c.vol[src] : c.off[src];
+    const uint64_t src_off = src_vol + (ds >= 16 ? uint64_t(blk) * 4096u : 0u);
     const uint32_t bytes = nvox * c.esz;
     const unsigned char* gsrc = static_cast<const unsigned char*>(c.base) + src_off * c.esz;
     if (threadIdx.x == 0) {
@@ -51,47 +92,42 @@ __global__ void __launch_bounds__(512) mip_pass(ChainLayout c, uint32_t src, uin
     }
     // block coordinates of this source block at level src+1 (in units of S/2 voxels)
     uint32_t Bx = 0, By = 0, Bz = 0;
-    if (ds >= 16) Bx = compact1by2(blockIdx.x), By = compact1by2(blockIdx.x >> 1), Bz = compact1by2(blockIdx.x >> 2);
+    if (ds >= 16) Bx = compact1by2(blk), By = compact1by2(blk >> 1), Bz = compact1by2(blk >> 2);
     uint32_t n = S / 2;  // output edge of the first produced level
     // level src+1 from the staged source
     const uint32_t t = threadIdx.x;
     if (t < n * n * n) {
-        uint32_t x = t % n, y = (t / n) % n, z = t / (n * n);
-        float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
-        for (int dz = 0; dz < 2; ++dz)
-            for (int dy = 0; dy < 2; ++dy)
-                for (int dx = 0; dx < 2; ++dx) {
-                    uint32_t sx = 2 * x + dx, sy = 2 * y + dy, sz = 2 * z + dz;
-                    uint32_t si;
-                    if (S >= 8) {
-                        uint32_t cb = ((sx >> 3) & 1u) | (((sy >> 3) & 1u) << 1) | (((sz >> 3) & 1u) << 2);
-                        si = cb * 512u + ((sz & 7u) << 6) + ((sy & 7u) << 3) + (sx & 7u);
-                    } else {
-                        si = (sz * S + sy) * S + sx;
-                    }
-                    acc = f4add(acc, raw_vox(smem, c.format, si));
-                }
-        acc = f4mul(acc, 0.125f);
+        const uint32_t x = t % n, y = (t / n) % n, z = t / (n * n);
+        const float4 acc = reduce8<ANISO>(dir, [&](int dx, int dy, int dz) {
+            const uint32_t sx = 2 * x + dx, sy = 2 * y + dy, sz = 2 * z + dz;
+            uint32_t si;
+            if (S >= 8) {
+                const uint32_t cb = ((sx >> 3) & 1u) | (((sy >> 3) & 1u) << 1) | (((sz >> 3) & 1u) << 2);
+                si = cb * 512u + ((sz & 7u) << 6) + ((sy & 7u) << 3) + (sx & 7u);
+            } else {
+                si = (sz * S + sy) * S + sx;
+            }
+            return raw_vox(smem, c.format, si);
+        });
         lvl[0][t] = acc;
-        uint32_t d1 = c.ldim[src + 1];
-        store_vox(c.base, c.format, c.off[src + 1] + vox_index(d1, Bx * n + x, By * n + y, Bz * n + z), acc);
+        const uint32_t d1 = c.ldim[src + 1];
+        const uint64_t dst = c.off[src + 1] + (ANISO ? uint64_t(dir) * c.vol[src + 1] : 0u);
+        store_vox(c.base, c.format, dst + vox_index(d1, Bx * n + x, By * n + y, Bz * n + z), acc);
     }
     __syncthreads();
     int cur = 0;
     for (uint32_t k = 2; k <= nout; ++k) {
-        uint32_t np = n;
+        const uint32_t np = n;
         n = n / 2;
         if (t < n * n * n) {
-            uint32_t x = t % n, y = (t / n) % n, z = t / (n * n);
-            float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
-            for (int dz = 0; dz < 2; ++dz)
-                for (int dy = 0; dy < 2; ++dy)
-                    for (int dx = 0; dx < 2; ++dx)
-                        acc = f4add(acc, lvl[cur][((2 * z + dz) * np + (2 * y + dy)) * np + (2 * x + dx)]);
-            acc = f4mul(acc, 0.125f);
+            const uint32_t x = t % n, y = (t / n) % n, z = t / (n * n);
+            const float4 acc = reduce8<ANISO>(dir, [&](int dx, int dy, int dz) {
+                return lvl[cur][((2 * z + dz) * np + (2 * y + dy)) * np + (2 * x + dx)];
+            });
             lvl[cur ^ 1][t] = acc;
-            uint32_t dk = c.ldim[src + k];
-            store_vox(c.base, c.format, c.off[src + k] + vox_index(dk, Bx * n + x, By * n + y, Bz * n + z), acc);
+            const uint32_t dk = c.ldim[src + k];
+            const uint64_t dst = c.off[src + k] + (ANISO ? uint64_t(dir) * c.vol[src + k] : 0u);
+            store_vox(c.base, c.format, dst + vox_index(dk, Bx * n + x, By * n + y, Bz * n + z), acc);
         }
         __syncthreads();
         cur ^= 1;
@@ -101,14 +137,16 @@ __global__ void __launch_bounds__(512) mip_pass(ChainLayout c, uint32_t src, uin
 }  // namespace
 
 int mip_launch(const ChainLayout& c, uint32_t levels, uint32_t* d_status, cudaStream_t s) {
-    if (c.aniso) return fail(F184GI_ERR_INVALID, "mip: anisotropic chains are built by mip_aniso_launch");
     if (levels > c.levels) levels = c.levels;
     static bool attr_set = false;
     if (!attr_set) {
-        cudaError_t e = cudaFuncSetAttribute(mip_pass, cudaFuncAttributeMaxDynamicSharedMemorySize, 4096 * 16);
+        cudaError_t e = cudaFuncSetAttribute(mip_pass<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 4096 * 16);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(mip_pass<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 4096 * 16);
         if (e != cudaSuccess) return cuda_fail(e, "mip: smem attribute");
         attr_set = true;
     }
+    const uint32_t ndir = c.aniso ? 6u : 1u;
     uint32_t l = 0;
     while (l + 1 < levels) {
         uint32_t ds = c.ldim[l];
@@ -116,9 +154,12 @@ int mip_launch(const ChainLayout& c, uint32_t levels, uint32_t* d_status, cudaSt
         uint32_t maxout = 0;
         for (uint32_t e = S; e > 1; e /= 2) ++maxout;  // S=16 -> 4 levels
         uint32_t nout = std::min(maxout, levels - 1 - l);
-        uint32_t blocks = ds >= 16 ? (ds / 16) * (ds / 16) * (ds / 16) : 1u;
+        uint32_t blocks = (ds >= 16 ? (ds / 16) * (ds / 16) * (ds / 16) : 1u) * ndir;
         size_t smem = size_t(S) * S * S * c.esz;
-        mip_pass<<<blocks, 512, smem, s>>>(c, l, nout, d_status);
+        if (c.aniso)
+            mip_pass<true><<<blocks, 512, smem, s>>>(c, l, nout, d_status);
+        else
+            mip_pass<false><<<blocks, 512, smem, s>>>(c, l, nout, d_status);
         note_launches(1);
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return cuda_fail(e, "mip");

@@ -148,10 +148,13 @@ int f184gi_scene_generate(uint64_t seed, uint64_t target_tris, uint32_t nobjects
     double budget = nsph ? (double(target_tris) - 12.0 - 12.0 * nbox) / double(nsph) : 0.0;
     int stacks = std::max(3, int(std::lround(std::sqrt(std::max(budget, 0.0) / 4.0))));
     int slices = std::max(3, int(std::lround(std::max(budget, 0.0) / (2.0 * (stacks - 1)))));
+    // object sizes shrink with the count so that every scene fills about the same share of the room as the
+    // 200-object one (~16% of its volume), whatever the number of objects
+    const float size_scale = nobjects > 200 ? float(std::cbrt(200.0 / double(nobjects))) : 1.0f;
     for (uint32_t j = 0; j < nobjects; ++j) {
         Rng r(substream(seed, j + 1));
         bool box = (j % 2) == 0;
-        float half = r.uni(0.3f, 1.5f);
+        float half = r.uni(0.3f, 1.5f) * size_scale;
         float reach = box ? half * 1.7320508f : half;
         float ctr[3];
         for (int a = 0; a < 3; ++a) ctr[a] = r.uni(-10.0f + reach + 0.05f, 10.0f - reach - 0.05f);
@@ -222,9 +225,32 @@ void f184gi_scene_free(f184gi_scene* s) {
 int f184gi_scene_camera(const f184gi_scene* s, uint64_t seed, uint32_t i, float eye[3], float target[3]) {
     if (!s || !eye || !target) return f184::fail(F184GI_ERR_INVALID, "scene_camera: null argument");
     Rng r(substream(seed ^ 0x5EED5EEDull, 0x10000000ull + i));
-    eye[0] = r.uni(-8.0f, 8.0f);
-    eye[1] = r.uni(-6.0f, 6.0f);
-    eye[2] = r.uni(-8.0f, 8.0f);
+    // the eye sits in free space: at least 0.5 m outside every object's bounding box (up to 256 draws)
+    std::vector<float> box(size_t(s->nobjects) * 6);
+    for (uint32_t o = 0; o < s->nobjects; ++o) {
+        float* bb = &box[size_t(o) * 6];
+        for (int a = 0; a < 3; ++a) bb[a] = 1e30f, bb[3 + a] = -1e30f;
+        if (o == 0) continue;  // the room itself
+        const float* p = s->tri_xyz + uint64_t(s->object_first[o]) * 9;
+        for (uint64_t v = 0; v < uint64_t(s->object_count[o]) * 3; ++v)
+            for (int a = 0; a < 3; ++a) {
+                bb[a] = std::min(bb[a], p[v * 3 + a]);
+                bb[3 + a] = std::max(bb[3 + a], p[v * 3 + a]);
+            }
+    }
+    for (int attempt = 0; attempt < 256; ++attempt) {
+        eye[0] = r.uni(-8.0f, 8.0f);
+        eye[1] = r.uni(-6.0f, 6.0f);
+        eye[2] = r.uni(-8.0f, 8.0f);
+        bool clear = true;
+        for (uint32_t o = 1; o < s->nobjects && clear; ++o) {
+            const float* bb = &box[size_t(o) * 6];
+            bool inside = true;
+            for (int a = 0; a < 3; ++a) inside = inside && eye[a] > bb[a] - 0.5f && eye[a] < bb[3 + a] + 0.5f;
+            clear = !inside;
+        }
+        if (clear) break;
+    }
     float d[3];
     float n;
     do {

@@ -190,6 +190,7 @@ int prepare_view(f184gi_server* S, const Scene* sc, const f184gi_view& v, TraceV
     if (!invert4(V, IV) || !invert4(P, IP)) return fail(F184GI_ERR_INVALID, "server: singular view or projection");
     t = TraceView{};
     for (int k = 0; k < 16; ++k) t.iview[k] = float(IV[k]), t.iproj[k] = float(IP[k]);
+    for (int k = 0; k < 8; ++k) t.iproj_zw[k] = IP[8 + k];
     t.eye[0] = float(IV[3]), t.eye[1] = float(IV[7]), t.eye[2] = float(IV[11]);
     t.width = v.width, t.height = v.height;
     t.depth = v.depth, t.normal = v.normal, t.rough = v.roughness, t.out = v.out, t.out_format = v.out_format;
@@ -538,8 +539,13 @@ int f184gi_server_add_scene(f184gi_server* S, uint32_t id, const f184gi_grid_des
     return F184GI_OK;
 }
 
-int f184gi_server_submit(f184gi_server* S, const f184gi_request* req, uint64_t* ticket) {
-    if (!S || !req || !ticket) return fail(F184GI_ERR_INVALID, "server_submit: null argument");
+}  // extern "C"
+
+namespace {
+
+// A request checked against its own fields (no server state): the copy that the server queues.
+int make_request(const f184gi_request* req, Request** out) {
+    *out = nullptr;
     if (req->nviews == 0 || !req->views) return fail(F184GI_ERR_INVALID, "server_submit: a request needs views");
     if (req->nmoves && !req->moves) return fail(F184GI_ERR_INVALID, "server_submit: null moves");
     for (uint32_t i = 0; i < req->nviews; ++i) {
@@ -555,30 +561,65 @@ int f184gi_server_submit(f184gi_server* S, const f184gi_request* req, uint64_t* 
     r->views.assign(req->views, req->views + req->nviews);
     for (const f184gi_view& v : r->views) r->pixels += uint64_t(v.width) * v.height;
     r->staging = staging_bytes(*req);
-    std::lock_guard<std::mutex> lk(S->mu);
-    auto it = S->scenes.find(req->scene_id);
-    if (it == S->scenes.end()) {
-        delete r;
-        return fail(F184GI_ERR_NOTFOUND, "server_submit: unknown scene");
-    }
+    *out = r;
+    return F184GI_OK;
+}
+
+// Checks against the server's scenes and limits (S->mu held).
+int admit_check(f184gi_server* S, const Request* r) {
+    auto it = S->scenes.find(r->scene);
+    if (it == S->scenes.end()) return fail(F184GI_ERR_NOTFOUND, "server_submit: unknown scene");
     for (const f184gi_move& m : r->moves)
-        if (uint64_t(m.first) + m.count > it->second->ntris) {
-            delete r;
+        if (uint64_t(m.first) + m.count > it->second->ntris)
             return fail(F184GI_ERR_INVALID, "server_submit: move range out of bounds");
-        }
-    if (req->nviews > S->cfg.max_batch_views) {
-        delete r;
+    if (r->views.size() > S->cfg.max_batch_views)
         return fail(F184GI_ERR_INVALID, "server_submit: more views than max_batch_views");
-    }
-    if (S->cfg.hbm_budget && r->staging > S->cfg.hbm_budget) {
-        delete r;
+    if (S->cfg.hbm_budget && r->staging > S->cfg.hbm_budget)
         return fail(F184GI_ERR_BUDGET, "server_submit: the request's staging exceeds the HBM budget");
-    }
+    return F184GI_OK;
+}
+
+void enqueue(f184gi_server* S, Request* r, Clock::time_point now) {
     r->ticket = S->next_ticket++;
-    r->t_submit = Clock::now();
+    r->t_submit = now;
     S->reqs[r->ticket] = r;
     S->pending.push_back(r);
-    *ticket = r->ticket;
+}
+
+}  // namespace
+
+extern "C" {
+
+int f184gi_server_submit(f184gi_server* S, const f184gi_request* req, uint64_t* ticket) {
+    return f184gi_server_submit_batch(S, req, 1, ticket);
+}
+
+int f184gi_server_submit_batch(f184gi_server* S, const f184gi_request* reqs, uint32_t n, uint64_t* tickets) {
+    if (!S || !reqs || !tickets) return fail(F184GI_ERR_INVALID, "server_submit: null argument");
+    std::vector<Request*> rs;
+    rs.reserve(n);
+    for (uint32_t k = 0; k < n; ++k) {
+        Request* r = nullptr;
+        int rc = make_request(&reqs[k], &r);
+        if (rc) {
+            for (Request* q : rs) delete q;
+            return rc;
+        }
+        rs.push_back(r);
+    }
+    std::lock_guard<std::mutex> lk(S->mu);
+    for (Request* r : rs) {
+        int rc = admit_check(S, r);
+        if (rc) {
+            for (Request* q : rs) delete q;
+            return rc;
+        }
+    }
+    const Clock::time_point now = Clock::now();
+    for (uint32_t k = 0; k < n; ++k) {
+        enqueue(S, rs[k], now);
+        tickets[k] = rs[k]->ticket;
+    }
     S->cv_sched.notify_all();
     return F184GI_OK;
 }

@@ -75,9 +75,11 @@ constexpr int kLut = 65;
 // volume read zero.  Interior samples (all taps inside) address the seven other taps from the first one with
 // one delta per axis: +1 / +8 / +64 inside a brick, or the Morton step to the next brick when the tap crosses a
 // brick face.  Samples touching the border take the general path with a validity test per tap.
-template <int FMT>
-__device__ __forceinline__ float4 tri_sample(const void* base, int d, uint32_t l, uint32_t vol_off, float3 x,
-                                             const uint32_t* lut) {
+template <int FMT, int NV>
+__device__ __forceinline__ void tri_sample(const void* base, int d, uint32_t l, const uint32_t (&vol_off)[NV],
+                                          float3 x, const uint32_t* lut, float4 (&acc)[NV]) {
+    // NV volumes of the same level share the tap coordinates and weights (the three directions an anisotropic
+    // sample blends); each volume accumulates its own taps in the single-volume order.
     const float s = __int_as_float((127 - int(l)) << 23);  // 2^-l
     const float u[3] = {x.x * s - 0.5f, x.y * s - 0.5f, x.z * s - 0.5f};
     int c0[3];
@@ -89,7 +91,8 @@ __device__ __forceinline__ float4 tri_sample(const void* base, int d, uint32_t l
         f[a] = u[a] - fl;
     }
     const float wx[2] = {1.0f - f[0], f[0]}, wy[2] = {1.0f - f[1], f[1]}, wz[2] = {1.0f - f[2], f[2]};
-    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+    for (int k = 0; k < NV; ++k) acc[k] = make_float4(0.f, 0.f, 0.f, 0.f);
     const unsigned lim = unsigned(d - 1);
     if (unsigned(c0[0]) < lim && unsigned(c0[1]) < lim && unsigned(c0[2]) < lim) {
         uint32_t i0, dx, dy, dz;
@@ -105,24 +108,27 @@ __device__ __forceinline__ float4 tri_sample(const void* base, int d, uint32_t l
             i0 = (uint32_t(c0[2]) * uint32_t(d) + uint32_t(c0[1])) * uint32_t(d) + uint32_t(c0[0]);
             dx = 1u, dy = uint32_t(d), dz = uint32_t(d) * uint32_t(d);
         }
-        const uint32_t ib = vol_off + i0;
 #pragma unroll
         for (int tz = 0; tz < 2; ++tz)
 #pragma unroll
             for (int ty = 0; ty < 2; ++ty) {
                 const float wyz = wy[ty] * wz[tz];
-                const uint32_t row = ib + (tz ? dz : 0u) + (ty ? dy : 0u);
+                const uint32_t row = i0 + (tz ? dz : 0u) + (ty ? dy : 0u);
 #pragma unroll
                 for (int tx = 0; tx < 2; ++tx) {
-                    float4 v = load_vox(base, FMT, row + (tx ? dx : 0u));
-                    float w = wx[tx] * wyz;
-                    acc.x += w * v.x;
-                    acc.y += w * v.y;
-                    acc.z += w * v.z;
-                    acc.w += w * v.w;
+                    const float w = wx[tx] * wyz;
+                    const uint32_t e = row + (tx ? dx : 0u);
+#pragma unroll
+                    for (int k = 0; k < NV; ++k) {
+                        const float4 v = load_vox(base, FMT, vol_off[k] + e);
+                        acc[k].x += w * v.x;
+                        acc[k].y += w * v.y;
+                        acc[k].z += w * v.z;
+                        acc[k].w += w * v.w;
+                    }
                 }
             }
-        return acc;
+        return;
     }
     // border: per-axis validity, high (Morton) and low (in-brick / linear) address parts
     bool ok[3][2];
@@ -151,34 +157,45 @@ __device__ __forceinline__ float4 tri_sample(const void* base, int d, uint32_t l
 #pragma unroll
             for (int tx = 0; tx < 2; ++tx) {
                 if (ok[0][tx] && ok[1][ty] && ok[2][tz]) {
-                    uint32_t idx = ((hi[0][tx] | hi[1][ty] | hi[2][tz]) << 9) | (lo[0][tx] | lo[1][ty] | lo[2][tz]);
-                    float4 v = load_vox(base, FMT, vol_off + idx);
-                    float w = wx[tx] * wyz;
-                    acc.x += w * v.x;
-                    acc.y += w * v.y;
-                    acc.z += w * v.z;
-                    acc.w += w * v.w;
+                    const uint32_t idx =
+                        ((hi[0][tx] | hi[1][ty] | hi[2][tz]) << 9) | (lo[0][tx] | lo[1][ty] | lo[2][tz]);
+                    const float w = wx[tx] * wyz;
+#pragma unroll
+                    for (int k = 0; k < NV; ++k) {
+                        const float4 v = load_vox(base, FMT, vol_off[k] + idx);
+                        acc[k].x += w * v.x;
+                        acc[k].y += w * v.y;
+                        acc[k].z += w * v.z;
+                        acc[k].w += w * v.w;
+                    }
                 }
             }
         }
-    return acc;
 }
 
 template <int FMT, bool ANISO>
 __device__ __forceinline__ float4 level_sample(const GridRef& g, const uint32_t* lut, uint32_t l, float3 x,
                                                float3 dir) {
     const int d = int(g.dim >> l);
-    if (!ANISO || l == 0) return tri_sample<FMT>(g.base, d, l, g.off[l], x, lut);
-    float w[3] = {dir.x * dir.x, dir.y * dir.y, dir.z * dir.z};
-    int sel[3] = {dir.x >= 0.0f ? 0 : 1, dir.y >= 0.0f ? 2 : 3, dir.z >= 0.0f ? 4 : 5};
+    if (!ANISO || l == 0) {
+        const uint32_t vo[1] = {g.off[l]};
+        float4 a[1];
+        tri_sample<FMT, 1>(g.base, d, l, vo, x, lut, a);
+        return a[0];
+    }
+    const float w[3] = {dir.x * dir.x, dir.y * dir.y, dir.z * dir.z};
+    const uint32_t vo[3] = {g.off[l] + (dir.x >= 0.0f ? 0u : 1u) * g.vol[l],
+                            g.off[l] + (dir.y >= 0.0f ? 2u : 3u) * g.vol[l],
+                            g.off[l] + (dir.z >= 0.0f ? 4u : 5u) * g.vol[l]};
+    float4 sa[3];
+    tri_sample<FMT, 3>(g.base, d, l, vo, x, lut, sa);
     float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
-        float4 s = tri_sample<FMT>(g.base, d, l, g.off[l] + uint32_t(sel[a]) * g.vol[l], x, lut);
-        acc.x += w[a] * s.x;
-        acc.y += w[a] * s.y;
-        acc.z += w[a] * s.z;
-        acc.w += w[a] * s.w;
+        acc.x += w[a] * sa[a].x;
+        acc.y += w[a] * sa[a].y;
+        acc.z += w[a] * sa[a].z;
+        acc.w += w[a] * sa[a].w;
     }
     return acc;
 }
@@ -187,13 +204,18 @@ template <int FMT, bool ANISO>
 __device__ float4 cone(const GridRef& g, const uint32_t* lut, const TraceConsts& tc, float3 o, float3 dir,
                        float tan_half) {
     float cr = 0.f, cg = 0.f, cb = 0.f, alpha = 0.f;
-    float t = tc.p.start_offset;
+    // The march distance is the float pair t + tl, advanced with error-free sums: a cone of small aperture takes
+    // a hundred steps much shorter than t, and plain FP32 sums would drift by ~n/2 ulp(t) (5e-3 voxel at the far
+    // end of a 512^3 grid), enough to move samples across opacity edges.
+    float t = tc.p.start_offset, tl = 0.0f;
     const float dimf = float(g.dim);
     const float maxl = float(g.levels - 1);
-    while (t <= g.tmax) {
-        float diam = fmaxf(1.0f, 2.0f * t * tan_half);
+    const float d2 = 2.0f * tan_half;
+    while (t < g.tmax || (t == g.tmax && tl <= 0.0f)) {
+        float diam = fmaxf(1.0f, fmaf(d2, t, d2 * tl));
         float lvl = fminf(fmaxf(log2f(diam), 0.0f), maxl);
-        float3 x = add3(o, mul3(dir, t));
+        float3 x = f3(fmaf(dir.x, t, fmaf(dir.x, tl, o.x)), fmaf(dir.y, t, fmaf(dir.y, tl, o.y)),
+                      fmaf(dir.z, t, fmaf(dir.z, tl, o.z)));
         float m = 2.0f * diam;
         if (x.x < -m || x.y < -m || x.z < -m || x.x > dimf + m || x.y > dimf + m || x.z > dimf + m) break;
         float fl = floorf(lvl);
@@ -213,7 +235,10 @@ __device__ float4 cone(const GridRef& g, const uint32_t* lut, const TraceConsts&
         cb += tr * s.z;
         alpha += tr * s.w;
         if (alpha >= tc.p.alpha_stop) break;
-        t += tc.p.step_factor * diam;
+        const float step = tc.p.step_factor * diam;
+        const float ts = t + step, tb = ts - t;
+        tl += (t - (ts - tb)) + (step - tb);
+        t = ts;
     }
     return make_float4(cr, cg, cb, alpha);
 }
@@ -245,10 +270,17 @@ __device__ void trace_pixel(const GridRef& g, const uint32_t* lut, const TraceCo
     const float* iv = v.iview;
     float nx = (float(px) + 0.5f) / float(v.width) * 2.0f - 1.0f;
     float ny = (float(py) + 0.5f) / float(v.height) * 2.0f - 1.0f;
-    float vp[4];
-#pragma unroll
-    for (int r = 0; r < 4; ++r) vp[r] = ip[r * 4 + 0] * nx + ip[r * 4 + 1] * ny + ip[r * 4 + 2] * d + ip[r * 4 + 3];
-    float3 cs = f3(vp[0] / vp[3], vp[1] / vp[3], vp[2] / vp[3]);
+    // View-space position.  The projective rows (z, w) run in FP64: for depths near 1, w is a small difference
+    // of O(1) terms and FP32 would lose ~5e-6 of it (a fraction of a voxel at 10 m).  x and y are well
+    // conditioned and stay FP32.
+    const double* iz = v.iproj_zw;
+    const double dnx = double(nx), dny = double(ny), dd = double(d);
+    const double vz = fma(iz[0], dnx, fma(iz[1], dny, fma(iz[2], dd, iz[3])));
+    const double vw = fma(iz[4], dnx, fma(iz[5], dny, fma(iz[6], dd, iz[7])));
+    const double rw = 1.0 / vw;
+    const float rwf = float(rw);
+    const float vx = ip[0] * nx + ip[1] * ny + ip[2] * d + ip[3], vy = ip[4] * nx + ip[5] * ny + ip[6] * d + ip[7];
+    float3 cs = f3(vx * rwf, vy * rwf, float(vz * rw));
     float3 wp = f3(iv[0] * cs.x + iv[1] * cs.y + iv[2] * cs.z + iv[3], iv[4] * cs.x + iv[5] * cs.y + iv[6] * cs.z + iv[7],
                    iv[8] * cs.x + iv[9] * cs.y + iv[10] * cs.z + iv[11]);
     float3 nv = oct_decode(v.normal[pi]);

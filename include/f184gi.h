@@ -133,7 +133,8 @@ typedef struct f184gi_cone_params {
     float diffuse_tilt_deg;  /* 60: tilt of the side cones from the normal */
     float step_factor;       /* 0.5: step = step_factor * cone diameter */
     float max_distance;      /* in L0 voxels; <= 0 means the grid diagonal */
-    float alpha_stop;        /* 0.999: stop a cone once its opacity reaches this */
+    float alpha_stop;        /* 1.0: stop a cone once its opacity reaches this (1.0 = only when opaque; a lower
+                              * threshold makes the result jump where rounding moves the crossing by a step) */
     float start_offset;      /* 1.0: origin offset along the normal, in L0 voxels */
     float min_spec_tan_half; /* 0.05: specular cone tan(half aperture) = max(roughness, this) */
     uint32_t specular;       /* 1 = trace the specular cone */
@@ -287,6 +288,9 @@ int f184gi_server_add_scene(f184gi_server* s, uint32_t scene_id, const f184gi_gr
                             const f184gi_light* light);
 /* Queue a request (moves and views are copied); returns a ticket.  F184GI_ERR_BUDGET if its staging can never fit. */
 int f184gi_server_submit(f184gi_server* s, const f184gi_request* req, uint64_t* ticket);
+/* Queue n requests at once (all or none): the scheduler sees them together, so they can share one batch.
+ * tickets[k] receives request k's ticket. */
+int f184gi_server_submit_batch(f184gi_server* s, const f184gi_request* reqs, uint32_t n, uint64_t* tickets);
 /* Wait until the ticket completes (timeout_ms 0 = no limit): F184GI_ERR_TIMEOUT when the wait expires. */
 int f184gi_server_wait(f184gi_server* s, uint64_t ticket, uint32_t timeout_ms, f184gi_request_result* out);
 /* Cancel a request that has not been admitted yet (F184GI_ERR_INVALID once it is running or done). */

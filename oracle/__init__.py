@@ -40,7 +40,7 @@ class ConeParams(C.Structure):
 
 
 def default_params():
-    return ConeParams(5, 0.57735026918962576, 60.0, 0.5, 0.0, 0.999, 1.0, 0.05, 1, 0)
+    return ConeParams(5, 0.57735026918962576, 60.0, 0.5, 0.0, 1.0, 1.0, 0.05, 1, 0)
 
 
 def lib():

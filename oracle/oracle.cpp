@@ -18,6 +18,7 @@
 #include <cmath>
 #include <cstring>
 #include <thread>
+#include <type_traits>
 #include <vector>
 
 namespace {
@@ -588,7 +589,7 @@ f184gi_cone_params default_params() {
     p.diffuse_tilt_deg = 60.0f;
     p.step_factor = 0.5f;
     p.max_distance = 0.0f;
-    p.alpha_stop = 0.999f;
+    p.alpha_stop = 1.0f;
     p.start_offset = 1.0f;
     p.min_spec_tan_half = 0.05f;
     p.specular = 1;
@@ -670,13 +671,19 @@ template <class T>
 void cone(const Chain<T>& ch, Vec3<T> o, Vec3<T> dir, T tan_half, const f184gi_cone_params& p, T tmax,
           T out[4]) {
     T c[3] = {T(0), T(0), T(0)}, alpha = T(0);
-    T t = T(p.start_offset);
+    // FP64: t accumulates plainly (the definition).  FP32 (the device arithmetic): the distance is the pair
+    // t + tl advanced with error-free sums, so long marches of small steps do not drift.
+    constexpr bool kPair = std::is_same<T, float>::value;
+    T t = T(p.start_offset), tl = T(0);
     const T dimf = T(ch.dim);
     const T maxl = T(ch.levels - 1);
-    while (t <= tmax) {
-        T diam = std::max(T(1), T(2) * t * tan_half);
+    const T d2 = T(2) * tan_half;
+    while (t < tmax || (t == tmax && tl <= T(0))) {
+        T diam = kPair ? std::max(T(1), std::fma(d2, t, d2 * tl)) : std::max(T(1), T(2) * t * tan_half);
         T lvl = std::min(std::max(std::log2(diam), T(0)), maxl);
-        Vec3<T> x = vadd(o, vmul(dir, t));
+        Vec3<T> x = kPair ? Vec3<T>{std::fma(dir.x, t, std::fma(dir.x, tl, o.x)), std::fma(dir.y, t, std::fma(dir.y, tl, o.y)),
+                                    std::fma(dir.z, t, std::fma(dir.z, tl, o.z))}
+                          : vadd(o, vmul(dir, t));
         T m = T(2) * diam;
         if (x.x < -m || x.y < -m || x.z < -m || x.x > dimf + m || x.y > dimf + m || x.z > dimf + m) break;
         T fl = std::floor(lvl);
@@ -693,7 +700,14 @@ void cone(const Chain<T>& ch, Vec3<T> o, Vec3<T> dir, T tan_half, const f184gi_c
         for (int k = 0; k < 3; ++k) c[k] += tr * s[k];
         alpha += tr * s[3];
         if (alpha >= T(p.alpha_stop)) break;
-        t += T(p.step_factor) * diam;
+        const T step = T(p.step_factor) * diam;
+        if (kPair) {
+            const T ts = t + step, tb = ts - t;
+            tl += (t - (ts - tb)) + (step - tb);
+            t = ts;
+        } else {
+            t += step;
+        }
     }
     out[0] = c[0];
     out[1] = c[1];
@@ -749,6 +763,14 @@ int trace_impl(const f184gi_grid_frame* frame, uint32_t dim, uint32_t levels, ui
                 T vp[4];
                 for (int r = 0; r < 4; ++r) vp[r] = ip[r * 4 + 0] * nx + ip[r * 4 + 1] * ny + ip[r * 4 + 2] * nz + ip[r * 4 + 3];
                 Vec3<T> cs{vp[0] / vp[3], vp[1] / vp[3], vp[2] / vp[3]};
+                if (std::is_same<T, float>::value) {
+                    // the device arithmetic: the projective rows (z, w) in FP64, x and y in FP32
+                    const double dnx = double(nx), dny = double(ny), ddz = double(nz);
+                    const double vz = IP[8] * dnx + IP[9] * dny + IP[10] * ddz + IP[11];
+                    const double vw = IP[12] * dnx + IP[13] * dny + IP[14] * ddz + IP[15];
+                    const double rw = 1.0 / vw;
+                    cs = Vec3<T>{vp[0] * T(rw), vp[1] * T(rw), T(vz * rw)};
+                }
                 Vec3<T> wp{iv[0] * cs.x + iv[1] * cs.y + iv[2] * cs.z + iv[3],
                            iv[4] * cs.x + iv[5] * cs.y + iv[6] * cs.z + iv[7],
                            iv[8] * cs.x + iv[9] * cs.y + iv[10] * cs.z + iv[11]};

@@ -34,7 +34,7 @@ class Case:
     """scene -> device buffers -> (voxelize, mip, gbuffer, trace) on the GPU, with oracle counterparts."""
 
     def __init__(self, seed=184, ntris=20000, nobj=200, dim=64, levels=6, res=1024, width=320, height=180,
-                 fmt=0, keep_counts=True):
+                 fmt=0, keep_counts=True, aniso=False):
         import torch
 
         import final184_gb300 as g
@@ -45,7 +45,9 @@ class Case:
         self.sc = g.SyntheticScene(seed, ntris, nobj)
         self.dim, self.levels, self.res, self.W, self.H, self.fmt = dim, levels, res, width, height, fmt
         self.gi = g.VoxelGI(0)
-        self.grid = self.gi.create_grid(dim, levels, fmt, 0, res, g.GRID_KEEP_COUNTS if keep_counts else 0)
+        self.aniso = aniso
+        self.grid = self.gi.create_grid(dim, levels, fmt, 1 if aniso else 0, res,
+                                        g.GRID_KEEP_COUNTS if keep_counts else 0)
         self.upload(self.sc.tri_xyz, self.sc.albedo)
         self.rough_d = torch.from_numpy(self.sc.roughness).to(self.dev)
         self.V = g.look_at(self.sc.eye, self.sc.target)

@@ -193,6 +193,29 @@ def test_every_trace_variant_matches_the_plain_path(fx):
 
 
 @pytest.mark.gpu
+def test_submit_many_shares_one_batch(fx):
+    """Requests queued together on distinct scenes run as one batch and give the bytes of separate requests."""
+    srv = fx.server(slots=1, max_batch_views=64)
+    picks = [(0, [0, 1]), (1, [2]), (2, [0, 3])]
+    alone = []
+    for si, vids in picks:
+        views, outs = fx.make_views(si, vids)
+        srv.wait(srv.submit(si, views, []))
+        alone.append([o.cpu().numpy() for o in outs])
+    keep, reqs = [], []
+    for si, vids in picks:
+        views, outs = fx.make_views(si, vids)
+        keep.append(outs)
+        reqs.append((si, views, []))
+    res = [srv.wait(t) for t in srv.submit_many(reqs)]
+    srv.close()
+    assert len({r.batch for r in res}) == 1
+    for a, b in zip(alone, keep):
+        for x, y in zip(a, b):
+            assert np.array_equal(x.view(np.uint32), y.cpu().numpy().view(np.uint32))
+
+
+@pytest.mark.gpu
 def test_host_buffer_requests_match_device_requests(fx):
     g = fx.g
     srv = fx.server(slots=2)
