@@ -108,6 +108,22 @@ class ClockSampler:
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def slowest_rank_ms(local_ms, device=None):
+    """The largest per-rank time (replicas report the slowest rank; a no-op for one process)."""
+    import torch
+
+    if not (torch.distributed.is_available() and torch.distributed.is_initialized()):
+        return float(local_ms)
+    t = torch.tensor([float(local_ms)], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_mpix(units_per_rank, slowest_ms, world):
+    """Whole-job throughput of `world` replicas that each processed units_per_rank pixels in at most slowest_ms."""
+    return world * units_per_rank / (slowest_ms * 1e-3) / 1e6
+
+
 def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -272,16 +288,12 @@ def run_gpu(args, cfg):
     launches = g.load().f184gi_kernel_launches() - launches0
     clk = clocks.stop()
     gi.sync(stream)
-    total_ms = t_start.elapsed_time(t_end)
-    if world > 1:
-        t = torch.tensor([total_ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = slowest_rank_ms(t_start.elapsed_time(t_end), dev)
     ms_per_step = total_ms / args.steps
     step_ms = [evs[k][0].elapsed_time(evs[k][3]) for k in range(args.steps)]
     stage = {"voxelize": [e[0].elapsed_time(e[1]) for e in evs], "mip": [e[1].elapsed_time(e[2]) for e in evs],
              "trace": [e[2].elapsed_time(e[3]) for e in evs]}
-    value = world * npix / (ms_per_step * 1e-3) / 1e6
+    value = replica_mpix(npix, ms_per_step, world)
 
     # ---- end to end through the API with host buffers ----
     gbuf_d = [depth, normal, rgh]
@@ -300,12 +312,8 @@ def run_gpu(args, cfg):
         out_h.copy_(out, non_blocking=True)
     e1.record(stream)
     barrier()
-    e2e_ms = e0.elapsed_time(e1) / args.steps
-    if world > 1:
-        t = torch.tensor([e2e_ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_ms = float(t.item())
-    e2e_value = world * npix / (e2e_ms * 1e-3) / 1e6
+    e2e_ms = slowest_rank_ms(e0.elapsed_time(e1) / args.steps, dev)
+    e2e_value = replica_mpix(npix, e2e_ms, world)
 
     # ---- roofline of the dominant kernel (HBM: nothing here is a dense contraction) ----
     # trace_kernel is the largest single kernel of a request (launch-list share ~42%); its stage is one launch
