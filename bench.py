@@ -186,7 +186,7 @@ def run_reference(args, cfg):
     import final184_gb300 as g
 
     sc = g.SyntheticScene(cfg["seed"], cfg["ntris"], cfg["nobjects"])
-    stride = 64 if cfg is PLAIN_LARGE else 16
+    stride = 2 if cfg is PLAIN_LARGE else 1
     for _ in range(min(args.warmup, 1)):
         cpu_request(cfg, stride * 4, scene=sc)
     times = []
@@ -349,8 +349,8 @@ def run_gpu(args, cfg):
                      "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_source": peak_kind,
                      "algorithmic_bytes": alg[top],
                      "traffic": (tr * 1.0 if isinstance(tr, (int, float)) else None),
-                     "note": "far below the HBM roof: the trace is instruction-issue bound (ncu: ~71% issue-active, "
-                             "L1 hit ~96%, DRAM ~0.2% of peak); algorithmic bytes = G-buffer 10 B + output 32 B per "
+                     "note": "far below the HBM roof: the trace is instruction-issue bound (ncu: ~68% issue-active, "
+                             "L1 hit ~96%, DRAM ~0.3% of peak); algorithmic bytes = G-buffer 10 B + output 32 B per "
                              "pixel + the whole chain once (upper bound of the touched part)"},
         "e2e": {"value": round(e2e_value, 4), "unit": "Mpix/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "ms_per_step": round(e2e_ms, 4)},
@@ -698,7 +698,7 @@ def main():
         from oracle import build as ob
 
         ob.build_oracle()
-        stride = 64 if cfg is PLAIN_LARGE else 16
+        stride = 1  # the whole request: voxelization, mips and every row of the trace
         t, info, _ = cpu_request(cfg, stride, scene=sc)
         line["cpu_baseline"] = {
             "value": round(cfg["width"] * cfg["height"] / t / 1e6, 4), "unit": "Mpix/s", "cores": os.cpu_count(),
