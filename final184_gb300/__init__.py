@@ -10,11 +10,11 @@ import ctypes as C
 import numpy as np
 
 from . import _abi
-from ._abi import (FMT_F16, FMT_F32, GRID_KEEP_COUNTS, Bounds, ConeParams, F184Error, GridDesc, GridFrame, Light,
+from ._abi import (FMT_F16, FMT_F32, FMT_RG16, GRID_KEEP_COUNTS, MarchParams, Bounds, ConeParams, F184Error, GridDesc, GridFrame, Light,
                    View, check, load)
 
 __all__ = ["VoxelGI", "Grid", "SyntheticScene", "Light", "Bounds", "View", "ConeParams", "GridDesc", "GridFrame",
-           "FMT_F32", "FMT_F16", "GRID_KEEP_COUNTS", "F184Error", "perspective", "ortho", "look_at", "mat4_inverse",
+           "FMT_F32", "FMT_F16", "FMT_RG16", "GRID_KEEP_COUNTS", "MarchParams", "default_march_params", "F184Error", "perspective", "ortho", "look_at", "mat4_inverse",
            "make_light", "make_bounds", "default_cone_params", "frame_from_bounds", "make_view", "load"]
 
 
@@ -68,6 +68,12 @@ def frame_from_bounds(bounds, dim, light_dir):
     f = GridFrame()
     check(load().f184gi_frame_from_bounds(C.byref(bounds), dim, _fa(light_dir, 3), C.byref(f)))
     return f
+
+
+def default_march_params():
+    p = MarchParams()
+    load().f184gi_march_params_default(C.byref(p))
+    return p
 
 
 def default_cone_params():
@@ -195,6 +201,12 @@ class VoxelGI:
         check(self.lib.f184gi_trace(self.ctx, grid.handle, arr, len(views),
                                     C.byref(params) if params is not None else None, _stream(stream)))
 
+    def march(self, grid, views, params=None, stream=None):
+        """The reference-faithful indirect pass over an RG16 grid (out: width*height RGBA FP32 per view)."""
+        arr = (View * len(views))(*views)
+        check(self.lib.f184gi_march(self.ctx, grid.handle, arr, len(views),
+                                    C.byref(params) if params is not None else None, _stream(stream)))
+
     def gbuffer(self, tri_ptr, rough_ptr, ntris, view, tri_id_ptr=None, stream=None):
         check(self.lib.f184gi_gbuffer(self.ctx, tri_ptr, rough_ptr, ntris, C.byref(view), tri_id_ptr,
                                       _stream(stream)))
@@ -209,6 +221,10 @@ class VoxelGI:
 
     def read_level(self, grid, level, direction=0):
         d = grid.level_dim(level)
+        if grid.desc.format == FMT_RG16:  # packed uint32 per voxel (565 albedo | 565 normal << 16)
+            out = np.empty((d, d, d), dtype=np.uint32)
+            check(self.lib.f184gi_grid_read_level(self.ctx, grid.handle, level, direction, out.ctypes.data))
+            return out
         out = np.empty((d, d, d, 4), dtype=np.float32)
         check(self.lib.f184gi_grid_read_level(self.ctx, grid.handle, level, direction, out.ctypes.data))
         return out

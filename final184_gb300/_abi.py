@@ -10,6 +10,7 @@ LIB_PATH = os.path.join(HERE, "libf184gi.so")
 
 FMT_F32 = 0
 FMT_F16 = 1
+FMT_RG16 = 2
 GRID_KEEP_COUNTS = 1
 GRID_RESIDENT_WEIGHTS = 2
 
@@ -63,6 +64,12 @@ class ConeParams(C.Structure):
 
 class Move(C.Structure):
     _fields_ = [("first", C.c_uint32), ("count", C.c_uint32), ("offset", C.c_float * 3)]
+
+
+class MarchParams(C.Structure):
+    _fields_ = [("rays", C.c_uint32), ("second_bounce", C.c_uint32), ("max_steps", C.c_uint32), ("frame", C.c_uint32),
+                ("step_size", C.c_float), ("normal_offset", C.c_float), ("shadow_bias", C.c_float),
+                ("sky", C.c_float * 3), ("sky_scale", C.c_float), ("pad", C.c_float)]
 
 
 class ServerConfig(C.Structure):
@@ -124,6 +131,8 @@ PROTOTYPES = {
     "f184gi_trace": (C.c_int, [P, U32, C.POINTER(View), U32, C.POINTER(ConeParams), P]),
     "f184gi_cone_params_default": (None, [C.POINTER(ConeParams)]),
     "f184gi_gbuffer": (C.c_int, [P, P, P, U64, C.POINTER(View), P, P]),
+    "f184gi_march_params_default": (None, [C.POINTER(MarchParams)]),
+    "f184gi_march": (C.c_int, [P, U32, C.POINTER(View), U32, C.POINTER(MarchParams), P]),
     "f184gi_gbuffer_static": (C.c_int, [P, P, P, U64, C.POINTER(View), P, P]),
     "f184gi_transform": (C.c_int, [P, P, U64, PF, P, P]),
     "f184gi_apply_moves": (C.c_int, [P, P, C.POINTER(Move), U32, U64, P]),

@@ -82,6 +82,7 @@ struct GridObj {
     size_t weights_bytes = 0;
     f184gi_grid_frame* d_frame = nullptr;
     bool voxelized = false;
+    f184gi_light light{};  // the light of the last voxelization (the march shades with it)
 };
 
 struct f184gi_ctx {
@@ -144,10 +145,17 @@ int check_desc(const f184gi_grid_desc* d) {
     for (uint32_t x = d->dim; x > 1; x >>= 1) ++maxl;  // log2(dim): keeps a 2^3 top level
     if (d->levels < 1 || d->levels > maxl || d->levels > uint32_t(kMaxLevels))
         return fail(F184GI_ERR_INVALID, "grid levels must be in 1..log2(dim)");
-    if (d->format != F184GI_FMT_F32 && d->format != F184GI_FMT_F16) return fail(F184GI_ERR_INVALID, "unknown grid format");
+    if (d->format != F184GI_FMT_F32 && d->format != F184GI_FMT_F16 && d->format != F184GI_FMT_RG16)
+        return fail(F184GI_ERR_INVALID, "unknown grid format");
+    if (d->format == F184GI_FMT_RG16 && (d->levels != 1 || d->anisotropic || d->flags))
+        return fail(F184GI_ERR_INVALID, "an RG16 (reference) grid has one level, no anisotropy and no flags");
     if (d->shadow_res < 64 || d->shadow_res > 8192) return fail(F184GI_ERR_INVALID, "shadow_res must be in 64..8192");
     if (d->anisotropic > 1) return fail(F184GI_ERR_INVALID, "anisotropic must be 0 or 1");
     return F184GI_OK;
+}
+
+uint32_t format_bytes(uint32_t format) {
+    return format == F184GI_FMT_F32 ? 16u : (format == F184GI_FMT_F16 ? 8u : 4u);
 }
 
 ChainLayout layout_for(const f184gi_grid_desc& d, void* base) {
@@ -157,7 +165,7 @@ ChainLayout layout_for(const f184gi_grid_desc& d, void* base) {
     c.levels = d.levels;
     c.format = d.format;
     c.aniso = d.anisotropic;
-    c.esz = d.format == F184GI_FMT_F32 ? 16 : 8;
+    c.esz = format_bytes(d.format);
     uint64_t off = 0;
     for (uint32_t l = 0; l < d.levels; ++l) {
         uint64_t dl = d.dim >> l;
@@ -249,7 +257,7 @@ int f184gi_grid_bytes(const f184gi_grid_desc* d, uint64_t* bytes) {
     int rc = check_desc(d);
     if (rc) return rc;
     if (!bytes) return fail(F184GI_ERR_INVALID, "grid_bytes: null output");
-    uint64_t esz = d->format == F184GI_FMT_F32 ? 16 : 8;
+    uint64_t esz = format_bytes(d->format);
     uint64_t b = chain_elems(*d) * esz + uint64_t(d->shadow_res) * d->shadow_res * 8 + sizeof(f184gi_grid_frame);
     if (d->flags & F184GI_GRID_KEEP_COUNTS) b += uint64_t(d->dim) * d->dim * d->dim * 4;
     if (d->flags & F184GI_GRID_RESIDENT_WEIGHTS) b += uint64_t(d->dim) * d->dim * d->dim * 16;
@@ -263,7 +271,7 @@ int f184gi_grid_create(f184gi_ctx* c, const f184gi_grid_desc* d, uint32_t* grid)
     if (rc) return rc;
     GridObj g;
     g.desc = *d;
-    uint64_t esz = d->format == F184GI_FMT_F32 ? 16 : 8;
+    uint64_t esz = format_bytes(d->format);
     g.chain_bytes = chain_elems(*d) * esz;
     void* base = nullptr;
     if ((rc = dev_alloc(c, &base, g.chain_bytes))) return rc;
@@ -355,6 +363,16 @@ int f184gi_voxelize(f184gi_ctx* c, uint32_t grid, const float* tri, const uint32
     rj.keys = g->shadow;
     if ((rc = scratch_get(c, c->raster, raster_scratch_bytes(ntris, d.shadow_res, d.shadow_res)))) return rc;
     if ((rc = raster_launch(rj, c->raster.ptr, c->raster.bytes, c->d_status, s))) return rc;
+    g->light = *light;
+    if (d.format == F184GI_FMT_RG16) {  // the reference's volume: 565 albedo and normal of the last fragment
+        if (ndirty) return fail(F184GI_ERR_INVALID, "voxelize: an RG16 grid is always voxelized whole");
+        if ((rc = scratch_get(c, c->vox, refvox_scratch_bytes(ntris, d.dim)))) return rc;
+        if ((rc = refvox_launch(tri, albedo, ntris, g->d_frame, d.dim, static_cast<uint32_t*>(g->chain.base),
+                                c->vox.ptr, c->vox.bytes, c->d_status, s)))
+            return rc;
+        g->voxelized = true;
+        return F184GI_OK;
+    }
     VoxelizeJob vj{};
     vj.tri = tri;
     vj.albedo = albedo;
@@ -392,6 +410,7 @@ int f184gi_mip(f184gi_ctx* c, uint32_t grid, uint32_t levels, uint32_t anisotrop
     GridObj* g = find_grid(c, grid);
     if (!g) return fail(F184GI_ERR_NOTFOUND, "mip: unknown grid");
     if (anisotropic != g->desc.anisotropic) return fail(F184GI_ERR_INVALID, "mip: anisotropy differs from the grid's");
+    if (g->desc.format == F184GI_FMT_RG16) return fail(F184GI_ERR_INVALID, "mip: an RG16 grid has one level");
     if (levels == 0 || levels > g->desc.levels) levels = g->desc.levels;
     return mip_launch(g->chain, levels, c->d_status, static_cast<cudaStream_t>(stream));
 }
@@ -415,6 +434,7 @@ int f184gi_trace(f184gi_ctx* c, uint32_t grid, const f184gi_view* views, uint32_
     if (!c || (nviews && !views)) return fail(F184GI_ERR_INVALID, "trace: null argument");
     GridObj* g = find_grid(c, grid);
     if (!g) return fail(F184GI_ERR_NOTFOUND, "trace: unknown grid");
+    if (g->desc.format == F184GI_FMT_RG16) return fail(F184GI_ERR_INVALID, "trace: an RG16 grid is marched (f184gi_march)");
     TraceConsts tc{};
     if (params)
         tc.p = *params;
@@ -458,6 +478,68 @@ int f184gi_trace(f184gi_ctx* c, uint32_t grid, const f184gi_view* views, uint32_
     if (rc) return rc;
     return trace_launch(g->chain, tc, g->d_frame, tv.data(), nviews, c->trace.ptr, c->trace.bytes, c->trace_variant,
                         &c->trace_stage, static_cast<cudaStream_t>(stream));
+}
+
+void f184gi_march_params_default(f184gi_march_params* p) {
+    if (!p) return;
+    *p = f184gi_march_params{};
+    p->rays = 4;
+    p->second_bounce = 1;
+    p->max_steps = 60;
+    p->frame = 0;
+    p->step_size = 0.2f;
+    p->normal_offset = 0.06f;
+    p->shadow_bias = 0.005f;
+    p->sky[0] = 0.7f;
+    p->sky[1] = 0.8f;
+    p->sky[2] = 1.0f;
+    p->sky_scale = 0.4f;
+}
+
+int f184gi_march(f184gi_ctx* c, uint32_t grid, const f184gi_view* views, uint32_t nviews,
+                 const f184gi_march_params* params, void* stream) {
+    if (!c || (nviews && !views)) return fail(F184GI_ERR_INVALID, "march: null argument");
+    GridObj* g = find_grid(c, grid);
+    if (!g) return fail(F184GI_ERR_NOTFOUND, "march: unknown grid");
+    if (g->desc.format != F184GI_FMT_RG16) return fail(F184GI_ERR_INVALID, "march: the grid is not an RG16 grid");
+    if (!g->voxelized) return fail(F184GI_ERR_INVALID, "march: the grid has not been voxelized");
+    MarchJobDev J{};
+    if (params)
+        J.p = *params;
+    else
+        f184gi_march_params_default(&J.p);
+    if (J.p.rays < 1 || J.p.rays > 64 || J.p.max_steps > 4096 || !(J.p.step_size > 0.0f) ||
+        !std::isfinite(J.p.step_size) || !std::isfinite(J.p.normal_offset) || !std::isfinite(J.p.shadow_bias))
+        return fail(F184GI_ERR_INVALID, "march: parameters out of range");
+    J.vol = static_cast<const uint32_t*>(g->chain.base);
+    J.shadow = g->shadow;
+    J.frame_ptr = g->d_frame;
+    J.dim = g->desc.dim;
+    J.res = g->desc.shadow_res;
+    for (int a = 0; a < 3; ++a) J.lum[a] = g->light.luminance[a], J.light_dir[a] = g->light.direction[a];
+    // the 565 decode, pow(k / 31, 2.2) and pow(k / 63, 2.2) of the FP32 quotients (indirect.frag:89-95,157)
+    for (int k = 0; k < 32; ++k) J.pow5[k] = float(std::pow(double(float(k) / 31.0f), 2.2));
+    for (int k = 0; k < 64; ++k) J.pow6[k] = float(std::pow(double(float(k) / 63.0f), 2.2));
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    for (uint32_t i = 0; i < nviews; ++i) {
+        const f184gi_view& v = views[i];
+        if (!v.depth || !v.normal || !v.out || v.width == 0 || v.height == 0 || v.width > 16384 || v.height > 16384)
+            return fail(F184GI_ERR_INVALID, "march: view " + std::to_string(i) + " has null buffers or a bad size");
+        double V[16], P[16], IV[16], IP[16];
+        for (int k = 0; k < 16; ++k) V[k] = v.view[k], P[k] = v.proj[k];
+        if (!invert4(V, IV) || !invert4(P, IP)) return fail(F184GI_ERR_INVALID, "march: singular view or projection");
+        MarchViewDev mv{};
+        for (int k = 0; k < 16; ++k) mv.iview[k] = float(IV[k]), mv.iproj[k] = float(IP[k]);
+        for (int k = 0; k < 8; ++k) mv.iproj_zw[k] = IP[8 + k];
+        mv.width = v.width;
+        mv.height = v.height;
+        mv.depth = v.depth;
+        mv.normal = v.normal;
+        mv.out = v.out;
+        int rc = march_launch(J, mv, s);
+        if (rc) return rc;
+    }
+    return F184GI_OK;
 }
 
 int f184gi_gbuffer(f184gi_ctx* c, const float* tri, const float* rough, uint64_t ntris, const f184gi_view* view,
@@ -526,6 +608,12 @@ int f184gi_grid_read_level(f184gi_ctx* c, uint32_t grid, uint32_t level, uint32_
     if (level >= g->desc.levels) return fail(F184GI_ERR_INVALID, "grid_read_level: level out of range");
     if (dir > 0 && !(g->desc.anisotropic && level > 0 && dir < 6)) return fail(F184GI_ERR_INVALID, "grid_read_level: bad direction");
     uint64_t d = g->chain.ldim[level];
+    if (g->desc.format == F184GI_FMT_RG16) {  // packed uint32 per voxel, x fastest
+        cudaDeviceSynchronize();
+        cudaError_t e = cudaMemcpy(host, g->chain.base, size_t(d * d * d) * 4, cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) return cuda_fail(e, "grid_read_level");
+        return read_status(c);
+    }
     size_t bytes = size_t(d * d * d) * 16;
     int rc = scratch_get(c, c->misc, bytes);
     if (rc) return rc;

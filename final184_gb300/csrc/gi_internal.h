@@ -145,6 +145,30 @@ int trace_graph_tune(TraceGraph* g, const TraceView* views, uint32_t nviews, cud
                      float* ms);
 void trace_graph_destroy(TraceGraph* g);
 
+// Reference-faithful volume and march (march.cu)
+size_t refvox_scratch_bytes(uint64_t ntris, uint32_t dim);
+int refvox_launch(const float* tri, const uint32_t* albedo, uint64_t ntris, const f184gi_grid_frame* d_frame,
+                  uint32_t dim, uint32_t* vol, void* scratch, size_t scratch_bytes, uint32_t* d_status,
+                  cudaStream_t s);
+struct MarchJobDev {
+    f184gi_march_params p;
+    const uint32_t* vol;
+    const unsigned long long* shadow;
+    const f184gi_grid_frame* frame_ptr;
+    uint32_t dim, res;
+    float lum[3], light_dir[3];
+    float pow5[32], pow6[64];  // (k / 31)^2.2 and (k / 63)^2.2, the 565 albedo decode (indirect.frag:157)
+};
+struct MarchViewDev {
+    float iview[16], iproj[16];
+    double iproj_zw[8];
+    uint32_t width, height;
+    const float* depth;
+    const uint32_t* normal;
+    void* out;
+};
+int march_launch(const MarchJobDev& job, const MarchViewDev& view, cudaStream_t s);
+
 // grid of a context as the kernels see it (chain layout and device frame)
 int grid_internal(f184gi_ctx* c, uint32_t grid, ChainLayout* chain, const f184gi_grid_frame** d_frame);
 // the context's device ordinal and device status word

@@ -73,6 +73,8 @@ typedef struct f184gi_light {
 /* storage formats of the radiance/opacity grid (RGB = radiance premultiplied by opacity, A = opacity) */
 #define F184GI_FMT_F32 0u /* float4 per voxel, 16 B */
 #define F184GI_FMT_F16 1u /* half4  per voxel,  8 B */
+#define F184GI_FMT_RG16 2u /* the reference's voxel volume (one level): uint32 per voxel = RGB565 albedo in the low
+                            * 16 bits, the 5-6-5 packed normal in the high 16 (main.lua:269-272); for f184gi_march */
 
 /* grid flags */
 #define F184GI_GRID_KEEP_COUNTS 1u /* also keep the per-voxel contribution count (u32, L0) for inspection */
@@ -221,6 +223,31 @@ int f184gi_gbuffer(f184gi_ctx* ctx, const float* tri_xyz, const float* roughness
  * kernels flag are reported by f184gi_sync(ctx, stream) as for f184gi_gbuffer. */
 int f184gi_gbuffer_static(f184gi_ctx* ctx, const float* tri_xyz, const float* roughness, uint64_t ntris,
                           const f184gi_view* view, uint32_t* tri_id_out, void* stream);
+
+/* Parameters of the reference-faithful march (indirect.frag:104-222); f184gi_march_params_default fills the
+ * reference's constants noted below. */
+typedef struct f184gi_march_params {
+    uint32_t rays;          /* 4 rays per pixel (indirect.frag:202-218) */
+    uint32_t second_bounce; /* 1: a ray that hits marches once more from the hit (indirect.frag:197) */
+    uint32_t max_steps;     /* 60 steps per ray (indirect.frag:138) */
+    uint32_t frame;         /* seed of the per-pixel random numbers (the reference's frameCount) */
+    float step_size;        /* 0.2 world units (indirect.frag:116) */
+    float normal_offset;    /* 0.06: shadow lookup pushed along the voxel normal (indirect.frag:161) */
+    float shadow_bias;      /* 0.005 in shadow clip depth (indirect.frag:165) */
+    float sky[3];           /* 0.7, 0.8, 1.0 (indirect.frag:180) */
+    float sky_scale;        /* 0.4 */
+    float pad;
+} f184gi_march_params;
+void f184gi_march_params_default(f184gi_march_params* p);
+
+/* The reference-faithful indirect pass over an F184GI_FMT_RG16 grid that f184gi_voxelize filled (its shadow map
+ * and light included): per pixel 4 rays with a second bounce, fixed steps, first-hit sun light behind the
+ * shadow map, sky for rays that take every step.  Writes width*height RGBA FP32 to view->out:
+ * [indirect.rgb, view-space distance] (the reference's outColor before its temporal blend, which is not
+ * restated).  The reference's frame-dependent sin-hash noise is replaced by an integer hash of (pixel, frame,
+ * ray).  roughness and out_format of the views are not used. */
+int f184gi_march(f184gi_ctx* ctx, uint32_t grid, const f184gi_view* views, uint32_t nviews,
+                 const f184gi_march_params* params, void* stream);
 
 /* Wait for the stream, then report (and clear) errors that kernels flagged on the device since the last
  * check: F184GI_ERR_OVERFLOW (a bounded structure overflowed), F184GI_ERR_TIMEOUT (a bounded wait expired). */

@@ -43,6 +43,17 @@ def default_params():
     return ConeParams(5, 0.57735026918962576, 60.0, 0.5, 0.0, 1.0, 1.0, 0.05, 1, 0)
 
 
+class MarchParams(C.Structure):
+    _fields_ = [("rays", C.c_uint32), ("second_bounce", C.c_uint32), ("max_steps", C.c_uint32), ("frame", C.c_uint32),
+                ("step_size", C.c_float), ("normal_offset", C.c_float), ("shadow_bias", C.c_float),
+                ("sky", C.c_float * 3), ("sky_scale", C.c_float), ("pad", C.c_float)]
+
+
+def default_march_params():
+    """The reference's constants (indirect.frag:116,138,161,165,180; four rays with a second bounce)."""
+    return MarchParams(4, 1, 60, 0, 0.2, 0.06, 0.005, (C.c_float * 3)(0.7, 0.8, 1.0), 0.4, 0.0)
+
+
 def lib():
     global _lib
     if _lib is None:
@@ -65,6 +76,12 @@ def lib():
         _lib.orc_cone_f64.argtypes = [V, C.c_uint32, C.c_uint32, C.c_uint32, V, V, C.c_double,
                                       C.POINTER(ConeParams), V]
         _lib.orc_make_coord_space.argtypes = [V, V]
+        _lib.orc_refvox.argtypes = [C.POINTER(GridFrame), C.c_uint32, V, V, C.c_uint64, V]
+        for n in ("orc_march_f32", "orc_march_f64"):
+            getattr(_lib, n).argtypes = [C.POINTER(GridFrame), C.c_uint32, V, V, C.c_uint32, C.POINTER(Light), V, V,
+                                         C.c_uint32, C.c_uint32, V, V, C.POINTER(MarchParams), V, C.c_uint32,
+                                         C.c_uint32, C.c_int]
+        _lib.orc_sincos_turns.argtypes = [C.c_float, V, V]
         _lib.orc_pack_color565.argtypes = [V]
         _lib.orc_pack_color565.restype = C.c_uint32
         _lib.orc_pack_normal565.argtypes = [V]
@@ -256,3 +273,38 @@ def make_coord_space(n):
     out = np.zeros(9, dtype=np.float64)
     lib().orc_make_coord_space(_p(n), _p(out))
     return out.reshape(3, 3)  # rows: x, y, z axes
+
+
+def refvox(frame, dim, tri, albedo):
+    """The reference's voxel volume: (dim, dim, dim) uint32 = RGB565 albedo | 565 normal << 16, x fastest."""
+    tri = np.ascontiguousarray(tri, dtype=np.float32).ravel()
+    albedo = np.ascontiguousarray(albedo, dtype=np.uint32).ravel()
+    vol = np.empty(dim ** 3, dtype=np.uint32)
+    assert lib().orc_refvox(C.byref(frame), dim, _p(tri), _p(albedo), tri.size // 9, _p(vol)) == 0
+    return vol.reshape(dim, dim, dim)
+
+
+def march(frame, dim, vol, shadow, light, view, proj, width, height, depth, normal, params=None, rows=None,
+          f64=False, nthreads=0):
+    """The reference-faithful march: (height, width, 4) [indirect.rgb, view distance].  FP32 = the device's
+    operation sequence; FP64 = the same method in double."""
+    vol = np.ascontiguousarray(vol, dtype=np.uint32)
+    shadow = np.ascontiguousarray(shadow, dtype=np.float32)
+    res = shadow.shape[0]
+    view = np.ascontiguousarray(view, dtype=np.float32).ravel()
+    proj = np.ascontiguousarray(proj, dtype=np.float32).ravel()
+    depth = np.ascontiguousarray(depth, dtype=np.float32)
+    normal = np.ascontiguousarray(normal, dtype=np.uint32)
+    out = np.zeros(width * height * 4, dtype=np.float64 if f64 else np.float32)
+    r0, r1 = rows if rows is not None else (0, height)
+    p = params if params is not None else default_march_params()
+    fn = lib().orc_march_f64 if f64 else lib().orc_march_f32
+    assert fn(C.byref(frame), dim, _p(vol), _p(shadow), res, C.byref(light), _p(view), _p(proj), width, height,
+              _p(depth), _p(normal), C.byref(p), _p(out), r0, r1, nthreads) == 0
+    return out.reshape(height, width, 4)
+
+
+def sincos_turns(v):
+    s, c = np.zeros(1, np.float32), np.zeros(1, np.float32)
+    lib().orc_sincos_turns(float(v), _p(s), _p(c))
+    return float(s[0]), float(c[0])

@@ -1072,3 +1072,421 @@ uint16_t orc_float_to_half(double x) { return f2h(x); }
 double orc_half_to_float(uint16_t h) { return h2f(h); }
 
 }  // extern "C"
+
+// ---------------- reference-faithful volume and march ----------------
+//
+// The reference's own voxelization (Pipelang/Internal/main.lua:83-144 VoxelGS, :242-275 VoxelPS: dominant-axis
+// raster at pixel centres, 565 packing) and its single-ray march with a second bounce
+// (Shader/Lighting/indirect.frag:104-222 without the temporal blend).  The FP32 march below is the device's
+// operation sequence (each operation rounded on its own, integer hash for the reference's noise, a Taylor sin/cos
+// of the sample angle), so it agrees bit for bit; the FP64 march is the same method in double with std::sin/cos
+// and std::pow.
+
+namespace {
+
+struct RefMaps32 {
+    float s, b[3], w2l[12];
+};
+RefMaps32 ref_maps(const f184gi_grid_frame* fr) {
+    RefMaps32 m;
+    const double inv = fr->inv_voxel_fixed * (1.0 / 256.0);
+    m.s = float(inv);
+    for (int a = 0; a < 3; ++a) m.b[a] = float(-fr->origin[a] * inv);
+    for (int k = 0; k < 12; ++k) m.w2l[k] = float(fr->light_clip[k]);
+    return m;
+}
+
+template <class T>
+struct RefMaps {
+    T s, b[3], w2l[12];
+};
+template <class T>
+RefMaps<T> ref_maps_t(const f184gi_grid_frame* fr) {
+    RefMaps<T> m;
+    if (std::is_same<T, float>::value) {
+        RefMaps32 f = ref_maps(fr);
+        m.s = T(f.s);
+        for (int a = 0; a < 3; ++a) m.b[a] = T(f.b[a]);
+        for (int k = 0; k < 12; ++k) m.w2l[k] = T(f.w2l[k]);
+    } else {
+        const double inv = fr->inv_voxel_fixed * (1.0 / 256.0);
+        m.s = T(inv);
+        for (int a = 0; a < 3; ++a) m.b[a] = T(-fr->origin[a] * inv);
+        for (int k = 0; k < 12; ++k) m.w2l[k] = T(fr->light_clip[k]);
+    }
+    return m;
+}
+
+inline uint32_t lowbias32(uint32_t x) {  // C. Wellons' integer hash
+    x ^= x >> 16;
+    x *= 0x7feb352du;
+    x ^= x >> 15;
+    x *= 0x846ca68bu;
+    x ^= x >> 16;
+    return x;
+}
+
+// sin, cos of 2 pi v (v in [0, 1)) as the device evaluates them: quadrant, exact remainder in turns, Taylor series
+void sincos_turns32(float v, float& s, float& c) {
+    const int q = int(std::floor(v * 4.0f + 0.5f));
+    const float r = v - float(q) * 0.25f;
+    const float x = r * 6.28318530717958647692f;
+    const float x2 = x * x;
+    float ps = -1.0f / 5040.0f + x2 * (1.0f / 362880.0f);
+    ps = 1.0f / 120.0f + x2 * ps;
+    ps = -1.0f / 6.0f + x2 * ps;
+    ps = 1.0f + x2 * ps;
+    const float sn = x * ps;
+    float pc = 1.0f / 40320.0f + x2 * (-1.0f / 3628800.0f);
+    pc = -1.0f / 720.0f + x2 * pc;
+    pc = 1.0f / 24.0f + x2 * pc;
+    pc = -0.5f + x2 * pc;
+    const float cs = 1.0f + x2 * pc;
+    switch (q & 3) {
+        case 0: s = sn, c = cs; break;
+        case 1: s = cs, c = -sn; break;
+        case 2: s = -sn, c = -cs; break;
+        default: s = -cs, c = sn; break;
+    }
+}
+
+template <class T>
+Vec3<T> rnorm(Vec3<T> v) {  // v / length(v), zero stays zero
+    T l = std::sqrt(vdot(v, v));
+    return l > T(0) ? Vec3<T>{v.x / l, v.y / l, v.z / l} : v;
+}
+template <class T>
+Vec3<T> rcross(Vec3<T> a, Vec3<T> b) {
+    return Vec3<T>{a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+
+template <class T>
+struct RefHit {
+    Vec3<T> wpos, wnorm, brdf;
+    bool hit;
+};
+
+template <class T>
+struct MarchCtx {
+    RefMaps<T> m;
+    const uint32_t* vol;
+    uint32_t dim, res;
+    const float* shadow;  // FP32 depth, 1.0 where empty
+    T lum[3], ldir[3];
+    T pow5[32], pow6[64];
+    f184gi_march_params p;
+};
+
+template <class T>
+Vec3<T> ref_w2v(const RefMaps<T>& m, Vec3<T> p) {
+    return Vec3<T>{p.x * m.s + m.b[0], p.y * m.s + m.b[1], p.z * m.s + m.b[2]};
+}
+
+template <class T>
+Vec3<T> march_ray(const MarchCtx<T>& C, uint32_t pix, Vec3<T> wpos, Vec3<T> wnorm, uint32_t seed, RefHit<T>& hit) {
+    hit.hit = false;
+    Vec3<T> lo{T(0), T(0), T(0)};
+    const uint32_t key = lowbias32(C.p.frame * 16u + seed * 2u);
+    const float ru = float(lowbias32(pix ^ key) >> 8) * 5.9604644775390625e-8f;
+    const float rv = float(lowbias32(pix ^ (key + 0x9e3779b9u)) >> 8) * 5.9604644775390625e-8f;
+    const T ct = std::sqrt(T(1) - T(ru));
+    const T st = std::sqrt(T(1) - ct * ct);
+    T sp, cp;
+    if (std::is_same<T, float>::value) {
+        float s32, c32;
+        sincos_turns32(rv, s32, c32);
+        sp = T(s32), cp = T(c32);
+    } else {
+        const double ang = double(rv) * 6.283185307179586476925;
+        sp = T(std::sin(ang)), cp = T(std::cos(ang));
+    }
+    const Vec3<T> dl{cp * st, sp * st, ct};
+    // make_coord_space (indirect.frag:71-86)
+    Vec3<T> h = wnorm;
+    {
+        const T ax = std::fabs(h.x), ay = std::fabs(h.y), az = std::fabs(h.z);
+        if (ax <= ay && ax <= az) h.x = T(1);
+        else if (ay <= ax && ay <= az) h.y = T(1);
+        else h.z = T(1);
+    }
+    const Vec3<T> bz = rnorm(wnorm);
+    const Vec3<T> by = rnorm(rcross(h, bz));
+    const Vec3<T> bx = rnorm(rcross(bz, by));
+    Vec3<T> dir{(bx.x * dl.x + by.x * dl.y) + bz.x * dl.z, (bx.y * dl.x + by.y * dl.y) + bz.y * dl.z,
+                (bx.z * dl.x + by.z * dl.y) + bz.z * dl.z};
+    if (vdot(dir, wnorm) < T(0)) dir = Vec3<T>{-dir.x, -dir.y, -dir.z};
+    const T ndd = vdot(dir, wnorm);
+    const T step = T(C.p.step_size);
+    const T so = T(1) + T(rv);
+    Vec3<T> mp{wpos.x + ((dir.x * so) * step) / ndd, wpos.y + ((dir.y * so) * step) / ndd,
+               wpos.z + ((dir.z * so) * step) / ndd};
+    const Vec3<T> sv = ref_w2v(C.m, wpos);
+    int px = int(sv.x), py = int(sv.y), pz = int(sv.z);
+    const T maxd = T(C.dim - 1);
+    uint32_t i = 0;
+    for (; i < C.p.max_steps; ++i) {
+        mp = Vec3<T>{mp.x + dir.x * step, mp.y + dir.y * step, mp.z + dir.z * step};
+        const Vec3<T> vp = ref_w2v(C.m, mp);
+        if (vp.x < T(0) || vp.y < T(0) || vp.z < T(0) || vp.x > maxd || vp.y > maxd || vp.z > maxd) break;
+        const int ix = int(vp.x), iy = int(vp.y), iz = int(vp.z);
+        if (ix == px && iy == py && iz == pz) continue;
+        const uint32_t data = C.vol[(uint64_t(iz) * C.dim + uint64_t(iy)) * C.dim + uint64_t(ix)];
+        px = ix, py = iy, pz = iz;
+        const uint32_t r = data & 0xffffu, g = data >> 16;
+        if (r == 0) continue;
+        const Vec3<T> col{C.pow5[(r >> 11) & 31u], C.pow6[(r >> 5) & 63u], C.pow5[r & 31u]};
+        const Vec3<T> vn = rnorm(Vec3<T>{T(g & 0x1fu) / T(16) - T(1), T((g >> 5) & 0x3fu) / T(32) - T(1),
+                                         T((g >> 11) & 0x1fu) / T(16) - T(1)});
+        const T no = T(C.p.normal_offset);
+        const Vec3<T> q{mp.x + vn.x * no, mp.y + vn.y * no, mp.z + vn.z * no};
+        const T* L = C.m.w2l;
+        const T lx = ((L[0] * q.x + L[1] * q.y) + L[2] * q.z) + L[3];
+        const T ly = ((L[4] * q.x + L[5] * q.y) + L[6] * q.z) + L[7];
+        const T lz = ((L[8] * q.x + L[9] * q.y) + L[10] * q.z) + L[11];
+        const int tx = int((lx * T(0.5) + T(0.5)) * T(C.res));
+        const int ty = int((ly * T(0.5) + T(0.5)) * T(C.res));
+        T shade = T(1);
+        if (unsigned(tx) < C.res && unsigned(ty) < C.res) {
+            const T sd = T(C.shadow[uint64_t(ty) * C.res + uint64_t(tx)]);
+            shade = sd < lz + T(C.p.shadow_bias) ? T(0) : T(1);
+        }
+        const T lam = std::fabs(vdot(Vec3<T>{-C.ldir[0], -C.ldir[1], -C.ldir[2]}, vn));
+        const T den = std::max(T(0.01f), ndd);
+        const Vec3<T> br{(lam * col.x) / den, (lam * col.y) / den, (lam * col.z) / den};
+        hit.brdf = br;
+        lo = Vec3<T>{lo.x + (C.lum[0] * shade) * br.x, lo.y + (C.lum[1] * shade) * br.y,
+                     lo.z + (C.lum[2] * shade) * br.z};
+        hit.wpos = mp;
+        hit.wnorm = vn;
+        hit.hit = true;
+        break;
+    }
+    if (!hit.hit && i == C.p.max_steps) {
+        const T den = std::max(T(0.01f), ndd);
+        T t = ndd / T(0.01f);
+        t = std::min(std::max(t, T(0)), T(1));
+        const T ss = (t * t) * (T(3) - T(2) * t);
+        const T sc = T(C.p.sky_scale);
+        lo = Vec3<T>{lo.x + ((T(C.p.sky[0]) * sc) / den) * ss, lo.y + ((T(C.p.sky[1]) * sc) / den) * ss,
+                     lo.z + ((T(C.p.sky[2]) * sc) / den) * ss};
+    }
+    return lo;
+}
+
+template <class T>
+int march_impl(const f184gi_grid_frame* frame, uint32_t dim, const uint32_t* vol, const float* shadow, uint32_t res,
+               const f184gi_light* light, const float view[16], const float proj[16], uint32_t W, uint32_t H,
+               const float* depth, const uint32_t* normal, const f184gi_march_params* params, T* out,
+               uint32_t row_begin, uint32_t row_end, int nthreads) {
+    if (!frame || !vol || !shadow || !light || !view || !proj || !depth || !normal || !params || !out) return -1;
+    MarchCtx<T> C;
+    C.m = ref_maps_t<T>(frame);
+    C.vol = vol;
+    C.dim = dim;
+    C.res = res;
+    C.shadow = shadow;
+    C.p = *params;
+    for (int a = 0; a < 3; ++a) C.lum[a] = T(light->luminance[a]), C.ldir[a] = T(light->direction[a]);
+    for (int k = 0; k < 32; ++k)
+        C.pow5[k] = std::is_same<T, float>::value ? T(float(std::pow(double(float(k) / 31.0f), 2.2)))
+                                                  : T(std::pow(double(k) / 31.0, 2.2));
+    for (int k = 0; k < 64; ++k)
+        C.pow6[k] = std::is_same<T, float>::value ? T(float(std::pow(double(float(k) / 63.0f), 2.2)))
+                                                  : T(std::pow(double(k) / 63.0, 2.2));
+    double V[16], P[16], IV[16], IP[16];
+    for (int i = 0; i < 16; ++i) V[i] = view[i], P[i] = proj[i];
+    if (!inverse4(V, IV) || !inverse4(P, IP)) return -1;
+    float iv[16], ip[16];
+    for (int i = 0; i < 16; ++i) iv[i] = float(IV[i]), ip[i] = float(IP[i]);
+    const int64_t p_begin = int64_t(row_begin) * W, p_end = int64_t(std::min(row_end, H)) * W;
+    parallel_for(p_begin, p_end, nthreads, [&](int64_t pb, int64_t pe) {
+        for (int64_t pix = pb; pix < pe; ++pix) {
+            const uint32_t px = uint32_t(pix % W), py = uint32_t(pix / W);
+            T* o = out + uint64_t(pix) * 4;
+            const float d = depth[pix];
+            if (!(d < 1.0f)) {
+                o[0] = o[1] = o[2] = o[3] = T(0);
+                continue;
+            }
+            Vec3<T> cs, wpos, wn;
+            if (std::is_same<T, float>::value) {  // the device's sequence
+                const float nx = ((float(px) + 0.5f) / float(W)) * 2.0f - 1.0f;
+                const float ny = ((float(py) + 0.5f) / float(H)) * 2.0f - 1.0f;
+                const float vx = ((ip[0] * nx + ip[1] * ny) + ip[2] * d) + ip[3];
+                const float vy = ((ip[4] * nx + ip[5] * ny) + ip[6] * d) + ip[7];
+                const double vz = ((IP[8] * double(nx) + IP[9] * double(ny)) + IP[10] * double(d)) + IP[11];
+                const double vw = ((IP[12] * double(nx) + IP[13] * double(ny)) + IP[14] * double(d)) + IP[15];
+                const double rw = 1.0 / vw;
+                const float rwf = float(rw);
+                const Vec3<float> c{vx * rwf, vy * rwf, float(vz * rw)};
+                const Vec3<float> w{((iv[0] * c.x + iv[1] * c.y) + iv[2] * c.z) + iv[3],
+                                    ((iv[4] * c.x + iv[5] * c.y) + iv[6] * c.z) + iv[7],
+                                    ((iv[8] * c.x + iv[9] * c.y) + iv[10] * c.z) + iv[11]};
+                const uint32_t pn = normal[pix];
+                Vec3<float> on{float(h2f(uint16_t(pn & 0xffffu))), float(h2f(uint16_t(pn >> 16))), 0.0f};
+                on.z = (1.0f - std::fabs(on.x)) - std::fabs(on.y);
+                if (on.z < 0.0f) {
+                    const float ox = on.x, oy = on.y;
+                    on.x = (1.0f - std::fabs(oy)) * (ox >= 0.0f ? 1.0f : -1.0f);
+                    on.y = (1.0f - std::fabs(ox)) * (oy >= 0.0f ? 1.0f : -1.0f);
+                }
+                const Vec3<float> cn = rnorm(on);
+                const Vec3<float> n{(iv[0] * cn.x + iv[1] * cn.y) + iv[2] * cn.z, (iv[4] * cn.x + iv[5] * cn.y) + iv[6] * cn.z,
+                                    (iv[8] * cn.x + iv[9] * cn.y) + iv[10] * cn.z};
+                cs = Vec3<T>{T(c.x), T(c.y), T(c.z)};
+                wpos = Vec3<T>{T(w.x), T(w.y), T(w.z)};
+                wn = Vec3<T>{T(n.x), T(n.y), T(n.z)};
+            } else {
+                const double nx = (double(px) + 0.5) / double(W) * 2.0 - 1.0;
+                const double ny = (double(py) + 0.5) / double(H) * 2.0 - 1.0;
+                double vp[4];
+                for (int r = 0; r < 4; ++r) vp[r] = IP[r * 4] * nx + IP[r * 4 + 1] * ny + IP[r * 4 + 2] * double(d) + IP[r * 4 + 3];
+                const Vec3<double> c{vp[0] / vp[3], vp[1] / vp[3], vp[2] / vp[3]};
+                const Vec3<double> cn = oct_decode<double>(normal[pix]);
+                cs = Vec3<T>{T(c.x), T(c.y), T(c.z)};
+                wpos = Vec3<T>{T(IV[0] * c.x + IV[1] * c.y + IV[2] * c.z + IV[3]),
+                               T(IV[4] * c.x + IV[5] * c.y + IV[6] * c.z + IV[7]),
+                               T(IV[8] * c.x + IV[9] * c.y + IV[10] * c.z + IV[11])};
+                wn = Vec3<T>{T(IV[0] * cn.x + IV[1] * cn.y + IV[2] * cn.z), T(IV[4] * cn.x + IV[5] * cn.y + IV[6] * cn.z),
+                             T(IV[8] * cn.x + IV[9] * cn.y + IV[10] * cn.z)};
+            }
+            Vec3<T> acc{T(0), T(0), T(0)};
+            RefHit<T> h;
+            for (uint32_t k = 0; k < C.p.rays; ++k) {
+                const Vec3<T> l1 = march_ray(C, uint32_t(pix), wpos, wn, 2 * k, h);
+                acc = Vec3<T>{acc.x + l1.x, acc.y + l1.y, acc.z + l1.z};
+                if (h.hit && C.p.second_bounce) {
+                    const Vec3<T> br = h.brdf;
+                    RefHit<T> h2;
+                    const Vec3<T> l2 = march_ray(C, uint32_t(pix), h.wpos, h.wnorm, 2 * k + 1, h2);
+                    acc = Vec3<T>{acc.x + br.x * l2.x, acc.y + br.y * l2.y, acc.z + br.z * l2.z};
+                }
+            }
+            const T sc = T(1) / T(float(C.p.rays));
+            o[0] = acc.x * sc, o[1] = acc.y * sc, o[2] = acc.z * sc, o[3] = -cs.z;
+        }
+    });
+    return 0;
+}
+
+// The reference volume: dominant-axis raster at pixel centres (edge ties: dy > 0, or dy == 0 and dx < 0), the
+// VoxelPS swizzles, highest triangle index wins, 565 packing of albedo and face normal.
+int refvox_impl(const f184gi_grid_frame* fr, uint32_t dim, const float* tri, const uint32_t* albedo, uint64_t ntris,
+                uint32_t* vol) {
+    const RefMaps32 m = ref_maps(fr);
+    const uint64_t nvox = uint64_t(dim) * dim * dim;
+    std::vector<uint32_t> owner(nvox, 0);
+    const float fd = float(dim), inv_dim = 1.0f / fd, maxd = float(dim - 1);
+    for (uint64_t t = 0; t < ntris; ++t) {
+        float u[3][3];
+        for (int v = 0; v < 3; ++v)
+            for (int a = 0; a < 3; ++a) u[v][a] = tri[t * 9 + 3 * v + a] * m.s + m.b[a];
+        const float e1[3] = {u[1][0] - u[0][0], u[1][1] - u[0][1], u[1][2] - u[0][2]};
+        const float e2[3] = {u[2][0] - u[0][0], u[2][1] - u[0][1], u[2][2] - u[0][2]};
+        const float n[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2], e1[0] * e2[1] - e1[1] * e2[0]};
+        const float ax = std::fabs(n[0]), ay = std::fabs(n[1]), az = std::fabs(n[2]);
+        const int o = ax > ay ? (ax > az ? 1 : 0) : (ay > az ? 2 : 0);
+        float sx[3], sy[3], sz[3];
+        bool ok = true;
+        for (int v = 0; v < 3; ++v) {
+            if (o == 0) sx[v] = u[v][0], sy[v] = u[v][1], sz[v] = u[v][2] * inv_dim;
+            else if (o == 1) sx[v] = u[v][2], sy[v] = u[v][1], sz[v] = 1.0f - u[v][0] * inv_dim;
+            else sx[v] = u[v][0], sy[v] = fd - u[v][2], sz[v] = u[v][1] * inv_dim;
+            ok = ok && std::fabs(sx[v]) < 4096.0f && std::fabs(sy[v]) < 4096.0f;
+        }
+        if (!ok) continue;
+        int32_t X[3], Y[3];
+        for (int v = 0; v < 3; ++v) X[v] = int32_t(std::nearbyint(sx[v] * 256.0f)), Y[v] = int32_t(std::nearbyint(sy[v] * 256.0f));
+        int64_t det = int64_t(X[1] - X[0]) * (Y[2] - Y[0]) - int64_t(X[2] - X[0]) * (Y[1] - Y[0]);
+        if (det == 0) continue;
+        int i1 = 1, i2 = 2;
+        if (det < 0) i1 = 2, i2 = 1, det = -det;
+        const int id[3] = {0, i1, i2};
+        int32_t RX[3], RY[3];
+        for (int v = 0; v < 3; ++v) RX[v] = X[id[v]], RY[v] = Y[id[v]];
+        const double z0 = sz[0], z1 = sz[i1], z2 = sz[i2];
+        const double dx1 = RX[1] - RX[0], dy1 = RY[1] - RY[0], dx2 = RX[2] - RX[0], dy2 = RY[2] - RY[0];
+        const double dz1 = z1 - z0, dz2 = z2 - z0;
+        const float fz0 = float(z0);
+        const float fa_ = float((dz1 * dy2 - dz2 * dy1) / double(det));
+        const float fb_ = float((dz2 * dx1 - dz1 * dx2) / double(det));
+        const int32_t mnx = std::min(RX[0], std::min(RX[1], RX[2])), mxx = std::max(RX[0], std::max(RX[1], RX[2]));
+        const int32_t mny = std::min(RY[0], std::min(RY[1], RY[2])), mxy = std::max(RY[0], std::max(RY[1], RY[2]));
+        const int32_t x0 = std::max(0, (mnx - 128 + 255) >> 8), x1 = std::min(int32_t(dim) - 1, (mxx - 128) >> 8);
+        const int32_t y0 = std::max(0, (mny - 128 + 255) >> 8), y1 = std::min(int32_t(dim) - 1, (mxy - 128) >> 8);
+        int64_t ex[3], ey[3];
+        bool incl[3];
+        for (int e = 0; e < 3; ++e) {
+            const int nn = (e + 1) % 3;
+            ex[e] = int64_t(RX[nn]) - RX[e];
+            ey[e] = int64_t(RY[nn]) - RY[e];
+            incl[e] = ey[e] > 0 || (ey[e] == 0 && ex[e] < 0);
+        }
+        for (int32_t py = y0; py <= y1; ++py)
+            for (int32_t px = x0; px <= x1; ++px) {
+                const int64_t cx = int64_t(px) * 256 + 128, cy = int64_t(py) * 256 + 128;
+                bool in = true;
+                for (int e = 0; e < 3; ++e) {
+                    const int64_t w = ex[e] * (cy - RY[e]) - ey[e] * (cx - RX[e]);
+                    in = in && (w > 0 || (w == 0 && incl[e]));
+                }
+                if (!in) continue;
+                const float z = (fz0 + fa_ * float(cx - RX[0])) + fb_ * float(cy - RY[0]);
+                int vx, vy, vz;
+                if (o == 0) vx = px, vy = py, vz = int(z * maxd);
+                else if (o == 1) vx = int((1.0f - z) * maxd), vy = py, vz = px;
+                else vx = px, vy = int(z * maxd), vz = int(maxd - (float(py) + 0.5f));
+                if (unsigned(vx) >= dim || unsigned(vy) >= dim || unsigned(vz) >= dim) continue;
+                uint32_t& ow = owner[(uint64_t(vz) * dim + uint64_t(vy)) * dim + uint64_t(vx)];
+                ow = std::max(ow, uint32_t(t + 1));
+            }
+    }
+    for (uint64_t v = 0; v < nvox; ++v) {
+        const uint32_t o = owner[v];
+        if (!o) {
+            vol[v] = 0;
+            continue;
+        }
+        const uint64_t t = o - 1;
+        const uint32_t al = albedo[t];
+        const float cr = float(al & 255u) / 255.0f, cg = float((al >> 8) & 255u) / 255.0f,
+                    cb = float((al >> 16) & 255u) / 255.0f;
+        const uint32_t color = (uint32_t(cr * 31.0f) << 11) | (uint32_t(cg * 63.0f) << 5) | uint32_t(cb * 31.0f);
+        const float* p = tri + t * 9;
+        const Vec3<float> n = rnorm(rcross(Vec3<float>{p[3] - p[0], p[4] - p[1], p[5] - p[2]},
+                                           Vec3<float>{p[6] - p[0], p[7] - p[1], p[8] - p[2]}));
+        const uint32_t nx = uint32_t(std::max(0.0f, n.x * 16.0f + 15.0f));
+        const uint32_t ny = uint32_t(std::max(0.0f, n.y * 32.0f + 31.0f));
+        const uint32_t nz = uint32_t(std::max(0.0f, n.z * 16.0f + 15.0f));
+        const uint32_t nn = ((nx << 11) | (ny << 5) | nz) & 0xffffu;
+        vol[v] = (color & 0xffffu) | (nn << 16);
+    }
+    return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int orc_refvox(const f184gi_grid_frame* frame, uint32_t dim, const float* tri, const uint32_t* albedo,
+               uint64_t ntris, uint32_t* vol) {
+    if (!frame || !vol || (ntris && (!tri || !albedo))) return -1;
+    return refvox_impl(frame, dim, tri, albedo, ntris, vol);
+}
+int orc_march_f32(const f184gi_grid_frame* frame, uint32_t dim, const uint32_t* vol, const float* shadow,
+                  uint32_t res, const f184gi_light* light, const float view[16], const float proj[16], uint32_t W,
+                  uint32_t H, const float* depth, const uint32_t* normal, const f184gi_march_params* params,
+                  float* out, uint32_t row_begin, uint32_t row_end, int nthreads) {
+    return march_impl<float>(frame, dim, vol, shadow, res, light, view, proj, W, H, depth, normal, params, out,
+                             row_begin, row_end, nthreads);
+}
+int orc_march_f64(const f184gi_grid_frame* frame, uint32_t dim, const uint32_t* vol, const float* shadow,
+                  uint32_t res, const f184gi_light* light, const float view[16], const float proj[16], uint32_t W,
+                  uint32_t H, const float* depth, const uint32_t* normal, const f184gi_march_params* params,
+                  double* out, uint32_t row_begin, uint32_t row_end, int nthreads) {
+    return march_impl<double>(frame, dim, vol, shadow, res, light, view, proj, W, H, depth, normal, params, out,
+                              row_begin, row_end, nthreads);
+}
+void orc_sincos_turns(float v, float* s, float* c) { sincos_turns32(v, *s, *c); }
+
+}  // extern "C"
