@@ -207,6 +207,10 @@ class VoxelGI:
         check(self.lib.f184gi_march(self.ctx, grid.handle, arr, len(views),
                                     C.byref(params) if params is not None else None, _stream(stream)))
 
+    def blur(self, in_ptr, depth_ptr, width, height, out_ptr, stream=None):
+        """The reference's depth-aware blur of an RGBA FP32 image (device pointers)."""
+        check(self.lib.f184gi_blur(self.ctx, in_ptr, depth_ptr, width, height, out_ptr, _stream(stream)))
+
     def gbuffer(self, tri_ptr, rough_ptr, ntris, view, tri_id_ptr=None, stream=None):
         check(self.lib.f184gi_gbuffer(self.ctx, tri_ptr, rough_ptr, ntris, C.byref(view), tri_id_ptr,
                                       _stream(stream)))

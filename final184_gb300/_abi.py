@@ -133,6 +133,7 @@ PROTOTYPES = {
     "f184gi_gbuffer": (C.c_int, [P, P, P, U64, C.POINTER(View), P, P]),
     "f184gi_march_params_default": (None, [C.POINTER(MarchParams)]),
     "f184gi_march": (C.c_int, [P, U32, C.POINTER(View), U32, C.POINTER(MarchParams), P]),
+    "f184gi_blur": (C.c_int, [P, P, P, U32, U32, P, P]),
     "f184gi_gbuffer_static": (C.c_int, [P, P, P, U64, C.POINTER(View), P, P]),
     "f184gi_transform": (C.c_int, [P, P, U64, PF, P, P]),
     "f184gi_apply_moves": (C.c_int, [P, P, C.POINTER(Move), U32, U64, P]),

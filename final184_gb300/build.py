@@ -17,7 +17,7 @@ NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_SOURCES = ["util.cu", "raster.cu", "voxelize.cu", "mip.cu", "trace.cu", "trace_f32_iso.cu", "trace_f32_aniso.cu",
-              "trace_f16_iso.cu", "trace_f16_aniso.cu", "march.cu", "noalloc.cu"]
+              "trace_f16_iso.cu", "trace_f16_aniso.cu", "march.cu", "blur.cu", "noalloc.cu"]
 CPP_SOURCES = ["api.cpp", "scene.cpp", "serve.cpp"]
 
 

@@ -542,6 +542,16 @@ int f184gi_march(f184gi_ctx* c, uint32_t grid, const f184gi_view* views, uint32_
     return F184GI_OK;
 }
 
+int f184gi_blur(f184gi_ctx* c, const float* in, const float* depth, uint32_t width, uint32_t height, float* out,
+                void* stream) {
+    if (!c || !in || !depth || !out) return fail(F184GI_ERR_INVALID, "blur: null argument");
+    if (width == 0 || height == 0 || width > 16384 || height > 16384) return fail(F184GI_ERR_INVALID, "blur: bad size");
+    if (in == out) return fail(F184GI_ERR_INVALID, "blur: the output may not alias the input");
+    int rc = scratch_get(c, c->keys, size_t(width) * height * 16);
+    if (rc) return rc;
+    return blur_launch(in, depth, width, height, static_cast<float*>(c->keys.ptr), out, static_cast<cudaStream_t>(stream));
+}
+
 int f184gi_gbuffer(f184gi_ctx* c, const float* tri, const float* rough, uint64_t ntris, const f184gi_view* view,
                    uint32_t* tri_id_out, void* stream) {
     if (!c || !view || !tri || !rough) return fail(F184GI_ERR_INVALID, "gbuffer: null argument");

@@ -169,6 +169,9 @@ struct MarchViewDev {
 };
 int march_launch(const MarchJobDev& job, const MarchViewDev& view, cudaStream_t s);
 
+// cross-bilateral blur of an RGBA FP32 image (two passes through tmp)
+int blur_launch(const float* in, const float* depth, uint32_t W, uint32_t H, float* tmp, float* out, cudaStream_t s);
+
 // grid of a context as the kernels see it (chain layout and device frame)
 int grid_internal(f184gi_ctx* c, uint32_t grid, ChainLayout* chain, const f184gi_grid_frame** d_frame);
 // the context's device ordinal and device status word

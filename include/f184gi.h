@@ -249,6 +249,13 @@ void f184gi_march_params_default(f184gi_march_params* p);
 int f184gi_march(f184gi_ctx* ctx, uint32_t grid, const f184gi_view* views, uint32_t nviews,
                  const f184gi_march_params* params, void* stream);
 
+/* The reference's depth-aware blur of the indirect image (blurX then blurY over
+ * Shader/Lighting/bilateralBlur.inc:19-73, MegaPipeline.cpp:270-284): rgba_in and rgba_out are width*height
+ * RGBA FP32 device images (rgb blurred, out alpha 0), depth the G-buffer's FP32 depth.  rgba_out may not alias
+ * rgba_in; the intermediate pass uses the context's scratch. */
+int f184gi_blur(f184gi_ctx* ctx, const float* rgba_in, const float* depth, uint32_t width, uint32_t height,
+                float* rgba_out, void* stream);
+
 /* Wait for the stream, then report (and clear) errors that kernels flagged on the device since the last
  * check: F184GI_ERR_OVERFLOW (a bounded structure overflowed), F184GI_ERR_TIMEOUT (a bounded wait expired). */
 int f184gi_sync(f184gi_ctx* ctx, void* stream);

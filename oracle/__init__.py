@@ -82,6 +82,10 @@ def lib():
                                          C.c_uint32, C.c_uint32, V, V, C.POINTER(MarchParams), V, C.c_uint32,
                                          C.c_uint32, C.c_int]
         _lib.orc_sincos_turns.argtypes = [C.c_float, V, V]
+        for n in ("orc_blur_f32", "orc_blur_f64"):
+            getattr(_lib, n).argtypes = [V, V, C.c_uint32, C.c_uint32, V]
+        _lib.orc_exp2_poly.argtypes = [C.c_float]
+        _lib.orc_exp2_poly.restype = C.c_float
         _lib.orc_pack_color565.argtypes = [V]
         _lib.orc_pack_color565.restype = C.c_uint32
         _lib.orc_pack_normal565.argtypes = [V]
@@ -308,3 +312,19 @@ def sincos_turns(v):
     s, c = np.zeros(1, np.float32), np.zeros(1, np.float32)
     lib().orc_sincos_turns(float(v), _p(s), _p(c))
     return float(s[0]), float(c[0])
+
+
+def blur(img, depth, f64=False):
+    """The reference's two blur passes: img (H, W, 4), depth (H, W) -> (H, W, 4) with alpha 0."""
+    dt = np.float64 if f64 else np.float32
+    img = np.ascontiguousarray(img, dtype=dt)
+    depth = np.ascontiguousarray(depth, dtype=np.float32)
+    H, W = depth.shape
+    out = np.empty((H, W, 4), dtype=dt)
+    fn = lib().orc_blur_f64 if f64 else lib().orc_blur_f32
+    assert fn(_p(img), _p(depth), W, H, _p(out)) == 0
+    return out
+
+
+def exp2_poly(t):
+    return float(lib().orc_exp2_poly(float(t)))

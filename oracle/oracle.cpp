@@ -1490,3 +1490,84 @@ int orc_march_f64(const f184gi_grid_frame* frame, uint32_t dim, const uint32_t* 
 void orc_sincos_turns(float v, float* s, float* c) { sincos_turns32(v, *s, *c); }
 
 }  // extern "C"
+
+// ---------------- depth-aware blur (Shader/Lighting/bilateralBlur.inc:19-73) ----------------
+
+namespace {
+
+float exp2_poly32(float t) {  // the device's exp2: 2^round(t) times a degree-7 Taylor polynomial
+    if (!(t > -126.0f)) return 0.0f;
+    t = std::min(t, 127.0f);
+    const int n = int(std::nearbyint(t));
+    const float x = (t - float(n)) * 0.693147180559945309f;
+    float p = 1.0f / 720.0f + x * (1.0f / 5040.0f);
+    p = 1.0f / 120.0f + x * p;
+    p = 1.0f / 24.0f + x * p;
+    p = 1.0f / 6.0f + x * p;
+    p = 0.5f + x * p;
+    p = 1.0f + x * p;
+    p = 1.0f + x * p;
+    const uint32_t bits = uint32_t(n + 127) << 23;
+    float scale;
+    std::memcpy(&scale, &bits, 4);
+    return p * scale;
+}
+
+template <class T>
+T blur_weight(T r, T d, T d0) {
+    const T dz = (d0 - d) * T(512);
+    const T t = ((-r * r) * (T(1) / T(32))) - dz * dz;
+    if (std::is_same<T, float>::value) return T(exp2_poly32(float(t)));
+    return T(std::exp2(double(t)));
+}
+
+template <class T>
+void blur_pass_impl(const T* in, const float* depth, uint32_t W, uint32_t H, int axis, T* out) {
+    const int n = axis ? int(W) : int(H);
+    for (uint32_t y = 0; y < H; ++y)
+        for (uint32_t x = 0; x < W; ++x) {
+            const int c = axis ? int(x) : int(y);
+            auto at = [&](int k) -> uint64_t {
+                k = k < 0 ? 0 : (k >= n ? n - 1 : k);
+                return axis ? uint64_t(y) * W + uint64_t(k) : uint64_t(k) * W + x;
+            };
+            const uint64_t p0 = uint64_t(y) * W + x;
+            const T z0 = T(depth[p0]);
+            T tr = in[p0 * 4], tg = in[p0 * 4 + 1], tb = in[p0 * 4 + 2], tw = T(1);
+            auto tap = [&](int off, T r) {
+                const uint64_t q = at(c + off);
+                const T w = blur_weight<T>(r, T(depth[q]), z0);
+                tr = tr + in[q * 4] * w;
+                tg = tg + in[q * 4 + 1] * w;
+                tb = tb + in[q * 4 + 2] * w;
+                tw = tw + w;
+            };
+            for (int i = 1; i <= 4; ++i) {
+                tap(2 * i, T(i));
+                tap(-2 * i, T(i));
+            }
+            for (int i = 5; i <= 7; i += 2) {
+                tap(2 * i + 1, T(i));
+                tap(-2 * i - 1, T(i));
+            }
+            out[p0 * 4] = tr / tw, out[p0 * 4 + 1] = tg / tw, out[p0 * 4 + 2] = tb / tw, out[p0 * 4 + 3] = T(0);
+        }
+}
+
+}  // namespace
+
+extern "C" {
+int orc_blur_f32(const float* in, const float* depth, uint32_t W, uint32_t H, float* out) {
+    std::vector<float> tmp(size_t(W) * H * 4);
+    blur_pass_impl<float>(in, depth, W, H, 0, tmp.data());
+    blur_pass_impl<float>(tmp.data(), depth, W, H, 1, out);
+    return 0;
+}
+int orc_blur_f64(const double* in, const float* depth, uint32_t W, uint32_t H, double* out) {
+    std::vector<double> tmp(size_t(W) * H * 4);
+    blur_pass_impl<double>(in, depth, W, H, 0, tmp.data());
+    blur_pass_impl<double>(tmp.data(), depth, W, H, 1, out);
+    return 0;
+}
+float orc_exp2_poly(float t) { return exp2_poly32(t); }
+}  // extern "C"
