@@ -85,10 +85,12 @@ def default_cone_params():
 class SyntheticScene:
     """Seeded scene (room + boxes/UV-spheres) owned by the library; arrays are numpy copies."""
 
-    def __init__(self, seed, target_tris, nobjects):
+    def __init__(self, seed, target_tris, nobjects, _ptr=None):
         lib = load()
-        ptr = C.POINTER(_abi.Scene)()
-        check(lib.f184gi_scene_generate(seed, target_tris, nobjects, C.byref(ptr)))
+        ptr = _ptr
+        if ptr is None:
+            ptr = C.POINTER(_abi.Scene)()
+            check(lib.f184gi_scene_generate(seed, target_tris, nobjects, C.byref(ptr)))
         self._ptr = ptr
         s = ptr.contents
         self.seed = seed
@@ -108,6 +110,13 @@ class SyntheticScene:
         self.roughness = np.ctypeslib.as_array(s.roughness, shape=(n,)).copy()
         self.object_first = np.ctypeslib.as_array(s.object_first, shape=(self.nobjects,)).copy()
         self.object_count = np.ctypeslib.as_array(s.object_count, shape=(self.nobjects,)).copy()
+
+    @classmethod
+    def from_gltf(cls, path):
+        """A glTF 2.0 file (.gltf / .glb) flattened to world-space triangles (f184gi_gltf_load)."""
+        ptr = C.POINTER(_abi.Scene)()
+        check(load().f184gi_gltf_load(str(path).encode(), C.byref(ptr)))
+        return cls(0, 0, 0, _ptr=ptr)
 
     def camera(self, i, seed=None):
         eye = (C.c_float * 3)()

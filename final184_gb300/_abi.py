@@ -160,6 +160,8 @@ PROTOTYPES = {
     "f184gi_scene_free": (None, [C.POINTER(Scene)]),
     "f184gi_scene_move_objects": (C.c_int, [C.POINTER(Scene), U64, F32, F32, C.POINTER(U32), C.POINTER(U32)]),
     "f184gi_scene_camera": (C.c_int, [C.POINTER(Scene), U64, U32, PF, PF]),
+    "f184gi_gltf_load": (C.c_int, [C.c_char_p, C.POINTER(C.POINTER(Scene))]),
+    "f184gi_reference_sun_direction": (None, [PF]),
 }
 
 _lib = None

@@ -18,7 +18,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_SOURCES = ["util.cu", "raster.cu", "voxelize.cu", "mip.cu", "trace.cu", "trace_f32_iso.cu", "trace_f32_aniso.cu",
               "trace_f16_iso.cu", "trace_f16_aniso.cu", "march.cu", "blur.cu", "noalloc.cu"]
-CPP_SOURCES = ["api.cpp", "scene.cpp", "serve.cpp"]
+CPP_SOURCES = ["api.cpp", "scene.cpp", "serve.cpp", "gltf.cpp"]
 
 
 def _run(cmd):

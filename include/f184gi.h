@@ -372,6 +372,18 @@ typedef struct f184gi_scene {
     float eye[3], target[3];  /* seeded camera inside the room */
 } f184gi_scene;
 
+/* Load a glTF 2.0 scene (.gltf with buffers beside it or in data URIs, or .glb) as world-space triangles: the
+ * default scene's node tree (matrix or T*R*S composed with the parent), triangle primitives (lists, strips,
+ * fans; u8/u16/u32 or no indices), one object per (node, primitive), per-triangle albedo = baseColorFactor
+ * (RGBA8, default white) and roughness = roughnessFactor (default 1).  Replaces the reference's importer
+ * (Foreground/SceneGraph/glTFSceneImporter.cpp:200-440), which returns silently on a bad file; here
+ * F184GI_ERR_NOTFOUND / F184GI_ERR_INVALID with the reason.  Light = the reference's sun
+ * (f184gi_reference_sun_direction, App/MainBehaviour.cpp:40-44), camera outside the bounds looking at the centre.
+ * Free with f184gi_scene_free. */
+int f184gi_gltf_load(const char* path, f184gi_scene** out);
+/* Direction of travel of the reference's sun: -Z of a node rotated by the Euler angles (-75, -30, 50) degrees. */
+void f184gi_reference_sun_direction(float dir[3]);
+
 /* Room (6 quads bounding [-10,10]^3) + nobjects boxes/UV-spheres (half each) with ~target_tris triangles
  * in total, seeded by `seed` (splitmix64 -> xoshiro256**). */
 int f184gi_scene_generate(uint64_t seed, uint64_t target_tris, uint32_t nobjects, f184gi_scene** out);

@@ -125,6 +125,8 @@ def ref_lib():
         _ref.ref_matrix4_inverse.argtypes = [V, V]
         _ref.ref_bbox_transformed.argtypes = [V, V, V, V]
         _ref.ref_frustum_box.argtypes = [V, V, V]
+        _ref.ref_quat_euler_rotate.argtypes = [F, F, F, V, V]
+        _ref.ref_matrix_trs.argtypes = [V, V, V, V]
     return _ref
 
 

@@ -9,6 +9,7 @@
 #include "Frustum.h"
 #include "Matrix3x4.h"
 #include "Matrix4.h"
+#include "Quaternion.h"
 #include "Vector3.h"
 
 extern "C" {
@@ -64,6 +65,18 @@ int ref_frustum_box(const float proj[16], const float mn[3], const float mx[3]) 
     fr.Define(tc::Matrix4(proj));
     tc::BoundingBox b(tc::Vector3(mn[0], mn[1], mn[2]), tc::Vector3(mx[0], mx[1], mx[2]));
     return int(fr.IsInsideFast(b));
+}
+
+// q(ex, ey, ez) * v for the Euler-angle constructor (degrees) of tc::Quaternion
+void ref_quat_euler_rotate(float ex, float ey, float ez, const float v[3], float out[3]) {
+    tc::Vector3 r = tc::Quaternion(ex, ey, ez) * tc::Vector3(v[0], v[1], v[2]);
+    out[0] = r.x, out[1] = r.y, out[2] = r.z;
+}
+
+// tc::Matrix3x4(translation, rotation (w, x, y, z), scale), row-major 3x4
+void ref_matrix_trs(const float t[3], const float q[4], const float s[3], float out[12]) {
+    tc::Matrix3x4 m(tc::Vector3(t[0], t[1], t[2]), tc::Quaternion(q[0], q[1], q[2], q[3]), tc::Vector3(s[0], s[1], s[2]));
+    std::memcpy(out, m.Data(), 12 * sizeof(float));
 }
 
 }  // extern "C"

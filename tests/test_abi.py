@@ -107,8 +107,8 @@ def test_inverse_matches_reference(lib, orc):
         tgt = eye + rng.normal(size=3)
         m = (g.perspective(59.0, 1.7, 0.1, 100.0).astype(np.float64) @ g.look_at(eye, tgt)).astype(np.float32)
         want = np.zeros(16, np.float32)
-        ref.ref_matrix4_inverse(np.ascontiguousarray(m.ravel()).ctypes.data_as(C.c_void_p),
-                                want.ctypes.data_as(C.c_void_p))
+        mm = np.ascontiguousarray(m.ravel())  # held by name: its buffer must outlive the call
+        ref.ref_matrix4_inverse(mm.ctypes.data_as(C.c_void_p), want.ctypes.data_as(C.c_void_p))
         got = g.mat4_inverse(m).ravel()
         assert np.allclose(got, want, rtol=1e-4, atol=1e-5)
 
