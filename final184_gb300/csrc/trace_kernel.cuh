@@ -21,6 +21,24 @@ __device__ __forceinline__ float dot3(float3 a, float3 b) { return a.x * b.x + a
 __device__ __forceinline__ float3 cross3(float3 a, float3 b) {
     return f3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
 }
+// acc += w * v per component as two packed FP32 FMAs (fma.rn.f32x2): each component is rounded once, exactly
+// as fmaf(w, v.c, acc.c), with half the instructions.
+__device__ __forceinline__ unsigned long long pack2(float a, float b) {
+    unsigned long long r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ void unpack2(unsigned long long r, float& a, float& b) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(r));
+}
+__device__ __forceinline__ void fma4(float4& acc, float w, const float4& v) {
+    const unsigned long long ww = pack2(w, w);
+    unsigned long long lo, hi;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(lo) : "l"(ww), "l"(pack2(v.x, v.y)), "l"(pack2(acc.x, acc.y)));
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(hi) : "l"(ww), "l"(pack2(v.z, v.w)), "l"(pack2(acc.z, acc.w)));
+    unpack2(lo, acc.x, acc.y);
+    unpack2(hi, acc.z, acc.w);
+}
 __device__ __forceinline__ float3 norm3(float3 a) {
     float l = sqrtf(dot3(a, a));
     return l > 0.0f ? mul3(a, 1.0f / l) : a;
@@ -121,10 +139,7 @@ __device__ __forceinline__ void tri_sample(const void* base, int d, uint32_t l, 
 #pragma unroll
                     for (int k = 0; k < NV; ++k) {
                         const float4 v = load_vox(base, FMT, vol_off[k] + e);
-                        acc[k].x += w * v.x;
-                        acc[k].y += w * v.y;
-                        acc[k].z += w * v.z;
-                        acc[k].w += w * v.w;
+                        fma4(acc[k], w, v);
                     }
                 }
             }
@@ -163,10 +178,7 @@ __device__ __forceinline__ void tri_sample(const void* base, int d, uint32_t l, 
 #pragma unroll
                     for (int k = 0; k < NV; ++k) {
                         const float4 v = load_vox(base, FMT, vol_off[k] + idx);
-                        acc[k].x += w * v.x;
-                        acc[k].y += w * v.y;
-                        acc[k].z += w * v.z;
-                        acc[k].w += w * v.w;
+                        fma4(acc[k], w, v);
                     }
                 }
             }
@@ -191,12 +203,7 @@ __device__ __forceinline__ float4 level_sample(const GridRef& g, const uint32_t*
     tri_sample<FMT, 3>(g.base, d, l, vo, x, lut, sa);
     float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
-    for (int a = 0; a < 3; ++a) {
-        acc.x += w[a] * sa[a].x;
-        acc.y += w[a] * sa[a].y;
-        acc.z += w[a] * sa[a].z;
-        acc.w += w[a] * sa[a].w;
-    }
+    for (int a = 0; a < 3; ++a) fma4(acc, w[a], sa[a]);
     return acc;
 }
 
@@ -235,9 +242,10 @@ __device__ float4 cone(const GridRef& g, const uint32_t* lut, const TraceConsts&
         cb += tr * s.z;
         alpha += tr * s.w;
         if (alpha >= tc.p.alpha_stop) break;
-        const float step = tc.p.step_factor * diam;
-        const float ts = t + step, tb = ts - t;
-        tl += (t - (ts - tb)) + (step - tb);
+        // error-free sum t + step (explicit rounding: no contraction of the step's product into the sum)
+        const float step = __fmul_rn(tc.p.step_factor, diam);
+        const float ts = __fadd_rn(t, step), tb = __fsub_rn(ts, t);
+        tl = __fadd_rn(tl, __fadd_rn(__fsub_rn(t, __fsub_rn(ts, tb)), __fsub_rn(step, tb)));
         t = ts;
     }
     return make_float4(cr, cg, cb, alpha);
