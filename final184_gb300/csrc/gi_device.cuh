@@ -50,9 +50,11 @@ __host__ __device__ __forceinline__ uint32_t morton3(uint32_t x, uint32_t y, uin
     return part1by2(x) | (part1by2(y) << 1) | (part1by2(z) << 2);
 }
 
-// element index of voxel (x, y, z) inside one volume of a level with `d` voxels per axis
-__host__ __device__ __forceinline__ uint64_t vox_index(uint32_t d, uint32_t x, uint32_t y, uint32_t z) {
-    if (d >= 8) {
+// element index of voxel (x, y, z) inside one volume of level `level` with `d` voxels per axis: level 0 is stored
+// in 8^3 bricks in Morton order (the voxelizer's unit), coarser levels linearly (x fastest)
+__host__ __device__ __forceinline__ uint64_t vox_index(uint32_t level, uint32_t d, uint32_t x, uint32_t y,
+                                                      uint32_t z) {
+    if (level == 0 && d >= 8) {
         uint32_t m = morton3(x >> 3, y >> 3, z >> 3);
         return (uint64_t(m) << 9) | ((z & 7u) << 6) | ((y & 7u) << 3) | (x & 7u);
     }

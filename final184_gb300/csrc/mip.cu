@@ -57,8 +57,11 @@ __device__ __forceinline__ float4 reduce8(uint32_t dir, Fetch fetch) {
     return f4mul(acc, 0.25f);
 }
 
-// Source block of S^3 voxels of level `src` (S = 16: eight bricks; S <= 8: the whole level) reduced into
-// levels src+1 .. src+nout.  Block b of the source level is the Morton-ordered group of 8 bricks 8b .. 8b+7.
+// Source block of S^3 voxels of level `src` (S = 16, or the whole level when it is smaller) reduced into
+// levels src+1 .. src+nout, which are stored linearly.  Blocks are numbered in Morton order of their position.
+// Level 0 is stored in Morton-ordered 8^3 bricks, so block b is bricks 8b .. 8b+7, contiguous: one bulk copy
+// (cp.async.bulk) stages it.  A linear level of 16^3 or less is one contiguous block as well; a larger linear
+// level's block is gathered row by row.
 // Anisotropic chains: CTA x = block * 6 + direction (the six CTAs of one block run together, so a level-0
 // block read by all six comes from DRAM once); direction d of a level reduces direction d of the level below
 // (level 0 has one volume).
@@ -73,26 +76,40 @@ __global__ void __launch_bounds__(512) mip_pass(ChainLayout c, uint32_t src, uin
     const uint32_t S = ds >= 16 ? 16u : ds;
     const uint32_t nvox = S * S * S;
     const uint64_t src_vol = (ANISO && src > 0) ? c.off[src] + uint64_t(dir) * c.vol[src] : c.off[src];
-    const uint64_t src_off = src_vol + (ds >= 16 ? uint64_t(blk) * 4096u : 0u);
-    const uint32_t bytes = nvox * c.esz;
-    const unsigned char* gsrc = static_cast<const unsigned char*>(c.base) + src_off * c.esz;
-    if (threadIdx.x == 0) {
-        mbar_init(&bar, 1);
-        fence_barrier_init();
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        mbar_expect_tx(&bar, bytes);
-        bulk_g2s(smem, gsrc, bytes, &bar);
-    }
-    if (!mbar_wait_bounded(&bar, 0, kWaitPolls)) {
-        if (threadIdx.x == 0) set_status(status, kStatusTimeout);
-        mbar_wait_bounded(&bar, 0, kWaitPolls);  // let the copy land before the CTA exits
-        return;
-    }
-    // block coordinates of this source block at level src+1 (in units of S/2 voxels)
+    const bool bricked = src == 0;
+    // block coordinates of this source block (in blocks of S voxels; at level src+1 in units of S/2 voxels)
     uint32_t Bx = 0, By = 0, Bz = 0;
     if (ds >= 16) Bx = compact1by2(blk), By = compact1by2(blk >> 1), Bz = compact1by2(blk >> 2);
+    if (bricked || ds <= 16) {
+        const uint64_t src_off = src_vol + (bricked && ds >= 16 ? uint64_t(blk) * 4096u : 0u);
+        const uint32_t bytes = nvox * c.esz;
+        const unsigned char* gsrc = static_cast<const unsigned char*>(c.base) + src_off * c.esz;
+        if (threadIdx.x == 0) {
+            mbar_init(&bar, 1);
+            fence_barrier_init();
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            mbar_expect_tx(&bar, bytes);
+            bulk_g2s(smem, gsrc, bytes, &bar);
+        }
+        if (!mbar_wait_bounded(&bar, 0, kWaitPolls)) {
+            if (threadIdx.x == 0) set_status(status, kStatusTimeout);
+            mbar_wait_bounded(&bar, 0, kWaitPolls);  // let the copy land before the CTA exits
+            return;
+        }
+    } else {  // 16 rows of 16 x 16: element e of row (y, z) -> smem (z * 16 + y) * 16 + e
+        const unsigned char* gbase = static_cast<const unsigned char*>(c.base);
+        for (uint32_t i = threadIdx.x; i < 4096u; i += blockDim.x) {
+            const uint32_t e = i & 15u, y = (i >> 4) & 15u, z = i >> 8;
+            const uint64_t g = src_vol + (uint64_t(Bz * 16 + z) * ds + uint64_t(By * 16 + y)) * ds + (Bx * 16 + e);
+            if (c.esz == 16)
+                reinterpret_cast<float4*>(smem)[i] = reinterpret_cast<const float4*>(gbase)[g];
+            else
+                reinterpret_cast<uint2*>(smem)[i] = reinterpret_cast<const uint2*>(gbase)[g];
+        }
+        __syncthreads();
+    }
     uint32_t n = S / 2;  // output edge of the first produced level
     // level src+1 from the staged source
     const uint32_t t = threadIdx.x;
@@ -101,7 +118,7 @@ __global__ void __launch_bounds__(512) mip_pass(ChainLayout c, uint32_t src, uin
         const float4 acc = reduce8<ANISO>(dir, [&](int dx, int dy, int dz) {
             const uint32_t sx = 2 * x + dx, sy = 2 * y + dy, sz = 2 * z + dz;
             uint32_t si;
-            if (S >= 8) {
+            if (bricked && S >= 8) {
                 const uint32_t cb = ((sx >> 3) & 1u) | (((sy >> 3) & 1u) << 1) | (((sz >> 3) & 1u) << 2);
                 si = cb * 512u + ((sz & 7u) << 6) + ((sy & 7u) << 3) + (sx & 7u);
             } else {
@@ -112,7 +129,7 @@ __global__ void __launch_bounds__(512) mip_pass(ChainLayout c, uint32_t src, uin
         lvl[0][t] = acc;
         const uint32_t d1 = c.ldim[src + 1];
         const uint64_t dst = c.off[src + 1] + (ANISO ? uint64_t(dir) * c.vol[src + 1] : 0u);
-        store_vox(c.base, c.format, dst + vox_index(d1, Bx * n + x, By * n + y, Bz * n + z), acc);
+        store_vox(c.base, c.format, dst + vox_index(src + 1, d1, Bx * n + x, By * n + y, Bz * n + z), acc);
     }
     __syncthreads();
     int cur = 0;
@@ -127,7 +144,7 @@ __global__ void __launch_bounds__(512) mip_pass(ChainLayout c, uint32_t src, uin
             lvl[cur ^ 1][t] = acc;
             const uint32_t dk = c.ldim[src + k];
             const uint64_t dst = c.off[src + k] + (ANISO ? uint64_t(dir) * c.vol[src + k] : 0u);
-            store_vox(c.base, c.format, dst + vox_index(dk, Bx * n + x, By * n + y, Bz * n + z), acc);
+            store_vox(c.base, c.format, dst + vox_index(src + k, dk, Bx * n + x, By * n + y, Bz * n + z), acc);
         }
         __syncthreads();
         cur ^= 1;

@@ -91,8 +91,9 @@ constexpr int kLut = 65;
 
 // 8-tap trilinear sample of one volume of level l (d voxels per axis) at x (L0 voxel units); taps outside the
 // volume read zero.  Interior samples (all taps inside) address the seven other taps from the first one with
-// one delta per axis: +1 / +8 / +64 inside a brick, or the Morton step to the next brick when the tap crosses a
-// brick face.  Samples touching the border take the general path with a validity test per tap.
+// one delta per axis: +1 / +d / +d^2 in a linear level; at level 0 (bricks) +1 / +8 / +64 inside a brick, or the
+// Morton step to the next brick when the tap crosses a brick face.  Samples touching the border take the general
+// path with a validity test per tap.
 template <int FMT, int NV>
 __device__ __forceinline__ void tri_sample(const void* base, int d, uint32_t l, const uint32_t (&vol_off)[NV],
                                           float3 x, const uint32_t* lut, float4 (&acc)[NV]) {
@@ -114,7 +115,7 @@ __device__ __forceinline__ void tri_sample(const void* base, int d, uint32_t l, 
     const unsigned lim = unsigned(d - 1);
     if (unsigned(c0[0]) < lim && unsigned(c0[1]) < lim && unsigned(c0[2]) < lim) {
         uint32_t i0, dx, dy, dz;
-        if (d >= 8) {
+        if (l == 0 && d >= 8) {  // level 0: Morton-ordered bricks
             const uint32_t bx = uint32_t(c0[0]) >> 3, by = uint32_t(c0[1]) >> 3, bz = uint32_t(c0[2]) >> 3;
             const uint32_t hx = lut[bx], hy = lut[kLut + by], hz = lut[2 * kLut + bz];
             i0 = hx + hy + hz + ((uint32_t(c0[2] & 7) << 6) | (uint32_t(c0[1] & 7) << 3) | uint32_t(c0[0] & 7));
@@ -148,7 +149,7 @@ __device__ __forceinline__ void tri_sample(const void* base, int d, uint32_t l, 
     // border: per-axis validity, high (Morton) and low (in-brick / linear) address parts
     bool ok[3][2];
     uint32_t hi[3][2], lo[3][2];
-    const bool bricked = d >= 8;
+    const bool bricked = l == 0 && d >= 8;
 #pragma unroll
     for (int a = 0; a < 3; ++a)
 #pragma unroll

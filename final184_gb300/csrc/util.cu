@@ -169,7 +169,7 @@ int frame_launch(const float* tri, uint64_t ntris, const f184gi_bounds* bounds, 
     return cuda_fail(cudaGetLastError(), "frame");
 }
 
-// ---------------- level read-back (bricked -> linear FP32) ----------------
+// ---------------- level read-back (level layout -> linear FP32) ----------------
 namespace {
 __global__ void read_level_kernel(ChainLayout c, uint32_t level, uint32_t dir, float4* out) {
     uint32_t d = c.ldim[level];
@@ -177,7 +177,7 @@ __global__ void read_level_kernel(ChainLayout c, uint32_t level, uint32_t dir, f
     uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (i >= n) return;
     uint32_t x = uint32_t(i % d), y = uint32_t((i / d) % d), z = uint32_t(i / (uint64_t(d) * d));
-    uint64_t e = c.off[level] + uint64_t(dir) * c.vol[level] + vox_index(d, x, y, z);
+    uint64_t e = c.off[level] + uint64_t(dir) * c.vol[level] + vox_index(level, d, x, y, z);
     out[i] = load_vox(c.base, c.format, e);
 }
 }  // namespace
