@@ -171,7 +171,7 @@ ChainLayout layout_for(const f184gi_grid_desc& d, void* base) {
         uint64_t dl = d.dim >> l;
         c.ldim[l] = uint32_t(dl);
         c.off[l] = off;
-        c.vol[l] = dl * dl * dl;
+        c.vol[l] = l == 0 ? dl * dl * dl : (dl + 2) * (dl + 2) * (dl + 2);  // levels >= 1: a ring of zeros
         off += c.vol[l] * ((d.anisotropic && l > 0) ? 6 : 1);
     }
     return c;
@@ -275,6 +275,7 @@ int f184gi_grid_create(f184gi_ctx* c, const f184gi_grid_desc* d, uint32_t* grid)
     g.chain_bytes = chain_elems(*d) * esz;
     void* base = nullptr;
     if ((rc = dev_alloc(c, &base, g.chain_bytes))) return rc;
+    cudaMemset(base, 0, g.chain_bytes);  // the zero rings of levels >= 1 are never written again
     g.chain = layout_for(*d, base);
     g.shadow_bytes = size_t(d->shadow_res) * d->shadow_res * 8;
     void* sh = nullptr;

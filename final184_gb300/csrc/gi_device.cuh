@@ -51,10 +51,15 @@ __host__ __device__ __forceinline__ uint32_t morton3(uint32_t x, uint32_t y, uin
 }
 
 // element index of voxel (x, y, z) inside one volume of level `level` with `d` voxels per axis: level 0 is stored
-// in 8^3 bricks in Morton order (the voxelizer's unit), coarser levels linearly (x fastest)
+// in 8^3 bricks in Morton order (the voxelizer's unit); coarser levels linearly (x fastest) inside a one-voxel
+// ring of zeros, (d + 2)^3 elements, so that every trilinear footprint touching the level is addressable
 __host__ __device__ __forceinline__ uint64_t vox_index(uint32_t level, uint32_t d, uint32_t x, uint32_t y,
                                                       uint32_t z) {
-    if (level == 0 && d >= 8) {
+    if (level > 0) {
+        const uint64_t dp = d + 2;
+        return (uint64_t(z + 1) * dp + (y + 1)) * dp + (x + 1);
+    }
+    if (d >= 8) {
         uint32_t m = morton3(x >> 3, y >> 3, z >> 3);
         return (uint64_t(m) << 9) | ((z & 7u) << 6) | ((y & 7u) << 3) | (x & 7u);
     }

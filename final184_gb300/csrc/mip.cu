@@ -58,10 +58,9 @@ __device__ __forceinline__ float4 reduce8(uint32_t dir, Fetch fetch) {
 }
 
 // Source block of S^3 voxels of level `src` (S = 16, or the whole level when it is smaller) reduced into
-// levels src+1 .. src+nout, which are stored linearly.  Blocks are numbered in Morton order of their position.
-// Level 0 is stored in Morton-ordered 8^3 bricks, so block b is bricks 8b .. 8b+7, contiguous: one bulk copy
-// (cp.async.bulk) stages it.  A linear level of 16^3 or less is one contiguous block as well; a larger linear
-// level's block is gathered row by row.
+// levels src+1 .. src+nout, which are stored linearly inside their zero rings.  Blocks are numbered in Morton
+// order of their position.  Level 0 is stored in Morton-ordered 8^3 bricks, so block b is bricks 8b .. 8b+7,
+// contiguous: one bulk copy (cp.async.bulk) stages it; a block of a coarser level is gathered row by row.
 // Anisotropic chains: CTA x = block * 6 + direction (the six CTAs of one block run together, so a level-0
 // block read by all six comes from DRAM once); direction d of a level reduces direction d of the level below
 // (level 0 has one volume).
@@ -80,8 +79,8 @@ __global__ void __launch_bounds__(512) mip_pass(ChainLayout c, uint32_t src, uin
     // block coordinates of this source block (in blocks of S voxels; at level src+1 in units of S/2 voxels)
     uint32_t Bx = 0, By = 0, Bz = 0;
     if (ds >= 16) Bx = compact1by2(blk), By = compact1by2(blk >> 1), Bz = compact1by2(blk >> 2);
-    if (bricked || ds <= 16) {
-        const uint64_t src_off = src_vol + (bricked && ds >= 16 ? uint64_t(blk) * 4096u : 0u);
+    if (bricked) {
+        const uint64_t src_off = src_vol + (ds >= 16 ? uint64_t(blk) * 4096u : 0u);
         const uint32_t bytes = nvox * c.esz;
         const unsigned char* gsrc = static_cast<const unsigned char*>(c.base) + src_off * c.esz;
         if (threadIdx.x == 0) {
@@ -98,11 +97,11 @@ __global__ void __launch_bounds__(512) mip_pass(ChainLayout c, uint32_t src, uin
             mbar_wait_bounded(&bar, 0, kWaitPolls);  // let the copy land before the CTA exits
             return;
         }
-    } else {  // 16 rows of 16 x 16: element e of row (y, z) -> smem (z * 16 + y) * 16 + e
+    } else {  // S rows of S x S from the ringed linear level: element e of row (y, z) -> smem (z S + y) S + e
         const unsigned char* gbase = static_cast<const unsigned char*>(c.base);
-        for (uint32_t i = threadIdx.x; i < 4096u; i += blockDim.x) {
-            const uint32_t e = i & 15u, y = (i >> 4) & 15u, z = i >> 8;
-            const uint64_t g = src_vol + (uint64_t(Bz * 16 + z) * ds + uint64_t(By * 16 + y)) * ds + (Bx * 16 + e);
+        for (uint32_t i = threadIdx.x; i < nvox; i += blockDim.x) {
+            const uint32_t e = i % S, y = (i / S) % S, z = i / (S * S);
+            const uint64_t g = src_vol + vox_index(src, ds, Bx * S + e, By * S + y, Bz * S + z);
             if (c.esz == 16)
                 reinterpret_cast<float4*>(smem)[i] = reinterpret_cast<const float4*>(gbase)[g];
             else

@@ -90,10 +90,10 @@ struct GridRef {
 constexpr int kLut = 65;
 
 // 8-tap trilinear sample of one volume of level l (d voxels per axis) at x (L0 voxel units); taps outside the
-// volume read zero.  Interior samples (all taps inside) address the seven other taps from the first one with
-// one delta per axis: +1 / +d / +d^2 in a linear level; at level 0 (bricks) +1 / +8 / +64 inside a brick, or the
-// Morton step to the next brick when the tap crosses a brick face.  Samples touching the border take the general
-// path with a validity test per tap.
+// volume read zero.  Levels >= 1 are linear inside a ring of zeros: a footprint that touches the volume is read
+// whole with deltas +1 / +(d+2) / +(d+2)^2, any other is zero.  Level 0 is bricked: interior samples address the
+// seven other taps from the first one with +1 / +8 / +64 inside a brick, or the Morton step to the next brick
+// when the tap crosses a brick face; samples touching its border test each tap.
 template <int FMT, int NV>
 __device__ __forceinline__ void tri_sample(const void* base, int d, uint32_t l, const uint32_t (&vol_off)[NV],
                                           float3 x, const uint32_t* lut, float4 (&acc)[NV]) {
@@ -112,10 +112,33 @@ __device__ __forceinline__ void tri_sample(const void* base, int d, uint32_t l, 
     const float wx[2] = {1.0f - f[0], f[0]}, wy[2] = {1.0f - f[1], f[1]}, wz[2] = {1.0f - f[2], f[2]};
 #pragma unroll
     for (int k = 0; k < NV; ++k) acc[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (l > 0) {
+        // ringed linear level: footprints that touch the volume are read whole (the ring reads zero), the others
+        // are zero outright
+        if (unsigned(c0[0] + 1) > unsigned(d) || unsigned(c0[1] + 1) > unsigned(d) || unsigned(c0[2] + 1) > unsigned(d))
+            return;
+        const uint32_t dp = uint32_t(d) + 2u;
+        const uint32_t i0 = (uint32_t(c0[2] + 1) * dp + uint32_t(c0[1] + 1)) * dp + uint32_t(c0[0] + 1);
+#pragma unroll
+        for (int tz = 0; tz < 2; ++tz)
+#pragma unroll
+            for (int ty = 0; ty < 2; ++ty) {
+                const float wyz = wy[ty] * wz[tz];
+                const uint32_t row = i0 + (tz ? dp * dp : 0u) + (ty ? dp : 0u);
+#pragma unroll
+                for (int tx = 0; tx < 2; ++tx) {
+                    const float w = wx[tx] * wyz;
+                    const uint32_t e = row + (tx ? 1u : 0u);
+#pragma unroll
+                    for (int k = 0; k < NV; ++k) fma4(acc[k], w, load_vox(base, FMT, vol_off[k] + e));
+                }
+            }
+        return;
+    }
     const unsigned lim = unsigned(d - 1);
     if (unsigned(c0[0]) < lim && unsigned(c0[1]) < lim && unsigned(c0[2]) < lim) {
         uint32_t i0, dx, dy, dz;
-        if (l == 0 && d >= 8) {  // level 0: Morton-ordered bricks
+        if (d >= 8) {  // level 0: Morton-ordered bricks
             const uint32_t bx = uint32_t(c0[0]) >> 3, by = uint32_t(c0[1]) >> 3, bz = uint32_t(c0[2]) >> 3;
             const uint32_t hx = lut[bx], hy = lut[kLut + by], hz = lut[2 * kLut + bz];
             i0 = hx + hy + hz + ((uint32_t(c0[2] & 7) << 6) | (uint32_t(c0[1] & 7) << 3) | uint32_t(c0[0] & 7));
@@ -149,7 +172,7 @@ __device__ __forceinline__ void tri_sample(const void* base, int d, uint32_t l, 
     // border: per-axis validity, high (Morton) and low (in-brick / linear) address parts
     bool ok[3][2];
     uint32_t hi[3][2], lo[3][2];
-    const bool bricked = l == 0 && d >= 8;
+    const bool bricked = d >= 8;  // level 0 only
 #pragma unroll
     for (int a = 0; a < 3; ++a)
 #pragma unroll

@@ -339,7 +339,10 @@ int f184gi_grid_read_level(f184gi_ctx* ctx, uint32_t grid, uint32_t level, uint3
 int f184gi_grid_read_shadow(f184gi_ctx* ctx, uint32_t grid, float* host_depth);
 /* per-voxel contribution counts at L0 (needs F184GI_GRID_KEEP_COUNTS), linear x fastest */
 int f184gi_grid_read_counts(f184gi_ctx* ctx, uint32_t grid, uint32_t* host_counts);
-/* device pointer and byte size of one level (for callers that sample the chain themselves) */
+/* device pointer and byte size of one level (for callers that sample the chain themselves).  Layout: level 0 in
+ * 8^3 bricks (voxels x fastest) in Morton order of brick coordinates; levels >= 1 linear, x fastest, inside a
+ * one-voxel ring of zeros ((d + 2)^3 elements; voxel (x, y, z) at ((z + 1) (d + 2) + y + 1) (d + 2) + x + 1);
+ * anisotropic levels hold six such volumes (+x, -x, +y, -y, +z, -z) back to back. */
 int f184gi_grid_level_ptr(f184gi_ctx* ctx, uint32_t grid, uint32_t level, void** dev_ptr, uint64_t* bytes);
 
 /* Host computation of the grid frame that f184gi_voxelize derives from `bounds` (bit-identical to it). */
