@@ -353,8 +353,8 @@ def run_gpu(args, cfg):
                      "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_source": peak_kind,
                      "algorithmic_bytes": alg[top],
                      "traffic": (tr * 1.0 if isinstance(tr, (int, float)) else None),
-                     "note": "far below the HBM roof: the trace is instruction-issue bound (ncu: ~68% issue-active, "
-                             "L1 hit ~96%, DRAM ~0.3% of peak); algorithmic bytes = G-buffer 10 B + output 32 B per "
+                     "note": "far below the HBM roof: the trace is instruction-issue bound (ncu: ~64% issue-active, "
+                             "L1 hit ~96%, DRAM ~0.4% of peak); algorithmic bytes = G-buffer 10 B + output 32 B per "
                              "pixel + the whole chain once (upper bound of the touched part)"},
         "e2e": {"value": round(e2e_value, 4), "unit": "Mpix/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "ms_per_step": round(e2e_ms, 4)},
