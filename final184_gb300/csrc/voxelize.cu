@@ -361,12 +361,25 @@ __global__ void __launch_bounds__(kChunk, 4) vox_bricks(VoxScratch sc, const f18
     const uint32_t nb = dim >> 3;
     if (m >= nb * nb * nb) return;
     const int32_t bx = int32_t(compact1by2(m)), by = int32_t(compact1by2(m >> 1)), bz = int32_t(compact1by2(m >> 2));
+    const uint32_t beg = sc.brick_start[m];
+    const uint32_t end = uint32_t(min(uint64_t(beg) + sc.brick_count[m], sc.list_cap));
+    if (beg == end) {  // an empty brick: zeros, without the shared-memory sums
+        for (int li = threadIdx.x; li < 512; li += kChunk) {
+            if (weights)
+                weights[(uint64_t(m) << 9) + li] = make_float4(0.f, 0.f, 0.f, 0.f);
+            else
+                store_vox(chain.base, chain.format, chain.off[0] + (uint64_t(m) << 9) + li, make_float4(0.f, 0.f, 0.f, 0.f));
+            if (counts) {
+                const int lx = li & 7, ly = (li >> 3) & 7, lz = li >> 6;
+                counts[(uint64_t(bz * 8 + lz) * dim + uint64_t(by * 8 + ly)) * dim + uint64_t(bx * 8 + lx)] = 0;
+            }
+        }
+        return;
+    }
     for (int i = threadIdx.x; i < 512; i += kChunk) {
         s_sum[0][i] = s_sum[1][i] = s_sum[2][i] = 0;
         s_cnt[i] = 0;
     }
-    const uint32_t beg = sc.brick_start[m];
-    const uint32_t end = uint32_t(min(uint64_t(beg) + sc.brick_count[m], sc.list_cap));
     const int64_t base[3] = {int64_t(bx) * kBrickFix, int64_t(by) * kBrickFix, int64_t(bz) * kBrickFix};
     for (uint32_t c0 = beg; c0 < end; c0 += kChunk) {
         // phase 1: one thread prepares one item
