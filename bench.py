@@ -300,20 +300,50 @@ def run_gpu(args, cfg):
     value = replica_mpix(npix, ms_per_step, world)
 
     # ---- end to end through the API with host buffers ----
-    gbuf_d = [depth, normal, rgh]
+    # Two request lanes (each its own context, grid, device buffers and stream) take the steps in turn, so one
+    # request's copies overlap the other's kernels; every step still copies its inputs in from pinned host memory
+    # and its traced image out.
     h2d = tri_h.numel() * 4 + alb_h.numel() * 4 + sum(x.numel() * x.element_size() for x in gbuf_h)
     d2h = out.numel() * 4
+    lanes = [dict(gi=gi, grid=grid, tri=tri, alb=alb, gbuf=[depth, normal, rgh], out=out, out_h=out_h, view=view,
+                  stream=stream)]
+    gi2 = g.VoxelGI(local)
+    d2 = [torch.empty_like(depth), torch.empty_like(normal), torch.empty_like(rgh)]
+    out2 = torch.empty_like(out)
+    lanes.append(dict(gi=gi2, grid=gi2.create_grid(dim, levels, g.FMT_F32, 0, res), tri=torch.empty_like(tri),
+                      alb=torch.empty_like(alb), gbuf=d2, out=out2, out_h=torch.empty_like(out_h).pin_memory(),
+                      view=g.make_view(V, P, W, H, d2[0].data_ptr(), d2[1].data_ptr(), d2[2].data_ptr(),
+                                       out2.data_ptr()),
+                      stream=torch.cuda.Stream(dev)))
+
+    def e2e_step(L):
+        with torch.cuda.stream(L["stream"]):
+            L["tri"].copy_(tri_h, non_blocking=True)
+            L["alb"].copy_(alb_h, non_blocking=True)
+            for d_, h_ in zip(L["gbuf"], gbuf_h):
+                d_.copy_(h_, non_blocking=True)
+            s_ = L["stream"].cuda_stream
+            L["gi"].voxelize(L["grid"], L["tri"].data_ptr(), L["alb"].data_ptr(), sc.ntris, light, bounds=sc.bounds,
+                             stream=s_)
+            L["gi"].mip(L["grid"], stream=s_)
+            L["gi"].trace(L["grid"], [L["view"]], stream=s_)
+            L["out_h"].copy_(L["out"], non_blocking=True)
+
+    for k in range(2):  # warm the second lane
+        e2e_step(lanes[k])
+    torch.cuda.synchronize(dev)
     barrier()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     e0.record(stream)
-    for _ in range(args.steps):
-        tri.copy_(tri_h, non_blocking=True)
-        alb.copy_(alb_h, non_blocking=True)
-        for d_, h_ in zip(gbuf_d, gbuf_h):
-            d_.copy_(h_, non_blocking=True)
-        step()
-        out_h.copy_(out, non_blocking=True)
+    for L in lanes:
+        L["stream"].wait_event(e0)
+    for k in range(args.steps):
+        e2e_step(lanes[k % 2])
+    for L in lanes[1:]:
+        done = torch.cuda.Event()
+        done.record(L["stream"])
+        stream.wait_event(done)
     e1.record(stream)
     barrier()
     e2e_ms = slowest_rank_ms(e0.elapsed_time(e1) / args.steps, dev)
@@ -357,7 +387,9 @@ def run_gpu(args, cfg):
                              "L1 hit ~96%, DRAM ~0.4% of peak); algorithmic bytes = G-buffer 10 B + output 32 B per "
                              "pixel + the whole chain once (upper bound of the touched part)"},
         "e2e": {"value": round(e2e_value, 4), "unit": "Mpix/s", "h2d_bytes_per_step": int(h2d),
-                "d2h_bytes_per_step": int(d2h), "ms_per_step": round(e2e_ms, 4)},
+                "d2h_bytes_per_step": int(d2h), "ms_per_step": round(e2e_ms, 4),
+                "note": "through the API from pinned host buffers; two request lanes (context, grid, stream) take "
+                        "the steps in turn so one request's copies overlap the other's kernels"},
         "gpu_launches": int(launches),
         "clocks": clk,
         # the traced image is lit (a black image would trace trivially short cones)
@@ -366,6 +398,7 @@ def run_gpu(args, cfg):
     }
     if world > 1:
         torch.distributed.barrier()
+    gi2.close()
     gi.close()
     return line, sc
 
