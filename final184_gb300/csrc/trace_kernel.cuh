@@ -252,13 +252,33 @@ __device__ float4 cone(const GridRef& g, const uint32_t* lut, const TraceConsts&
         float fl = floorf(lvl);
         uint32_t l0 = uint32_t(fl);
         float f = lvl - fl;
-        float4 s = level_sample<FMT, ANISO>(g, lut, l0, x, dir);
-        if (f > 0.0f && l0 + 1 < g.levels) {
-            float4 s1 = level_sample<FMT, ANISO>(g, lut, l0 + 1, x, dir);
-            s.x = s.x + f * (s1.x - s.x);
-            s.y = s.y + f * (s1.y - s.y);
-            s.z = s.z + f * (s1.z - s.z);
-            s.w = s.w + f * (s1.w - s.w);
+        float4 s;
+        if (ANISO) {
+            // the two levels share one copy of the (three-volume) sampling code: the instruction cache
+            // outweighs the overlap of two inlined copies here, not in the single-volume kernel
+            const uint32_t nl = (f > 0.0f && l0 + 1 < g.levels) ? 2u : 1u;
+            s = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll 1
+            for (uint32_t k = 0; k < nl; ++k) {
+                const float4 v = level_sample<FMT, ANISO>(g, lut, l0 + k, x, dir);
+                if (k == 0) {
+                    s = v;
+                } else {
+                    s.x = s.x + f * (v.x - s.x);
+                    s.y = s.y + f * (v.y - s.y);
+                    s.z = s.z + f * (v.z - s.z);
+                    s.w = s.w + f * (v.w - s.w);
+                }
+            }
+        } else {
+            s = level_sample<FMT, ANISO>(g, lut, l0, x, dir);
+            if (f > 0.0f && l0 + 1 < g.levels) {
+                const float4 s1 = level_sample<FMT, ANISO>(g, lut, l0 + 1, x, dir);
+                s.x = s.x + f * (s1.x - s.x);
+                s.y = s.y + f * (s1.y - s.y);
+                s.z = s.z + f * (s1.z - s.z);
+                s.w = s.w + f * (s1.w - s.w);
+            }
         }
         float tr = 1.0f - alpha;
         cr += tr * s.x;
