@@ -66,6 +66,22 @@ int compute_frame(const f184gi_bounds& b, uint32_t dim, const float light_dir[3]
     return F184GI_OK;
 }
 
+// The diffuse cones' march recurrence, step by step as the kernel's cone loop advances it: diameter
+// max(1, 2 tan (t + tl)) with the low part's product rounded first, step = step_factor * diameter and the
+// error-free sum t + step (this file is compiled without floating-point contraction).
+void trace_consts_schedule(TraceConsts& tc) {
+    float t = tc.p.start_offset, tl = 0.0f;
+    const float d2 = 2.0f * tc.p.diffuse_tan_half;
+    for (uint32_t k = 0; k < kDiffuseSched; ++k) {
+        const float diam = std::max(1.0f, std::fma(d2, t, d2 * tl));
+        tc.sched[k] = SchedEntry{t, tl, diam, std::max(std::log2(diam), 0.0f)};
+        const float step = tc.p.step_factor * diam;
+        const float ts = t + step, tb = ts - t;
+        tl = tl + ((t - (ts - tb)) + (step - tb));
+        t = ts;
+    }
+}
+
 }  // namespace f184
 
 using namespace f184;
@@ -451,6 +467,7 @@ int f184gi_trace(f184gi_ctx* c, uint32_t grid, const f184gi_view* views, uint32_
     double tilt = double(tc.p.diffuse_tilt_deg) * M_PI / 180.0;
     tc.cos_tilt = float(std::cos(tilt));
     tc.sin_tilt = float(std::sin(tilt));
+    trace_consts_schedule(tc);
     std::vector<TraceView> tv(nviews);
     for (uint32_t i = 0; i < nviews; ++i) {
         const f184gi_view& v = views[i];

@@ -107,11 +107,22 @@ struct TraceView {
     float tmax;
     uint64_t off[kMaxLevels], vol[kMaxLevels];
 };
+// The march schedule of the diffuse cones.  All diffuse cones start at start_offset with one aperture, so their
+// k-th sample has the same distance t (a float pair t + tl), diameter and unclamped level log2(diameter) at every
+// pixel; the host computes the first kDiffuseSched samples once per launch (trace_consts_schedule) and the
+// kernel reads them instead of re-deriving them per cone and step.  Marches longer than the table continue with
+// the same recurrence on the device.
+constexpr uint32_t kDiffuseSched = 24;
+struct SchedEntry {
+    float t, tl, diam, lvl;  // lvl = max(log2(diam), 0), before the clamp to the grid's last level
+};
 struct TraceConsts {
     float tmax;
     float cos_tilt, sin_tilt;
     f184gi_cone_params p;
+    SchedEntry sched[kDiffuseSched];
 };
+void trace_consts_schedule(TraceConsts& tc);  // fills tc.sched from tc.p
 // Cone-trace kernel variants: the tile shape (tw x th pixels, one thread each) and the CTAs kept resident per SM
 // (the register budget).  Every variant computes each pixel with the same arithmetic, so results are identical;
 // the batched launch picks the fastest by timing them on the work it serves.
@@ -121,7 +132,7 @@ struct TraceVariant {
 constexpr uint32_t kTraceVariantCount = 5;
 constexpr TraceVariant kTraceVariants[kTraceVariantCount] = {
     {16, 8, 4}, {16, 8, 5}, {16, 8, 6}, {8, 16, 5}, {8, 16, 6}};
-constexpr uint32_t kTraceDefaultVariant = 4;  // 8x16 tiles, 6 CTAs per SM: fastest measured on 1080p views
+constexpr uint32_t kTraceDefaultVariant = 3;  // 8x16 tiles, 5 CTAs per SM: fastest one-shot launch on 1080p views
 const void* trace_kernel_fn(uint32_t fmt, bool aniso, uint32_t variant);
 uint32_t trace_view_tiles(uint32_t width, uint32_t height, uint32_t variant);
 void trace_view_set_grid(TraceView& v, const ChainLayout& c, const f184gi_grid_frame* d_frame, float tmax);

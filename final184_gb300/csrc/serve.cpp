@@ -428,6 +428,7 @@ int f184gi_server_create(const f184gi_server_config* cfg, f184gi_server** out) {
     S->tc.cos_tilt = float(std::cos(tilt));
     S->tc.sin_tilt = float(std::sin(tilt));
     S->tc.tmax = 0.0f;  // per view
+    trace_consts_schedule(S->tc);
     if (c.trace_variant) S->variant = int(c.trace_variant) - 1;
     S->slots.resize(c.slots);
     for (Slot& sl : S->slots) {

@@ -231,9 +231,10 @@ __device__ __forceinline__ float4 level_sample(const GridRef& g, const uint32_t*
     return acc;
 }
 
+// sched: the first ns samples of this cone's march (the diffuse schedule; ns = 0 for the specular cone)
 template <int FMT, bool ANISO>
 __device__ float4 cone(const GridRef& g, const uint32_t* lut, const TraceConsts& tc, float3 o, float3 dir,
-                       float tan_half) {
+                       float tan_half, const SchedEntry* sched, uint32_t ns) {
     float cr = 0.f, cg = 0.f, cb = 0.f, alpha = 0.f;
     // The march distance is the float pair t + tl, advanced with error-free sums: a cone of small aperture takes
     // a hundred steps much shorter than t, and plain FP32 sums would drift by ~n/2 ulp(t) (5e-3 voxel at the far
@@ -242,9 +243,17 @@ __device__ float4 cone(const GridRef& g, const uint32_t* lut, const TraceConsts&
     const float dimf = float(g.dim);
     const float maxl = float(g.levels - 1);
     const float d2 = 2.0f * tan_half;
-    while (t < g.tmax || (t == g.tmax && tl <= 0.0f)) {
-        float diam = fmaxf(1.0f, fmaf(d2, t, d2 * tl));
-        float lvl = fminf(fmaxf(log2f(diam), 0.0f), maxl);
+    for (uint32_t k = 0;; ++k) {
+        float diam, lraw;
+        if (k < ns) {
+            const SchedEntry e = sched[k];
+            t = e.t, tl = e.tl, diam = e.diam, lraw = e.lvl;
+        } else {
+            diam = fmaxf(1.0f, fmaf(d2, t, d2 * tl));
+            lraw = fmaxf(log2f(diam), 0.0f);
+        }
+        if (!(t < g.tmax || (t == g.tmax && tl <= 0.0f))) break;
+        float lvl = fminf(lraw, maxl);
         float3 x = f3(fmaf(dir.x, t, fmaf(dir.x, tl, o.x)), fmaf(dir.y, t, fmaf(dir.y, tl, o.y)),
                       fmaf(dir.z, t, fmaf(dir.z, tl, o.z)));
         float m = 2.0f * diam;
@@ -286,11 +295,13 @@ __device__ float4 cone(const GridRef& g, const uint32_t* lut, const TraceConsts&
         cb += tr * s.z;
         alpha += tr * s.w;
         if (alpha >= tc.p.alpha_stop) break;
-        // error-free sum t + step (explicit rounding: no contraction of the step's product into the sum)
-        const float step = __fmul_rn(tc.p.step_factor, diam);
-        const float ts = __fadd_rn(t, step), tb = __fsub_rn(ts, t);
-        tl = __fadd_rn(tl, __fadd_rn(__fsub_rn(t, __fsub_rn(ts, tb)), __fsub_rn(step, tb)));
-        t = ts;
+        if (k + 1 >= ns) {
+            // error-free sum t + step (explicit rounding: no contraction of the step's product into the sum)
+            const float step = __fmul_rn(tc.p.step_factor, diam);
+            const float ts = __fadd_rn(t, step), tb = __fsub_rn(ts, t);
+            tl = __fadd_rn(tl, __fadd_rn(__fsub_rn(t, __fsub_rn(ts, tb)), __fsub_rn(step, tb)));
+            t = ts;
+        }
     }
     return make_float4(cr, cg, cb, alpha);
 }
@@ -309,7 +320,7 @@ __device__ __forceinline__ void store_out(void* out, uint32_t fmt, uint64_t i, f
 
 template <int FMT, bool ANISO>
 __device__ void trace_pixel(const GridRef& g, const uint32_t* lut, const TraceConsts& tc, const TraceView& v,
-                            uint32_t px, uint32_t py) {
+                            uint32_t px, uint32_t py, const SchedEntry* sched) {
     const uint64_t npix = uint64_t(v.width) * v.height;
     const uint64_t pi = uint64_t(py) * v.width + px;
     float d = v.depth[pi];
@@ -345,7 +356,7 @@ __device__ void trace_pixel(const GridRef& g, const uint32_t* lut, const TraceCo
     coord_space(nw, bx, by, bz);
     float4 acc;
     if (tc.p.diffuse_cones >= 5) {
-        float4 c0 = cone<FMT, ANISO>(g, lut, tc, o, bz, tc.p.diffuse_tan_half);
+        float4 c0 = cone<FMT, ANISO>(g, lut, tc, o, bz, tc.p.diffuse_tan_half, sched, kDiffuseSched);
         acc = make_float4(0.25f * c0.x, 0.25f * c0.y, 0.25f * c0.z, 0.25f * c0.w);
 #pragma unroll 1
         for (int k = 0; k < 4; ++k) {
@@ -353,14 +364,14 @@ __device__ void trace_pixel(const GridRef& g, const uint32_t* lut, const TraceCo
             float3 side = (k & 1) ? by : bx;
             if (k & 2) side = f3(-side.x, -side.y, -side.z);
             float3 dir = norm3(add3(mul3(bz, tc.cos_tilt), mul3(side, tc.sin_tilt)));
-            float4 ck = cone<FMT, ANISO>(g, lut, tc, o, dir, tc.p.diffuse_tan_half);
+            float4 ck = cone<FMT, ANISO>(g, lut, tc, o, dir, tc.p.diffuse_tan_half, sched, kDiffuseSched);
             acc.x += 0.1875f * ck.x;
             acc.y += 0.1875f * ck.y;
             acc.z += 0.1875f * ck.z;
             acc.w += 0.1875f * ck.w;
         }
     } else {
-        acc = cone<FMT, ANISO>(g, lut, tc, o, bz, tc.p.diffuse_tan_half);
+        acc = cone<FMT, ANISO>(g, lut, tc, o, bz, tc.p.diffuse_tan_half, sched, kDiffuseSched);
     }
     store_out(v.out, v.out_format, pi, acc);
     float4 sp = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -369,7 +380,7 @@ __device__ void trace_pixel(const GridRef& g, const uint32_t* lut, const TraceCo
         float dn = dot3(vd, nw);
         float3 rd = norm3(sub3(vd, mul3(nw, 2.0f * dn)));
         float th = fmaxf(rough, tc.p.min_spec_tan_half);
-        sp = cone<FMT, ANISO>(g, lut, tc, o, rd, th);
+        sp = cone<FMT, ANISO>(g, lut, tc, o, rd, th, nullptr, 0u);
     }
     store_out(v.out, v.out_format, npix + pi, sp);
 }
@@ -385,7 +396,12 @@ __global__ void __launch_bounds__(TW * TH, MINB) trace_kernel(TraceConsts tc, co
     __shared__ GridRef g;
     __shared__ uint32_t s_lut[3 * kLut];
     __shared__ uint32_t s_tile, s_view;
+    __shared__ SchedEntry s_sched[kDiffuseSched];  // read by every lane at the same step: broadcast
     for (uint32_t i = threadIdx.x; i < 3 * kLut; i += TW * TH) s_lut[i] = part1by2(i % kLut) << (9 + i / kLut);
+    if (threadIdx.x == 0) {  // constant indices: the schedule is read straight from the parameter bank
+#pragma unroll
+        for (uint32_t i = 0; i < kDiffuseSched; ++i) s_sched[i] = tc.sched[i];
+    }
     const uint32_t ntiles = tile_base[nviews];
     uint32_t cur_view = 0xffffffffu;
     for (uint32_t it = 0;; ++it) {
@@ -424,7 +440,7 @@ __global__ void __launch_bounds__(TW * TH, MINB) trace_kernel(TraceConsts tc, co
         const uint32_t tiles_x = (v.width + TW - 1) / TW;
         const uint32_t px = (local % tiles_x) * TW + (threadIdx.x % TW);
         const uint32_t py = (local / tiles_x) * TH + (threadIdx.x / TW);
-        if (px < v.width && py < v.height) trace_pixel<FMT, ANISO>(g, s_lut, tc, v, px, py);
+        if (px < v.width && py < v.height) trace_pixel<FMT, ANISO>(g, s_lut, tc, v, px, py, s_sched);
         __syncthreads();  // s_tile / g are rewritten for the next tile
     }
 }
