@@ -215,6 +215,25 @@ def run_reference(args, cfg):
 
 # ---------------------------------------------------------------- GPU arm
 
+def l2_copy_gbs(dev, stream, mib=16, reps=100):
+    """Read + write GB/s of a device copy whose source and destination (2 x mib MiB) stay in L2."""
+    import torch
+
+    a = torch.empty(mib << 20, dtype=torch.uint8, device=dev)
+    b = torch.empty_like(a)
+    a.fill_(1)
+    for _ in range(10):
+        b.copy_(a)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        b.copy_(a)
+    e1.record(stream)
+    e1.synchronize()
+    return 2.0 * a.numel() * reps / (e0.elapsed_time(e1) * 1e-3) / 1e9
+
+
 def run_gpu(args, cfg):
     import numpy as np
     import torch
@@ -366,6 +385,11 @@ def run_gpu(args, cfg):
     }
     peak, peak_kind = peaks()
     achieved = alg[top] / (means[top] * 1e-3) / 1e9
+    # secondary figure: the voxel bytes the trace samples (8 taps x 16 B per level sample), counted by the
+    # instrumented kernel on the same view after the timed region, against an L2-resident copy measured here
+    n_steps, n_samples = gi.trace_count(grid, [view], stream=stream)
+    sampled = n_samples * 8 * esz
+    l2_gbs = l2_copy_gbs(dev, stream)
     kernel_names = {"voxelize": "vox_bricks", "mip": "mip_pass", "trace": "trace_kernel"}
     tr = traffic_record(kernel_names[top])
     line = {
@@ -385,7 +409,16 @@ def run_gpu(args, cfg):
                      "traffic": (tr * 1.0 if isinstance(tr, (int, float)) else None),
                      "note": "far below the HBM roof: the trace is instruction-issue bound (ncu: ~64% issue-active, "
                              "L1 hit ~96%, DRAM ~0.4% of peak); algorithmic bytes = G-buffer 10 B + output 32 B per "
-                             "pixel + the whole chain once (upper bound of the touched part)"},
+                             "pixel + the whole chain once (upper bound of the touched part)",
+                     "sampled": {"bytes": int(sampled), "achieved": round(sampled / (means[top] * 1e-3) / 1e9, 1),
+                                 "unit": "GB/s", "l2_copy_gbs": round(l2_gbs, 1),
+                                 "frac_of_l2_copy": round(sampled / (means[top] * 1e-3) / 1e9 / l2_gbs, 3),
+                                 "steps_per_pixel": round(n_steps / max(1, npix), 2),
+                                 "level_samples_per_pixel": round(n_samples / max(1, npix), 2),
+                                 "note": "secondary figure, not the roofline: voxel bytes sampled by the cones "
+                                         "(level samples x 8 taps x 16 B, counted by the instrumented kernel) per "
+                                         "trace launch time; most are L1 hits, so it may exceed the L2 figure, "
+                                         "a torch copy of 2 x 16 MiB held in L2"}},
         "e2e": {"value": round(e2e_value, 4), "unit": "Mpix/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "ms_per_step": round(e2e_ms, 4),
                 "note": "through the API from pinned host buffers; two request lanes (context, grid, stream) take "
@@ -543,7 +576,7 @@ BATCHED = dict(seed=3184, scenes=64, dims=(64, 128, 256), tris=(10000, 1000000),
 
 def run_precision(args, cfg=PRECISION):
     """Precision form: 512^3 FP16 chain with six-direction anisotropic mips (9 levels), 2M triangles, 3840x2160,
-    FP32 cone accumulation; optional error against the FP64 oracle on a row sample (--precision-check)."""
+    FP32 cone accumulation (its error against the FP64 oracle is a GPU test)."""
     import numpy as np
     import torch
 
@@ -592,45 +625,12 @@ def run_precision(args, cfg=PRECISION):
                                          cfg["shadow_res"], W, H),
            "value": round(npix / (step_ms * 1e-3) / 1e6, 2), "unit": "Mpix/s", "steps": steps,
            "ms_per_step": round(step_ms, 3), "stages_ms": {k: round(v, 3) for k, v in ms.items()},
-           "device_bytes": int(gi.memory_used()), "error_vs_fp64": None,
+           "device_bytes": int(gi.memory_used()),
+           "error_vs_fp64": "gated by tests/test_precision_form.py (every 64th row against the FP64 oracle)",
            "image": {"mean_diffuse_rgb": round(float(out.view(2, -1, 4)[0, :, :3].mean()), 6),
                      "mean_specular_rgb": round(float(out.view(2, -1, 4)[1, :, :3].mean()), 6)}}
-    if getattr(args, "precision_check", False):
-        res["error_vs_fp64"] = precision_error(g, sc, cfg, out.cpu().numpy().reshape(2, H, W, 4), depth, normal,
-                                               rgh, V, P)
     gi.close()
     return res
-
-
-def precision_error(g, sc, cfg, got, depth, normal, rgh, V, P, row_stride=64):
-    """Max / RMS relative error of the GPU output against the FP64 oracle (full voxelization and anisotropic mip
-    chain in FP64, cone trace of every row_stride-th row)."""
-    import numpy as np
-
-    import oracle as o
-
-    o.build.build_oracle()
-    W, H, dim, levels, res = cfg["width"], cfg["height"], cfg["dim"], cfg["levels"], cfg["shadow_res"]
-    b = sc.bounds
-    fo = o.grid_frame(o.make_bounds((b.min.x, b.min.y, b.min.z), (b.max.x, b.max.y, b.max.z)), dim,
-                      np.array(sc.light.direction, np.float32))
-    sd = o.shadow_depth(o.raster(o.frame_matrix(fo), res, res, sc.tri_xyz))
-    l0, _ = o.voxelize(fo, dim, res, sc.tri_xyz, sc.albedo,
-                       o.make_light(list(sc.light.luminance), list(sc.light.direction)), sd)
-    chain, _ = o.mip(l0, levels, aniso=True)
-    del l0
-    dep = depth.cpu().numpy().reshape(H, W)
-    nrm = normal.cpu().numpy().view(np.uint32).reshape(H, W)
-    rg = rgh.cpu().numpy().view(np.uint16).reshape(H, W)
-    emax, esq, n = 0.0, 0.0, 0
-    for r in range(0, H, row_stride):
-        ref = o.trace(fo, dim, levels, chain, V, P, W, H, dep, nrm, rg, rows=(r, r + 1), aniso=True)[:, r]
-        e = np.abs(got[:, r].astype(np.float64) - ref) / np.maximum(np.abs(ref), 1e-2)
-        emax = max(emax, float(e.max()))
-        esq += float((e ** 2).sum())
-        n += e.size
-    return {"max": emax, "rms": (esq / n) ** 0.5, "rows": len(range(0, H, row_stride)), "values": n,
-            "floor": 1e-2, "tolerance": 1e-3}
 
 
 def run_march(args, cfg=PLAIN_LARGE, dim=128):
@@ -772,8 +772,6 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-served", action="store_true", help="skip the served-vs-plain request stream")
     ap.add_argument("--no-precision", action="store_true", help="skip the 512^3 anisotropic FP16 precision form")
-    ap.add_argument("--precision-check", action="store_true",
-                    help="also measure the precision form's error against the FP64 oracle (CPU heavy)")
     ap.add_argument("--no-batched", action="store_true", help="skip the 64-scene batched form")
     ap.add_argument("--no-march", action="store_true", help="skip the reference-faithful march mode")
     args = ap.parse_args()

@@ -210,6 +210,14 @@ class VoxelGI:
         check(self.lib.f184gi_trace(self.ctx, grid.handle, arr, len(views),
                                     C.byref(params) if params is not None else None, _stream(stream)))
 
+    def trace_count(self, grid, views, params=None, stream=None):
+        """trace() through the instrumented kernel; returns (cone steps, level samples) over all pixels."""
+        arr = (View * len(views))(*views)
+        counts = (C.c_uint64 * 2)()
+        check(self.lib.f184gi_trace_count(self.ctx, grid.handle, arr, len(views),
+                                          C.byref(params) if params is not None else None, counts, _stream(stream)))
+        return int(counts[0]), int(counts[1])
+
     def march(self, grid, views, params=None, stream=None):
         """The reference-faithful indirect pass over an RG16 grid (out: width*height RGBA FP32 per view)."""
         arr = (View * len(views))(*views)

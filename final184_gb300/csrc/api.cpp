@@ -107,7 +107,7 @@ struct f184gi_ctx {
     uint64_t used = 0;
     std::map<uint32_t, GridObj> grids;
     uint32_t next_id = 1;
-    Scratch raster, vox, trace, misc, keys;
+    Scratch raster, vox, trace, misc, keys, counts;
     uint32_t* d_status = nullptr;
     TraceStaging* trace_stage = nullptr;
     uint32_t trace_variant = kTraceDefaultVariant;
@@ -256,7 +256,7 @@ int f184gi_destroy(f184gi_ctx* c) {
         dev_free(c, g.weights, g.weights_bytes);
         dev_free(c, g.d_frame, sizeof(f184gi_grid_frame));
     }
-    for (Scratch* s : {&c->raster, &c->vox, &c->trace, &c->misc, &c->keys}) dev_free(c, s->ptr, s->bytes);
+    for (Scratch* s : {&c->raster, &c->vox, &c->trace, &c->misc, &c->keys, &c->counts}) dev_free(c, s->ptr, s->bytes);
     trace_staging_destroy(c->trace_stage);
     dev_free(c, c->d_status, 256);
     delete c;
@@ -446,8 +446,10 @@ void f184gi_cone_params_default(f184gi_cone_params* p) {
     p->pad = 0;
 }
 
-int f184gi_trace(f184gi_ctx* c, uint32_t grid, const f184gi_view* views, uint32_t nviews,
-                 const f184gi_cone_params* params, void* stream) {
+namespace {
+// f184gi_trace; with d_counts set, through the instrumented kernel that adds its totals there
+int trace_views(f184gi_ctx* c, uint32_t grid, const f184gi_view* views, uint32_t nviews,
+                const f184gi_cone_params* params, void* stream, unsigned long long* d_counts) {
     if (!c || (nviews && !views)) return fail(F184GI_ERR_INVALID, "trace: null argument");
     GridObj* g = find_grid(c, grid);
     if (!g) return fail(F184GI_ERR_NOTFOUND, "trace: unknown grid");
@@ -494,8 +496,34 @@ int f184gi_trace(f184gi_ctx* c, uint32_t grid, const f184gi_view* views, uint32_
     }
     int rc = scratch_get(c, c->trace, trace_scratch_bytes(nviews));
     if (rc) return rc;
+    tc.counts = d_counts;
     return trace_launch(g->chain, tc, g->d_frame, tv.data(), nviews, c->trace.ptr, c->trace.bytes, c->trace_variant,
-                        &c->trace_stage, static_cast<cudaStream_t>(stream));
+                        &c->trace_stage, static_cast<cudaStream_t>(stream), d_counts != nullptr);
+}
+}  // namespace
+
+int f184gi_trace(f184gi_ctx* c, uint32_t grid, const f184gi_view* views, uint32_t nviews,
+                 const f184gi_cone_params* params, void* stream) {
+    return trace_views(c, grid, views, nviews, params, stream, nullptr);
+}
+
+int f184gi_trace_count(f184gi_ctx* c, uint32_t grid, const f184gi_view* views, uint32_t nviews,
+                       const f184gi_cone_params* params, uint64_t counts[2], void* stream) {
+    if (!c || !counts) return fail(F184GI_ERR_INVALID, "trace_count: null argument");
+    int rc = scratch_get(c, c->counts, 2 * sizeof(unsigned long long));
+    if (rc) return rc;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    unsigned long long* d = static_cast<unsigned long long*>(c->counts.ptr);
+    cudaError_t e = cudaMemsetAsync(d, 0, 2 * sizeof(unsigned long long), s);
+    if (e != cudaSuccess) return cuda_fail(e, "trace_count: reset");
+    if ((rc = trace_views(c, grid, views, nviews, params, stream, d))) return rc;
+    unsigned long long h[2] = {0, 0};
+    if ((e = cudaMemcpyAsync(h, d, sizeof(h), cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(s)) != cudaSuccess)
+        return cuda_fail(e, "trace_count: totals");
+    counts[0] = h[0];
+    counts[1] = h[1];
+    return F184GI_OK;
 }
 
 void f184gi_march_params_default(f184gi_march_params* p) {

@@ -121,6 +121,7 @@ struct TraceConsts {
     float cos_tilt, sin_tilt;
     f184gi_cone_params p;
     SchedEntry sched[kDiffuseSched];
+    unsigned long long* counts;  // the counting kernel's totals: cone steps, level samples (null otherwise)
 };
 void trace_consts_schedule(TraceConsts& tc);  // fills tc.sched from tc.p
 // Cone-trace kernel variants: the tile shape (tw x th pixels, one thread each) and the CTAs kept resident per SM
@@ -134,6 +135,7 @@ constexpr TraceVariant kTraceVariants[kTraceVariantCount] = {
     {16, 8, 4}, {16, 8, 5}, {16, 8, 6}, {8, 16, 5}, {8, 16, 6}};
 constexpr uint32_t kTraceDefaultVariant = 3;  // 8x16 tiles, 5 CTAs per SM: fastest one-shot launch on 1080p views
 const void* trace_kernel_fn(uint32_t fmt, bool aniso, uint32_t variant);
+const void* trace_kernel_count_fn(uint32_t fmt, bool aniso);  // instrumented, default variant's tile shape
 uint32_t trace_view_tiles(uint32_t width, uint32_t height, uint32_t variant);
 void trace_view_set_grid(TraceView& v, const ChainLayout& c, const f184gi_grid_frame* d_frame, float tmax);
 
@@ -141,9 +143,10 @@ void trace_view_set_grid(TraceView& v, const ChainLayout& c, const f184gi_grid_f
 struct TraceStaging;
 void trace_staging_destroy(TraceStaging* st);
 size_t trace_scratch_bytes(uint32_t nviews);
+// count: launch the instrumented kernel (tc.counts set) with the default variant's shape
 int trace_launch(const ChainLayout& chain, const TraceConsts& tc, const f184gi_grid_frame* d_frame,
                  const TraceView* views, uint32_t nviews, void* scratch, size_t scratch_bytes, uint32_t variant,
-                 TraceStaging** staging, cudaStream_t s);
+                 TraceStaging** staging, cudaStream_t s, bool count = false);
 
 // Batched persistent trace replayed from CUDA graphs: [view table H2D] -> [work counter = 0] -> [kernel].
 struct TraceGraph;

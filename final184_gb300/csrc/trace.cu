@@ -12,11 +12,20 @@ const void* trace_kernel_f32_iso(uint32_t variant);
 const void* trace_kernel_f32_aniso(uint32_t variant);
 const void* trace_kernel_f16_iso(uint32_t variant);
 const void* trace_kernel_f16_aniso(uint32_t variant);
+const void* trace_kernel_count_f32_iso();
+const void* trace_kernel_count_f32_aniso();
+const void* trace_kernel_count_f16_iso();
+const void* trace_kernel_count_f16_aniso();
 
 const void* trace_kernel_fn(uint32_t fmt, bool aniso, uint32_t variant) {
     if (variant >= kTraceVariantCount) return nullptr;
     if (fmt == F184GI_FMT_F32) return aniso ? trace_kernel_f32_aniso(variant) : trace_kernel_f32_iso(variant);
     return aniso ? trace_kernel_f16_aniso(variant) : trace_kernel_f16_iso(variant);
+}
+
+const void* trace_kernel_count_fn(uint32_t fmt, bool aniso) {
+    if (fmt == F184GI_FMT_F32) return aniso ? trace_kernel_count_f32_aniso() : trace_kernel_count_f32_iso();
+    return aniso ? trace_kernel_count_f16_aniso() : trace_kernel_count_f16_iso();
 }
 
 uint32_t trace_view_tiles(uint32_t width, uint32_t height, uint32_t variant) {
@@ -89,10 +98,11 @@ size_t trace_scratch_bytes(uint32_t nviews) { return table_bytes(nviews) + 256; 
 
 int trace_launch(const ChainLayout& c, const TraceConsts& tc, const f184gi_grid_frame* d_frame, const TraceView* views,
                  uint32_t nviews, void* scratch, size_t scratch_bytes, uint32_t variant, TraceStaging** staging,
-                 cudaStream_t s) {
+                 cudaStream_t s, bool count) {
     if (nviews == 0) return F184GI_OK;
     if (scratch_bytes < trace_scratch_bytes(nviews)) return fail(F184GI_ERR_INVALID, "trace: scratch too small");
-    const void* fn = trace_kernel_fn(c.format, c.aniso != 0, variant);
+    if (count) variant = kTraceDefaultVariant;
+    const void* fn = count ? trace_kernel_count_fn(c.format, c.aniso != 0) : trace_kernel_fn(c.format, c.aniso != 0, variant);
     if (!fn) return fail(F184GI_ERR_INVALID, "trace: unknown kernel variant");
     const size_t need = table_bytes(nviews);
     TraceStaging* st = *staging;

@@ -4,4 +4,5 @@
 
 namespace f184 {
 const void* trace_kernel_f16_aniso(uint32_t variant) { return kernel_for<F184GI_FMT_F16, true>(variant); }
+const void* trace_kernel_count_f16_aniso() { return count_kernel<F184GI_FMT_F16, true>(); }
 }  // namespace f184

@@ -4,4 +4,5 @@
 
 namespace f184 {
 const void* trace_kernel_f32_iso(uint32_t variant) { return kernel_for<F184GI_FMT_F32, false>(variant); }
+const void* trace_kernel_count_f32_iso() { return count_kernel<F184GI_FMT_F32, false>(); }
 }  // namespace f184

@@ -231,10 +231,11 @@ __device__ __forceinline__ float4 level_sample(const GridRef& g, const uint32_t*
     return acc;
 }
 
-// sched: the first ns samples of this cone's march (the diffuse schedule; ns = 0 for the specular cone)
-template <int FMT, bool ANISO>
+// sched: the first ns samples of this cone's march (the diffuse schedule; ns = 0 for the specular cone).
+// COUNT (the instrumented kernel): cnt[0] += steps, cnt[1] += level samples.
+template <int FMT, bool ANISO, bool COUNT>
 __device__ float4 cone(const GridRef& g, const uint32_t* lut, const TraceConsts& tc, float3 o, float3 dir,
-                       float tan_half, const SchedEntry* sched, uint32_t ns) {
+                       float tan_half, const SchedEntry* sched, uint32_t ns, uint32_t* cnt) {
     float cr = 0.f, cg = 0.f, cb = 0.f, alpha = 0.f;
     // The march distance is the float pair t + tl, advanced with error-free sums: a cone of small aperture takes
     // a hundred steps much shorter than t, and plain FP32 sums would drift by ~n/2 ulp(t) (5e-3 voxel at the far
@@ -261,6 +262,10 @@ __device__ float4 cone(const GridRef& g, const uint32_t* lut, const TraceConsts&
         float fl = floorf(lvl);
         uint32_t l0 = uint32_t(fl);
         float f = lvl - fl;
+        if constexpr (COUNT) {
+            cnt[0] += 1u;
+            cnt[1] += (f > 0.0f && l0 + 1 < g.levels) ? 2u : 1u;
+        }
         float4 s;
         if (ANISO) {
             // the two levels share one copy of the (three-volume) sampling code: the instruction cache
@@ -318,9 +323,9 @@ __device__ __forceinline__ void store_out(void* out, uint32_t fmt, uint64_t i, f
     }
 }
 
-template <int FMT, bool ANISO>
+template <int FMT, bool ANISO, bool COUNT>
 __device__ void trace_pixel(const GridRef& g, const uint32_t* lut, const TraceConsts& tc, const TraceView& v,
-                            uint32_t px, uint32_t py, const SchedEntry* sched) {
+                            uint32_t px, uint32_t py, const SchedEntry* sched, uint32_t* cnt) {
     const uint64_t npix = uint64_t(v.width) * v.height;
     const uint64_t pi = uint64_t(py) * v.width + px;
     float d = v.depth[pi];
@@ -356,7 +361,7 @@ __device__ void trace_pixel(const GridRef& g, const uint32_t* lut, const TraceCo
     coord_space(nw, bx, by, bz);
     float4 acc;
     if (tc.p.diffuse_cones >= 5) {
-        float4 c0 = cone<FMT, ANISO>(g, lut, tc, o, bz, tc.p.diffuse_tan_half, sched, kDiffuseSched);
+        float4 c0 = cone<FMT, ANISO, COUNT>(g, lut, tc, o, bz, tc.p.diffuse_tan_half, sched, kDiffuseSched, cnt);
         acc = make_float4(0.25f * c0.x, 0.25f * c0.y, 0.25f * c0.z, 0.25f * c0.w);
 #pragma unroll 1
         for (int k = 0; k < 4; ++k) {
@@ -364,14 +369,14 @@ __device__ void trace_pixel(const GridRef& g, const uint32_t* lut, const TraceCo
             float3 side = (k & 1) ? by : bx;
             if (k & 2) side = f3(-side.x, -side.y, -side.z);
             float3 dir = norm3(add3(mul3(bz, tc.cos_tilt), mul3(side, tc.sin_tilt)));
-            float4 ck = cone<FMT, ANISO>(g, lut, tc, o, dir, tc.p.diffuse_tan_half, sched, kDiffuseSched);
+            float4 ck = cone<FMT, ANISO, COUNT>(g, lut, tc, o, dir, tc.p.diffuse_tan_half, sched, kDiffuseSched, cnt);
             acc.x += 0.1875f * ck.x;
             acc.y += 0.1875f * ck.y;
             acc.z += 0.1875f * ck.z;
             acc.w += 0.1875f * ck.w;
         }
     } else {
-        acc = cone<FMT, ANISO>(g, lut, tc, o, bz, tc.p.diffuse_tan_half, sched, kDiffuseSched);
+        acc = cone<FMT, ANISO, COUNT>(g, lut, tc, o, bz, tc.p.diffuse_tan_half, sched, kDiffuseSched, cnt);
     }
     store_out(v.out, v.out_format, pi, acc);
     float4 sp = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -380,7 +385,7 @@ __device__ void trace_pixel(const GridRef& g, const uint32_t* lut, const TraceCo
         float dn = dot3(vd, nw);
         float3 rd = norm3(sub3(vd, mul3(nw, 2.0f * dn)));
         float th = fmaxf(rough, tc.p.min_spec_tan_half);
-        sp = cone<FMT, ANISO>(g, lut, tc, o, rd, th, nullptr, 0u);
+        sp = cone<FMT, ANISO, COUNT>(g, lut, tc, o, rd, th, nullptr, 0u, cnt);
     }
     store_out(v.out, v.out_format, npix + pi, sp);
 }
@@ -389,10 +394,11 @@ __device__ void trace_pixel(const GridRef& g, const uint32_t* lut, const TraceCo
 // one tile at a time: blockIdx.x in the one-shot launch (work == nullptr), or tiles taken from a device work
 // counter in the persistent launch (one resident wave of CTAs that drains the whole batch, so views of different
 // size balance).  The tile shape and the CTAs resident per SM (MINB) are the variants the tuner picks from.
-template <int FMT, bool ANISO, int TW, int TH, int MINB>
+template <int FMT, bool ANISO, int TW, int TH, int MINB, bool COUNT = false>
 __global__ void __launch_bounds__(TW * TH, MINB) trace_kernel(TraceConsts tc, const TraceView* __restrict__ views,
                                                              const uint32_t* __restrict__ tile_base, uint32_t nviews,
                                                              uint32_t* work) {
+    uint32_t cnt[2] = {0u, 0u};  // COUNT only: this thread's steps and level samples
     __shared__ GridRef g;
     __shared__ uint32_t s_lut[3 * kLut];
     __shared__ uint32_t s_tile, s_view;
@@ -440,7 +446,15 @@ __global__ void __launch_bounds__(TW * TH, MINB) trace_kernel(TraceConsts tc, co
         const uint32_t tiles_x = (v.width + TW - 1) / TW;
         const uint32_t px = (local % tiles_x) * TW + (threadIdx.x % TW);
         const uint32_t py = (local / tiles_x) * TH + (threadIdx.x / TW);
-        if (px < v.width && py < v.height) trace_pixel<FMT, ANISO>(g, s_lut, tc, v, px, py, s_sched);
+        if (px < v.width && py < v.height) trace_pixel<FMT, ANISO, COUNT>(g, s_lut, tc, v, px, py, s_sched, cnt);
+        if constexpr (COUNT) {  // warp totals, one atomic per warp and counter
+            const unsigned long long a = __reduce_add_sync(0xffffffffu, cnt[0]), b = __reduce_add_sync(0xffffffffu, cnt[1]);
+            if ((threadIdx.x & 31u) == 0u) {
+                atomicAdd(&tc.counts[0], a);
+                atomicAdd(&tc.counts[1], b);
+            }
+            cnt[0] = cnt[1] = 0u;
+        }
         __syncthreads();  // s_tile / g are rewritten for the next tile
     }
 }
@@ -450,6 +464,13 @@ template <int FMT, bool ANISO, int V>
 const void* variant_fn() {
     constexpr TraceVariant tv = kTraceVariants[V];
     return reinterpret_cast<const void*>(&trace_kernel<FMT, ANISO, int(tv.tw), int(tv.th), int(tv.minb)>);
+}
+
+// The instrumented kernel (same outputs, plus the step and sample totals) in the default variant's shape.
+template <int FMT, bool ANISO>
+const void* count_kernel() {
+    constexpr TraceVariant tv = kTraceVariants[kTraceDefaultVariant];
+    return reinterpret_cast<const void*>(&trace_kernel<FMT, ANISO, int(tv.tw), int(tv.th), int(tv.minb), true>);
 }
 
 template <int FMT, bool ANISO>

@@ -187,6 +187,13 @@ int f184gi_trace(f184gi_ctx* ctx, uint32_t grid, const f184gi_view* views, uint3
 
 void f184gi_cone_params_default(f184gi_cone_params* p);
 
+/* Diagnostic, with no counterpart in the reference: the same trace as f184gi_trace (same outputs) through an
+ * instrumented kernel that also counts, over all pixels of all views, the cone steps (counts[0]) and the level
+ * samples (counts[1]; a step samples one mip level or two, 8 voxel taps each).  counts is a host array; the
+ * call waits for the stream.  Slower than f184gi_trace: for stating the sampled-bytes figure of a trace. */
+int f184gi_trace_count(f184gi_ctx* ctx, uint32_t grid, const f184gi_view* views, uint32_t nviews,
+                       const f184gi_cone_params* params, uint64_t counts[2], void* stream);
+
 /* ---- supporting passes ---- */
 
 /* A rigid move of one object: triangles [first, first + count) translated by offset (FP32 adds per vertex). */

@@ -73,6 +73,9 @@ def lib():
             getattr(_lib, n).argtypes = [C.POINTER(GridFrame), C.c_uint32, C.c_uint32, C.c_uint32, V, V, V,
                                          C.c_uint32, C.c_uint32, V, V, V, C.POINTER(ConeParams), V, C.c_uint32,
                                          C.c_uint32, C.c_int]
+        _lib.orc_trace_count_f32.argtypes = [C.POINTER(GridFrame), C.c_uint32, C.c_uint32, C.c_uint32, V, V, V,
+                                             C.c_uint32, C.c_uint32, V, V, V, C.POINTER(ConeParams), V, C.c_uint32,
+                                             C.c_uint32, C.c_int, V]
         _lib.orc_cone_f64.argtypes = [V, C.c_uint32, C.c_uint32, C.c_uint32, V, V, C.c_double,
                                       C.POINTER(ConeParams), V]
         _lib.orc_make_coord_space.argtypes = [V, V]
@@ -261,6 +264,24 @@ def trace(frame, dim, levels, chain, view, proj, width, height, depth, normal, r
     assert fn(C.byref(frame), dim, levels, 1 if aniso else 0, _p(chain), _p(view), _p(proj), width, height,
               _p(depth), _p(normal), _p(rough), C.byref(p), _p(out), r0, r1, nthreads) == 0
     return out.reshape(2, height, width, 4)
+
+
+def trace_count(frame, dim, levels, chain, view, proj, width, height, depth, normal, rough, params=None,
+                aniso=False, nthreads=0):
+    """FP32 trace of the whole image plus its totals: (out, cone steps, level samples)."""
+    chain = np.ascontiguousarray(chain, dtype=np.float32)
+    view = np.ascontiguousarray(view, dtype=np.float32).ravel()
+    proj = np.ascontiguousarray(proj, dtype=np.float32).ravel()
+    depth = np.ascontiguousarray(depth, dtype=np.float32)
+    normal = np.ascontiguousarray(normal, dtype=np.uint32)
+    rough = np.ascontiguousarray(rough, dtype=np.uint16)
+    out = np.zeros(2 * width * height * 4, dtype=np.float32)
+    counts = np.zeros(2, dtype=np.uint64)
+    p = params if params is not None else default_params()
+    assert lib().orc_trace_count_f32(C.byref(frame), dim, levels, 1 if aniso else 0, _p(chain), _p(view), _p(proj),
+                                     width, height, _p(depth), _p(normal), _p(rough), C.byref(p), _p(out), 0, height,
+                                     nthreads, _p(counts)) == 0
+    return out.reshape(2, height, width, 4), int(counts[0]), int(counts[1])
 
 
 def cone(chain, dim, levels, origin, direction, tan_half, params=None, aniso=False):

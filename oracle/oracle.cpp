@@ -667,9 +667,10 @@ void level_sample(const Chain<T>& ch, uint32_t l, Vec3<T> x, Vec3<T> dir, T out[
     }
 }
 
+// cnt (optional): cnt[0] += steps, cnt[1] += level samples (one or two per step)
 template <class T>
 void cone(const Chain<T>& ch, Vec3<T> o, Vec3<T> dir, T tan_half, const f184gi_cone_params& p, T tmax,
-          T out[4]) {
+          T out[4], uint64_t* cnt = nullptr) {
     T c[3] = {T(0), T(0), T(0)}, alpha = T(0);
     // FP64: t accumulates plainly (the definition).  FP32 (the device arithmetic): the distance is the pair
     // t + tl advanced with error-free sums, so long marches of small steps do not drift.
@@ -689,6 +690,10 @@ void cone(const Chain<T>& ch, Vec3<T> o, Vec3<T> dir, T tan_half, const f184gi_c
         T fl = std::floor(lvl);
         uint32_t l0 = uint32_t(fl);
         T f = lvl - fl;
+        if (cnt) {
+            cnt[0] += 1;
+            cnt[1] += (f > T(0) && l0 + 1 < ch.levels) ? 2 : 1;
+        }
         T s[4];
         level_sample(ch, l0, x, dir, s);
         if (f > T(0) && l0 + 1 < ch.levels) {
@@ -719,7 +724,7 @@ template <class T>
 int trace_impl(const f184gi_grid_frame* frame, uint32_t dim, uint32_t levels, uint32_t aniso, const T* chain,
                const float view[16], const float proj[16], uint32_t W, uint32_t H, const float* depth,
                const uint32_t* normal, const uint16_t* rough, const f184gi_cone_params* params, T* out,
-               uint32_t row_begin, uint32_t row_end, int nthreads) {
+               uint32_t row_begin, uint32_t row_end, int nthreads, uint64_t* counts = nullptr) {
     if (!frame || !chain || !view || !proj || !depth || !normal || !rough || !out) return -1;
     f184gi_cone_params p = default_params();
     if (params) p = *params;
@@ -747,6 +752,8 @@ int trace_impl(const f184gi_grid_frame* frame, uint32_t dim, uint32_t levels, ui
     // pixels of rows [row_begin, row_end), split evenly over the threads
     const int64_t p_begin = int64_t(row_begin) * W, p_end = int64_t(std::min(row_end, H)) * W;
     parallel_for(p_begin, p_end, nthreads, [&](int64_t pb, int64_t pe) {
+        uint64_t lc[2] = {0, 0};
+        uint64_t* cnt = counts ? lc : nullptr;
         for (int64_t pix = pb; pix < pe; ++pix) {
             {
                 const int64_t py = pix / W;
@@ -786,18 +793,18 @@ int trace_impl(const f184gi_grid_frame* frame, uint32_t dim, uint32_t levels, ui
                 T acc[4] = {T(0), T(0), T(0), T(0)};
                 if (p.diffuse_cones >= 5) {
                     T c0[4];
-                    cone(ch, o, bz, T(p.diffuse_tan_half), p, tmax, c0);
+                    cone(ch, o, bz, T(p.diffuse_tan_half), p, tmax, c0, cnt);
                     for (int k = 0; k < 4; ++k) acc[k] += T(0.25) * c0[k];
                     const T cphi[4] = {T(1), T(0), T(-1), T(0)}, sphi[4] = {T(0), T(1), T(0), T(-1)};
                     for (int s = 0; s < 4; ++s) {
                         Vec3<T> side = vadd(vmul(bx, cphi[s]), vmul(by, sphi[s]));
                         Vec3<T> d = vnorm(vadd(vmul(bz, ct), vmul(side, st)));
                         T cs4[4];
-                        cone(ch, o, d, T(p.diffuse_tan_half), p, tmax, cs4);
+                        cone(ch, o, d, T(p.diffuse_tan_half), p, tmax, cs4, cnt);
                         for (int k = 0; k < 4; ++k) acc[k] += T(0.1875) * cs4[k];
                     }
                 } else {
-                    cone(ch, o, bz, T(p.diffuse_tan_half), p, tmax, acc);
+                    cone(ch, o, bz, T(p.diffuse_tan_half), p, tmax, acc, cnt);
                 }
                 for (int k = 0; k < 4; ++k) od[k] = acc[k];
                 if (p.specular) {
@@ -806,10 +813,14 @@ int trace_impl(const f184gi_grid_frame* frame, uint32_t dim, uint32_t levels, ui
                     Vec3<T> rd = vnorm(vsub(vdir, vmul(nw, T(2) * dn)));
                     T th = std::max(r, T(p.min_spec_tan_half));
                     T sc[4];
-                    cone(ch, o, rd, th, p, tmax, sc);
+                    cone(ch, o, rd, th, p, tmax, sc, cnt);
                     for (int k = 0; k < 4; ++k) os[k] = sc[k];
                 }
             }
+        }
+        if (counts) {
+            __atomic_fetch_add(&counts[0], lc[0], __ATOMIC_RELAXED);
+            __atomic_fetch_add(&counts[1], lc[1], __ATOMIC_RELAXED);
         }
     });
     return 0;
@@ -998,6 +1009,17 @@ int orc_trace_f32(const f184gi_grid_frame* frame, uint32_t dim, uint32_t levels,
                   const f184gi_cone_params* params, float* out, uint32_t rb, uint32_t re, int nthreads) {
     return trace_impl<float>(frame, dim, levels, aniso, chain, view, proj, W, H, depth, normal, rough, params,
                              out, rb, re, nthreads);
+}
+
+int orc_trace_count_f32(const f184gi_grid_frame* frame, uint32_t dim, uint32_t levels, uint32_t aniso,
+                        const float* chain, const float view[16], const float proj[16], uint32_t W, uint32_t H,
+                        const float* depth, const uint32_t* normal, const uint16_t* rough,
+                        const f184gi_cone_params* params, float* out, uint32_t rb, uint32_t re, int nthreads,
+                        uint64_t counts[2]) {
+    if (!counts) return -1;
+    counts[0] = counts[1] = 0;
+    return trace_impl<float>(frame, dim, levels, aniso, chain, view, proj, W, H, depth, normal, rough, params, out,
+                             rb, re, nthreads, counts);
 }
 
 int orc_cone_f64(const double* chain, uint32_t dim, uint32_t levels, uint32_t aniso, const double o[3],

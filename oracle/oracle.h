@@ -71,6 +71,12 @@ int orc_trace_f32(const f184gi_grid_frame* frame, uint32_t dim, uint32_t levels,
                   uint32_t height, const float* depth, const uint32_t* normal, const uint16_t* roughness,
                   const f184gi_cone_params* params, float* out, uint32_t row_begin, uint32_t row_end,
                   int nthreads);
+/* orc_trace_f32 that also totals the cone steps (counts[0]) and level samples (counts[1]) over the traced rows */
+int orc_trace_count_f32(const f184gi_grid_frame* frame, uint32_t dim, uint32_t levels, uint32_t aniso,
+                        const float* chain, const float view[16], const float proj[16], uint32_t W, uint32_t H,
+                        const float* depth, const uint32_t* normal, const uint16_t* rough,
+                        const f184gi_cone_params* params, float* out, uint32_t rb, uint32_t re, int nthreads,
+                        uint64_t counts[2]);
 
 /* One cone from `o` (L0 voxel units) along unit `dir` (for known-answer tests of the march). */
 int orc_cone_f64(const double* chain, uint32_t dim, uint32_t levels, uint32_t aniso, const double o[3],

@@ -36,6 +36,19 @@ def test_oracle_reproduces_golden(orc, gold):
     assert np.allclose(out, gold["trace"], rtol=1e-12, atol=1e-15)
 
 
+def test_oracle_trace_count_same_image(orc, gold):
+    """The counting oracle trace returns the plain FP32 trace's image and positive, consistent totals."""
+    dim, levels, res, W, H = (int(x) for x in gold["dims"])
+    fo = orc.grid_frame(orc.make_bounds((-10, -10, -10), (10, 10, 10)), dim, gold["ldir"])
+    chain, _ = orc.mip(gold["l0"], levels, f64=False)
+    args = (fo, dim, levels, chain, gold["view"], gold["proj"], W, H, gold["depth"], gold["normal"], gold["rough_px"])
+    plain = orc.trace(*args, f64=False)
+    img, steps, samples = orc.trace_count(*args)
+    assert np.array_equal(img.view(np.uint32), plain.view(np.uint32))
+    lit = int((gold["depth"] < 1.0).sum())
+    assert 10 * lit < steps < 400 * lit and steps <= samples <= 2 * steps
+
+
 @pytest.mark.gpu
 def test_gpu_matches_golden(lib, gold):
     import torch

@@ -108,6 +108,26 @@ def test_trace_matches_oracle(case, orc, oracle_l0):
     assert ref[0, ..., :3].mean() > 1e-3  # lit scene
 
 
+def test_trace_count_outputs_and_totals(case, orc, oracle_l0):
+    """The instrumented trace writes the plain trace's bytes, and its step / level-sample totals equal the FP32
+    oracle's over the same chain (read back from the device) up to a few cones whose exit test sits within an ulp
+    of the grid margin."""
+    ref_img = case.trace().copy()
+    steps, samples = case.gi.trace_count(case.grid, [case.view])
+    case.gi.sync()
+    got = case.out.cpu().numpy().reshape(2, case.H, case.W, 4)
+    assert np.array_equal(got.view(np.uint32), ref_img.view(np.uint32))
+    chain = np.concatenate([case.gi.read_level(case.grid, l).ravel() for l in range(case.levels)])
+    dep, nrm, rgh, _ = case.gbuffer_host()
+    _, osteps, osamples = orc.trace_count(oracle_l0[0], case.dim, case.levels, chain, case.V, case.P, case.W, case.H,
+                                          dep, nrm, rgh)
+    lit = int((dep < 1.0).sum())
+    print("steps/px %.2f (oracle %.2f), samples/px %.2f (oracle %.2f)" % (steps / lit, osteps / lit, samples / lit,
+                                                                          osamples / lit))
+    assert 10 * lit < steps < 400 * lit and steps <= samples <= 2 * steps
+    assert abs(steps - osteps) <= 1e-4 * osteps and abs(samples - osamples) <= 1e-4 * osamples
+
+
 def test_shuffled_triangle_order_bit_identical(case):
     rng = np.random.default_rng(7)
     perm = rng.permutation(case.sc.ntris)
