@@ -215,7 +215,7 @@ def run_reference(args, cfg):
 
 # ---------------------------------------------------------------- GPU arm
 
-def l2_copy_gbs(dev, stream, mib=16, reps=100):
+def l2_copy_gbs(dev, stream, mib=40, reps=100):
     """Read + write GB/s of a device copy whose source and destination (2 x mib MiB) stay in L2."""
     import torch
 
@@ -418,7 +418,7 @@ def run_gpu(args, cfg):
                                  "note": "secondary figure, not the roofline: voxel bytes sampled by the cones "
                                          "(level samples x 8 taps x 16 B, counted by the instrumented kernel) per "
                                          "trace launch time; most are L1 hits, so it may exceed the L2 figure, "
-                                         "a torch copy of 2 x 16 MiB held in L2"}},
+                                         "a torch copy of 2 x 40 MiB held in L2"}},
         "e2e": {"value": round(e2e_value, 4), "unit": "Mpix/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "ms_per_step": round(e2e_ms, 4),
                 "note": "through the API from pinned host buffers; two request lanes (context, grid, stream) take "
