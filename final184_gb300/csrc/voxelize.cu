@@ -348,7 +348,10 @@ __device__ void item_setup(const TriRec& r, const int64_t base[3], const int32_t
 
 constexpr int kChunk = 128;  // items prepared per round (one per thread; = threads per CTA)
 
-__global__ void __launch_bounds__(kChunk, 4) vox_bricks(VoxScratch sc, const f184gi_grid_frame* __restrict__ fr,
+// Eight CTAs per SM (64 registers, 26 KB of shared memory each): a brick's phases are separated by barriers at
+// which most of its threads wait, so other bricks' CTAs are what keeps the SM busy (0.59 -> 0.40 ms per 256^3
+// voxelization against four CTAs per SM).
+__global__ void __launch_bounds__(kChunk, 8) vox_bricks(VoxScratch sc, const f184gi_grid_frame* __restrict__ fr,
                                                   uint32_t dim, ChainLayout chain, f184gi_light light,
                                                   const unsigned long long* __restrict__ shadow, uint32_t res,
                                                   uint32_t* counts, const uint32_t* __restrict__ dirty,
