@@ -111,6 +111,10 @@ struct f184gi_ctx {
     uint32_t* d_status = nullptr;
     TraceStaging* trace_stage = nullptr;
     uint32_t trace_variant = kTraceDefaultVariant;
+    // voxelize forks the triangle lists onto aux (after the frame) beside the shadow raster on the caller's
+    // stream, and joins before the bricks
+    cudaStream_t aux = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
 };
 
 namespace {
@@ -240,6 +244,12 @@ int f184gi_create(const f184gi_config* cfg, f184gi_ctx** out) {
     }
     c->d_status = static_cast<uint32_t*>(st);
     cudaMemset(c->d_status, 0, 4);
+    if ((e = cudaStreamCreateWithFlags(&c->aux, cudaStreamNonBlocking)) != cudaSuccess ||
+        (e = cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming)) != cudaSuccess ||
+        (e = cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming)) != cudaSuccess) {
+        f184gi_destroy(c);
+        return cuda_fail(e, "create: auxiliary stream");
+    }
     *out = c;
     return F184GI_OK;
 }
@@ -259,6 +269,9 @@ int f184gi_destroy(f184gi_ctx* c) {
     for (Scratch* s : {&c->raster, &c->vox, &c->trace, &c->misc, &c->keys, &c->counts}) dev_free(c, s->ptr, s->bytes);
     trace_staging_destroy(c->trace_stage);
     dev_free(c, c->d_status, 256);
+    if (c->ev_fork) cudaEventDestroy(c->ev_fork);
+    if (c->ev_join) cudaEventDestroy(c->ev_join);
+    if (c->aux) cudaStreamDestroy(c->aux);
     delete c;
     return F184GI_OK;
 }
@@ -370,26 +383,15 @@ int f184gi_voxelize(f184gi_ctx* c, uint32_t grid, const float* tri, const uint32
     const f184gi_grid_desc& d = g->desc;
     int rc = scratch_get(c, c->misc, 4096);
     if (rc) return rc;
-    if ((rc = frame_launch(tri, ntris, bounds, d.dim, light->direction, g->d_frame, c->misc.ptr, s))) return rc;
-    // shadow map over the grid's light frame
-    RasterJob rj{};
-    rj.tri = tri;
-    rj.ntris = ntris;
-    rj.d_M = g->d_frame->light_clip;
-    rj.width = rj.height = d.shadow_res;
-    rj.keys = g->shadow;
+    if (d.format == F184GI_FMT_RG16 && ndirty)
+        return fail(F184GI_ERR_INVALID, "voxelize: an RG16 grid is always voxelized whole");
+    if (g->weights && ndirty && !g->voxelized)
+        return fail(F184GI_ERR_INVALID, "voxelize: a dirty-brick update needs one full voxelization first");
     if ((rc = scratch_get(c, c->raster, raster_scratch_bytes(ntris, d.shadow_res, d.shadow_res)))) return rc;
-    if ((rc = raster_launch(rj, c->raster.ptr, c->raster.bytes, c->d_status, s))) return rc;
-    g->light = *light;
-    if (d.format == F184GI_FMT_RG16) {  // the reference's volume: 565 albedo and normal of the last fragment
-        if (ndirty) return fail(F184GI_ERR_INVALID, "voxelize: an RG16 grid is always voxelized whole");
-        if ((rc = scratch_get(c, c->vox, refvox_scratch_bytes(ntris, d.dim)))) return rc;
-        if ((rc = refvox_launch(tri, albedo, ntris, g->d_frame, d.dim, static_cast<uint32_t*>(g->chain.base),
-                                c->vox.ptr, c->vox.bytes, c->d_status, s)))
-            return rc;
-        g->voxelized = true;
-        return F184GI_OK;
-    }
+    if ((rc = scratch_get(c, c->vox, d.format == F184GI_FMT_RG16 ? refvox_scratch_bytes(ntris, d.dim)
+                                                                   : voxelize_scratch_bytes(ntris, d.dim))))
+        return rc;
+    if ((rc = frame_launch(tri, ntris, bounds, d.dim, light->direction, g->d_frame, c->misc.ptr, s))) return rc;
     VoxelizeJob vj{};
     vj.tri = tri;
     vj.albedo = albedo;
@@ -402,11 +404,34 @@ int f184gi_voxelize(f184gi_ctx* c, uint32_t grid, const float* tri, const uint32
     vj.counts = g->counts;
     vj.dirty_bricks = dirty;
     vj.ndirty = ndirty;
-    if (g->weights && ndirty && !g->voxelized)
-        return fail(F184GI_ERR_INVALID, "voxelize: a dirty-brick update needs one full voxelization first");
     vj.weights = g->weights;
-    if ((rc = scratch_get(c, c->vox, voxelize_scratch_bytes(ntris, d.dim)))) return rc;
-    if ((rc = voxelize_launch(vj, c->vox.ptr, c->vox.bytes, c->d_status, s))) return rc;
+    const bool lists = d.format != F184GI_FMT_RG16;
+    cudaError_t e;
+    if (lists) {  // the triangle lists need the frame, not the shadow map: build them beside the raster
+        if ((e = cudaEventRecord(c->ev_fork, s)) != cudaSuccess || (e = cudaStreamWaitEvent(c->aux, c->ev_fork, 0)) != cudaSuccess)
+            return cuda_fail(e, "voxelize: fork");
+        if ((rc = voxelize_lists_launch(vj, c->vox.ptr, c->vox.bytes, c->d_status, c->aux))) return rc;
+        if ((e = cudaEventRecord(c->ev_join, c->aux)) != cudaSuccess) return cuda_fail(e, "voxelize: join");
+    }
+    // shadow map over the grid's light frame
+    RasterJob rj{};
+    rj.tri = tri;
+    rj.ntris = ntris;
+    rj.d_M = g->d_frame->light_clip;
+    rj.width = rj.height = d.shadow_res;
+    rj.keys = g->shadow;
+    rc = raster_launch(rj, c->raster.ptr, c->raster.bytes, c->d_status, s);
+    if (lists && (e = cudaStreamWaitEvent(s, c->ev_join, 0)) != cudaSuccess) return cuda_fail(e, "voxelize: join");
+    if (rc) return rc;
+    g->light = *light;
+    if (d.format == F184GI_FMT_RG16) {  // the reference's volume: 565 albedo and normal of the last fragment
+        if ((rc = refvox_launch(tri, albedo, ntris, g->d_frame, d.dim, static_cast<uint32_t*>(g->chain.base),
+                                c->vox.ptr, c->vox.bytes, c->d_status, s)))
+            return rc;
+        g->voxelized = true;
+        return F184GI_OK;
+    }
+    if ((rc = voxelize_bricks_launch(vj, c->vox.ptr, c->vox.bytes, c->d_status, s))) return rc;
     if (g->weights && (rc = relight_launch(g->weights, g->d_frame, g->chain, *light, g->shadow, d.shadow_res, s)))
         return rc;
     g->voxelized = true;

@@ -502,19 +502,11 @@ size_t voxelize_scratch_bytes(uint64_t ntris, uint32_t dim) {
            list_capacity(ntris, nbricks) * 4 + (ntris + 2) * 4 + 20 * 256;
 }
 
-int voxelize_launch(const VoxelizeJob& job, void* scratch, size_t scratch_bytes, uint32_t* d_status, cudaStream_t s) {
-    const uint32_t dim = job.chain.dim;
-    if (dim < 16 || dim > 512 || (dim & (dim - 1))) return fail(F184GI_ERR_INVALID, "voxelize: dim must be 2^k in 16..512");
-    if (job.ntris >= 0xffff0000ull) return fail(F184GI_ERR_INVALID, "voxelize: too many triangles");
-    if (scratch_bytes < voxelize_scratch_bytes(job.ntris, dim)) return fail(F184GI_ERR_INVALID, "voxelize: scratch too small");
-    if (!g_lut_ready) {
-        float lut[256];
-        for (int i = 0; i < 256; ++i) lut[i] = float(std::pow(double(i) / 255.0, 2.2));
-        cudaError_t e = cudaMemcpyToSymbol(c_albedo_lut, lut, sizeof(lut));
-        if (e != cudaSuccess) return cuda_fail(e, "voxelize: albedo table");
-        g_lut_ready = true;
-    }
-    const uint32_t nb = dim / 8, nbricks = nb * nb * nb;
+namespace {
+
+// The scratch layout shared by the two phases.
+VoxScratch carve_scratch(const VoxelizeJob& job, void* scratch, uint32_t** mask) {
+    const uint32_t nb = job.chain.dim / 8, nbricks = nb * nb * nb;
     char* p = static_cast<char*>(scratch);
     VoxScratch sc;
     sc.recs = carve<TriRec>(p, job.ntris);
@@ -523,17 +515,44 @@ int voxelize_launch(const VoxelizeJob& job, void* scratch, size_t scratch_bytes,
     sc.brick_fill = carve<uint32_t>(p, nbricks);
     sc.total = carve<uint32_t>(p, 1);
     sc.scan_tmp = carve<uint32_t>(p, scan_scratch_bytes(nbricks) / 4);
-    uint32_t* mask = carve<uint32_t>(p, nbricks / 32 + 1);
+    *mask = carve<uint32_t>(p, nbricks / 32 + 1);
     sc.list_cap = list_capacity(job.ntris, nbricks);
     sc.list = carve<uint32_t>(p, sc.list_cap);
     sc.big = carve<uint32_t>(p, job.ntris + 1);
     sc.big_count = carve<uint32_t>(p, 1);
-    sc.dirty_mask = nullptr;
+    sc.dirty_mask = job.ndirty ? *mask : nullptr;
+    return sc;
+}
+
+int check_job(const VoxelizeJob& job, size_t scratch_bytes) {
+    const uint32_t dim = job.chain.dim;
+    if (dim < 16 || dim > 512 || (dim & (dim - 1))) return fail(F184GI_ERR_INVALID, "voxelize: dim must be 2^k in 16..512");
+    if (job.ntris >= 0xffff0000ull) return fail(F184GI_ERR_INVALID, "voxelize: too many triangles");
+    if (scratch_bytes < voxelize_scratch_bytes(job.ntris, dim)) return fail(F184GI_ERR_INVALID, "voxelize: scratch too small");
+    return F184GI_OK;
+}
+
+}  // namespace
+
+int voxelize_lists_launch(const VoxelizeJob& job, void* scratch, size_t scratch_bytes, uint32_t* d_status,
+                          cudaStream_t s) {
+    int rc = check_job(job, scratch_bytes);
+    if (rc) return rc;
+    const uint32_t dim = job.chain.dim;
+    if (!g_lut_ready) {
+        float lut[256];
+        for (int i = 0; i < 256; ++i) lut[i] = float(std::pow(double(i) / 255.0, 2.2));
+        cudaError_t e = cudaMemcpyToSymbol(c_albedo_lut, lut, sizeof(lut));
+        if (e != cudaSuccess) return cuda_fail(e, "voxelize: albedo table");
+        g_lut_ready = true;
+    }
+    const uint32_t nb = dim / 8, nbricks = nb * nb * nb;
+    uint32_t* mask = nullptr;
+    VoxScratch sc = carve_scratch(job, scratch, &mask);
     cudaMemsetAsync(sc.big_count, 0, 4, s);
     cudaMemsetAsync(sc.brick_count, 0, size_t(nbricks) * 4, s);
     cudaMemsetAsync(sc.brick_fill, 0, size_t(nbricks) * 4, s);
     if (job.ndirty) {
-        sc.dirty_mask = mask;
         cudaMemsetAsync(mask, 0, size_t(nbricks / 32 + 1) * 4, s);
         vox_dirty_mask<<<(job.ndirty + 255) / 256, 256, 0, s>>>(job.dirty_bricks, job.ndirty, nbricks, mask);
         note_launches(1);
@@ -544,18 +563,32 @@ int voxelize_launch(const VoxelizeJob& job, void* scratch, size_t scratch_bytes,
         vox_bin_big<<<2 * 152, 256, 0, s>>>(dim, sc, d_status, 0);
         note_launches(2);
     }
-    int rc = exclusive_scan(sc.brick_count, nbricks, sc.brick_start, sc.total, sc.scan_tmp, s);
-    if (rc) return rc;
+    if ((rc = exclusive_scan(sc.brick_count, nbricks, sc.brick_start, sc.total, sc.scan_tmp, s))) return rc;
     if (job.ntris) {
         vox_emit<<<uint32_t((job.ntris + 127) / 128), 128, 0, s>>>(job.ntris, dim, sc, d_status);
         vox_bin_big<<<2 * 152, 256, 0, s>>>(dim, sc, d_status, 1);
         note_launches(2);
     }
-    uint32_t nblocks = job.ndirty ? job.ndirty : nbricks;
+    return cuda_fail(cudaGetLastError(), "voxelize lists");
+}
+
+int voxelize_bricks_launch(const VoxelizeJob& job, void* scratch, size_t scratch_bytes, uint32_t* d_status,
+                           cudaStream_t s) {
+    int rc = check_job(job, scratch_bytes);
+    if (rc) return rc;
+    const uint32_t dim = job.chain.dim, nb = dim / 8, nbricks = nb * nb * nb;
+    uint32_t* mask = nullptr;
+    VoxScratch sc = carve_scratch(job, scratch, &mask);
+    const uint32_t nblocks = job.ndirty ? job.ndirty : nbricks;
     vox_bricks<<<nblocks, kChunk, 0, s>>>(sc, job.d_frame, dim, job.chain, job.light, job.shadow_keys, job.shadow_res,
                                        job.counts, job.ndirty ? job.dirty_bricks : nullptr, job.weights, d_status);
     note_launches(1);
     return cuda_fail(cudaGetLastError(), "voxelize");
+}
+
+int voxelize_launch(const VoxelizeJob& job, void* scratch, size_t scratch_bytes, uint32_t* d_status, cudaStream_t s) {
+    int rc = voxelize_lists_launch(job, scratch, scratch_bytes, d_status, s);
+    return rc ? rc : voxelize_bricks_launch(job, scratch, scratch_bytes, d_status, s);
 }
 
 }  // namespace f184
