@@ -411,6 +411,9 @@ int f184gi_voxelize(f184gi_ctx* c, uint32_t grid, const float* tri, const uint32
         if ((e = cudaEventRecord(c->ev_fork, s)) != cudaSuccess || (e = cudaStreamWaitEvent(c->aux, c->ev_fork, 0)) != cudaSuccess)
             return cuda_fail(e, "voxelize: fork");
         if ((rc = voxelize_lists_launch(vj, c->vox.ptr, c->vox.bytes, c->d_status, c->aux))) return rc;
+        // with resident weights the bricks write the geometry-only mean weights: no shadow map needed either
+        if (g->weights && (rc = voxelize_bricks_launch(vj, c->vox.ptr, c->vox.bytes, c->d_status, c->aux)))
+            return rc;
         if ((e = cudaEventRecord(c->ev_join, c->aux)) != cudaSuccess) return cuda_fail(e, "voxelize: join");
     }
     // shadow map over the grid's light frame
@@ -431,7 +434,7 @@ int f184gi_voxelize(f184gi_ctx* c, uint32_t grid, const float* tri, const uint32
         g->voxelized = true;
         return F184GI_OK;
     }
-    if ((rc = voxelize_bricks_launch(vj, c->vox.ptr, c->vox.bytes, c->d_status, s))) return rc;
+    if (!g->weights && (rc = voxelize_bricks_launch(vj, c->vox.ptr, c->vox.bytes, c->d_status, s))) return rc;
     if (g->weights && (rc = relight_launch(g->weights, g->d_frame, g->chain, *light, g->shadow, d.shadow_res, s)))
         return rc;
     g->voxelized = true;
