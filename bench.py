@@ -15,9 +15,7 @@ import argparse
 import json
 import os
 import statistics
-import subprocess
 import sys
-import tempfile
 import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
@@ -58,54 +56,87 @@ def traffic_record(kernel):
 
 
 class ClockSampler:
-    """nvidia-smi clock/throttle samples during the timed region."""
+    """SM clock and clock-event reasons sampled every 10 ms through NVML (read only) during the timed region,
+    which begin() and end() bracket."""
 
-    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
-             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
-             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown", 0x40: "hw_thermal_slowdown"}
 
-    def __init__(self, index):
-        self.index = index
-        self.proc = None
-        self.path = None
+    def __init__(self, device):
+        import ctypes as C
+        import threading
+
+        self.C, self.samples, self.t0, self.t1 = C, [], None, None
+        self.stop_flag = threading.Event()
+        self.thread = None
+        self.nvml = self.handle = None
+        try:
+            nvml = C.CDLL("libnvidia-ml.so.1")
+            if nvml.nvmlInit_v2() != 0:
+                return
+            h = C.c_void_p()
+            bus = self._bus_id(device)
+            ok = bus is not None and nvml.nvmlDeviceGetHandleByPciBusId_v2(bus.encode(), C.byref(h)) == 0
+            if not ok and nvml.nvmlDeviceGetHandleByIndex_v2(C.c_uint(device.index or 0), C.byref(h)) != 0:
+                return
+            self.nvml, self.handle = nvml, h
+            self.reasons_fn = getattr(nvml, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+                nvml.nvmlDeviceGetCurrentClocksThrottleReasons
+        except (OSError, AttributeError):
+            self.nvml = None
+
+    @staticmethod
+    def _bus_id(device):
+        import torch
+
+        p = torch.cuda.get_device_properties(device)
+        if not hasattr(p, "pci_bus_id"):
+            return None
+        return "%08x:%02x:%02x.0" % (getattr(p, "pci_domain_id", 0), p.pci_bus_id, getattr(p, "pci_device_id", 0))
+
+    def _read(self):
+        C = self.C
+        clk, mx, r = C.c_uint(0), C.c_uint(0), C.c_ulonglong(0)
+        if self.nvml.nvmlDeviceGetClockInfo(self.handle, 1, C.byref(clk)) != 0:
+            return None
+        self.nvml.nvmlDeviceGetMaxClockInfo(self.handle, 1, C.byref(mx))
+        self.reasons_fn(self.handle, C.byref(r))
+        return time.time(), clk.value, mx.value, r.value
+
+    def _loop(self):
+        while not self.stop_flag.is_set():
+            s = self._read()
+            if s:
+                self.samples.append(s)
+            time.sleep(0.01)
 
     def start(self):
-        fd, self.path = tempfile.mkstemp(suffix=".csv")
-        os.close(fd)
-        try:
-            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.QUERY,
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
-                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
-        except (OSError, FileNotFoundError):
-            self.proc = None
+        if self.nvml is None:
+            return
+        import threading
+
+        self.thread = threading.Thread(target=self._loop, daemon=True)
+        self.thread.start()
+
+    def begin(self):
+        self.t0 = time.time()
+
+    def end(self):
+        self.t1 = time.time()
 
     def stop(self):
-        if self.proc is None:
+        if self.thread is None:
             return None
-        self.proc.terminate()
-        try:
-            self.proc.wait(timeout=5)
-        except subprocess.TimeoutExpired:
-            self.proc.kill()
-        sm, mx, reasons = [], 0.0, set()
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        with open(self.path) as f:
-            for line in f:
-                parts = [p.strip() for p in line.split(",")]
-                if len(parts) < 9:
-                    continue
-                try:
-                    sm.append(float(parts[1]))
-                    mx = max(mx, float(parts[2]))
-                except ValueError:
-                    continue
-                for n, v in zip(names, parts[5:9]):
-                    if v.lower().startswith("active"):
-                        reasons.add(n)
-        os.unlink(self.path)
-        if not sm:
+        self.stop_flag.set()
+        self.thread.join()
+        t0, t1 = self.t0 or 0.0, self.t1 or time.time()
+        win = [s for s in self.samples if t0 <= s[0] <= t1]
+        if not win:  # a region shorter than the sampling period: the samples nearest to it
+            win = sorted(self.samples, key=lambda s: abs(s[0] - 0.5 * (t0 + t1)))[:2]
+        if not win:
             return None
-        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+        reasons = sorted({n for s in win for bit, n in self.REASONS.items() if s[3] & bit})
+        return {"sm_mhz": statistics.median([s[1] for s in win]), "sm_max_mhz": max(s[2] for s in win),
+                "reasons": reasons, "samples": len(win), "source": "NVML, every 10 ms over the timed region"}
 
 
 def slowest_rank_ms(local_ms, device=None):
@@ -297,10 +328,11 @@ def run_gpu(args, cfg):
 
     # ---- device-resident timing ----
     evs = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(args.steps)]
-    clocks = ClockSampler(local)
+    clocks = ClockSampler(dev)
     clocks.start()
     launches0 = g.load().f184gi_kernel_launches()
     barrier()
+    clocks.begin()
     t_start = torch.cuda.Event(enable_timing=True)
     t_end = torch.cuda.Event(enable_timing=True)
     t_start.record(stream)
@@ -308,6 +340,7 @@ def run_gpu(args, cfg):
         step(evs[k])
     t_end.record(stream)
     barrier()
+    clocks.end()
     launches = g.load().f184gi_kernel_launches() - launches0
     clk = clocks.stop()
     gi.sync(stream)
@@ -765,7 +798,7 @@ def run_batched(args, cfg=BATCHED):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--small", action="store_true", help="the 20k-triangle 64^3 640x360 case (profiling)")

@@ -160,6 +160,9 @@ __global__ void raster_setup(const float* __restrict__ tri, uint64_t ntris, Rast
     uint64_t t = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (t >= ntris) return;
     const double* M = job.d_M ? job.d_M : job.M;
+    // an orthographic frame (last row 0 0 0 1, the shadow map's) gives w = ((0 x + 0 y) + 0 z) + 1 = 1 exactly:
+    // its row and the guard band's 16 w products are skipped, with the same values
+    const bool ortho = M[12] == 0.0 && M[13] == 0.0 && M[14] == 0.0 && M[15] == 1.0;
     V4 poly[12];
     bool inside = true;
     for (int v = 0; v < 3; ++v) {
@@ -167,9 +170,16 @@ __global__ void raster_setup(const float* __restrict__ tri, uint64_t ntris, Rast
         poly[v].x = drow(M, x, y, z);
         poly[v].y = drow(M + 4, x, y, z);
         poly[v].z = drow(M + 8, x, y, z);
-        poly[v].w = drow(M + 12, x, y, z);
-        for (int k = 0; k < 6; ++k)
-            if (!(plane_dist(k, poly[v]) >= 0.0)) inside = false;
+        poly[v].w = ortho ? 1.0 : drow(M + 12, x, y, z);
+        if (ortho) {
+            const V4& p = poly[v];
+            if (!(p.z >= 0.0 && dsub(1.0, p.z) >= 0.0 && dsub(kGuard, p.x) >= 0.0 && dadd(p.x, kGuard) >= 0.0 &&
+                  dsub(kGuard, p.y) >= 0.0 && dadd(p.y, kGuard) >= 0.0))
+                inside = false;
+        } else {
+            for (int k = 0; k < 6; ++k)
+                if (!(plane_dist(k, poly[v]) >= 0.0)) inside = false;
+        }
     }
     int n = 3;
     if (!inside) n = clip_polygon(poly, 3);
