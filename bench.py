@@ -725,7 +725,7 @@ def run_march(args, cfg=PLAIN_LARGE, dim=128):
 
 def run_batched(args, cfg=BATCHED):
     """Batched form: 64 resident scenes of mixed grid and triangle counts, 1-8 views each, all traces in one
-    persistent launch replayed from a CUDA graph (kernel variant tuned on the first batch)."""
+    launch replayed from a CUDA graph (kernel variant tuned on the first batch)."""
     import math
 
     import numpy as np
@@ -783,7 +783,7 @@ def run_batched(args, cfg=BATCHED):
     nviews = sum(len(v) for _, v, _ in reqs)
     lat = sorted(r.latency_ms for r in res)
     return {"workload": "%d resident scenes (grids %s^3, %.1fM triangles in all), %d views of 256^2..1920x1080, "
-                        "FP16 storage, all traces in one persistent launch per batch under a CUDA graph"
+                        "FP16 storage, all traces in one launch per batch under a CUDA graph"
                         % (cfg["scenes"], "/".join(str(d) for d in cfg["dims"]), tris_total / 1e6, nviews),
             "value": round(pixels / wall / 1e6, 2), "unit": "Mpix/s", "pixels": int(pixels), "views": nviews,
             "batches_per_submit": len({r.batch for r in res}), "wall_ms": round(wall * 1e3, 3),

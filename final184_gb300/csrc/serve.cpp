@@ -8,7 +8,7 @@
 //   - per touched scene: rigid moves on the device, dirty bricks from the moved objects' old and new boxes
 //     (computed on a host mirror of the geometry), geometry re-voxelization of those bricks, relight of the grid
 //     from the new shadow map, mip rebuild;
-//   - one persistent trace launch over all views of the batch, replayed from the slot's CUDA graph.
+//   - one trace launch over all views of the batch, replayed from the slot's CUDA graph.
 // A completer thread retires batches in launch order and records per-request latency.  Batches on different
 // slots overlap on the device; requests that arrive meanwhile join the next batch.
 #include <algorithm>

@@ -30,7 +30,8 @@ const void* trace_kernel_count_fn(uint32_t fmt, bool aniso) {
 
 uint32_t trace_view_tiles(uint32_t width, uint32_t height, uint32_t variant) {
     const TraceVariant& v = kTraceVariants[variant];
-    return ((width + v.tw - 1) / v.tw) * ((height + v.th - 1) / v.th);
+    const uint32_t wh = 32 / v.tw;  // warp tiles of tw x (32 / tw) pixels
+    return ((width + v.tw - 1) / v.tw) * ((height + wh - 1) / wh);
 }
 
 void trace_view_set_grid(TraceView& v, const ChainLayout& c, const f184gi_grid_frame* d_frame, float tmax) {
@@ -129,7 +130,8 @@ int trace_launch(const ChainLayout& c, const TraceConsts& tc, const f184gi_grid_
         return cuda_fail(e, "trace: view table");
     if ((e = cudaEventRecord(st->copied, s)) != cudaSuccess) return cuda_fail(e, "trace: staging event");
     if (tiles == 0) return F184GI_OK;
-    e = launch(fn, variant, tiles, tc, d_table, nviews, nullptr, s);
+    const uint32_t warps = kTraceVariants[variant].tw * kTraceVariants[variant].th / 32;
+    e = launch(fn, variant, (tiles + warps - 1) / warps, tc, d_table, nviews, nullptr, s);
     note_launches(1);
     return cuda_fail(e, "trace");
 }
@@ -137,7 +139,7 @@ int trace_launch(const ChainLayout& c, const TraceConsts& tc, const f184gi_grid_
 // ---------------- batched trace under CUDA graphs ----------------
 
 // One graph per kernel variant, instantiated on first use:
-//   [view table H2D] -> [work counter = 0] -> [persistent kernel: one resident wave of CTAs]
+//   [view table H2D] -> [work counter = 0] -> [kernel: one warp per warp tile, or a capped persistent wave]
 struct TraceGraphVariant {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
@@ -157,6 +159,8 @@ struct TraceGraph {
     uint32_t nviews = 0;
     const TraceView* kviews = nullptr;
     const uint32_t* kbase = nullptr;
+    uint32_t* kwork = nullptr;  // null: static warp tiles
+    uint32_t tiles = 0;         // warp tiles of the current batch
     TraceGraphVariant var[kTraceVariantCount];
 };
 
@@ -176,11 +180,16 @@ static void graph_params(TraceGraph* g, uint32_t variant, cudaKernelNodeParams& 
     args[1] = &g->kviews;
     args[2] = &g->kbase;
     args[3] = &g->nviews;
-    args[4] = &g->d_work;
+    args[4] = &g->kwork;
     const TraceVariant& v = kTraceVariants[variant];
     kp = cudaKernelNodeParams{};
     kp.func = const_cast<void*>(trace_kernel_fn(g->fmt, g->aniso, variant));
-    kp.gridDim = dim3(g->var[variant].blocks);
+    // per_sm 0: every warp tile of the batch gets its own warp (the hardware block scheduler balances the views;
+    // measured as fast as a persistent wave).  per_sm > 0: a persistent wave of per_sm CTAs per SM whose warps
+    // take tiles from the work counter, leaving the rest of each SM to other work.
+    const uint32_t warps = v.tw * v.th / 32;
+    g->kwork = g->per_sm ? g->d_work : nullptr;
+    kp.gridDim = dim3(g->per_sm ? g->var[variant].blocks : std::max<uint32_t>(1u, (g->tiles + warps - 1) / warps));
     kp.blockDim = dim3(v.tw * v.th);
     kp.sharedMemBytes = 0;
     kp.kernelParams = args;
@@ -242,7 +251,7 @@ int trace_graph_launch(TraceGraph* g, const TraceView* views, uint32_t nviews, u
     cudaError_t e = graph_variant(g, variant);
     if (e != cudaSuccess) return cuda_fail(e, "trace graph");
     TraceGraphVariant& gv = g->var[variant];
-    fill_table(views, nviews, variant, g->h_table);
+    g->tiles = fill_table(views, nviews, variant, g->h_table);
     g->nviews = nviews;
     g->kbase = reinterpret_cast<const uint32_t*>(g->d_table);
     g->kviews = reinterpret_cast<const TraceView*>(g->d_table + table_header(nviews));

@@ -390,47 +390,53 @@ __device__ void trace_pixel(const GridRef& g, const uint32_t* lut, const TraceCo
     store_out(v.out, v.out_format, npix + pi, sp);
 }
 
-// Tiles of TW x TH pixels of all views are numbered in view order (tile_base = per-view prefix).  A CTA traces
-// one tile at a time: blockIdx.x in the one-shot launch (work == nullptr), or tiles taken from a device work
-// counter in the persistent launch (one resident wave of CTAs that drains the whole batch, so views of different
-// size balance).  The tile shape and the CTAs resident per SM (MINB) are the variants the tuner picks from.
+// Work is handed out per warp: a warp tile is TW x (32 / TW) pixels, one lane each, and the warp tiles of all
+// views are numbered in view order (tile_base = per-view prefix).  In the one-shot launch (work == nullptr) warp
+// w of CTA b traces warp tile b * (TW * TH / 32) + w; in the persistent launch each warp takes tiles from a device
+// work counter until the batch is drained (one resident wave of CTAs, so views of different size balance).  A
+// warp never waits for the other warps of its CTA: the only CTA barrier is the staging of the tables at the
+// start.  The CTA shape and the CTAs resident per SM (MINB) are the variants the tuner picks from.
 template <int FMT, bool ANISO, int TW, int TH, int MINB, bool COUNT = false>
 __global__ void __launch_bounds__(TW * TH, MINB) trace_kernel(TraceConsts tc, const TraceView* __restrict__ views,
                                                              const uint32_t* __restrict__ tile_base, uint32_t nviews,
                                                              uint32_t* work) {
+    constexpr int kWarps = TW * TH / 32, WW = TW, WH = 32 / TW;
+    static_assert(TW * TH % 32 == 0 && 32 % TW == 0, "warp tiles of 32 pixels");
     uint32_t cnt[2] = {0u, 0u};  // COUNT only: this thread's steps and level samples
-    __shared__ GridRef g;
+    __shared__ GridRef gs[kWarps];  // the grid of each warp's current view
     __shared__ uint32_t s_lut[3 * kLut];
-    __shared__ uint32_t s_tile, s_view;
     __shared__ SchedEntry s_sched[kDiffuseSched];  // read by every lane at the same step: broadcast
     for (uint32_t i = threadIdx.x; i < 3 * kLut; i += TW * TH) s_lut[i] = part1by2(i % kLut) << (9 + i / kLut);
     if (threadIdx.x == 0) {  // constant indices: the schedule is read straight from the parameter bank
 #pragma unroll
         for (uint32_t i = 0; i < kDiffuseSched; ++i) s_sched[i] = tc.sched[i];
     }
+    __syncthreads();
+    const uint32_t lane = threadIdx.x & 31u, wid = threadIdx.x >> 5;
+    GridRef& g = gs[wid];
     const uint32_t ntiles = tile_base[nviews];
     uint32_t cur_view = 0xffffffffu;
     for (uint32_t it = 0;; ++it) {
-        if (threadIdx.x == 0) {
-            uint32_t tile = work ? atomicAdd(work, 1u) : (it == 0 ? blockIdx.x : ntiles);
+        uint32_t tile = 0, vi = 0;
+        if (lane == 0) {
+            tile = work ? atomicAdd(work, 1u) : (it == 0 ? blockIdx.x * kWarps + wid : ntiles);
             uint32_t lo = 0, hi = nviews;  // last view with tile_base[v] <= tile
             while (hi - lo > 1) {
                 uint32_t mid = (lo + hi) / 2;
                 if (tile_base[mid] <= tile) lo = mid; else hi = mid;
             }
-            s_tile = tile;
-            s_view = lo;
+            vi = lo;
         }
-        __syncthreads();
-        const uint32_t tile = s_tile, vi = s_view;
+        tile = __shfl_sync(0xffffffffu, tile, 0);
+        vi = __shfl_sync(0xffffffffu, vi, 0);
         if (tile >= ntiles) return;
         const TraceView& v = views[vi];
         if (vi != cur_view) {  // stage the view's grid description
-            if (threadIdx.x < kMaxLevels) {
-                g.off[threadIdx.x] = uint32_t(v.off[threadIdx.x]);
-                g.vol[threadIdx.x] = uint32_t(v.vol[threadIdx.x]);
+            if (lane < kMaxLevels) {
+                g.off[lane] = uint32_t(v.off[lane]);
+                g.vol[lane] = uint32_t(v.vol[lane]);
             }
-            if (threadIdx.x == 0) {
+            if (lane == 0) {
                 g.base = v.grid_base;
                 g.dim = v.grid_dim;
                 g.levels = v.grid_levels;
@@ -440,22 +446,22 @@ __global__ void __launch_bounds__(TW * TH, MINB) trace_kernel(TraceConsts tc, co
                 g.inv_vs = float(v.frame->inv_voxel_fixed * (1.0 / 256.0));
             }
             cur_view = vi;
-            __syncthreads();
+            __syncwarp();
         }
         const uint32_t local = tile - tile_base[vi];
-        const uint32_t tiles_x = (v.width + TW - 1) / TW;
-        const uint32_t px = (local % tiles_x) * TW + (threadIdx.x % TW);
-        const uint32_t py = (local / tiles_x) * TH + (threadIdx.x / TW);
+        const uint32_t tiles_x = (v.width + WW - 1) / WW;
+        const uint32_t px = (local % tiles_x) * WW + (lane % WW);
+        const uint32_t py = (local / tiles_x) * WH + (lane / WW);
         if (px < v.width && py < v.height) trace_pixel<FMT, ANISO, COUNT>(g, s_lut, tc, v, px, py, s_sched, cnt);
         if constexpr (COUNT) {  // warp totals, one atomic per warp and counter
             const unsigned long long a = __reduce_add_sync(0xffffffffu, cnt[0]), b = __reduce_add_sync(0xffffffffu, cnt[1]);
-            if ((threadIdx.x & 31u) == 0u) {
+            if (lane == 0u) {
                 atomicAdd(&tc.counts[0], a);
                 atomicAdd(&tc.counts[1], b);
             }
             cnt[0] = cnt[1] = 0u;
         }
-        __syncthreads();  // s_tile / g are rewritten for the next tile
+        __syncwarp();  // g may be restaged for the next tile
     }
 }
 

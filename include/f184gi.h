@@ -273,7 +273,7 @@ int f184gi_sync(f184gi_ctx* ctx, void* stream);
  * requests (rigid object moves + a set of views) queue on the host; whenever one of `slots` in-flight batches
  * is free, the scheduler admits pending requests (one per scene per batch, HBM budget for their staging
  * buffers, at most max_batch_views views), re-voxelizes the moved objects' bricks, relights and rebuilds the
- * mips of each touched scene, and traces every view of the batch in one persistent launch replayed from a CUDA
+ * mips of each touched scene, and traces every view of the batch in one launch replayed from a CUDA
  * graph.  Requests that arrive while batches run join the next batch; batches on different slots overlap.
  * Results are the same as running each request alone (per scene, requests apply in submission order). */
 typedef struct f184gi_server f184gi_server;
@@ -282,7 +282,7 @@ typedef struct f184gi_server_config {
     int device;
     uint32_t slots;           /* batches in flight (1..4, 0 = 2) */
     uint32_t max_batch_views; /* views per batched launch (0 = 64) */
-    uint32_t blocks_per_sm;   /* persistent trace CTAs per SM (0 = occupancy maximum) */
+    uint32_t blocks_per_sm;   /* 0: one trace warp per 32-pixel tile; k: a persistent wave of k CTAs per SM */
     uint64_t hbm_budget;      /* bytes for resident scenes + request staging (0 = no limit) */
     f184gi_cone_params cone;  /* cone parameters for every request (diffuse_cones == 0: defaults) */
     uint32_t trace_variant;   /* 0 = tune the cone-trace kernel variant on the first batch; k = use variant k-1 */

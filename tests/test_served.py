@@ -159,7 +159,8 @@ def test_dirty_updates_equal_full_voxelization(fx):
 
 @pytest.mark.gpu
 def test_every_trace_variant_matches_the_plain_path(fx):
-    """Each cone-trace kernel variant (tile shape, CTAs per SM) gives the plain one-shot launch's bytes."""
+    """Each cone-trace kernel variant (tile shape, CTAs per SM), launched with a warp per tile or as a capped
+    persistent wave, gives the plain one-shot launch's bytes."""
     g, torch = fx.g, fx.torch
     si, vids = 2, [0, 1, 2, 3]
     sc = fx.scenes[si]
@@ -183,13 +184,14 @@ def test_every_trace_variant_matches_the_plain_path(fx):
     for a, b in zip(ref, outs):
         assert np.array_equal(a.view(np.uint32), b.cpu().numpy().view(np.uint32))
     for k in range(st.trace_variants):
-        srv = fx.server(slots=1, trace_variant=k)
-        views, outs = fx.make_views(si, vids)
-        srv.wait(srv.submit(si, views, []))
-        assert srv.stats().trace_variant == k
-        srv.close()
-        for a, b in zip(ref, outs):
-            assert np.array_equal(a.view(np.uint32), b.cpu().numpy().view(np.uint32)), k
+        for per_sm in (0, 2):  # one warp per tile, or a persistent wave of 2 CTAs per SM on a work counter
+            srv = fx.server(slots=1, trace_variant=k, blocks_per_sm=per_sm)
+            views, outs = fx.make_views(si, vids)
+            srv.wait(srv.submit(si, views, []))
+            assert srv.stats().trace_variant == k
+            srv.close()
+            for a, b in zip(ref, outs):
+                assert np.array_equal(a.view(np.uint32), b.cpu().numpy().view(np.uint32)), (k, per_sm)
 
 
 @pytest.mark.gpu
