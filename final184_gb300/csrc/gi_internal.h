@@ -83,13 +83,12 @@ int relight_launch(const float4* weights, const f184gi_grid_frame* d_frame, cons
 size_t voxelize_scratch_bytes(uint64_t ntris, uint32_t dim);
 // Two phases: the triangle setup and (triangle, brick) lists, which do not read the shadow map, then the bricks
 // (coverage, injection through the shadow map, L0 written).  The lists phase may run on another stream beside
-// the shadow raster; the bricks phase must follow both.  voxelize_launch runs them one after the other on s.
+// the shadow raster; the bricks phase must follow both (with resident weights it reads no shadow map and may
+// follow the lists alone).
 int voxelize_lists_launch(const VoxelizeJob& job, void* scratch, size_t scratch_bytes, uint32_t* d_status,
                           cudaStream_t s);
 int voxelize_bricks_launch(const VoxelizeJob& job, void* scratch, size_t scratch_bytes, uint32_t* d_status,
                            cudaStream_t s);
-int voxelize_launch(const VoxelizeJob& job, void* scratch, size_t scratch_bytes, uint32_t* d_status,
-                    cudaStream_t s);
 
 // device-side frame from bounds (or from the triangles' AABB when bounds == nullptr)
 int frame_launch(const float* tri, uint64_t ntris, const f184gi_bounds* bounds, uint32_t dim,

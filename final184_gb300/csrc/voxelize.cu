@@ -586,10 +586,6 @@ int voxelize_bricks_launch(const VoxelizeJob& job, void* scratch, size_t scratch
     return cuda_fail(cudaGetLastError(), "voxelize");
 }
 
-int voxelize_launch(const VoxelizeJob& job, void* scratch, size_t scratch_bytes, uint32_t* d_status, cudaStream_t s) {
-    int rc = voxelize_lists_launch(job, scratch, scratch_bytes, d_status, s);
-    return rc ? rc : voxelize_bricks_launch(job, scratch, scratch_bytes, d_status, s);
-}
 
 }  // namespace f184
 
