@@ -199,9 +199,25 @@ __global__ void __launch_bounds__(128) vox_setup(const float* __restrict__ tri, 
         float3 a = make_float3(p[3] - p[0], p[4] - p[1], p[5] - p[2]);
         float3 b = make_float3(p[6] - p[0], p[7] - p[1], p[8] - p[2]);
         float3 n = make_float3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
-        float len = sqrtf(n.x * n.x + n.y * n.y + n.z * n.z);
+        const float nn = n.x * n.x + n.y * n.y + n.z * n.z;
         float wi0 = -float(fr->light_dir[0]), wi1 = -float(fr->light_dir[1]), wi2 = -float(fr->light_dir[2]);
-        float cosv = len > 0.0f ? fabsf(wi0 * n.x + wi1 * n.y + wi2 * n.z) / len : 0.0f;
+        float cosv;
+        if (nn >= 0x1p-20f * (a.x * a.x + a.y * a.y + a.z * a.z) * (b.x * b.x + b.y * b.y + b.z * b.z)) {
+            // the edges are more than ~0.06 degrees apart: the FP32 normal's direction is good to ~1e-4
+            const float len = sqrtf(nn);
+            cosv = len > 0.0f ? fabsf(wi0 * n.x + wi1 * n.y + wi2 * n.z) / len : 0.0f;
+        } else {
+            // a sliver: its FP32 cross product is mostly rounding, so the normal is formed in FP64 from the
+            // FP32 positions (the oracle's sequence: edge differences, cross, |n|, |dot(-L, n)| / |n|)
+            const double ax = dsub(p[3], p[0]), ay = dsub(p[4], p[1]), az = dsub(p[5], p[2]);
+            const double bx = dsub(p[6], p[0]), by = dsub(p[7], p[1]), bz = dsub(p[8], p[2]);
+            const double nx = dsub(dmul(ay, bz), dmul(az, by)), ny = dsub(dmul(az, bx), dmul(ax, bz)),
+                         nz = dsub(dmul(ax, by), dmul(ay, bx));
+            const double len = __dsqrt_rn(dadd(dadd(dmul(nx, nx), dmul(ny, ny)), dmul(nz, nz)));
+            const double d = dadd(dadd(dmul(-fr->light_dir[0], nx), dmul(-fr->light_dir[1], ny)),
+                                  dmul(-fr->light_dir[2], nz));
+            cosv = len > 0.0 ? float(__ddiv_rn(fabs(d), len)) : 0.0f;
+        }
         uint32_t al = albedo[t];
         for (int c = 0; c < 3; ++c) {
             float w = cosv * c_albedo_lut[(al >> (8 * c)) & 255u];

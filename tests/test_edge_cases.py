@@ -1,0 +1,176 @@
+"""Edge cases of the CUDA path against the oracle (run on a GPU).
+
+- ragged views (1x1, sizes that are not multiples of any warp tile) traced together in one call: each equals the
+  same view traced alone, byte for byte, and the oracle within REL_TOL;
+- a view with no geometry (every depth at the far plane) traces to exact zeros;
+- an empty scene (no triangles, explicit bounds): far shadow map, empty grid, zero image;
+- degenerate triangles (repeated vertices, collinear) and triangles partly or wholly outside the grid: shadow map,
+  occupancy and counts bit-exact against the oracle;
+- cone parameters off the defaults, including diffuse cones narrow enough that their marches run past the
+  per-launch schedule table into the device recurrence: within REL_TOL of the oracle.
+"""
+import numpy as np
+import pytest
+
+from gi_case import REL_TOL, Case, rel_err
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def case(lib):
+    c = Case()
+    c.voxelize()
+    c.mip()
+    c.gbuffer()
+    return c
+
+
+@pytest.fixture(scope="module")
+def oracle_chain(case, orc):
+    fo = case.oracle_frame()
+    sd = orc.shadow_depth(orc.raster(orc.frame_matrix(fo), case.res, case.res, case.sc.tri_xyz))
+    l0, _ = orc.voxelize(fo, case.dim, case.res, case.sc.tri_xyz, case.sc.albedo, case.oracle_light(), sd)
+    chain, _ = orc.mip(l0, case.levels)
+    return fo, chain
+
+
+def make_view(case, W, H):
+    """A device G-buffer of the case's camera at W x H and an output buffer."""
+    g, torch = case.g, case.torch
+    P = g.perspective(59.0, W / H, 0.1, 100.0)
+    n = W * H
+    bufs = (torch.empty(n, dtype=torch.float32, device=case.dev), torch.empty(n, dtype=torch.int32, device=case.dev),
+            torch.empty(n, dtype=torch.int16, device=case.dev), torch.zeros(2 * n * 4, dtype=torch.float32, device=case.dev))
+    view = g.make_view(case.V, P, W, H, bufs[0].data_ptr(), bufs[1].data_ptr(), bufs[2].data_ptr(), bufs[3].data_ptr())
+    case.gi.gbuffer(case.tri_d.data_ptr(), case.rough_d.data_ptr(), case.ntris, view)
+    case.gi.sync()
+    return view, P, bufs
+
+
+def host_gbuffer(bufs, W, H):
+    return (bufs[0].cpu().numpy().reshape(H, W), bufs[1].cpu().numpy().view(np.uint32).reshape(H, W),
+            bufs[2].cpu().numpy().view(np.uint16).reshape(H, W))
+
+
+SIZES = [(1, 1), (37, 23), (129, 7), (8, 4), (31, 33)]
+
+
+def test_ragged_views_one_call_equal_alone_and_oracle(case, orc, oracle_chain):
+    fo, chain = oracle_chain
+    made = [make_view(case, W, H) for W, H in SIZES]
+    case.gi.trace(case.grid, [m[0] for m in made])
+    case.gi.sync()
+    together = [m[2][3].cpu().numpy().copy() for m in made]
+    for (W, H), (view, P, bufs), got in zip(SIZES, made, together):
+        bufs[3].zero_()
+        case.gi.trace(case.grid, [view])
+        case.gi.sync()
+        alone = bufs[3].cpu().numpy()
+        assert np.array_equal(alone.view(np.uint32), got.view(np.uint32)), (W, H)
+        dep, nrm, rgh = host_gbuffer(bufs, W, H)
+        ref = orc.trace(fo, case.dim, case.levels, chain, case.V, P, W, H, dep, nrm, rgh)
+        mx, _ = rel_err(got.reshape(2, H, W, 4), ref)
+        assert mx < REL_TOL, (W, H, mx)
+
+
+def test_view_without_geometry_traces_to_zero(case):
+    view, P, bufs = make_view(case, 64, 48)
+    bufs[0].fill_(1.0)  # every pixel at the far plane
+    bufs[3].fill_(7.0)
+    case.gi.trace(case.grid, [view])
+    case.gi.sync()
+    assert not bufs[3].any()
+
+
+def test_empty_scene(lib, orc):
+    import torch
+
+    import final184_gb300 as g
+
+    dim, levels, res, W, H = 32, 5, 256, 48, 32
+    gi = g.VoxelGI(0)
+    grid = gi.create_grid(dim, levels, g.FMT_F32, 0, res, g.GRID_KEEP_COUNTS)
+    light = g.make_light([4.4, 3.7, 3.2], [0.3, -0.8, 0.2])
+    bounds = g.make_bounds((-5, -5, -5), (5, 5, 5))
+    dummy = torch.zeros(9, dtype=torch.float32, device="cuda:0")
+    gi.voxelize(grid, dummy.data_ptr(), dummy.data_ptr(), 0, light, bounds=bounds)
+    gi.mip(grid)
+    gi.sync()
+    fo = orc.grid_frame(orc.make_bounds((-5, -5, -5), (5, 5, 5)), dim, np.array(light.direction, np.float32))
+    sd = orc.shadow_depth(orc.raster(orc.frame_matrix(fo), res, res, np.zeros(0, np.float32)))
+    assert np.array_equal(gi.read_shadow(grid).view(np.uint32), sd.view(np.uint32))
+    assert not gi.read_counts(grid).any()
+    for lv in range(levels):
+        assert not gi.read_level(grid, lv).any()
+    n = W * H
+    depth = torch.full((n,), 0.5, dtype=torch.float32, device="cuda:0")
+    normal = torch.zeros(n, dtype=torch.int32, device="cuda:0")  # octahedral (0, 0): +z
+    rgh = torch.zeros(n, dtype=torch.int16, device="cuda:0")
+    out = torch.full((2 * n * 4,), 3.0, dtype=torch.float32, device="cuda:0")
+    V = g.look_at([0, 0, 8], [0, 0, 0])
+    view = g.make_view(V, g.perspective(59.0, W / H, 0.1, 100.0), W, H, depth.data_ptr(), normal.data_ptr(),
+                       rgh.data_ptr(), out.data_ptr())
+    gi.trace(grid, [view])
+    gi.sync()
+    assert not out.any()
+    gi.close()
+
+
+def test_degenerate_and_outside_triangles_bit_exact(lib, orc):
+    c = Case(seed=31, ntris=4000, nobj=40, dim=64, levels=6, res=512, width=64, height=36)
+    rng = np.random.default_rng(9)
+    base = c.sc.tri_xyz.reshape(-1, 3, 3)
+    extra = []
+    for k in range(300):
+        t = base[rng.integers(0, len(base))].copy()
+        kind = k % 5
+        if kind == 0:
+            t[1] = t[0]  # two equal vertices
+        elif kind == 1:
+            t[2] = 0.5 * (t[0] + t[1])  # collinear
+        elif kind == 2:
+            t[:] = t[0]  # a point
+        elif kind == 3:
+            t += np.float32(rng.uniform(8, 30)) * np.sign(rng.normal(size=3)).astype(np.float32)  # partly / wholly out
+        else:
+            t *= np.float32(3.0)  # stretched across and beyond the grid
+        extra.append(t)
+    tri = np.concatenate([base, np.asarray(extra, np.float32)]).astype(np.float32).ravel()
+    alb = np.concatenate([c.sc.albedo, rng.integers(0, 2 ** 32, len(extra), dtype=np.uint64).astype(np.uint32)])
+    c.upload(tri, alb)
+    c.voxelize()
+    fo = c.oracle_frame()
+    sd = orc.shadow_depth(orc.raster(orc.frame_matrix(fo), c.res, c.res, tri))
+    assert np.array_equal(c.gi.read_shadow(c.grid).view(np.uint32), sd.view(np.uint32))
+    l0, cnt = orc.voxelize(fo, c.dim, c.res, tri, alb, c.oracle_light(), sd)
+    assert np.array_equal(c.gi.read_counts(c.grid), cnt.astype(np.uint32))
+    got = c.gi.read_level(c.grid, 0)
+    assert np.array_equal(got[..., 3] > 0, l0[..., 3] > 0)
+    mx, _ = rel_err(got, l0)
+    assert mx < REL_TOL
+
+
+@pytest.mark.parametrize("kw", [
+    dict(diffuse_tan_half=0.08),  # narrow diffuse cones: ~50 steps, past the 24-step schedule table
+    dict(diffuse_cones=1, specular=0),
+    dict(max_distance=20.0, step_factor=1.0, start_offset=2.0),
+    dict(diffuse_tilt_deg=30.0, min_spec_tan_half=0.2),
+])
+def test_cone_parameters_against_oracle(case, orc, oracle_chain, kw):
+    import final184_gb300 as g
+
+    fo, chain = oracle_chain
+    p = g.default_cone_params()
+    q = orc.default_params()
+    for k, v in kw.items():
+        setattr(p, k, v)
+        setattr(q, k, v)
+    got = case.trace(p)
+    dep, nrm, rgh, _ = case.gbuffer_host()
+    ref = orc.trace(fo, case.dim, case.levels, chain, case.V, case.P, case.W, case.H, dep, nrm, rgh, params=q)
+    mx, rms = rel_err(got, ref)
+    print(kw, "rel err max %.3g rms %.3g" % (mx, rms))
+    assert mx < REL_TOL
+    if kw.get("specular", 1) == 0:
+        assert not got[1].any()
