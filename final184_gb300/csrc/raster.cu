@@ -3,11 +3,14 @@
 // Replaces the fixed-function depth-only raster of the reference's shadow pass
 // (Foreground/Renderer/ZOnlyRenderer.cpp:79-114, StaticMeshZOnlyVS Pipelang/Internal/main.lua:146-156) and the
 // G-buffer pass (GBufferRenderer.cpp:79-116).  Coverage and depth are exact functions of the input:
-//   clip = M * (x, y, z, 1) in FP64, clipped to 0 <= z <= w and |x|,|y| <= 16 w (Sutherland-Hodgman, FP64),
-//   vertices snapped to 1/16 pixel, coverage by inclusive int64 edge functions at pixel centres,
-//   depth plane z0 + a (X - X0) + b (Y - Y0) solved in FP64 per triangle, rounded to FP32 and evaluated in FP32
-//   in that operation order; per pixel the minimum of key = (depth bits << 32 | triangle index) wins.
-// Per-fragment work is FP32/int only (the FP64 pipe of GB300 is narrow); FP64 is per vertex.
+//   clip = M * (x, y, z, 1) with M rounded to FP32, each product and sum rounded in order; a triangle inside
+//   0 <= z <= w, |x|,|y| <= 16 w is divided by w (skipped for w == 1) and snapped to 1/16 pixel in FP32; any
+//   other is clipped against those planes in FP64 (Sutherland-Hodgman on FP64 clip coordinates) and snapped in
+//   FP64; coverage by inclusive int64 edge functions at pixel centres; depth plane z0 + a (X - X0) + b (Y - Y0)
+//   solved in FP64 per triangle, rounded to FP32 and evaluated in FP32 in that operation order; per pixel the
+//   minimum of key = (depth bits << 32 | triangle index) wins.
+// Per-fragment work is FP32/int only and FP64 is left to the plane solve and to clipped triangles (the FP64
+// pipe of GB300 is narrow: an FP64 transform and snap of every triangle kept it 85% busy).
 // Work is binned into 16x16 pixel tiles (one CTA per tile, keys in shared memory).  Triangles spanning many
 // tiles are walked by a whole warp, so no thread serialises over a screen-sized triangle.
 #include "gi_device.cuh"
@@ -73,17 +76,10 @@ __device__ int clip_polygon(V4* poly, int n) {
 // x / w with the division skipped when w is exactly 1 (orthographic frames): x / 1 == x in IEEE arithmetic
 __device__ __forceinline__ double persp_div(double x, double w) { return w == 1.0 ? x : __ddiv_rn(x, w); }
 
-__device__ bool snap(const V4& a, const V4& b, const V4& c, uint32_t W, uint32_t H, uint32_t tri, SubTri& s) {
-    const V4* v[3] = {&a, &b, &c};
-    int64_t X[3], Y[3];
-    double Z[3];
-    for (int i = 0; i < 3; ++i) {
-        if (!(v[i]->w > 0.0)) return false;
-        double nx = persp_div(v[i]->x, v[i]->w), ny = persp_div(v[i]->y, v[i]->w), nz = persp_div(v[i]->z, v[i]->w);
-        X[i] = __double2ll_rn(dmul(dadd(nx, 1.0), 8.0 * double(W)));
-        Y[i] = __double2ll_rn(dmul(dadd(ny, 1.0), 8.0 * double(H)));
-        Z[i] = nz;
-    }
+// Snapped triangle from its vertices in 1/16 pixel (X, Y) and NDC depth Z: orientation, the depth plane through
+// the three (FP64 solve, FP32 result) and the pixel range.
+__device__ __forceinline__ bool snap_finish(int64_t (&X)[3], int64_t (&Y)[3], double (&Z)[3], uint32_t W, uint32_t H,
+                                            uint32_t tri, SubTri& s) {
     int64_t area2 = (X[1] - X[0]) * (Y[2] - Y[0]) - (Y[1] - Y[0]) * (X[2] - X[0]);
     if (area2 == 0) return false;
     if (area2 < 0) {
@@ -118,6 +114,50 @@ __device__ bool snap(const V4& a, const V4& b, const V4& c, uint32_t W, uint32_t
     s.tri = tri;
     s.x0 = uint16_t(x0), s.x1 = uint16_t(x1), s.y0 = uint16_t(y0), s.y1 = uint16_t(y1);
     return true;
+}
+
+// A clipped polygon's fan triangle (FP64 clip coordinates).
+__device__ bool snap(const V4& a, const V4& b, const V4& c, uint32_t W, uint32_t H, uint32_t tri, SubTri& s) {
+    const V4* v[3] = {&a, &b, &c};
+    int64_t X[3], Y[3];
+    double Z[3];
+    for (int i = 0; i < 3; ++i) {
+        if (!(v[i]->w > 0.0)) return false;
+        double nx = persp_div(v[i]->x, v[i]->w), ny = persp_div(v[i]->y, v[i]->w), nz = persp_div(v[i]->z, v[i]->w);
+        X[i] = __double2ll_rn(dmul(dadd(nx, 1.0), 8.0 * double(W)));
+        Y[i] = __double2ll_rn(dmul(dadd(ny, 1.0), 8.0 * double(H)));
+        Z[i] = nz;
+    }
+    return snap_finish(X, Y, Z, W, H, tri, s);
+}
+
+// The common case: a triangle inside the clip volume (0 <= z <= w, |x|, |y| <= 16 w), its clip coordinates in
+// FP32 (row . (x, y, z, 1) with the FP32-rounded matrix, each product and sum rounded in order), the perspective
+// division (skipped for w == 1) and the snap to 1/16 pixel in FP32.  FP64 is left to the plane solve.
+struct V4f {
+    float x, y, z, w;
+};
+__device__ __forceinline__ float frow(const float* r, float x, float y, float z) {
+    return __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(r[0], x), __fmul_rn(r[1], y)), __fmul_rn(r[2], z)), r[3]);
+}
+__device__ __forceinline__ bool inside_f(const V4f& v) {
+    const float g = __fmul_rn(16.0f, v.w);
+    return v.z >= 0.0f && __fsub_rn(v.w, v.z) >= 0.0f && __fsub_rn(g, v.x) >= 0.0f && __fadd_rn(v.x, g) >= 0.0f &&
+           __fsub_rn(g, v.y) >= 0.0f && __fadd_rn(v.y, g) >= 0.0f;
+}
+__device__ __forceinline__ float persp_div_f(float x, float w) { return w == 1.0f ? x : __fdiv_rn(x, w); }
+__device__ __forceinline__ bool snap_f(const V4f (&v)[3], uint32_t W, uint32_t H, uint32_t tri, SubTri& s) {
+    int64_t X[3], Y[3];
+    double Z[3];
+    const float sw = 8.0f * float(W), sh = 8.0f * float(H);  // exact: W, H <= 8192
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        if (!(v[i].w > 0.0f)) return false;
+        X[i] = __float2ll_rn(__fmul_rn(__fadd_rn(persp_div_f(v[i].x, v[i].w), 1.0f), sw));
+        Y[i] = __float2ll_rn(__fmul_rn(__fadd_rn(persp_div_f(v[i].y, v[i].w), 1.0f), sh));
+        Z[i] = double(persp_div_f(v[i].z, v[i].w));
+    }
+    return snap_finish(X, Y, Z, W, H, tri, s);
 }
 
 // Edge function of edge (a -> b) at fixed-point point (px, py).
@@ -155,34 +195,37 @@ struct RasterScratch {
     uint64_t ovf_cap;
 };
 
-__global__ void raster_setup(const float* __restrict__ tri, uint64_t ntris, RasterJob job, RasterScratch sc,
-                             uint32_t* status) {
+__global__ void __launch_bounds__(128) raster_setup(const float* __restrict__ tri, uint64_t ntris, RasterJob job,
+                                                    RasterScratch sc, uint32_t* status) {
+    const double* M = job.d_M ? job.d_M : job.M;
+    __shared__ float mf[16];
+    if (threadIdx.x < 16) mf[threadIdx.x] = __double2float_rn(M[threadIdx.x]);
+    __syncthreads();
     uint64_t t = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (t >= ntris) return;
-    const double* M = job.d_M ? job.d_M : job.M;
-    // an orthographic frame (last row 0 0 0 1, the shadow map's) gives w = ((0 x + 0 y) + 0 z) + 1 = 1 exactly:
-    // its row and the guard band's 16 w products are skipped, with the same values
-    const bool ortho = M[12] == 0.0 && M[13] == 0.0 && M[14] == 0.0 && M[15] == 1.0;
-    V4 poly[12];
+    V4f cf[3];
     bool inside = true;
+#pragma unroll
     for (int v = 0; v < 3; ++v) {
-        double x = tri[t * 9 + v * 3], y = tri[t * 9 + v * 3 + 1], z = tri[t * 9 + v * 3 + 2];
-        poly[v].x = drow(M, x, y, z);
-        poly[v].y = drow(M + 4, x, y, z);
-        poly[v].z = drow(M + 8, x, y, z);
-        poly[v].w = ortho ? 1.0 : drow(M + 12, x, y, z);
-        if (ortho) {
-            const V4& p = poly[v];
-            if (!(p.z >= 0.0 && dsub(1.0, p.z) >= 0.0 && dsub(kGuard, p.x) >= 0.0 && dadd(p.x, kGuard) >= 0.0 &&
-                  dsub(kGuard, p.y) >= 0.0 && dadd(p.y, kGuard) >= 0.0))
-                inside = false;
-        } else {
-            for (int k = 0; k < 6; ++k)
-                if (!(plane_dist(k, poly[v]) >= 0.0)) inside = false;
-        }
+        const float x = tri[t * 9 + v * 3], y = tri[t * 9 + v * 3 + 1], z = tri[t * 9 + v * 3 + 2];
+        cf[v] = V4f{frow(mf, x, y, z), frow(mf + 4, x, y, z), frow(mf + 8, x, y, z), frow(mf + 12, x, y, z)};
+        inside = inside && inside_f(cf[v]);
     }
-    int n = 3;
-    if (!inside) n = clip_polygon(poly, 3);
+    if (inside) {  // one sub-triangle, the record of the triangle itself
+        SubTri s;
+        if (snap_f(cf, job.width, job.height, uint32_t(t), s))
+            sc.recs[t] = s;
+        else
+            sc.recs[t].tri = kNone;
+        return;
+    }
+    // clipped against the near/far planes or the guard band: FP64 clip coordinates and Sutherland-Hodgman
+    V4 poly[12];
+    for (int v = 0; v < 3; ++v) {
+        const double x = tri[t * 9 + v * 3], y = tri[t * 9 + v * 3 + 1], z = tri[t * 9 + v * 3 + 2];
+        poly[v] = V4{drow(M, x, y, z), drow(M + 4, x, y, z), drow(M + 8, x, y, z), drow(M + 12, x, y, z)};
+    }
+    const int n = clip_polygon(poly, 3);
     bool primary_done = false;
     for (int i = 1; i + 1 < n; ++i) {
         SubTri s;

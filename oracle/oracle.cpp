@@ -131,15 +131,8 @@ struct SnapTri {
     int64_t x0, x1, y0, y1;  // pixel range, inclusive
 };
 
-bool snap_tri(const V4& a, const V4& b, const V4& c, uint32_t W, uint32_t H, SnapTri& s) {
-    const V4* v[3] = {&a, &b, &c};
-    for (int i = 0; i < 3; ++i) {
-        if (!(v[i]->w > 0.0)) return false;
-        double nx = v[i]->x / v[i]->w, ny = v[i]->y / v[i]->w, nz = v[i]->z / v[i]->w;
-        s.X[i] = std::llrint((nx + 1.0) * (8.0 * double(W)));
-        s.Y[i] = std::llrint((ny + 1.0) * (8.0 * double(H)));
-        s.Z[i] = nz;
-    }
+// orientation, FP64 depth plane (rounded to FP32) and pixel range of a triangle already snapped to X, Y, Z
+bool snap_finish(SnapTri& s, uint32_t W, uint32_t H) {
     int64_t area2 = (s.X[1] - s.X[0]) * (s.Y[2] - s.Y[0]) - (s.Y[1] - s.Y[0]) * (s.X[2] - s.X[0]);
     if (area2 == 0) return false;
     if (area2 < 0) {
@@ -170,6 +163,50 @@ bool snap_tri(const V4& a, const V4& b, const V4& c, uint32_t W, uint32_t H, Sna
     s.y0 = std::max<int64_t>(0, -floor_div(-(mny - 8), 16));
     s.y1 = std::min<int64_t>(int64_t(H) - 1, floor_div(mxy - 8, 16));
     return s.x0 <= s.x1 && s.y0 <= s.y1;
+}
+
+// a clipped polygon's fan triangle, FP64 clip coordinates
+bool snap_tri(const V4& a, const V4& b, const V4& c, uint32_t W, uint32_t H, SnapTri& s) {
+    const V4* v[3] = {&a, &b, &c};
+    for (int i = 0; i < 3; ++i) {
+        if (!(v[i]->w > 0.0)) return false;
+        double nx = v[i]->x / v[i]->w, ny = v[i]->y / v[i]->w, nz = v[i]->z / v[i]->w;
+        s.X[i] = std::llrint((nx + 1.0) * (8.0 * double(W)));
+        s.Y[i] = std::llrint((ny + 1.0) * (8.0 * double(H)));
+        s.Z[i] = nz;
+    }
+    return snap_finish(s, W, H);
+}
+
+// The common case, a triangle inside the clip volume: clip coordinates in FP32 with the FP32-rounded matrix
+// (each product and sum rounded in order), division by w unless w == 1, snap in FP32; FP64 only in the plane.
+struct V4f {
+    float x, y, z, w;
+};
+inline float frow(const float* r, float x, float y, float z) {
+    float a = r[0] * x;
+    float b = r[1] * y;
+    float c = r[2] * z;
+    float t = a + b;
+    t = t + c;
+    return t + r[3];
+}
+inline bool inside_f(const V4f& v) {
+    const float g = 16.0f * v.w;
+    return v.z >= 0.0f && v.w - v.z >= 0.0f && g - v.x >= 0.0f && v.x + g >= 0.0f && g - v.y >= 0.0f &&
+           v.y + g >= 0.0f;
+}
+inline float persp_div_f(float x, float w) { return w == 1.0f ? x : x / w; }
+bool snap_tri_f(const V4f v[3], uint32_t W, uint32_t H, SnapTri& s) {
+    const float sw = 8.0f * float(W), sh = 8.0f * float(H);
+    for (int i = 0; i < 3; ++i) {
+        if (!(v[i].w > 0.0f)) return false;
+        const float nx = persp_div_f(v[i].x, v[i].w) + 1.0f, ny = persp_div_f(v[i].y, v[i].w) + 1.0f;
+        s.X[i] = std::llrint(nx * sw);
+        s.Y[i] = std::llrint(ny * sh);
+        s.Z[i] = double(persp_div_f(v[i].z, v[i].w));
+    }
+    return snap_finish(s, W, H);
 }
 
 void raster_tri(const SnapTri& s, uint32_t tri, uint32_t W, int64_t row_lo, int64_t row_hi, uint64_t* keys) {
@@ -909,18 +946,31 @@ int orc_raster(const double M[16], uint32_t W, uint32_t H, const float* tri, uin
     // snap every triangle once, then rasterize row slabs in parallel
     std::vector<uint32_t> owner;
     std::vector<SnapTri> all;
+    float mf[16];
+    for (int i = 0; i < 16; ++i) mf[i] = float(M[i]);
     for (uint64_t t = 0; t < ntris; ++t) {
         const float* p = tri + t * 9;
-        V4 poly[12];
+        V4f cf[3];
         bool inside = true;
+        for (int v = 0; v < 3; ++v) {
+            const float x = p[v * 3], y = p[v * 3 + 1], z = p[v * 3 + 2];
+            cf[v] = {frow(mf, x, y, z), frow(mf + 4, x, y, z), frow(mf + 8, x, y, z), frow(mf + 12, x, y, z)};
+            inside = inside && inside_f(cf[v]);
+        }
+        if (inside) {
+            SnapTri s;
+            if (snap_tri_f(cf, W, H, s)) {
+                all.push_back(s);
+                owner.push_back(uint32_t(t));
+            }
+            continue;
+        }
+        V4 poly[12];
         for (int v = 0; v < 3; ++v) {
             double x = p[v * 3], y = p[v * 3 + 1], z = p[v * 3 + 2];
             poly[v] = {mrow(M, x, y, z), mrow(M + 4, x, y, z), mrow(M + 8, x, y, z), mrow(M + 12, x, y, z)};
-            for (int k = 0; k < 6; ++k)
-                if (!(plane_dist(k, poly[v]) >= 0.0)) inside = false;
         }
-        int n = 3;
-        if (!inside) n = clip_polygon(poly, 3);
+        const int n = clip_polygon(poly, 3);
         for (int i = 1; i + 1 < n; ++i) {
             SnapTri s;
             if (snap_tri(poly[0], poly[i], poly[i + 1], W, H, s)) {
