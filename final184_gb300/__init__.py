@@ -235,6 +235,10 @@ class VoxelGI:
     def sync(self, stream=None):
         check(self.lib.f184gi_sync(self.ctx, _stream(stream)))
 
+    def selftest_bounded_wait(self, polls, complete, stream=None):
+        """One bounded device wait that expires unless `complete`; the expiry surfaces at the next sync()."""
+        check(self.lib.f184gi_selftest_bounded_wait(self.ctx, polls, 1 if complete else 0, _stream(stream)))
+
     def frame(self, grid):
         f = GridFrame()
         check(self.lib.f184gi_grid_get_frame(self.ctx, grid.handle, C.byref(f)))

@@ -129,6 +129,7 @@ PROTOTYPES = {
     "f184gi_voxelize": (C.c_int, [P, U32, P, P, U64, C.POINTER(Bounds), C.POINTER(Light), P, U32, P]),
     "f184gi_mip": (C.c_int, [P, U32, U32, U32, P]),
     "f184gi_trace": (C.c_int, [P, U32, C.POINTER(View), U32, C.POINTER(ConeParams), P]),
+    "f184gi_selftest_bounded_wait": (C.c_int, [P, U32, U32, P]),
     "f184gi_trace_count": (C.c_int, [P, U32, C.POINTER(View), U32, C.POINTER(ConeParams), C.POINTER(C.c_uint64), P]),
     "f184gi_cone_params_default": (None, [C.POINTER(ConeParams)]),
     "f184gi_gbuffer": (C.c_int, [P, P, P, U64, C.POINTER(View), P, P]),

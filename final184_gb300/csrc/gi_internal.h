@@ -90,6 +90,9 @@ int voxelize_lists_launch(const VoxelizeJob& job, void* scratch, size_t scratch_
 int voxelize_bricks_launch(const VoxelizeJob& job, void* scratch, size_t scratch_bytes, uint32_t* d_status,
                            cudaStream_t s);
 
+// one bounded mbarrier wait that expires unless `complete` (the failure path of bounded device waits, on demand)
+int bounded_wait_selftest_launch(uint32_t polls, uint32_t complete, uint32_t* status, cudaStream_t s);
+
 // device-side frame from bounds (or from the triangles' AABB when bounds == nullptr)
 int frame_launch(const float* tri, uint64_t ntris, const f184gi_bounds* bounds, uint32_t dim,
                  const float light_dir[3], f184gi_grid_frame* d_frame, void* scratch, cudaStream_t s);

@@ -244,6 +244,28 @@ __global__ void moves_kernel(float* __restrict__ tri, MoveTable t) {
 }
 }  // namespace
 
+namespace {
+// One bounded wait on a shared-memory mbarrier whose phase completes only if `complete` (one arrival); on expiry
+// the status word gets the timeout bit, as the library's own bounded waits (the mip pass's bulk-copy wait) do.
+__global__ void bounded_wait_selftest(uint32_t polls, uint32_t complete, uint32_t* status) {
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        fence_barrier_init();
+    }
+    __syncthreads();
+    if (complete && threadIdx.x == 0) mbar_arrive(&bar);
+    const bool done = mbar_wait_bounded(&bar, 0, polls);
+    if (!done && threadIdx.x == 0) set_status(status, kStatusTimeout);
+}
+}  // namespace
+
+int bounded_wait_selftest_launch(uint32_t polls, uint32_t complete, uint32_t* status, cudaStream_t s) {
+    bounded_wait_selftest<<<1, 32, 0, s>>>(polls, complete, status);
+    note_launches(1);
+    return cuda_fail(cudaGetLastError(), "bounded wait self-test");
+}
+
 int moves_launch(float* tri, const f184gi_move* moves, uint32_t nmoves, cudaStream_t s) {
     for (uint32_t b = 0; b < nmoves; b += kMovesPerLaunch) {
         MoveTable t{};

@@ -156,6 +156,11 @@ const char* f184gi_last_error(void);
 int f184gi_abi_version(void);
 /* number of kernels this library has launched in this process (diagnostics) */
 uint64_t f184gi_kernel_launches(void);
+/* Diagnostic, with no counterpart in the reference: one device wait on a shared-memory mbarrier, bounded to
+ * `polls` polls (1..2^24), whose phase completes only when `complete` is nonzero.  An expired wait is recorded in
+ * the context's status exactly as the library's own bounded waits record theirs, so the next f184gi_sync returns
+ * F184GI_ERR_TIMEOUT and the context stays usable: the failure path, exercised without a GPU fault. */
+int f184gi_selftest_bounded_wait(f184gi_ctx* ctx, uint32_t polls, uint32_t complete, void* stream);
 int f184gi_create(const f184gi_config* cfg, f184gi_ctx** out);
 int f184gi_destroy(f184gi_ctx* ctx);
 /* bytes currently held on the device by the context */

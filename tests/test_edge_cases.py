@@ -7,7 +7,9 @@
 - degenerate triangles (repeated vertices, collinear) and triangles partly or wholly outside the grid: shadow map,
   occupancy and counts bit-exact against the oracle;
 - cone parameters off the defaults, including diffuse cones narrow enough that their marches run past the
-  per-launch schedule table into the device recurrence: within REL_TOL of the oracle.
+  per-launch schedule table into the device recurrence: within REL_TOL of the oracle;
+- a bounded device wait that expires is reported as F184GI_ERR_TIMEOUT by the next sync, and the context goes on
+  working (the failure path of the library's bounded waits, without a GPU fault).
 """
 import numpy as np
 import pytest
@@ -174,3 +176,18 @@ def test_cone_parameters_against_oracle(case, orc, oracle_chain, kw):
     assert mx < REL_TOL
     if kw.get("specular", 1) == 0:
         assert not got[1].any()
+
+
+def test_expired_bounded_wait_is_reported_and_the_context_stays_usable(case):
+    from final184_gb300 import _abi
+
+    before = case.trace().copy()
+    case.gi.selftest_bounded_wait(1000, complete=True)
+    case.gi.sync()  # a completed wait leaves no status
+    case.gi.selftest_bounded_wait(1000, complete=False)
+    with pytest.raises(_abi.F184Error) as err:
+        case.gi.sync()
+    assert err.value.code == _abi.ERR_TIMEOUT and "bounded device wait" in str(err.value)
+    case.gi.sync()  # the status was consumed by the report
+    after = case.trace()
+    assert np.array_equal(before.view(np.uint32), after.view(np.uint32))
