@@ -23,6 +23,7 @@ constexpr int kTile = 16;
 constexpr double kGuard = 16.0;
 constexpr uint32_t kNone = 0xffffffffu;
 constexpr int kBigCells = 8;  // records touching more tiles than this are binned by a whole CTA
+constexpr uint32_t kStage = 256;  // records staged per round by raster_tiles (one per thread)
 
 struct SubTri {
     int32_t X[3], Y[3];
@@ -306,29 +307,37 @@ __global__ void __launch_bounds__(256) raster_tiles(RasterScratch sc, uint32_t t
     const uint32_t beg = sc.tile_start[tile], cnt = sc.tile_count[tile];
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t end = uint32_t(min(uint64_t(beg) + cnt, sc.list_cap));
-    for (uint32_t it = beg + warp; it < end; it += 8) {
-        const SubTri s = sc.recs[sc.list[it]];
-        int x0 = max(int(s.x0), tx * kTile), x1 = min(int(s.x1), tx * kTile + kTile - 1);
-        int y0 = max(int(s.y0), ty * kTile), y1 = min(int(s.y1), ty * kTile + kTile - 1);
-        if (x0 > x1 || y0 > y1) continue;
-        int w = x1 - x0 + 1, npx = w * (y1 - y0 + 1);
-        for (int p = int(lane); p < npx; p += 32) {
-            int px = x0 + p % w, py = y0 + p / w;
-            int64_t Px = int64_t(px) * 16 + 8, Py = int64_t(py) * 16 + 8;
-            int64_t e0 = edge(s, 1, 2, Px, Py);
-            int64_t e1 = edge(s, 2, 0, Px, Py);
-            int64_t e2 = edge(s, 0, 1, Px, Py);
-            if (e0 < 0 || e1 < 0 || e2 < 0) continue;
-            // |P - X0| < 2^21: the int32 -> float conversion is exact (an int64 conversion would use the FP64 pipe)
-            const int32_t dX = int32_t(Px) - s.X[0], dY = int32_t(Py) - s.Y[0];
-            float z = __fadd_rn(__fadd_rn(s.z0, __fmul_rn(s.a, float(dX))), __fmul_rn(s.b, float(dY)));
-            if (!(z > 0.0f)) z = 0.0f;  // also maps -0 and NaN to +0
-            if (z > 1.0f) z = 1.0f;
-            unsigned long long key = (uint64_t(__float_as_uint(z)) << 32) | s.tri;
-            atomicMin(&sk[(py - ty * kTile) * kTile + (px - tx * kTile)], key);
+    // the tile's records are staged kStage at a time, one per thread (the two dependent loads of every record
+    // in flight together), then walked from shared memory by the warps
+    __shared__ SubTri srec[kStage];
+    for (uint32_t c0 = beg; c0 < end; c0 += kStage) {
+        const uint32_t n = min(end - c0, uint32_t(kStage));
+        if (threadIdx.x < n) srec[threadIdx.x] = sc.recs[sc.list[c0 + threadIdx.x]];
+        __syncthreads();
+        for (uint32_t r = warp; r < n; r += 8) {
+          const SubTri& s = srec[r];
+          int x0 = max(int(s.x0), tx * kTile), x1 = min(int(s.x1), tx * kTile + kTile - 1);
+          int y0 = max(int(s.y0), ty * kTile), y1 = min(int(s.y1), ty * kTile + kTile - 1);
+          if (x0 > x1 || y0 > y1) continue;
+          int w = x1 - x0 + 1, npx = w * (y1 - y0 + 1);
+          for (int p = int(lane); p < npx; p += 32) {
+              int px = x0 + p % w, py = y0 + p / w;
+              int64_t Px = int64_t(px) * 16 + 8, Py = int64_t(py) * 16 + 8;
+              int64_t e0 = edge(s, 1, 2, Px, Py);
+              int64_t e1 = edge(s, 2, 0, Px, Py);
+              int64_t e2 = edge(s, 0, 1, Px, Py);
+              if (e0 < 0 || e1 < 0 || e2 < 0) continue;
+              // |P - X0| < 2^21: the int32 -> float conversion is exact (an int64 conversion would use the FP64 pipe)
+              const int32_t dX = int32_t(Px) - s.X[0], dY = int32_t(Py) - s.Y[0];
+              float z = __fadd_rn(__fadd_rn(s.z0, __fmul_rn(s.a, float(dX))), __fmul_rn(s.b, float(dY)));
+              if (!(z > 0.0f)) z = 0.0f;  // also maps -0 and NaN to +0
+              if (z > 1.0f) z = 1.0f;
+              unsigned long long key = (uint64_t(__float_as_uint(z)) << 32) | s.tri;
+              atomicMin(&sk[(py - ty * kTile) * kTile + (px - tx * kTile)], key);
+          }
         }
+        __syncthreads();  // srec is restaged for the next records
     }
-    __syncthreads();
     int px = tx * kTile + int(threadIdx.x % kTile), py = ty * kTile + int(threadIdx.x / kTile);
     if (px < int(W) && py < int(H)) keys[uint64_t(py) * W + px] = sk[threadIdx.x];
 }
