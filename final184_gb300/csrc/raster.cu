@@ -315,26 +315,27 @@ __global__ void __launch_bounds__(256) raster_tiles(RasterScratch sc, uint32_t t
         if (threadIdx.x < n) srec[threadIdx.x] = sc.recs[sc.list[c0 + threadIdx.x]];
         __syncthreads();
         for (uint32_t r = warp; r < n; r += 8) {
-          const SubTri& s = srec[r];
-          int x0 = max(int(s.x0), tx * kTile), x1 = min(int(s.x1), tx * kTile + kTile - 1);
-          int y0 = max(int(s.y0), ty * kTile), y1 = min(int(s.y1), ty * kTile + kTile - 1);
-          if (x0 > x1 || y0 > y1) continue;
-          int w = x1 - x0 + 1, npx = w * (y1 - y0 + 1);
-          for (int p = int(lane); p < npx; p += 32) {
-              int px = x0 + p % w, py = y0 + p / w;
-              int64_t Px = int64_t(px) * 16 + 8, Py = int64_t(py) * 16 + 8;
-              int64_t e0 = edge(s, 1, 2, Px, Py);
-              int64_t e1 = edge(s, 2, 0, Px, Py);
-              int64_t e2 = edge(s, 0, 1, Px, Py);
-              if (e0 < 0 || e1 < 0 || e2 < 0) continue;
-              // |P - X0| < 2^21: the int32 -> float conversion is exact (an int64 conversion would use the FP64 pipe)
-              const int32_t dX = int32_t(Px) - s.X[0], dY = int32_t(Py) - s.Y[0];
-              float z = __fadd_rn(__fadd_rn(s.z0, __fmul_rn(s.a, float(dX))), __fmul_rn(s.b, float(dY)));
-              if (!(z > 0.0f)) z = 0.0f;  // also maps -0 and NaN to +0
-              if (z > 1.0f) z = 1.0f;
-              unsigned long long key = (uint64_t(__float_as_uint(z)) << 32) | s.tri;
-              atomicMin(&sk[(py - ty * kTile) * kTile + (px - tx * kTile)], key);
-          }
+            const SubTri& s = srec[r];
+            int x0 = max(int(s.x0), tx * kTile), x1 = min(int(s.x1), tx * kTile + kTile - 1);
+            int y0 = max(int(s.y0), ty * kTile), y1 = min(int(s.y1), ty * kTile + kTile - 1);
+            if (x0 > x1 || y0 > y1) continue;
+            int w = x1 - x0 + 1, npx = w * (y1 - y0 + 1);
+            for (int p = int(lane); p < npx; p += 32) {
+                int px = x0 + p % w, py = y0 + p / w;
+                int64_t Px = int64_t(px) * 16 + 8, Py = int64_t(py) * 16 + 8;
+                int64_t e0 = edge(s, 1, 2, Px, Py);
+                int64_t e1 = edge(s, 2, 0, Px, Py);
+                int64_t e2 = edge(s, 0, 1, Px, Py);
+                if (e0 < 0 || e1 < 0 || e2 < 0) continue;
+                // |P - X0| < 2^21: the int32 -> float conversion is exact (an int64 conversion would use the FP64
+                // pipe)
+                const int32_t dX = int32_t(Px) - s.X[0], dY = int32_t(Py) - s.Y[0];
+                float z = __fadd_rn(__fadd_rn(s.z0, __fmul_rn(s.a, float(dX))), __fmul_rn(s.b, float(dY)));
+                if (!(z > 0.0f)) z = 0.0f;  // also maps -0 and NaN to +0
+                if (z > 1.0f) z = 1.0f;
+                unsigned long long key = (uint64_t(__float_as_uint(z)) << 32) | s.tri;
+                atomicMin(&sk[(py - ty * kTile) * kTile + (px - tx * kTile)], key);
+            }
         }
         __syncthreads();  // srec is restaged for the next records
     }
