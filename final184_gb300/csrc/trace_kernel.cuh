@@ -72,8 +72,8 @@ __device__ __forceinline__ float3 oct_decode(uint32_t p) {
     return norm3(v);
 }
 
-// The grid a tile traces against, staged in shared memory per CTA: lanes index the level table with their own
-// (divergent) level, which the constant bank would serialise, and batched launches trace many grids.
+// The grid a warp's tile traces against, staged in shared memory per warp: lanes index the level table with their
+// own (divergent) level, which the constant bank would serialise, and batched launches trace many grids.
 struct GridRef {
     uint32_t off[kMaxLevels];  // element offsets (a chain holds < 2^32 elements: dim <= 512)
     uint32_t vol[kMaxLevels];
