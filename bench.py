@@ -546,6 +546,11 @@ def run_served(args, cfg=SERVED):
     for k, (sc, dim, levels) in enumerate(scenes):
         srv.add_scene(k, g.GridDesc(dim, levels, g.FMT_F16, 0, cfg["shadow_res"], 0), sc.tri_xyz, sc.albedo,
                       sc.bounds, sc.light)
+    # warm-up, outside the timing: one request per scene with every view (the first batch tunes the trace kernel
+    # variant; graphs, staging and scratch are set up)
+    warm = [srv.submit(k, views_for(k, list(range(8)), g.FMT_F16), []) for k in range(len(scenes))]
+    for tk in warm:
+        srv.wait(tk)
     tickets = [None] * len(reqs)
 
     def submitter():
@@ -560,11 +565,13 @@ def run_served(args, cfg=SERVED):
     th = threading.Thread(target=submitter)
     th.start()
     th.join()
-    for tk in tickets:
-        srv.wait(tk)
+    results = [srv.wait(tk) for tk in tickets]
     served_s = time.perf_counter() - w0
-    st = srv.stats()
     srv.close()
+    served_lat = sorted(r.latency_ms for r in results)
+    batch_views = {}  # batches of the timed stream -> their views
+    for r, (_, _, _, vids) in zip(results, reqs):
+        batch_views[r.batch] = batch_views.get(r.batch, 0) + len(vids)
     # ---- plain: the same stream back to back, one request at a time, FP32 grids, full voxelization ----
     plain_lat = []
     geo = [sc.tri_xyz.copy() for sc, _, _ in scenes]
@@ -572,6 +579,11 @@ def run_served(args, cfg=SERVED):
     dtri = [torch.from_numpy(x).to(dev) for x in geo]
     dalb = [torch.from_numpy(sc.albedo.view(np.int32)).to(dev) for sc, _, _ in scenes]
     outs = [torch.empty(2 * max_px * 4, dtype=torch.float32, device=dev) for _ in range(16)]
+    for si, (sc, _, _) in enumerate(scenes):  # warm-up, outside the timing: scratch and first launches
+        gi.voxelize(grids[si], dtri[si].data_ptr(), dalb[si].data_ptr(), sc.ntris, sc.light, bounds=sc.bounds)
+        gi.mip(grids[si])
+        gi.trace(grids[si], views_for(si, [0], g.FMT_F32))
+    gi.sync()
     torch.cuda.synchronize()
     p0 = time.perf_counter()
     for ta, si, moves, vids in reqs:
@@ -594,13 +606,16 @@ def run_served(args, cfg=SERVED):
     plain_mpix = pixels / plain_s / 1e6
     return {
         "workload": "%d requests, Poisson arrivals at %.0f req/s, 0-5%% of a scene's objects moved, 1-16 views of "
-                    "512x512..1920x1080 on resident grids %s, %.0f GB admission budget"
+                    "512x512..1920x1080 on resident grids %s, %.0f GB admission budget; both arms warmed up first "
+                    "(the served form's first batch tunes its kernel variant)"
                     % (len(reqs), cfg["rate"], "/".join("%d^3:%dk" % (d, n // 1000) for d, _, n, _ in cfg["scenes"]),
                        cfg["budget"] / 2 ** 30),
         "pixels": int(pixels),
-        "served": {"value": round(served_mpix, 2), "unit": "Mpix/s", "p50_ms": round(st.p50_ms, 2),
-                   "p99_ms": round(st.p99_ms, 2), "batches": int(st.batches),
-                   "mean_batch_views": round(st.mean_batch_views, 2), "wall_s": round(served_s, 3),
+        "served": {"value": round(served_mpix, 2), "unit": "Mpix/s", "p50_ms": round(served_lat[len(served_lat) // 2], 2),
+                   "p99_ms": round(served_lat[min(len(served_lat) - 1, int(0.99 * len(served_lat)))], 2),
+                   "batches": len(batch_views),
+                   "mean_batch_views": round(sum(batch_views.values()) / max(1, len(batch_views)), 2),
+                   "wall_s": round(served_s, 3),
                    "storage": "fp16, resident weights + dirty-brick re-voxelization"},
         "plain": {"value": round(plain_mpix, 2), "unit": "Mpix/s", "p50_ms": round(plain_lat[len(plain_lat) // 2], 2),
                   "p99_ms": round(plain_lat[min(len(plain_lat) - 1, int(0.99 * len(plain_lat)))], 2),
