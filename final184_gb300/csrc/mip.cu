@@ -48,11 +48,12 @@ __device__ __forceinline__ float4 reduce8(uint32_t dir, Fetch fetch) {
             of[o2] = ob[o2] = v;
             const float4 f = fetch(of[0], of[1], of[2]);
             const float4 b = fetch(ob[0], ob[1], ob[2]);
-            const float tr = 1.0f - f.w;
-            acc.x += f.x + tr * b.x;
-            acc.y += f.y + tr * b.y;
-            acc.z += f.z + tr * b.z;
-            acc.w += f.w + tr * b.w;
+            // explicit rounding (one fused multiply-add, then the sum): the same bytes in every kernel that inlines it
+            const float tr = __fsub_rn(1.0f, f.w);
+            acc.x = __fadd_rn(acc.x, __fmaf_rn(tr, b.x, f.x));
+            acc.y = __fadd_rn(acc.y, __fmaf_rn(tr, b.y, f.y));
+            acc.z = __fadd_rn(acc.z, __fmaf_rn(tr, b.z, f.z));
+            acc.w = __fadd_rn(acc.w, __fmaf_rn(tr, b.w, f.w));
         }
     return f4mul(acc, 0.25f);
 }
@@ -150,6 +151,79 @@ __global__ void __launch_bounds__(512) mip_pass(ChainLayout c, uint32_t src, uin
     }
 }
 
+// Anisotropic chains, level 0 -> levels 1 .. nout: level 0 has one volume, so one CTA per 16^3 block stages it
+// once (bulk copy) and reduces it along all six directions (six CTAs of mip_pass per block would each stage it);
+// each thread keeps its voxel's six level-1 results, which then replace the staged block in shared memory as the
+// sources of levels 2 .. nout (per direction, the reductions of mip_pass in its order, hence its bytes).
+__global__ void __launch_bounds__(512, 2) mip_aniso_l0(ChainLayout c, uint32_t nout, uint32_t* status) {
+    extern __shared__ __align__(128) unsigned char smem[];  // the staged block, then level 1: float4 [6][512]
+    __shared__ float4 l2[6 * 64];
+    __shared__ float4 l3[6 * 8];
+    __shared__ __align__(8) uint64_t bar;
+    const uint32_t blk = blockIdx.x;
+    const uint32_t Bx = compact1by2(blk), By = compact1by2(blk >> 1), Bz = compact1by2(blk >> 2);
+    const uint32_t bytes = 4096u * c.esz;
+    const unsigned char* gsrc = static_cast<const unsigned char*>(c.base) + (c.off[0] + uint64_t(blk) * 4096u) * c.esz;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        fence_barrier_init();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        mbar_expect_tx(&bar, bytes);
+        bulk_g2s(smem, gsrc, bytes, &bar);
+    }
+    if (!mbar_wait_bounded(&bar, 0, kWaitPolls)) {
+        if (threadIdx.x == 0) set_status(status, kStatusTimeout);
+        mbar_wait_bounded(&bar, 0, kWaitPolls);  // let the copy land before the CTA exits
+        return;
+    }
+    const uint32_t t = threadIdx.x;
+    const uint32_t x = t % 8u, y = (t / 8u) % 8u, z = t / 64u;
+    float4 acc[6];
+#pragma unroll
+    for (uint32_t dir = 0; dir < 6; ++dir) {
+        acc[dir] = reduce8<true>(dir, [&](int dx, int dy, int dz) {
+            const uint32_t sx = 2 * x + dx, sy = 2 * y + dy, sz = 2 * z + dz;
+            const uint32_t cb = ((sx >> 3) & 1u) | (((sy >> 3) & 1u) << 1) | (((sz >> 3) & 1u) << 2);
+            return raw_vox(smem, c.format, cb * 512u + ((sz & 7u) << 6) + ((sy & 7u) << 3) + (sx & 7u));
+        });
+        store_vox(c.base, c.format,
+                  c.off[1] + uint64_t(dir) * c.vol[1] + vox_index(1, c.ldim[1], Bx * 8 + x, By * 8 + y, Bz * 8 + z),
+                  acc[dir]);
+    }
+    __syncthreads();  // every thread has read the staged block
+    float4* l1 = reinterpret_cast<float4*>(smem);
+#pragma unroll
+    for (uint32_t dir = 0; dir < 6; ++dir) l1[dir * 512 + t] = acc[dir];
+    __syncthreads();
+    if (nout >= 2 && t < 6 * 64) {
+        const uint32_t dir = t / 64u, v = t % 64u, vx = v % 4u, vy = (v / 4u) % 4u, vz = v / 16u;
+        const float4 a = reduce8<true>(dir, [&](int dx, int dy, int dz) {
+            return l1[dir * 512 + ((2 * vz + dz) * 8 + (2 * vy + dy)) * 8 + (2 * vx + dx)];
+        });
+        l2[t] = a;
+        store_vox(c.base, c.format,
+                  c.off[2] + uint64_t(dir) * c.vol[2] + vox_index(2, c.ldim[2], Bx * 4 + vx, By * 4 + vy, Bz * 4 + vz), a);
+    }
+    __syncthreads();
+    if (nout >= 3 && t < 6 * 8) {
+        const uint32_t dir = t / 8u, v = t % 8u, vx = v % 2u, vy = (v / 2u) % 2u, vz = v / 4u;
+        const float4 a = reduce8<true>(dir, [&](int dx, int dy, int dz) {
+            return l2[dir * 64 + ((2 * vz + dz) * 4 + (2 * vy + dy)) * 4 + (2 * vx + dx)];
+        });
+        l3[t] = a;
+        store_vox(c.base, c.format,
+                  c.off[3] + uint64_t(dir) * c.vol[3] + vox_index(3, c.ldim[3], Bx * 2 + vx, By * 2 + vy, Bz * 2 + vz), a);
+    }
+    __syncthreads();
+    if (nout >= 4 && t < 6) {
+        const uint32_t dir = t;
+        const float4 a = reduce8<true>(dir, [&](int dx, int dy, int dz) { return l3[dir * 8 + (dz * 2 + dy) * 2 + dx]; });
+        store_vox(c.base, c.format, c.off[4] + uint64_t(dir) * c.vol[4] + vox_index(4, c.ldim[4], Bx, By, Bz), a);
+    }
+}
+
 }  // namespace
 
 int mip_launch(const ChainLayout& c, uint32_t levels, uint32_t* d_status, cudaStream_t s) {
@@ -159,6 +233,8 @@ int mip_launch(const ChainLayout& c, uint32_t levels, uint32_t* d_status, cudaSt
         cudaError_t e = cudaFuncSetAttribute(mip_pass<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 4096 * 16);
         if (e == cudaSuccess)
             e = cudaFuncSetAttribute(mip_pass<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 4096 * 16);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(mip_aniso_l0, cudaFuncAttributeMaxDynamicSharedMemorySize, 4096 * 16);
         if (e != cudaSuccess) return cuda_fail(e, "mip: smem attribute");
         attr_set = true;
     }
@@ -172,7 +248,9 @@ int mip_launch(const ChainLayout& c, uint32_t levels, uint32_t* d_status, cudaSt
         uint32_t nout = std::min(maxout, levels - 1 - l);
         uint32_t blocks = (ds >= 16 ? (ds / 16) * (ds / 16) * (ds / 16) : 1u) * ndir;
         size_t smem = size_t(S) * S * S * c.esz;
-        if (c.aniso)
+        if (c.aniso && l == 0 && ds >= 16)  // one CTA per block for all six directions
+            mip_aniso_l0<<<blocks / 6, 512, std::max<size_t>(smem, 6 * 512 * 16), s>>>(c, nout, d_status);
+        else if (c.aniso)
             mip_pass<true><<<blocks, 512, smem, s>>>(c, l, nout, d_status);
         else
             mip_pass<false><<<blocks, 512, smem, s>>>(c, l, nout, d_status);
