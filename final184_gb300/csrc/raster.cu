@@ -320,16 +320,23 @@ __global__ void __launch_bounds__(256) raster_tiles(RasterScratch sc, uint32_t t
             int y0 = max(int(s.y0), ty * kTile), y1 = min(int(s.y1), ty * kTile + kTile - 1);
             if (x0 > x1 || y0 > y1) continue;
             int w = x1 - x0 + 1, npx = w * (y1 - y0 + 1);
+            // Edge functions at the box's first pixel centre (int64), stepped exactly in int32 within the tile:
+            // |edge delta| < 2^21 and the offsets are below 16 pixels (256 units), so each step term is < 2^29.
+            const int64_t Px0 = int64_t(x0) * 16 + 8, Py0 = int64_t(y0) * 16 + 8;
+            const int64_t E0 = edge(s, 1, 2, Px0, Py0), E1 = edge(s, 2, 0, Px0, Py0), E2 = edge(s, 0, 1, Px0, Py0);
+            const int32_t ax0 = s.X[2] - s.X[1], ay0 = s.Y[2] - s.Y[1], ax1 = s.X[0] - s.X[2], ay1 = s.Y[0] - s.Y[2],
+                          ax2 = s.X[1] - s.X[0], ay2 = s.Y[1] - s.Y[0];
+            const uint32_t wmagic = (65536u + uint32_t(w) - 1u) / uint32_t(w);  // p / w = (p * wmagic) >> 16, p < 256
             for (int p = int(lane); p < npx; p += 32) {
-                int px = x0 + p % w, py = y0 + p / w;
-                int64_t Px = int64_t(px) * 16 + 8, Py = int64_t(py) * 16 + 8;
-                int64_t e0 = edge(s, 1, 2, Px, Py);
-                int64_t e1 = edge(s, 2, 0, Px, Py);
-                int64_t e2 = edge(s, 0, 1, Px, Py);
-                if (e0 < 0 || e1 < 0 || e2 < 0) continue;
+                const int ly = int((uint32_t(p) * wmagic) >> 16), lx = p - ly * w;
+                const int px = x0 + lx, py = y0 + ly;
+                const int32_t ox = 16 * lx, oy = 16 * ly;
+                if (E0 + int64_t(ax0 * oy - ay0 * ox) < 0 || E1 + int64_t(ax1 * oy - ay1 * ox) < 0 ||
+                    E2 + int64_t(ax2 * oy - ay2 * ox) < 0)
+                    continue;
                 // |P - X0| < 2^21: the int32 -> float conversion is exact (an int64 conversion would use the FP64
                 // pipe)
-                const int32_t dX = int32_t(Px) - s.X[0], dY = int32_t(Py) - s.Y[0];
+                const int32_t dX = (16 * px + 8) - s.X[0], dY = (16 * py + 8) - s.Y[0];
                 float z = __fadd_rn(__fadd_rn(s.z0, __fmul_rn(s.a, float(dX))), __fmul_rn(s.b, float(dY)));
                 if (!(z > 0.0f)) z = 0.0f;  // also maps -0 and NaN to +0
                 if (z > 1.0f) z = 1.0f;
