@@ -302,11 +302,12 @@ struct ItemSetup {
 
 __device__ void item_setup(const TriRec& r, const int64_t base[3], const int32_t l0[3], const int32_t l1[3],
                            ItemSetup& out) {
-    int64_t v[3][3];
+    // brick-relative vertices and edges fit 32 bits (|q| < 2^19, base <= 2^17): products widen 32 x 32 -> 64
+    int32_t v[3][3];
 #pragma unroll
     for (int a = 0; a < 3; ++a)
 #pragma unroll
-        for (int b = 0; b < 3; ++b) v[a][b] = int64_t(r.q[a * 3 + b]) - base[b];
+        for (int b = 0; b < 3; ++b) v[a][b] = r.q[a * 3 + b] - int32_t(base[b]);
     unsigned long long mk[3] = {0ull, 0ull, 0ull};
 #pragma unroll
     for (int P = 0; P < 3; ++P) {
@@ -315,17 +316,18 @@ __device__ void item_setup(const TriRec& r, const int64_t base[3], const int32_t
         int32_t cu[3], cw[3], lo[3], hi[3];
 #pragma unroll
         for (int e = 0; e < 3; ++e) {
-            int64_t ed[3];
+            int32_t ed[3];
 #pragma unroll
             for (int b = 0; b < 3; ++b) ed[b] = v[(e + 1) % 3][b] - v[e][b];
-            int64_t a[3] = {0, 0, 0};
+            int32_t a[3] = {0, 0, 0};
             if (P == 0) a[1] = ed[2], a[2] = -ed[1];
             if (P == 1) a[0] = -ed[2], a[2] = ed[0];
             if (P == 2) a[0] = ed[1], a[1] = -ed[0];
-            int64_t p0 = a[0] * v[0][0] + a[1] * v[0][1] + a[2] * v[0][2];
-            int64_t p1 = a[0] * v[1][0] + a[1] * v[1][1] + a[2] * v[1][2];
-            int64_t p2 = a[0] * v[2][0] + a[1] * v[2][1] + a[2] * v[2][2];
-            int64_t rr = kHalf * (iabs64(a[0]) + iabs64(a[1]) + iabs64(a[2]));
+            auto dotw = [&](const int32_t (&x)[3]) {
+                return int64_t(a[0]) * x[0] + int64_t(a[1]) * x[1] + int64_t(a[2]) * x[2];
+            };
+            int64_t p0 = dotw(v[0]), p1 = dotw(v[1]), p2 = dotw(v[2]);
+            int64_t rr = kHalf * (int64_t(abs(a[0])) + abs(a[1]) + abs(a[2]));
             int64_t pmin = min(p0, min(p1, p2)), pmax = max(p0, max(p1, p2));
             cu[e] = int32_t(a[ku]);
             cw[e] = int32_t(a[kw]);
@@ -346,11 +348,11 @@ __device__ void item_setup(const TriRec& r, const int64_t base[3], const int32_t
             }
         }
     }
-    int64_t e0[3], e1[3];
+    int32_t e0[3], e1[3];
 #pragma unroll
     for (int b = 0; b < 3; ++b) e0[b] = v[1][b] - v[0][b], e1[b] = v[2][b] - v[0][b];
-    const int64_t n0 = e0[1] * e1[2] - e0[2] * e1[1], n1 = e0[2] * e1[0] - e0[0] * e1[2],
-                  n2 = e0[0] * e1[1] - e0[1] * e1[0];
+    const int64_t n0 = int64_t(e0[1]) * e1[2] - int64_t(e0[2]) * e1[1], n1 = int64_t(e0[2]) * e1[0] - int64_t(e0[0]) * e1[2],
+                  n2 = int64_t(e0[0]) * e1[1] - int64_t(e0[1]) * e1[0];
     const int64_t sp = n0 * v[0][0] + n1 * v[0][1] + n2 * v[0][2];
     const int64_t rr = kHalf * (iabs64(n0) + iabs64(n1) + iabs64(n2));
     out.mask[0] = mk[0], out.mask[1] = mk[1], out.mask[2] = mk[2];
