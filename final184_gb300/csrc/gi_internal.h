@@ -157,7 +157,7 @@ int trace_launch(const ChainLayout& chain, const TraceConsts& tc, const f184gi_g
                  const TraceView* views, uint32_t nviews, void* scratch, size_t scratch_bytes, uint32_t variant,
                  TraceStaging** staging, cudaStream_t s, bool count = false);
 
-// Batched persistent trace replayed from CUDA graphs: [view table H2D] -> [work counter = 0] -> [kernel].
+// Batched trace replayed from CUDA graphs: [view table H2D] -> [work counter = 0] -> [kernel over all views].
 struct TraceGraph;
 uint32_t trace_persistent_blocks(uint32_t fmt, bool aniso, uint32_t variant, uint32_t per_sm);  // per_sm 0 = max
 int trace_graph_create(TraceGraph** out, uint32_t fmt, bool aniso, uint32_t max_views, uint32_t per_sm,

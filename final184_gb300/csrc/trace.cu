@@ -1,6 +1,6 @@
 // trace.cu -- host side of the cone trace: view tables, launches of the kernel variants (trace_kernel.cuh, one
-// translation unit per storage format and mip kind), the batched persistent launch under CUDA graphs, and the
-// variant tuner.
+// translation unit per storage format and mip kind), the batched launch under CUDA graphs (all views of a batch
+// in one kernel), and the variant tuner.
 #include <algorithm>
 #include <vector>
 
