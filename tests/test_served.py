@@ -123,6 +123,39 @@ def test_each_request_same_alone_and_in_the_mix(fx):
 
 
 @pytest.mark.gpu
+def test_concurrent_submitters_match_alone(fx):
+    """One host thread per scene submits that scene's requests (in order) while the others submit theirs: every
+    result equals the same request run alone."""
+    import threading
+
+    srv = fx.server(slots=2, max_batch_views=32)
+    alone, _ = run_all(fx, srv, one_at_a_time=True)
+    srv.close()
+    srv = fx.server(slots=3, max_batch_views=32)
+    tickets, keep = [None] * len(fx.requests), [None] * len(fx.requests)
+
+    def submitter(scene):
+        for i, (si, vids, moves) in enumerate(fx.requests):
+            if si == scene:
+                views, outs = fx.make_views(si, vids)
+                keep[i] = outs
+                tickets[i] = srv.submit(si, views, moves)
+
+    threads = [threading.Thread(target=submitter, args=(k,)) for k in range(len(fx.scenes))]
+    for th in threads:
+        th.start()
+    for th in threads:
+        th.join()
+    for tk in tickets:
+        assert srv.wait(tk).status == 0
+    fx.torch.cuda.synchronize()
+    srv.close()
+    for a, outs in zip(alone, keep):
+        for x, y in zip(a, outs):
+            assert np.array_equal(x.view(np.uint32), y.cpu().numpy().view(np.uint32))
+
+
+@pytest.mark.gpu
 def test_dirty_updates_equal_full_voxelization(fx):
     g, torch = fx.g, fx.torch
     srv = fx.server(slots=1)
