@@ -110,7 +110,6 @@ struct f184gi_ctx {
     Scratch raster, vox, trace, misc, keys, counts;
     uint32_t* d_status = nullptr;
     TraceStaging* trace_stage = nullptr;
-    uint32_t trace_variant = kTraceDefaultVariant;
     // voxelize forks the triangle lists onto aux (after the frame) beside the shadow raster on the caller's
     // stream, and joins before the bricks
     cudaStream_t aux = nullptr;
@@ -525,7 +524,8 @@ int trace_views(f184gi_ctx* c, uint32_t grid, const f184gi_view* views, uint32_t
     int rc = scratch_get(c, c->trace, trace_scratch_bytes(nviews));
     if (rc) return rc;
     tc.counts = d_counts;
-    return trace_launch(g->chain, tc, g->d_frame, tv.data(), nviews, c->trace.ptr, c->trace.bytes, c->trace_variant,
+    return trace_launch(g->chain, tc, g->d_frame, tv.data(), nviews, c->trace.ptr, c->trace.bytes,
+                        trace_default_variant(g->chain.format, g->chain.aniso != 0),
                         &c->trace_stage, static_cast<cudaStream_t>(stream), d_counts != nullptr);
 }
 }  // namespace

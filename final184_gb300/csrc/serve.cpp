@@ -264,7 +264,7 @@ int issue_batch(f184gi_server* S, Slot& slot) {
     }
     int rc = F184GI_OK;
     if (S->variant < 0) {  // first batch: it runs alone (the scheduler issues nothing else meanwhile)
-        uint32_t best = kTraceDefaultVariant;
+        uint32_t best = trace_default_variant(uint32_t(S->fmt), S->aniso != 0);
         float ms[kTraceVariantCount];
         if ((rc = trace_graph_tune(slot.graph, slot.tv.data(), uint32_t(slot.tv.size()), s, &best, ms))) return rc;
         std::lock_guard<std::mutex> lk(S->mu);

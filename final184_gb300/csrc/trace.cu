@@ -102,7 +102,7 @@ int trace_launch(const ChainLayout& c, const TraceConsts& tc, const f184gi_grid_
                  cudaStream_t s, bool count) {
     if (nviews == 0) return F184GI_OK;
     if (scratch_bytes < trace_scratch_bytes(nviews)) return fail(F184GI_ERR_INVALID, "trace: scratch too small");
-    if (count) variant = kTraceDefaultVariant;
+    if (count) variant = trace_default_variant(c.format, c.aniso != 0);
     const void* fn = count ? trace_kernel_count_fn(c.format, c.aniso != 0) : trace_kernel_fn(c.format, c.aniso != 0, variant);
     if (!fn) return fail(F184GI_ERR_INVALID, "trace: unknown kernel variant");
     const size_t need = table_bytes(nviews);

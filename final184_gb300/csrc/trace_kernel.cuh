@@ -475,7 +475,7 @@ const void* variant_fn() {
 // The instrumented kernel (same outputs, plus the step and sample totals) in the default variant's shape.
 template <int FMT, bool ANISO>
 const void* count_kernel() {
-    constexpr TraceVariant tv = kTraceVariants[kTraceDefaultVariant];
+    constexpr TraceVariant tv = kTraceVariants[trace_default_variant(FMT, ANISO)];
     return reinterpret_cast<const void*>(&trace_kernel<FMT, ANISO, int(tv.tw), int(tv.th), int(tv.minb), true>);
 }
 
