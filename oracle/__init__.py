@@ -112,11 +112,10 @@ def ref_lib():
     global _ref
     if _ref is None:
         path = _build.REF_LIB
-        if not os.path.exists(path):
-            try:
-                _build.build_ref()
-            except RuntimeError:
-                return None
+        try:
+            _build.build_ref()  # rebuilt when ref_shim.cpp changed; a no-op where the reference tree is absent
+        except RuntimeError:
+            return None
         if not os.path.exists(path):
             return None
         _ref = C.CDLL(path)
@@ -130,6 +129,9 @@ def ref_lib():
         _ref.ref_frustum_box.argtypes = [V, V, V]
         _ref.ref_quat_euler_rotate.argtypes = [F, F, F, V, V]
         _ref.ref_matrix_trs.argtypes = [V, V, V, V]
+        _ref.ref_frustum_define.argtypes = [V, V]
+        _ref.ref_frustum_transformed.argtypes = [V, V, V]
+        _ref.ref_frustum_inside_fast.argtypes = [V, V, V]
     return _ref
 
 

@@ -37,13 +37,14 @@ def build_ref(force=False):
     if not os.path.isdir(REF_ROOT):
         return None
     os.makedirs(os.path.dirname(REF_LIB), exist_ok=True)
-    if os.path.exists(REF_LIB) and not force:
+    shim = os.path.join(HERE, "ref_shim.cpp")
+    if os.path.exists(REF_LIB) and not force and os.path.getmtime(shim) <= os.path.getmtime(REF_LIB):
         return REF_LIB
     math_src = sorted(glob.glob(os.path.join(REF_ROOT, "Math", "*.cpp")))
     cam_src = os.path.join(REF_ROOT, "Foreground", "SceneGraph", "Camera.cpp")
-    shim = os.path.join(HERE, "ref_shim.cpp")
     stub_dir = os.path.join(HERE, "ref_stub")  # MathAPI.h: the export macro CMake would generate
-    _run(["g++", "-std=c++17", "-O2", "-fPIC", "-shared", "-w", "-I", stub_dir, "-I", os.path.join(REF_ROOT, "Math"),
+    # -ffp-contract=off: the scalar Math code rounds every operation, on Arm (which has FMA) as on x86
+    _run(["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-w", "-I", stub_dir, "-I", os.path.join(REF_ROOT, "Math"),
           "-I", os.path.join(REF_ROOT, "Foreground", "SceneGraph"), *math_src, cam_src, shim, "-o", REF_LIB])
     return REF_LIB
 

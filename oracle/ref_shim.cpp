@@ -67,6 +67,30 @@ int ref_frustum_box(const float proj[16], const float mn[3], const float mx[3]) 
     return int(fr.IsInsideFast(b));
 }
 
+static_assert(sizeof(tc::Frustum) == 264, "tc::Frustum: 6 planes of 28 bytes, 8 corners of 12");
+
+// Frustum::Define(projection), its 264 bytes (planes, then corners)
+void ref_frustum_define(const float proj[16], void* out) {
+    tc::Frustum fr;
+    fr.Define(tc::Matrix4(proj));
+    std::memcpy(out, &fr, sizeof fr);
+}
+
+// a Frustum given as its 264 bytes, Transformed(Matrix3x4(m12)) -> 264 bytes
+void ref_frustum_transformed(const void* in, const float m12[12], void* out) {
+    tc::Frustum fr;
+    std::memcpy(static_cast<void*>(&fr), in, sizeof fr);
+    tc::Frustum t = fr.Transformed(tc::Matrix3x4(m12));
+    std::memcpy(out, &t, sizeof t);
+}
+
+// a Frustum given as its 264 bytes, IsInsideFast(BoundingBox(mn, mx)): 0 outside, 2 inside
+int ref_frustum_inside_fast(const void* in, const float mn[3], const float mx[3]) {
+    tc::Frustum fr;
+    std::memcpy(static_cast<void*>(&fr), in, sizeof fr);
+    return int(fr.IsInsideFast(tc::BoundingBox(tc::Vector3(mn[0], mn[1], mn[2]), tc::Vector3(mx[0], mx[1], mx[2]))));
+}
+
 // q(ex, ey, ez) * v for the Euler-angle constructor (degrees) of tc::Quaternion
 void ref_quat_euler_rotate(float ex, float ey, float ez, const float v[3], float out[3]) {
     tc::Vector3 r = tc::Quaternion(ex, ey, ez) * tc::Vector3(v[0], v[1], v[2]);
