@@ -33,6 +33,11 @@ struct GIMatrix3x4 {
     float m[12];
 };
 static_assert(sizeof(GIMatrix3x4) == 48, "tc::Matrix3x4 is 48 bytes");
+// Layout of tc::Matrix4 (Math/Matrix4.h): 16 floats, row-major; f184gi_view's view/proj and GIFrustumDefine take it.
+struct GIMatrix4 {
+    float m[16];
+};
+static_assert(sizeof(GIMatrix4) == 64, "tc::Matrix4 is 64 bytes");
 static_assert(sizeof(f184gi_vec3) == 12, "tc::Vector3 is 12 bytes");
 static_assert(sizeof(f184gi_bounds) == 32, "tc::BoundingBox is 32 bytes");
 
