@@ -296,8 +296,11 @@ private:
             return F184GI_ERR_OOM;
         }
         if (cudaMemcpyAsync(r.xyz, p->xyz, p->ntris * 36, cudaMemcpyHostToDevice, stream) != cudaSuccess ||
-            cudaMemcpyAsync(r.albedo, p->albedo, p->ntris * 4, cudaMemcpyHostToDevice, stream) != cudaSuccess)
+            cudaMemcpyAsync(r.albedo, p->albedo, p->ntris * 4, cudaMemcpyHostToDevice, stream) != cudaSuccess) {
+            cudaFree(r.xyz);
+            cudaFree(r.albedo);
             return F184GI_ERR_CUDA;
+        }
         *out = &(cache_[p] = r);
         return F184GI_OK;
     }

@@ -91,11 +91,12 @@ def test_half_conversion_matches_ieee(orc):
     rng = np.random.default_rng(2)
     xs = np.concatenate([rng.normal(size=4000) * 10.0 ** rng.integers(-8, 5, 4000),
                          [0.0, -0.0, 65504.0, 65519.9, 65520.0, 6e-8, 2.0 ** -25, 1.0 + 2.0 ** -11]])
-    for x in xs:
-        h = lib.orc_float_to_half(float(x))
-        assert h == int(np.array([x], np.float64).astype(np.float16).view(np.uint16)[0]), x
-        if not math.isinf(np.float16(x)):
-            assert lib.orc_half_to_float(h) == float(np.float16(x))
+    with np.errstate(over="ignore"):  # values past 65520 round to infinity on purpose
+        for x in xs:
+            h = lib.orc_float_to_half(float(x))
+            assert h == int(np.array([x], np.float64).astype(np.float16).view(np.uint16)[0]), x
+            if not math.isinf(np.float16(x)):
+                assert lib.orc_half_to_float(h) == float(np.float16(x))
 
 
 def test_oct_codec_round_trip(orc):
