@@ -29,12 +29,12 @@ SMALL = dict(name="plain-small-gpu", seed=184, ntris=20000, nobjects=200, dim=64
              width=640, height=360)
 
 
-def workload_desc(cfg):
-    return ("%s: %dk-triangle seeded scene (%d objects), %d^3 FP32 RGBA radiance/opacity grid in 8^3 bricks, "
+def workload_desc(cfg, storage="f32"):
+    return ("%s: %dk-triangle seeded scene (%d objects), %d^3 %s RGBA radiance/opacity grid in 8^3 bricks, "
             "%d-level mip chain, %d^2 shadow map, %dx%d G-buffer, 5 diffuse (60 deg) + 1 specular cone, "
             "max distance = grid diagonal, step = 0.5 x diameter"
-            % (cfg["name"], cfg["ntris"] // 1000, cfg["nobjects"], cfg["dim"], cfg["levels"], cfg["shadow_res"],
-               cfg["width"], cfg["height"]))
+            % (cfg["name"], cfg["ntris"] // 1000, cfg["nobjects"], cfg["dim"], "FP16" if storage == "f16" else "FP32",
+               cfg["levels"], cfg["shadow_res"], cfg["width"], cfg["height"]))
 
 
 def peaks():
@@ -290,7 +290,8 @@ def run_gpu(args, cfg):
     sc = g.SyntheticScene(cfg["seed"], cfg["ntris"], cfg["nobjects"])
     gi = g.VoxelGI(local)
     dim, levels, res, W, H = cfg["dim"], cfg["levels"], cfg["shadow_res"], cfg["width"], cfg["height"]
-    grid = gi.create_grid(dim, levels, g.FMT_F32, 0, res)
+    fmt = g.FMT_F16 if args.storage == "f16" else g.FMT_F32
+    grid = gi.create_grid(dim, levels, fmt, 0, res)
     npix = W * H
     # host inputs (pinned) and device copies
     tri_h = torch.from_numpy(sc.tri_xyz).pin_memory()
@@ -370,7 +371,7 @@ def run_gpu(args, cfg):
     gi2 = g.VoxelGI(local)
     d2 = [torch.empty_like(depth), torch.empty_like(normal), torch.empty_like(rgh)]
     out2 = torch.empty_like(out)
-    lanes.append(dict(gi=gi2, grid=gi2.create_grid(dim, levels, g.FMT_F32, 0, res), tri=torch.empty_like(tri),
+    lanes.append(dict(gi=gi2, grid=gi2.create_grid(dim, levels, fmt, 0, res), tri=torch.empty_like(tri),
                       alb=torch.empty_like(alb), gbuf=d2, out=out2, out_h=torch.empty_like(out_h).pin_memory(),
                       view=g.make_view(V, P, W, H, d2[0].data_ptr(), d2[1].data_ptr(), d2[2].data_ptr(),
                                        out2.data_ptr()),
@@ -413,7 +414,7 @@ def run_gpu(args, cfg):
     # trace_kernel is the largest single kernel of a request (launch-list share ~42%); its stage is one launch
     means = {k: statistics.mean(v) for k, v in stage.items()}
     top = "trace"
-    esz = 16
+    esz = 8 if args.storage == "f16" else 16
     chain_bytes = sum((dim >> l) ** 3 for l in range(levels)) * esz
     l0_bytes = dim ** 3 * esz
     alg = {
@@ -426,18 +427,19 @@ def run_gpu(args, cfg):
     }
     peak, peak_kind = peaks()
     achieved = alg[top] / (means[top] * 1e-3) / 1e9
-    # secondary figure: the voxel bytes the trace samples (8 taps x 16 B per level sample), counted by the
+    # secondary figure: the voxel bytes the trace samples (8 taps x esz B per level sample), counted by the
     # instrumented kernel on the same view after the timed region, against an L2-resident copy measured here
     n_steps, n_samples = gi.trace_count(grid, [view], stream=stream)
     sampled = n_samples * 8 * esz
     l2_gbs = l2_copy_gbs(dev, stream)
     kernel_names = {"voxelize": "vox_bricks", "mip": "mip_pass", "trace": "trace_kernel"}
-    tr = traffic_record(kernel_names[top])
+    tr = traffic_record(kernel_names[top] + ("_f16" if args.storage == "f16" else ""))
     line = {
         "metric": METRIC, "value": round(value, 4), "unit": "Mpix/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms_per_step, 4), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": workload_desc(cfg), "form": "plain per-request FP32 GPU path",
+        "config": {"workload": workload_desc(cfg, args.storage),
+                   "form": "plain per-request %s GPU path" % ("FP32" if args.storage == "f32" else "FP16-storage"),
                    "parallelism": "replicas" if world > 1 else "single GPU",
                    "l2": "per-step working set > 129 MB L2 (the %d MB grid chain is rewritten and re-read every step)"
                          % (chain_bytes // 2 ** 20)},
@@ -448,8 +450,8 @@ def run_gpu(args, cfg):
                      "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_source": peak_kind,
                      "algorithmic_bytes": alg[top],
                      "traffic": (tr * 1.0 if isinstance(tr, (int, float)) else None),
-                     "note": "far below the HBM roof: the trace is instruction-issue bound (ncu: ~65% issue-active, "
-                             "L1 hit ~94%, L2 ~1% and DRAM ~0.4% of peak); algorithmic bytes = G-buffer 10 B + output 32 B per "
+                     "note": "far below the HBM roof: the trace is instruction-issue bound (ncu: ~67% issue-active, "
+                             "L1 hit ~92%, L2 ~2% and DRAM ~0.4% of peak); algorithmic bytes = G-buffer 10 B + output 32 B per "
                              "pixel + the whole chain once (upper bound of the touched part)",
                      "sampled": {"bytes": int(sampled), "achieved": round(sampled / (means[top] * 1e-3) / 1e9, 1),
                                  "unit": "GB/s", "l2_copy_gbs": round(l2_gbs, 1),
@@ -457,9 +459,9 @@ def run_gpu(args, cfg):
                                  "steps_per_pixel": round(n_steps / max(1, npix), 2),
                                  "level_samples_per_pixel": round(n_samples / max(1, npix), 2),
                                  "note": "secondary figure, not the roofline: voxel bytes sampled by the cones "
-                                         "(level samples x 8 taps x 16 B, counted by the instrumented kernel) per "
+                                         "(level samples x 8 taps x %d B, counted by the instrumented kernel) per "
                                          "trace launch time; most are L1 hits, so it may exceed the L2 figure, "
-                                         "a torch copy of 2 x 40 MiB held in L2"}},
+                                         "a torch copy of 2 x 40 MiB held in L2" % esz}},
         "e2e": {"value": round(e2e_value, 4), "unit": "Mpix/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "ms_per_step": round(e2e_ms, 4),
                 "note": "through the API from pinned host buffers; two request lanes (context, grid, stream) take "
@@ -830,6 +832,8 @@ def main():
     ap.add_argument("--no-precision", action="store_true", help="skip the 512^3 anisotropic FP16 precision form")
     ap.add_argument("--no-batched", action="store_true", help="skip the 64-scene batched form")
     ap.add_argument("--no-march", action="store_true", help="skip the reference-faithful march mode")
+    ap.add_argument("--storage", choices=["f32", "f16"], default="f32",
+                    help="grid storage of the plain leg (f32, the headline; f16 is the served form's storage)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     cfg = SMALL if args.small else PLAIN_LARGE
