@@ -498,10 +498,16 @@ int trace_views(f184gi_ctx* c, uint32_t grid, const f184gi_view* views, uint32_t
     tc.sin_tilt = float(std::sin(tilt));
     trace_consts_schedule(tc);
     std::vector<TraceView> tv(nviews);
+    uint64_t pixels = 0;
     for (uint32_t i = 0; i < nviews; ++i) {
         const f184gi_view& v = views[i];
         if (!v.depth || !v.normal || !v.roughness || !v.out || v.width == 0 || v.height == 0)
             return fail(F184GI_ERR_INVALID, "trace: view " + std::to_string(i) + " has null buffers or zero size");
+        if (v.width > kMaxViewSide || v.height > kMaxViewSide)
+            return fail(F184GI_ERR_INVALID, "trace: view " + std::to_string(i) + " is larger than " +
+                                                std::to_string(kMaxViewSide) + " pixels on a side");
+        if ((pixels += uint64_t(v.width) * v.height) > kMaxTracePixels)
+            return fail(F184GI_ERR_INVALID, "trace: the views hold more than 2^36 pixels in all");
         if (v.out_format != F184GI_FMT_F32 && v.out_format != F184GI_FMT_F16)
             return fail(F184GI_ERR_INVALID, "trace: unknown output format");
         double V[16], P[16], IV[16], IP[16];
@@ -630,6 +636,8 @@ int f184gi_gbuffer(f184gi_ctx* c, const float* tri, const float* rough, uint64_t
                    uint32_t* tri_id_out, void* stream) {
     if (!c || !view || !tri || !rough) return fail(F184GI_ERR_INVALID, "gbuffer: null argument");
     if (!view->depth || !view->normal || !view->roughness) return fail(F184GI_ERR_INVALID, "gbuffer: null G-buffer planes");
+    if (view->width == 0 || view->height == 0 || view->width > kMaxViewSide || view->height > kMaxViewSide)
+        return fail(F184GI_ERR_INVALID, "gbuffer: view sides must be 1.." + std::to_string(kMaxViewSide) + " pixels");
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     RasterJob rj{};
     rj.tri = tri;

@@ -18,6 +18,10 @@ constexpr uint32_t kFixedFrac = 31;  // per-contribution injection weights are 1
 // device status bits (set by kernels, read by f184gi_sync / inspection calls)
 constexpr uint32_t kStatusOverflow = 1u;
 constexpr uint32_t kStatusTimeout = 2u;
+// View sides of 1..kMaxViewSide pixels; one trace call covers at most kMaxTracePixels pixels in all, so that its
+// warp-tile numbering (32 pixels a tile) stays inside uint32.
+constexpr uint32_t kMaxViewSide = 16384;
+constexpr uint64_t kMaxTracePixels = 1ull << 36;
 constexpr uint32_t kStatusRange = 4u;  // geometry outside the fixed-point range was skipped
 
 // process-wide count of kernels this library has launched (f184gi_kernel_launches)

@@ -309,6 +309,7 @@ void scheduler(f184gi_server* S) {
         std::vector<Request*> batch;
         std::set<uint32_t> blocked;  // scenes whose next request cannot run in this batch
         uint32_t nviews = 0;
+        uint64_t npix = 0;
         for (auto it = S->pending.begin(); it != S->pending.end();) {
             Request* r = *it;
             Scene* sc = S->scenes.at(r->scene);
@@ -317,7 +318,7 @@ void scheduler(f184gi_server* S) {
                 ++it;
                 continue;
             }
-            if (nviews + r->views.size() > S->cfg.max_batch_views) break;
+            if (nviews + r->views.size() > S->cfg.max_batch_views || npix + r->pixels > kMaxTracePixels) break;
             if (S->cfg.hbm_budget && S->hbm_used + r->staging > S->cfg.hbm_budget) {
                 blocked.insert(r->scene);  // waits for memory; later requests of the scene wait behind it
                 ++it;
@@ -327,6 +328,7 @@ void scheduler(f184gi_server* S) {
             blocked.insert(r->scene);
             sc->busy = true;
             nviews += uint32_t(r->views.size());
+            npix += r->pixels;
             S->hbm_used += r->staging;
             it = S->pending.erase(it);
         }
@@ -552,6 +554,7 @@ int make_request(const f184gi_request* req, Request** out) {
     for (uint32_t i = 0; i < req->nviews; ++i) {
         const f184gi_view& v = req->views[i];
         if (!v.depth || !v.normal || !v.roughness || !v.out || v.width == 0 || v.height == 0 ||
+            v.width > kMaxViewSide || v.height > kMaxViewSide ||
             (v.out_format != F184GI_FMT_F32 && v.out_format != F184GI_FMT_F16))
             return fail(F184GI_ERR_INVALID, "server_submit: malformed view " + std::to_string(i));
     }
@@ -575,6 +578,7 @@ int admit_check(f184gi_server* S, const Request* r) {
             return fail(F184GI_ERR_INVALID, "server_submit: move range out of bounds");
     if (r->views.size() > S->cfg.max_batch_views)
         return fail(F184GI_ERR_INVALID, "server_submit: more views than max_batch_views");
+    if (r->pixels > kMaxTracePixels) return fail(F184GI_ERR_INVALID, "server_submit: more than 2^36 pixels");
     if (S->cfg.hbm_budget && r->staging > S->cfg.hbm_budget)
         return fail(F184GI_ERR_BUDGET, "server_submit: the request's staging exceeds the HBM budget");
     return F184GI_OK;

@@ -8,6 +8,8 @@
   occupancy and counts bit-exact against the oracle;
 - cone parameters off the defaults, including diffuse cones narrow enough that their marches run past the
   per-launch schedule table into the device recurrence: within REL_TOL of the oracle;
+- views past the size limits (a side over 16384 pixels) are refused on the host with F184GI_ERR_INVALID by the
+  trace and the G-buffer raster, before any launch;
 - a bounded device wait that expires is reported as F184GI_ERR_TIMEOUT by the next sync, and the context goes on
   working (the failure path of the library's bounded waits, without a GPU fault).
 """
@@ -191,3 +193,20 @@ def test_expired_bounded_wait_is_reported_and_the_context_stays_usable(case):
     case.gi.sync()  # the status was consumed by the report
     after = case.trace()
     assert np.array_equal(before.view(np.uint32), after.view(np.uint32))
+
+
+def test_oversize_views_are_refused_before_any_launch(case):
+    import final184_gb300 as g
+    from final184_gb300 import _abi
+
+    view, P, bufs = make_view(case, 8, 4)
+    for W, H in [(16385, 1), (1, 16385)]:
+        big = g.make_view(case.V, P, W, H, bufs[0].data_ptr(), bufs[1].data_ptr(), bufs[2].data_ptr(),
+                          bufs[3].data_ptr())
+        with pytest.raises(_abi.F184Error) as err:
+            case.gi.trace(case.grid, [big])
+        assert err.value.code == _abi.ERR_INVALID and "16384" in str(err.value)
+        with pytest.raises(_abi.F184Error) as err:
+            case.gi.gbuffer(case.tri_d.data_ptr(), case.rough_d.data_ptr(), case.ntris, big)
+        assert err.value.code == _abi.ERR_INVALID
+    case.gi.sync()  # nothing was launched: no device status

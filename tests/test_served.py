@@ -284,7 +284,7 @@ def test_admission_budget_cancel_and_timeout(fx):
     srv.close()
     # a host-buffer request whose staging can never fit is refused at submission
     srv = fx.server(slots=1, hbm_budget=2 << 30)
-    big = 1 << 15
+    big = 1 << 14  # the largest view side: 16384^2 pixels stage ~11 GB of G-buffer and output
     bogus = np.zeros(16, np.float32)
     v = g.make_view(np.eye(4), g.perspective(59.0, 1.0, 0.1, 100.0), big, big, bogus.ctypes.data, bogus.ctypes.data,
                     bogus.ctypes.data, bogus.ctypes.data)
