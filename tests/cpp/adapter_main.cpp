@@ -83,7 +83,48 @@ int main() {
     bool same = std::memcmp(a.data(), b.data(), a.size() * 4) == 0;
     std::printf("adapter %s the C ABI path (%llu triangles in %u primitives, mean output %.6f)\n",
                 same ? "matches" : "DIFFERS FROM", (unsigned long long)sc->ntris, sc->nobjects, sum / a.size());
+
+    // view culling: the camera frustum placed in the world, the primitives outside it dropped by CullList, the
+    // kept ones voxelized through the adapter and, concatenated on the host, through the C ABI: same L0 bytes
+    Foreground::GIFrustum cam;
+    CHECK(Foreground::GIFrustumDefine(proj, &cam));
+    float world[16];
+    CHECK(f184gi_mat4_inverse(view, world));  // the camera node's world transform
+    Foreground::GIMatrix3x4 cam_world;
+    std::memcpy(cam_world.m, world, 48);
+    std::vector<Foreground::GIMatrix3x4> kept_mats;
+    std::vector<const Foreground::GIPrimitive*> kept;
+    Foreground::CullList(Foreground::GIFrustumTransformed(cam, cam_world), mats, list, kept_mats, kept);
+    Foreground::CVoxelGI culled(desc);
+    CHECK(culled.Status());
+    CHECK(culled.RenderList(kept_mats, kept, sc->light, &sc->bounds));
+    std::vector<float> soup;
+    std::vector<uint32_t> soup_alb;
+    for (const Foreground::GIPrimitive* p : kept) {
+        soup.insert(soup.end(), p->xyz, p->xyz + p->ntris * 9);
+        soup_alb.insert(soup_alb.end(), p->albedo, p->albedo + p->ntris);
+    }
+    uint64_t nkept = soup_alb.size();
+    float* d_soup = nullptr;
+    uint32_t* d_soup_alb = nullptr;
+    cudaMalloc(&d_soup, nkept * 36);
+    cudaMalloc(&d_soup_alb, nkept * 4);
+    cudaMemcpy(d_soup, soup.data(), nkept * 36, cudaMemcpyHostToDevice);
+    cudaMemcpy(d_soup_alb, soup_alb.data(), nkept * 4, cudaMemcpyHostToDevice);
+    uint32_t grid2 = 0;
+    CHECK(f184gi_grid_create(ctx, &desc, &grid2));
+    CHECK(f184gi_voxelize(ctx, grid2, d_soup, d_soup_alb, nkept, &sc->bounds, &sc->light, nullptr, 0, nullptr));
+    CHECK(f184gi_sync(ctx, nullptr));
+    CHECK(f184gi_sync(culled.Context(), nullptr));
+    const size_t nvox = size_t(desc.dim) * desc.dim * desc.dim * 4;
+    std::vector<float> la(nvox), lb(nvox);
+    CHECK(f184gi_grid_read_level(culled.Context(), culled.Grid(), 0, 0, la.data()));
+    CHECK(f184gi_grid_read_level(ctx, grid2, 0, 0, lb.data()));
+    const bool same_culled = std::memcmp(la.data(), lb.data(), nvox * 4) == 0;
+    std::printf("culled adapter %s the C ABI path (%zu of %u primitives kept, %llu triangles)\n",
+                same_culled ? "matches" : "DIFFERS FROM", kept.size(), sc->nobjects, (unsigned long long)nkept);
+    const bool culled_some = !kept.empty() && kept.size() < sc->nobjects;
     f184gi_destroy(ctx);
     f184gi_scene_free(sc);
-    return same && sum > 0.0 ? 0 : 2;
+    return same && sum > 0.0 && same_culled && culled_some ? 0 : 2;
 }
