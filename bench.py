@@ -574,38 +574,47 @@ def run_served(args, cfg=SERVED):
     batch_views = {}  # batches of the timed stream -> their views
     for r, (_, _, _, vids) in zip(results, reqs):
         batch_views[r.batch] = batch_views.get(r.batch, 0) + len(vids)
-    # ---- plain: the same stream back to back, one request at a time, FP32 grids, full voxelization ----
-    plain_lat = []
-    geo = [sc.tri_xyz.copy() for sc, _, _ in scenes]
-    grids = [gi.create_grid(dim, levels, g.FMT_F32, 0, cfg["shadow_res"]) for _, dim, levels in scenes]
-    dtri = [torch.from_numpy(x).to(dev) for x in geo]
-    dalb = [torch.from_numpy(sc.albedo.view(np.int32)).to(dev) for sc, _, _ in scenes]
-    outs = [torch.empty(2 * max_px * 4, dtype=torch.float32, device=dev) for _ in range(16)]
-    for si, (sc, _, _) in enumerate(scenes):  # warm-up, outside the timing: scratch and first launches
-        gi.voxelize(grids[si], dtri[si].data_ptr(), dalb[si].data_ptr(), sc.ntris, sc.light, bounds=sc.bounds)
-        gi.mip(grids[si])
-        gi.trace(grids[si], views_for(si, [0], g.FMT_F32))
-    gi.sync()
-    torch.cuda.synchronize()
-    p0 = time.perf_counter()
-    for ta, si, moves, vids in reqs:
-        r0 = time.perf_counter()
-        sc = scenes[si][0]
-        for f, c, off in moves:  # the caller moves its geometry and re-uploads it
-            seg = geo[si][f * 9:(f + c) * 9].reshape(-1, 3)
-            seg += np.asarray(off, dtype=np.float32)
-        dtri[si].copy_(torch.from_numpy(geo[si]))
-        gi.voxelize(grids[si], dtri[si].data_ptr(), dalb[si].data_ptr(), sc.ntris, sc.light, bounds=sc.bounds)
-        gi.mip(grids[si])
-        for v in views_for(si, vids, g.FMT_F32):
-            gi.trace(grids[si], [v])
+
+    def plain_arm(fmt):
+        """The same stream back to back, one request at a time, full voxelization, `fmt` grids and output;
+        returns (Mpix/s, sorted request latencies in ms, wall seconds)."""
+        lat = []
+        geo = [sc.tri_xyz.copy() for sc, _, _ in scenes]
+        grids = [gi.create_grid(dim, levels, fmt, 0, cfg["shadow_res"]) for _, dim, levels in scenes]
+        dtri = [torch.from_numpy(x).to(dev) for x in geo]
+        dalb = [torch.from_numpy(sc.albedo.view(np.int32)).to(dev) for sc, _, _ in scenes]
+        odt = torch.float32 if fmt == g.FMT_F32 else torch.float16
+        outs[:] = [torch.empty(2 * max_px * 4, dtype=odt, device=dev) for _ in range(16)]
+        for si, (sc, _, _) in enumerate(scenes):  # warm-up, outside the timing: scratch and first launches
+            gi.voxelize(grids[si], dtri[si].data_ptr(), dalb[si].data_ptr(), sc.ntris, sc.light, bounds=sc.bounds)
+            gi.mip(grids[si])
+            gi.trace(grids[si], views_for(si, [0], fmt))
         gi.sync()
-        plain_lat.append((time.perf_counter() - r0) * 1e3)
-    plain_s = time.perf_counter() - p0
+        torch.cuda.synchronize()
+        p0 = time.perf_counter()
+        for ta, si, moves, vids in reqs:
+            r0 = time.perf_counter()
+            sc = scenes[si][0]
+            for f, c, off in moves:  # the caller moves its geometry and re-uploads it
+                seg = geo[si][f * 9:(f + c) * 9].reshape(-1, 3)
+                seg += np.asarray(off, dtype=np.float32)
+            dtri[si].copy_(torch.from_numpy(geo[si]))
+            gi.voxelize(grids[si], dtri[si].data_ptr(), dalb[si].data_ptr(), sc.ntris, sc.light, bounds=sc.bounds)
+            gi.mip(grids[si])
+            for v in views_for(si, vids, fmt):
+                gi.trace(grids[si], [v])
+            gi.sync()
+            lat.append((time.perf_counter() - r0) * 1e3)
+        wall = time.perf_counter() - p0
+        for gr in grids:
+            gi.destroy_grid(gr)
+        return pixels / wall / 1e6, sorted(lat), wall
+
+    # ---- plain: FP32 grids (the per-request path the served form is held against), then FP16 grids ----
+    plain_mpix, plain_lat, plain_s = plain_arm(g.FMT_F32)
+    p16_mpix, p16_lat, p16_s = plain_arm(g.FMT_F16)
     gi.close()
-    plain_lat.sort()
     served_mpix = pixels / served_s / 1e6
-    plain_mpix = pixels / plain_s / 1e6
     return {
         "workload": "%d requests, Poisson arrivals at %.0f req/s, 0-5%% of a scene's objects moved, 1-16 views of "
                     "512x512..1920x1080 on resident grids %s, %.0f GB admission budget; both arms warmed up first "
@@ -622,7 +631,13 @@ def run_served(args, cfg=SERVED):
         "plain": {"value": round(plain_mpix, 2), "unit": "Mpix/s", "p50_ms": round(plain_lat[len(plain_lat) // 2], 2),
                   "p99_ms": round(plain_lat[min(len(plain_lat) - 1, int(0.99 * len(plain_lat)))], 2),
                   "wall_s": round(plain_s, 3), "storage": "fp32, full voxelization per request, one launch per view"},
+        "plain_fp16": {"value": round(p16_mpix, 2), "unit": "Mpix/s", "p50_ms": round(p16_lat[len(p16_lat) // 2], 2),
+                       "p99_ms": round(p16_lat[min(len(p16_lat) - 1, int(0.99 * len(p16_lat)))], 2),
+                       "wall_s": round(p16_s, 3),
+                       "storage": "fp16, full voxelization per request, one launch per view (the served form's "
+                                  "storage without its serving)"},
         "served_over_plain": round(served_mpix / plain_mpix, 3),
+        "served_over_plain_fp16": round(served_mpix / p16_mpix, 3),
     }
 
 
