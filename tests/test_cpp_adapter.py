@@ -14,7 +14,8 @@ CUDA = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 def build_adapter(tmp):
     exe = os.path.join(tmp, "adapter_main")
     libdir = os.path.join(ROOT, "final184_gb300")
-    cmd = ["g++", "-std=c++17", "-O2", "-I", os.path.join(ROOT, "include"), "-I", os.path.join(CUDA, "include"),
+    # the header is included by the renderer's own sources: it must build warning-free under strict flags
+    cmd = ["g++", "-std=c++17", "-O2", "-Wall", "-Wextra", "-Werror", "-I", os.path.join(ROOT, "include"), "-I", os.path.join(CUDA, "include"),
            os.path.join(ROOT, "tests", "cpp", "adapter_main.cpp"), "-o", exe, "-L", libdir, "-lf184gi",
            "-Wl,-rpath," + libdir, "-L", os.path.join(CUDA, "lib64"), "-lcudart", "-Wl,-rpath," + os.path.join(CUDA, "lib64")]
     subprocess.run(cmd, check=True, capture_output=True, text=True)
