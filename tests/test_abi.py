@@ -42,7 +42,10 @@ def test_struct_layouts_match_c():
 
     structs = {"f184gi_vec3": _abi.Vec3, "f184gi_bounds": _abi.Bounds, "f184gi_light": _abi.Light,
                "f184gi_grid_desc": _abi.GridDesc, "f184gi_grid_frame": _abi.GridFrame, "f184gi_view": _abi.View,
-               "f184gi_cone_params": _abi.ConeParams, "f184gi_config": _abi.Config, "f184gi_scene": _abi.Scene}
+               "f184gi_cone_params": _abi.ConeParams, "f184gi_config": _abi.Config, "f184gi_scene": _abi.Scene,
+               "f184gi_move": _abi.Move, "f184gi_march_params": _abi.MarchParams,
+               "f184gi_server_config": _abi.ServerConfig, "f184gi_request": _abi.Request,
+               "f184gi_request_result": _abi.RequestResult, "f184gi_server_stats": _abi.ServerStats}
     src = '#include <stdio.h>\n#include "f184gi.h"\nint main(){\n'
     for name in structs:
         src += '  printf("%%zu\\n", sizeof(%s));\n' % name
@@ -51,7 +54,9 @@ def test_struct_layouts_match_c():
         c = os.path.join(d, "s.c")
         open(c, "w").write(src)
         exe = os.path.join(d, "s")
-        subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), c, "-o", exe], check=True)
+        # plain C99 with strict warnings: the header is what a C (or cgo / ctypes) caller includes
+        subprocess.run(["gcc", "-std=c99", "-Wall", "-Wextra", "-Werror", "-pedantic", "-I", os.path.join(ROOT, "include"),
+                        c, "-o", exe], check=True)
         sizes = [int(x) for x in subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split()]
     for (name, cls), sz in zip(structs.items(), sizes):
         assert C.sizeof(cls) == sz, name
