@@ -46,9 +46,12 @@ def test_struct_layouts_match_c():
                "f184gi_move": _abi.Move, "f184gi_march_params": _abi.MarchParams,
                "f184gi_server_config": _abi.ServerConfig, "f184gi_request": _abi.Request,
                "f184gi_request_result": _abi.RequestResult, "f184gi_server_stats": _abi.ServerStats}
-    src = '#include <stdio.h>\n#include "f184gi.h"\nint main(){\n'
+    src = '#include <stddef.h>\n#include <stdio.h>\n#include "f184gi.h"\nint main(void){\n'
     for name in structs:
         src += '  printf("%%zu\\n", sizeof(%s));\n' % name
+    for name, cls in structs.items():  # then every field's offset, in the mirror's order
+        for field, _ in cls._fields_:
+            src += '  printf("%%zu\\n", offsetof(%s, %s));\n' % (name, field)
     src += "  return 0;\n}\n"
     with tempfile.TemporaryDirectory() as d:
         c = os.path.join(d, "s.c")
@@ -60,6 +63,10 @@ def test_struct_layouts_match_c():
         sizes = [int(x) for x in subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split()]
     for (name, cls), sz in zip(structs.items(), sizes):
         assert C.sizeof(cls) == sz, name
+    offsets = iter(sizes[len(structs):])
+    for name, cls in structs.items():
+        for field, _ in cls._fields_:
+            assert getattr(cls, field).offset == next(offsets), (name, field)
     assert C.sizeof(_abi.Vec3) == 12 and C.sizeof(_abi.Bounds) == 32
 
 
