@@ -636,8 +636,8 @@ int f184gi_gbuffer(f184gi_ctx* c, const float* tri, const float* rough, uint64_t
                    uint32_t* tri_id_out, void* stream) {
     if (!c || !view || !tri || !rough) return fail(F184GI_ERR_INVALID, "gbuffer: null argument");
     if (!view->depth || !view->normal || !view->roughness) return fail(F184GI_ERR_INVALID, "gbuffer: null G-buffer planes");
-    if (view->width == 0 || view->height == 0 || view->width > kMaxViewSide || view->height > kMaxViewSide)
-        return fail(F184GI_ERR_INVALID, "gbuffer: view sides must be 1.." + std::to_string(kMaxViewSide) + " pixels");
+    if (view->width == 0 || view->height == 0 || view->width > kMaxRasterSide || view->height > kMaxRasterSide)
+        return fail(F184GI_ERR_INVALID, "gbuffer: view sides must be 1.." + std::to_string(kMaxRasterSide) + " pixels");
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     RasterJob rj{};
     rj.tri = tri;

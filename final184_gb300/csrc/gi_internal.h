@@ -21,6 +21,7 @@ constexpr uint32_t kStatusTimeout = 2u;
 // View sides of 1..kMaxViewSide pixels; one trace call covers at most kMaxTracePixels pixels in all, so that its
 // warp-tile numbering (32 pixels a tile) stays inside uint32.
 constexpr uint32_t kMaxViewSide = 16384;
+constexpr uint32_t kMaxRasterSide = 8192;  // rasterized images (shadow maps, G-buffers): 1/16-pixel snaps in range
 constexpr uint64_t kMaxTracePixels = 1ull << 36;
 constexpr uint32_t kStatusRange = 4u;  // geometry outside the fixed-point range was skipped
 

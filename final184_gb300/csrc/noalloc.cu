@@ -65,8 +65,9 @@ extern "C" int f184gi_gbuffer_static(f184gi_ctx* c, const float* tri, const floa
     if (!c || !view || !tri || !rough) return fail(F184GI_ERR_INVALID, "gbuffer_static: null argument");
     if (!view->depth || !view->normal || !view->roughness)
         return fail(F184GI_ERR_INVALID, "gbuffer_static: null G-buffer planes");
-    if (view->width == 0 || view->height == 0 || view->width > kMaxViewSide || view->height > kMaxViewSide)
-        return fail(F184GI_ERR_INVALID, "gbuffer_static: view sides must be 1.." + std::to_string(kMaxViewSide) + " pixels");
+    if (view->width == 0 || view->height == 0 || view->width > kMaxRasterSide || view->height > kMaxRasterSide)
+        return fail(F184GI_ERR_INVALID,
+                    "gbuffer_static: view sides must be 1.." + std::to_string(kMaxRasterSide) + " pixels");
     const uint64_t npix = uint64_t(view->width) * view->height;
     if (ntris > kStaticMaxTris)
         return fail(F184GI_ERR_INVALID, "gbuffer_static: " + std::to_string(ntris) + " triangles exceed the limit of " +

@@ -372,7 +372,7 @@ size_t raster_scratch_bytes(uint64_t ntris, uint32_t W, uint32_t H) {
 }
 
 int raster_launch(const RasterJob& job, void* scratch, size_t scratch_bytes, uint32_t* d_status, cudaStream_t s) {
-    if (job.width == 0 || job.height == 0 || job.width > 8192 || job.height > 8192)
+    if (job.width == 0 || job.height == 0 || job.width > kMaxRasterSide || job.height > kMaxRasterSide)
         return fail(F184GI_ERR_INVALID, "raster: viewport out of range");
     if (job.ntris >= 0xffff0000ull) return fail(F184GI_ERR_INVALID, "raster: too many triangles");
     const uint32_t tiles_x = (job.width + kTile - 1) / kTile, tiles_y = (job.height + kTile - 1) / kTile;

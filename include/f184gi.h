@@ -119,7 +119,8 @@ typedef struct f184gi_grid_frame {
 typedef struct f184gi_view {
     float view[16]; /* world -> view, row-major */
     float proj[16]; /* view -> clip, row-major (CCamera::CalcPerspective convention) */
-    uint32_t width, height; /* 1..16384 each; one trace call (or served batch) covers at most 2^36 pixels */
+    uint32_t width, height; /* 1..16384 each (1..8192 for f184gi_gbuffer); a trace call or served batch covers
+                             * at most 2^36 pixels */
     const float* depth;
     const uint32_t* normal;
     const uint16_t* roughness;

@@ -8,8 +8,8 @@
   occupancy and counts bit-exact against the oracle;
 - cone parameters off the defaults, including diffuse cones narrow enough that their marches run past the
   per-launch schedule table into the device recurrence: within REL_TOL of the oracle;
-- views past the size limits (a side over 16384 pixels) are refused on the host with F184GI_ERR_INVALID by the
-  trace and the G-buffer raster, before any launch;
+- views past the size limits (a side over 16384 pixels for the trace, over 8192 for the G-buffer raster) are
+  refused on the host with F184GI_ERR_INVALID, before any launch;
 - a bounded device wait that expires is reported as F184GI_ERR_TIMEOUT by the next sync, and the context goes on
   working (the failure path of the library's bounded waits, without a GPU fault).
 """
@@ -200,7 +200,7 @@ def test_oversize_views_are_refused_before_any_launch(case):
     from final184_gb300 import _abi
 
     view, P, bufs = make_view(case, 8, 4)
-    for W, H in [(16385, 1), (1, 16385)]:
+    for W, H in [(16385, 1), (1, 16385)]:  # past both limits
         big = g.make_view(case.V, P, W, H, bufs[0].data_ptr(), bufs[1].data_ptr(), bufs[2].data_ptr(),
                           bufs[3].data_ptr())
         with pytest.raises(_abi.F184Error) as err:
@@ -209,4 +209,10 @@ def test_oversize_views_are_refused_before_any_launch(case):
         with pytest.raises(_abi.F184Error) as err:
             case.gi.gbuffer(case.tri_d.data_ptr(), case.rough_d.data_ptr(), case.ntris, big)
         assert err.value.code == _abi.ERR_INVALID
+    # past the raster's limit only: the G-buffer call refuses it (the view is never traced: its buffers are small)
+    wide = g.make_view(case.V, P, 8193, 1, bufs[0].data_ptr(), bufs[1].data_ptr(), bufs[2].data_ptr(),
+                       bufs[3].data_ptr())
+    with pytest.raises(_abi.F184Error) as err:
+        case.gi.gbuffer(case.tri_d.data_ptr(), case.rough_d.data_ptr(), case.ntris, wide)
+    assert err.value.code == _abi.ERR_INVALID and "8192" in str(err.value)
     case.gi.sync()  # nothing was launched: no device status
