@@ -450,8 +450,8 @@ def run_gpu(args, cfg):
                      "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_source": peak_kind,
                      "algorithmic_bytes": alg[top],
                      "traffic": (tr * 1.0 if isinstance(tr, (int, float)) else None),
-                     "note": "far below the HBM roof: the trace is instruction-issue bound (ncu: ~67% issue-active, "
-                             "L1 hit ~92%, L2 ~2% and DRAM ~0.4% of peak); algorithmic bytes = G-buffer 10 B + output 32 B per "
+                     "note": "far below the HBM roof: the trace is instruction-issue bound (ncu: ~68% issue-active, "
+                             "L1 hit ~93%, L2 ~2% and DRAM ~0.4% of peak); algorithmic bytes = G-buffer 10 B + output 32 B per "
                              "pixel + the whole chain once (upper bound of the touched part)",
                      "sampled": {"bytes": int(sampled), "achieved": round(sampled / (means[top] * 1e-3) / 1e9, 1),
                                  "unit": "GB/s", "l2_copy_gbs": round(l2_gbs, 1),
