@@ -2,15 +2,18 @@
 
   oracle/_build/liboracle.so  -- the CPU restatement in oracle.cpp (FP64 oracle + FP32 CPU baseline)
   oracle/_ref/libf184ref.so   -- the reference's own Math library and CCamera (Foreground/SceneGraph/Camera.cpp),
-                                 compiled from /root/reference sources where they lie, plus ref_shim.cpp; only
+                                 compiled from the reference sources where they lie, plus ref_shim.cpp; only
                                  built when that tree is present (it is not on GPU machines).
+  oracle/_ref/libf184glsl.so  -- the reference's shader functions compiled as C++ (glsl_pin.py), same condition.
+
+The reference tree is taken from the F184_REFERENCE environment variable (default /root/reference).
 """
 import glob
 import os
 import subprocess
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_ROOT = "/root/reference"
+REF_ROOT = os.environ.get("F184_REFERENCE", "/root/reference")
 LIB = os.path.join(HERE, "_build", "liboracle.so")
 REF_LIB = os.path.join(HERE, "_ref", "libf184ref.so")
 
@@ -55,6 +58,14 @@ def build(force=False):
         build_ref(force)
     except RuntimeError as e:  # the reference pin is optional; the oracle is not
         print("warning: reference Math/Camera build failed:", str(e).splitlines()[0])
+    try:
+        from . import glsl_pin
+    except ImportError:  # run as a script
+        import glsl_pin
+    try:
+        glsl_pin.build(force)
+    except RuntimeError as e:
+        print("warning: reference shader pin build failed:", str(e).splitlines()[0])
 
 
 if __name__ == "__main__":

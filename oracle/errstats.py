@@ -1,0 +1,70 @@
+"""Error statistics of a device result against the FP64 oracle.  TEST INFRASTRUCTURE ONLY.
+
+The parity gate is a TRUE relative error per value, |got - ref| / |ref|, taken over every value above a
+near-black floor.  The floor is stated, not tuned: FLOOR_FRAC (1e-3) times the 99th percentile of |ref| over the
+nonzero values of the same channel group.  Values at or below the floor are counted and their absolute error is
+reported (and bounded by the callers: REL_TOL times the floor, i.e. the error a value exactly at the floor would be
+allowed).  The groups are the radiance channels (RGB) and the opacity / occlusion channel (A) of RGBA data, whose
+scales differ by orders of magnitude; data whose last axis is not 4 is one group.
+
+Why this floor: below ~1e-3 of the image's bright end a pixel is black on any display (an 8-bit channel steps by
+1/255 ~ 3.9e-3 of full scale), and there an FP32 evaluation has a constant ABSOLUTE error of ~1e-8 (the trilinear
+weights of a cone sample carry the rounding of its FP32 position, ~3e-5 voxel at 256 voxels), so its relative
+error grows without bound as the value goes to zero.  An FP16-stored chain has a bounded RELATIVE error instead.
+"""
+from typing import NamedTuple
+
+import numpy as np
+
+REL_TOL = 1e-3
+FLOOR_FRAC = 1e-3
+
+
+class Err(NamedTuple):
+    max: float        # max true relative error over the values above the floor
+    rms: float        # RMS of the same
+    n: int            # values above the floor
+    below: int        # values at or below the floor (near-black), not in max / rms
+    below_abs: float  # max |got - ref| over those
+    below_ok: bool    # below_abs <= REL_TOL * floor of each group
+    floor: float      # the radiance (or single-group) floor
+    floor_a: float    # the alpha floor (RGBA data), else 0
+
+    def ok(self, tol=REL_TOL):
+        return self.max < tol and self.below_ok
+
+    def __str__(self):
+        return ("max %.3e rms %.3e over %d values; %d near-black (floor %.2e%s) max abs %.2e"
+                % (self.max, self.rms, self.n, self.below, self.floor,
+                   ", alpha floor %.2e" % self.floor_a if self.floor_a else "", self.below_abs))
+
+
+def group_floor(ref, frac=FLOOR_FRAC):
+    a = np.abs(np.asarray(ref, dtype=np.float64)).ravel()
+    nz = a[a > 0]
+    return float(frac * np.percentile(nz, 99)) if nz.size else 0.0
+
+
+def rel_err(got, ref, frac=FLOOR_FRAC, tol=REL_TOL):
+    got = np.asarray(got, dtype=np.float64)
+    ref = np.asarray(ref, dtype=np.float64)
+    assert got.shape == ref.shape, (got.shape, ref.shape)
+    groups = [(got[..., :3], ref[..., :3]), (got[..., 3], ref[..., 3])] if ref.shape and ref.shape[-1] == 4 \
+        else [(got, ref)]
+    errs, n, below, below_abs, below_ok, floors = [], 0, 0, 0.0, True, []
+    for g, r in groups:
+        fl = group_floor(r, frac)
+        floors.append(fl)
+        d = np.abs(g - r)
+        above = np.abs(r) > fl
+        e = d[above] / np.abs(r[above])
+        errs.append(e)
+        n += int(above.sum())
+        b = d[~above]
+        below += int(b.size)
+        if b.size:
+            below_abs = max(below_abs, float(b.max()))
+            below_ok = below_ok and float(b.max()) <= tol * max(fl, 0.0)
+    e = np.concatenate(errs) if errs else np.zeros(0)
+    return Err(float(e.max()) if e.size else 0.0, float(np.sqrt(np.mean(e ** 2))) if e.size else 0.0, n, below,
+               below_abs, below_ok, floors[0], floors[1] if len(floors) > 1 else 0.0)

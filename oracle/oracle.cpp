@@ -1254,13 +1254,20 @@ Vec3<T> ref_w2v(const RefMaps<T>& m, Vec3<T> p) {
     return Vec3<T>{p.x * m.s + m.b[0], p.y * m.s + m.b[1], p.z * m.s + m.b[2]};
 }
 
+// The two uniform numbers of ray `seed` of pixel `pix` in frame `frame`: they stand where indirect.frag:113-117
+// draws rands.x (the cosine-sampling u) and rands.y (the angle v, also the start offset) from its frame-dependent noise.
+inline void march_rands(uint32_t frame, uint32_t pix, uint32_t seed, float& ru, float& rv) {
+    const uint32_t key = lowbias32(frame * 16u + seed * 2u);
+    ru = float(lowbias32(pix ^ key) >> 8) * 5.9604644775390625e-8f;
+    rv = float(lowbias32(pix ^ (key + 0x9e3779b9u)) >> 8) * 5.9604644775390625e-8f;
+}
+
 template <class T>
 Vec3<T> march_ray(const MarchCtx<T>& C, uint32_t pix, Vec3<T> wpos, Vec3<T> wnorm, uint32_t seed, RefHit<T>& hit) {
     hit.hit = false;
     Vec3<T> lo{T(0), T(0), T(0)};
-    const uint32_t key = lowbias32(C.p.frame * 16u + seed * 2u);
-    const float ru = float(lowbias32(pix ^ key) >> 8) * 5.9604644775390625e-8f;
-    const float rv = float(lowbias32(pix ^ (key + 0x9e3779b9u)) >> 8) * 5.9604644775390625e-8f;
+    float ru, rv;
+    march_rands(C.p.frame, pix, seed, ru, rv);
     const T ct = std::sqrt(T(1) - T(ru));
     const T st = std::sqrt(T(1) - ct * ct);
     T sp, cp;
@@ -1346,11 +1353,8 @@ Vec3<T> march_ray(const MarchCtx<T>& C, uint32_t pix, Vec3<T> wpos, Vec3<T> wnor
 }
 
 template <class T>
-int march_impl(const f184gi_grid_frame* frame, uint32_t dim, const uint32_t* vol, const float* shadow, uint32_t res,
-               const f184gi_light* light, const float view[16], const float proj[16], uint32_t W, uint32_t H,
-               const float* depth, const uint32_t* normal, const f184gi_march_params* params, T* out,
-               uint32_t row_begin, uint32_t row_end, int nthreads) {
-    if (!frame || !vol || !shadow || !light || !view || !proj || !depth || !normal || !params || !out) return -1;
+MarchCtx<T> march_ctx(const f184gi_grid_frame* frame, uint32_t dim, const uint32_t* vol, const float* shadow,
+                      uint32_t res, const f184gi_light* light, const f184gi_march_params* params) {
     MarchCtx<T> C;
     C.m = ref_maps_t<T>(frame);
     C.vol = vol;
@@ -1365,6 +1369,36 @@ int march_impl(const f184gi_grid_frame* frame, uint32_t dim, const uint32_t* vol
     for (int k = 0; k < 64; ++k)
         C.pow6[k] = std::is_same<T, float>::value ? T(float(std::pow(double(float(k) / 63.0f), 2.2)))
                                                   : T(std::pow(double(k) / 63.0, 2.2));
+    return C;
+}
+
+// One pixel of the reference's combine (indirect.frag:197-222 without the temporal blend): `rays` rays, each with
+// its second bounce weighted by the first hit's brdf, times 1 / rays.
+template <class T>
+Vec3<T> march_pixel(const MarchCtx<T>& C, uint32_t pix, Vec3<T> wpos, Vec3<T> wn) {
+    Vec3<T> acc{T(0), T(0), T(0)};
+    RefHit<T> h;
+    for (uint32_t k = 0; k < C.p.rays; ++k) {
+        const Vec3<T> l1 = march_ray(C, pix, wpos, wn, 2 * k, h);
+        acc = Vec3<T>{acc.x + l1.x, acc.y + l1.y, acc.z + l1.z};
+        if (h.hit && C.p.second_bounce) {
+            const Vec3<T> br = h.brdf;
+            RefHit<T> h2;
+            const Vec3<T> l2 = march_ray(C, pix, h.wpos, h.wnorm, 2 * k + 1, h2);
+            acc = Vec3<T>{acc.x + br.x * l2.x, acc.y + br.y * l2.y, acc.z + br.z * l2.z};
+        }
+    }
+    const T sc = T(1) / T(float(C.p.rays));
+    return Vec3<T>{acc.x * sc, acc.y * sc, acc.z * sc};
+}
+
+template <class T>
+int march_impl(const f184gi_grid_frame* frame, uint32_t dim, const uint32_t* vol, const float* shadow, uint32_t res,
+               const f184gi_light* light, const float view[16], const float proj[16], uint32_t W, uint32_t H,
+               const float* depth, const uint32_t* normal, const f184gi_march_params* params, T* out,
+               uint32_t row_begin, uint32_t row_end, int nthreads) {
+    if (!frame || !vol || !shadow || !light || !view || !proj || !depth || !normal || !params || !out) return -1;
+    const MarchCtx<T> C = march_ctx<T>(frame, dim, vol, shadow, res, light, params);
     double V[16], P[16], IV[16], IP[16];
     for (int i = 0; i < 16; ++i) V[i] = view[i], P[i] = proj[i];
     if (!inverse4(V, IV) || !inverse4(P, IP)) return -1;
@@ -1422,20 +1456,8 @@ int march_impl(const f184gi_grid_frame* frame, uint32_t dim, const uint32_t* vol
                 wn = Vec3<T>{T(IV[0] * cn.x + IV[1] * cn.y + IV[2] * cn.z), T(IV[4] * cn.x + IV[5] * cn.y + IV[6] * cn.z),
                              T(IV[8] * cn.x + IV[9] * cn.y + IV[10] * cn.z)};
             }
-            Vec3<T> acc{T(0), T(0), T(0)};
-            RefHit<T> h;
-            for (uint32_t k = 0; k < C.p.rays; ++k) {
-                const Vec3<T> l1 = march_ray(C, uint32_t(pix), wpos, wn, 2 * k, h);
-                acc = Vec3<T>{acc.x + l1.x, acc.y + l1.y, acc.z + l1.z};
-                if (h.hit && C.p.second_bounce) {
-                    const Vec3<T> br = h.brdf;
-                    RefHit<T> h2;
-                    const Vec3<T> l2 = march_ray(C, uint32_t(pix), h.wpos, h.wnorm, 2 * k + 1, h2);
-                    acc = Vec3<T>{acc.x + br.x * l2.x, acc.y + br.y * l2.y, acc.z + br.z * l2.z};
-                }
-            }
-            const T sc = T(1) / T(float(C.p.rays));
-            o[0] = acc.x * sc, o[1] = acc.y * sc, o[2] = acc.z * sc, o[3] = -cs.z;
+            const Vec3<T> acc = march_pixel(C, uint32_t(pix), wpos, wn);
+            o[0] = acc.x, o[1] = acc.y, o[2] = acc.z, o[3] = -cs.z;
         }
     });
     return 0;
@@ -1560,6 +1582,30 @@ int orc_march_f64(const f184gi_grid_frame* frame, uint32_t dim, const uint32_t* 
                               row_begin, row_end, nthreads);
 }
 void orc_sincos_turns(float v, float* s, float* c) { sincos_turns32(v, *s, *c); }
+
+// The FP32 march of n world-space points (position, normal), pixel index pix[i] for the ray numbers: the part of
+// orc_march_f32 after the G-buffer decode, for comparison with the reference's own getIndirect text.
+int orc_march_points_f32(const f184gi_grid_frame* frame, uint32_t dim, const uint32_t* vol, const float* shadow,
+                         uint32_t res, const f184gi_light* light, const f184gi_march_params* params,
+                         const uint32_t* pix, const float* wpos, const float* wnorm, uint64_t n, float* out) {
+    if (!frame || !vol || !shadow || !light || !params || !pix || !wpos || !wnorm || !out) return -1;
+    const MarchCtx<float> C = march_ctx<float>(frame, dim, vol, shadow, res, light, params);
+    parallel_for(0, int64_t(n), 0, [&](int64_t b, int64_t e) {
+        for (int64_t i = b; i < e; ++i) {
+            const Vec3<float> p{wpos[i * 3], wpos[i * 3 + 1], wpos[i * 3 + 2]};
+            const Vec3<float> nn{wnorm[i * 3], wnorm[i * 3 + 1], wnorm[i * 3 + 2]};
+            const Vec3<float> o = march_pixel(C, pix[i], p, nn);
+            out[i * 3] = o.x, out[i * 3 + 1] = o.y, out[i * 3 + 2] = o.z;
+        }
+    });
+    return 0;
+}
+
+// rands[i][seed][0..1] = (u, v) of ray `seed` (0 .. 2 * rays - 1) of pixel pix[i]
+void orc_march_rands(uint32_t frame, const uint32_t* pix, uint64_t n, uint32_t seeds, float* rands) {
+    for (uint64_t i = 0; i < n; ++i)
+        for (uint32_t k = 0; k < seeds; ++k) march_rands(frame, pix[i], k, rands[(i * seeds + k) * 2], rands[(i * seeds + k) * 2 + 1]);
+}
 
 }  // extern "C"
 

@@ -2,8 +2,8 @@
 bricks with six-direction anisotropic mips (9 levels), 4096^2 shadow map, 3840x2160 G-buffer.
 
 The oracle voxelizes the whole scene and builds the anisotropic chain in FP64, then traces every 64th row of the
-device's own G-buffer; the device output must be within REL_TOL (relative error with the 1e-2 absolute floor of
-gi_case.py) of it.  This is the error that the precision leg of bench.py runs under.
+device's own G-buffer; the device output must be within REL_TOL (true relative error per value above the
+near-black floor, oracle/errstats.py) of it.  This is the error that the precision leg of bench.py runs under.
 """
 import numpy as np
 import pytest
@@ -59,7 +59,7 @@ def test_precision_form_error_vs_fp64(lib, orc):
     rows = list(range(0, H, 64))
     ref = np.stack([orc.trace(fo, dim, levels, chain, V, P, W, H, dep, nrm, rg, rows=(r, r + 1), aniso=True)[:, r]
                     for r in rows], axis=1)
-    mx, rms = rel_err(got[:, rows], ref)
-    print("precision form vs FP64: %d rows, max %.3g rms %.3g" % (len(rows), mx, rms))
-    assert mx < REL_TOL
+    e = rel_err(got[:, rows], ref)
+    print("precision form vs FP64: %d rows," % len(rows), e)
+    assert e.ok(), str(e)
     assert ref[0, ..., :3].mean() > 1e-4  # lit
