@@ -15,6 +15,8 @@ import subprocess
 HERE = os.path.dirname(os.path.abspath(__file__))
 REF_ROOT = os.environ.get("F184_REFERENCE", "/root/reference")
 LIB = os.path.join(HERE, "_build", "liboracle.so")
+SCENE_LIB = os.path.join(HERE, "_build", "libscenehost.so")
+PRODUCT_CSRC = os.path.join(HERE, "..", "final184_gb300", "csrc")
 REF_LIB = os.path.join(HERE, "_ref", "libf184ref.so")
 
 
@@ -33,6 +35,19 @@ def build_oracle(force=False):
         _run(["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared", "-pthread",
               src[0], "-o", LIB])
     return LIB
+
+
+def build_scene_host(force=False):
+    """The product's seeded scene generator and camera helpers (csrc/scene.cpp, host C++) as a library of their own,
+    for the CPU arms of the benchmark, which must not load the CUDA library."""
+    os.makedirs(os.path.dirname(SCENE_LIB), exist_ok=True)
+    src = [os.path.join(PRODUCT_CSRC, "scene.cpp"), os.path.join(HERE, "scene_host_shim.cpp")]
+    deps = src + [os.path.join(PRODUCT_CSRC, "gi_internal.h"), os.path.join(HERE, "..", "include", "f184gi.h")]
+    if force or not os.path.exists(SCENE_LIB) or any(os.path.getmtime(s) > os.path.getmtime(SCENE_LIB) for s in deps):
+        cuda_inc = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "include")
+        _run(["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-I", cuda_inc, *src, "-o",
+              SCENE_LIB])
+    return SCENE_LIB
 
 
 def build_ref(force=False):
@@ -54,6 +69,7 @@ def build_ref(force=False):
 
 def build(force=False):
     build_oracle(force)
+    build_scene_host(force)
     try:
         build_ref(force)
     except RuntimeError as e:  # the reference pin is optional; the oracle is not
