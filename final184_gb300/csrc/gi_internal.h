@@ -106,7 +106,7 @@ int mip_launch(const ChainLayout& chain, uint32_t levels, uint32_t* d_status, cu
 
 struct TraceView {
     float iview[16], iproj[16];     // inverses (FP32 of FP64 inverses)
-    double iproj_zw[8];             // rows 2 and 3 of the FP64 inverse projection (depth reconstruction)
+    float iproj_zw_hi[8], iproj_zw_lo[8];  // rows 2 and 3 of the FP64 inverse projection as FP32 pairs hi + lo
     float eye[3];
     uint32_t width, height;
     const float* depth;
@@ -138,6 +138,13 @@ struct TraceConsts {
     unsigned long long* counts;  // the counting kernel's totals: cone steps, level samples (null otherwise)
 };
 void trace_consts_schedule(TraceConsts& tc);  // fills tc.sched from tc.p
+// rows 2 and 3 of the FP64 inverse projection, split into FP32 pairs (the trace's float-float depth rows)
+inline void trace_view_set_depth_rows(TraceView& t, const double IP[16]) {
+    for (int k = 0; k < 8; ++k) {
+        t.iproj_zw_hi[k] = float(IP[8 + k]);
+        t.iproj_zw_lo[k] = float(IP[8 + k] - double(t.iproj_zw_hi[k]));
+    }
+}
 // Cone-trace kernel variants: the tile shape (tw x th pixels, one thread each) and the CTAs kept resident per SM
 // (the register budget).  Every variant computes each pixel with the same arithmetic, so results are identical;
 // the batched launch picks the fastest by timing them on the work it serves.

@@ -72,6 +72,57 @@ __device__ __forceinline__ float3 oct_decode(uint32_t p) {
     return norm3(v);
 }
 
+// Address of element `idx` of a chain and the voxel `k` elements further (k an immediate offset of the load).
+template <int FMT>
+__device__ __forceinline__ const unsigned char* vox_ptr(const void* base, uint32_t idx) {
+    return static_cast<const unsigned char*>(base) + size_t(idx) * (FMT == F184GI_FMT_F32 ? 16u : 8u);
+}
+template <int FMT>
+__device__ __forceinline__ float4 load_vox_at(const unsigned char* p, int k) {
+    if (FMT == F184GI_FMT_F32) return __ldg(reinterpret_cast<const float4*>(p) + k);
+    const uint2 raw = __ldg(reinterpret_cast<const uint2*>(p) + k);
+    const float2 fa = __half22float2(*reinterpret_cast<const __half2*>(&raw.x));
+    const float2 fb = __half22float2(*reinterpret_cast<const __half2*>(&raw.y));
+    return make_float4(fa.x, fa.y, fb.x, fb.y);
+}
+
+// Float-float (unevaluated pairs hi + lo of FP32) arithmetic for the depth reconstruction, every operation
+// explicitly rounded: Knuth's two-sum and the FMA two-product are exact, so a row of the inverse projection,
+// split into FP32 pairs on the host, is evaluated to ~2^-46 of its largest term.
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+    s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+// (hi[0..3] + lo[0..3]) . (x, y, z, 1) as a pair
+__device__ __forceinline__ void ff_row(const float* hi, const float* lo, float x, float y, float z, float& rh,
+                                       float& rl) {
+    const float p0 = __fmul_rn(hi[0], x), p1 = __fmul_rn(hi[1], y), p2 = __fmul_rn(hi[2], z);
+    const float e0 = __fmaf_rn(hi[0], x, -p0), e1 = __fmaf_rn(hi[1], y, -p1), e2 = __fmaf_rn(hi[2], z, -p2);
+    float s0, s1, s2, t0, t1, t2;
+    two_sum(p0, p1, s0, t0);
+    two_sum(s0, p2, s1, t1);
+    two_sum(s1, hi[3], s2, t2);
+    const float small = __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(t0, t1), t2), __fadd_rn(__fadd_rn(e0, e1), e2)),
+                                  __fadd_rn(__fadd_rn(__fmul_rn(lo[0], x), __fmul_rn(lo[1], y)),
+                                            __fadd_rn(__fmul_rn(lo[2], z), lo[3])));
+    rh = __fadd_rn(s2, small);
+    rl = __fsub_rn(small, __fsub_rn(rh, s2));
+}
+// 1 / w and z / w of the view-space point (rows 2 and 3 of the inverse projection as FP32 pairs)
+__device__ __forceinline__ void depth_zw(const float* hi, const float* lo, float nx, float ny, float d, float& rw,
+                                         float& z) {
+    float zh, zl, wh, wl;
+    ff_row(hi, lo, nx, ny, d, zh, zl);
+    ff_row(hi + 4, lo + 4, nx, ny, d, wh, wl);
+    const float r = __frcp_rn(wh);
+    const float e = __fmaf_rn(-r, wl, __fmaf_rn(-r, wh, 1.0f));  // 1 - r (wh + wl)
+    rw = __fmaf_rn(r, e, r);
+    const float q = __fmul_rn(zh, rw);
+    const float qe = __fadd_rn(__fmaf_rn(-q, wh, zh), __fmaf_rn(-q, wl, zl));  // (zh + zl) - q (wh + wl)
+    z = __fmaf_rn(qe, rw, q);
+}
+
 // The grid a warp's tile traces against, staged in shared memory per warp: lanes index the level table with their
 // own (divergent) level, which the constant bank would serialise, and batched launches trace many grids.
 struct GridRef {
@@ -94,9 +145,11 @@ constexpr int kLut = 65;
 // whole with deltas +1 / +(d+2) / +(d+2)^2, any other is zero.  Level 0 is bricked: interior samples address the
 // seven other taps from the first one with +1 / +8 / +64 inside a brick, or the Morton step to the next brick
 // when the tap crosses a brick face; samples touching its border test each tap.
+// The sample is ADDED to acc scaled by `scale` (the weight of this level in the quadrilinear blend), which is
+// folded into the z weights: acc += scale * sum_taps w_tap v_tap.
 template <int FMT, int NV>
 __device__ __forceinline__ void tri_sample(const void* base, int d, uint32_t l, const uint32_t (&vol_off)[NV],
-                                          float3 x, const uint32_t* lut, float4 (&acc)[NV]) {
+                                          float3 x, const uint32_t* lut, float scale, float4 (&acc)[NV]) {
     // NV volumes of the same level share the tap coordinates and weights (the three directions an anisotropic
     // sample blends); each volume accumulates its own taps in the single-volume order.
     const float s = __int_as_float((127 - int(l)) << 23);  // 2^-l
@@ -109,28 +162,29 @@ __device__ __forceinline__ void tri_sample(const void* base, int d, uint32_t l, 
         c0[a] = int(fl);
         f[a] = u[a] - fl;
     }
-    const float wx[2] = {1.0f - f[0], f[0]}, wy[2] = {1.0f - f[1], f[1]}, wz[2] = {1.0f - f[2], f[2]};
-#pragma unroll
-    for (int k = 0; k < NV; ++k) acc[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+    const float wx[2] = {1.0f - f[0], f[0]}, wy[2] = {1.0f - f[1], f[1]};
+    const float wz[2] = {(1.0f - f[2]) * scale, f[2] * scale};
     if (l > 0) {
         // ringed linear level: footprints that touch the volume are read whole (the ring reads zero), the others
         // are zero outright
         if (unsigned(c0[0] + 1) > unsigned(d) || unsigned(c0[1] + 1) > unsigned(d) || unsigned(c0[2] + 1) > unsigned(d))
             return;
+        // one address per x-row of the footprint: the row's second tap is the next element (an immediate offset)
         const uint32_t dp = uint32_t(d) + 2u;
         const uint32_t i0 = (uint32_t(c0[2] + 1) * dp + uint32_t(c0[1] + 1)) * dp + uint32_t(c0[0] + 1);
+        const uint32_t ry = dp, rz = dp * dp;
 #pragma unroll
         for (int tz = 0; tz < 2; ++tz)
 #pragma unroll
             for (int ty = 0; ty < 2; ++ty) {
                 const float wyz = wy[ty] * wz[tz];
-                const uint32_t row = i0 + (tz ? dp * dp : 0u) + (ty ? dp : 0u);
+                const uint32_t row = i0 + (tz ? rz : 0u) + (ty ? ry : 0u);
+                const float w0 = wx[0] * wyz, w1 = wx[1] * wyz;
 #pragma unroll
-                for (int tx = 0; tx < 2; ++tx) {
-                    const float w = wx[tx] * wyz;
-                    const uint32_t e = row + (tx ? 1u : 0u);
-#pragma unroll
-                    for (int k = 0; k < NV; ++k) fma4(acc[k], w, load_vox(base, FMT, vol_off[k] + e));
+                for (int k = 0; k < NV; ++k) {
+                    const unsigned char* pr = vox_ptr<FMT>(base, vol_off[k] + row);
+                    fma4(acc[k], w0, load_vox_at<FMT>(pr, 0));
+                    fma4(acc[k], w1, load_vox_at<FMT>(pr, 1));
                 }
             }
         return;
@@ -209,26 +263,27 @@ __device__ __forceinline__ void tri_sample(const void* base, int d, uint32_t l, 
         }
 }
 
+// acc += scale * (the sample of level l at x): isotropic, or the three direction volumes facing the cone
+// weighted by dir^2 (anisotropic levels >= 1)
 template <int FMT, bool ANISO>
-__device__ __forceinline__ float4 level_sample(const GridRef& g, const uint32_t* lut, uint32_t l, float3 x,
-                                               float3 dir) {
+__device__ __forceinline__ void level_sample(const GridRef& g, const uint32_t* lut, uint32_t l, float3 x,
+                                             float3 dir, float scale, float4& acc) {
     const int d = int(g.dim >> l);
     if (!ANISO || l == 0) {
         const uint32_t vo[1] = {g.off[l]};
-        float4 a[1];
-        tri_sample<FMT, 1>(g.base, d, l, vo, x, lut, a);
-        return a[0];
+        float4 a[1] = {acc};
+        tri_sample<FMT, 1>(g.base, d, l, vo, x, lut, scale, a);
+        acc = a[0];
+        return;
     }
-    const float w[3] = {dir.x * dir.x, dir.y * dir.y, dir.z * dir.z};
+    const float w[3] = {dir.x * dir.x * scale, dir.y * dir.y * scale, dir.z * dir.z * scale};
     const uint32_t vo[3] = {g.off[l] + (dir.x >= 0.0f ? 0u : 1u) * g.vol[l],
                             g.off[l] + (dir.y >= 0.0f ? 2u : 3u) * g.vol[l],
                             g.off[l] + (dir.z >= 0.0f ? 4u : 5u) * g.vol[l]};
-    float4 sa[3];
-    tri_sample<FMT, 3>(g.base, d, l, vo, x, lut, sa);
-    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+    float4 sa[3] = {make_float4(0.f, 0.f, 0.f, 0.f), make_float4(0.f, 0.f, 0.f, 0.f), make_float4(0.f, 0.f, 0.f, 0.f)};
+    tri_sample<FMT, 3>(g.base, d, l, vo, x, lut, 1.0f, sa);
 #pragma unroll
     for (int a = 0; a < 3; ++a) fma4(acc, w[a], sa[a]);
-    return acc;
 }
 
 // sched: the first ns samples of this cone's march (the diffuse schedule; ns = 0 for the specular cone).
@@ -266,33 +321,19 @@ __device__ float4 cone(const GridRef& g, const uint32_t* lut, const TraceConsts&
             cnt[0] += 1u;
             cnt[1] += (f > 0.0f && l0 + 1 < g.levels) ? 2u : 1u;
         }
-        float4 s;
+        // quadrilinear: (1 - f) * level l0 + f * level l0 + 1, the level weights folded into the tap weights
+        const bool two = f > 0.0f && l0 + 1 < g.levels;
+        float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
         if (ANISO) {
             // the two levels share one copy of the (three-volume) sampling code: the instruction cache
             // outweighs the overlap of two inlined copies here, not in the single-volume kernel
-            const uint32_t nl = (f > 0.0f && l0 + 1 < g.levels) ? 2u : 1u;
-            s = make_float4(0.f, 0.f, 0.f, 0.f);
+            const uint32_t nl = two ? 2u : 1u;
 #pragma unroll 1
-            for (uint32_t k = 0; k < nl; ++k) {
-                const float4 v = level_sample<FMT, ANISO>(g, lut, l0 + k, x, dir);
-                if (k == 0) {
-                    s = v;
-                } else {
-                    s.x = s.x + f * (v.x - s.x);
-                    s.y = s.y + f * (v.y - s.y);
-                    s.z = s.z + f * (v.z - s.z);
-                    s.w = s.w + f * (v.w - s.w);
-                }
-            }
+            for (uint32_t k = 0; k < nl; ++k)
+                level_sample<FMT, ANISO>(g, lut, l0 + k, x, dir, k ? f : (two ? 1.0f - f : 1.0f), s);
         } else {
-            s = level_sample<FMT, ANISO>(g, lut, l0, x, dir);
-            if (f > 0.0f && l0 + 1 < g.levels) {
-                const float4 s1 = level_sample<FMT, ANISO>(g, lut, l0 + 1, x, dir);
-                s.x = s.x + f * (s1.x - s.x);
-                s.y = s.y + f * (s1.y - s.y);
-                s.z = s.z + f * (s1.z - s.z);
-                s.w = s.w + f * (s1.w - s.w);
-            }
+            level_sample<FMT, ANISO>(g, lut, l0, x, dir, two ? 1.0f - f : 1.0f, s);
+            if (two) level_sample<FMT, ANISO>(g, lut, l0 + 1, x, dir, f, s);
         }
         float tr = 1.0f - alpha;
         cr += tr * s.x;
@@ -338,17 +379,13 @@ __device__ void trace_pixel(const GridRef& g, const uint32_t* lut, const TraceCo
     const float* iv = v.iview;
     float nx = (float(px) + 0.5f) / float(v.width) * 2.0f - 1.0f;
     float ny = (float(py) + 0.5f) / float(v.height) * 2.0f - 1.0f;
-    // View-space position.  The projective rows (z, w) run in FP64: for depths near 1, w is a small difference
-    // of O(1) terms and FP32 would lose ~5e-6 of it (a fraction of a voxel at 10 m).  x and y are well
-    // conditioned and stay FP32.
-    const double* iz = v.iproj_zw;
-    const double dnx = double(nx), dny = double(ny), dd = double(d);
-    const double vz = fma(iz[0], dnx, fma(iz[1], dny, fma(iz[2], dd, iz[3])));
-    const double vw = fma(iz[4], dnx, fma(iz[5], dny, fma(iz[6], dd, iz[7])));
-    const double rw = 1.0 / vw;
-    const float rwf = float(rw);
+    // View-space position.  The projective rows (z, w) are float-float: for depths near 1, w is a small
+    // difference of O(1) terms and plain FP32 would lose ~5e-6 of it (a fraction of a voxel at 10 m); x and y
+    // are well conditioned and stay FP32.
+    float rwf, csz;
+    depth_zw(v.iproj_zw_hi, v.iproj_zw_lo, nx, ny, d, rwf, csz);
     const float vx = ip[0] * nx + ip[1] * ny + ip[2] * d + ip[3], vy = ip[4] * nx + ip[5] * ny + ip[6] * d + ip[7];
-    float3 cs = f3(vx * rwf, vy * rwf, float(vz * rw));
+    float3 cs = f3(vx * rwf, vy * rwf, csz);
     float3 wp = f3(iv[0] * cs.x + iv[1] * cs.y + iv[2] * cs.z + iv[3], iv[4] * cs.x + iv[5] * cs.y + iv[6] * cs.z + iv[7],
                    iv[8] * cs.x + iv[9] * cs.y + iv[10] * cs.z + iv[11]);
     float3 nv = oct_decode(v.normal[pi]);
@@ -357,6 +394,15 @@ __device__ void trace_pixel(const GridRef& g, const uint32_t* lut, const TraceCo
     float rough = __half2float(__ushort_as_half(v.rough[pi]));
     float3 pv = f3((wp.x - g.org[0]) * g.inv_vs, (wp.y - g.org[1]) * g.inv_vs, (wp.z - g.org[2]) * g.inv_vs);
     float3 o = add3(pv, mul3(nw, tc.p.start_offset));
+    // the specular cone's direction and aperture first: the view position and normal die here
+    float3 rd = f3(0.f, 0.f, 0.f);
+    float th = 0.f;
+    if (tc.p.specular) {
+        float3 vd = norm3(sub3(wp, f3(v.eye[0], v.eye[1], v.eye[2])));
+        float dn = dot3(vd, nw);
+        rd = norm3(sub3(vd, mul3(nw, 2.0f * dn)));
+        th = fmaxf(rough, tc.p.min_spec_tan_half);
+    }
     float3 bx, by, bz;
     coord_space(nw, bx, by, bz);
     float4 acc;
@@ -380,13 +426,7 @@ __device__ void trace_pixel(const GridRef& g, const uint32_t* lut, const TraceCo
     }
     store_out(v.out, v.out_format, pi, acc);
     float4 sp = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (tc.p.specular) {
-        float3 vd = norm3(sub3(wp, f3(v.eye[0], v.eye[1], v.eye[2])));
-        float dn = dot3(vd, nw);
-        float3 rd = norm3(sub3(vd, mul3(nw, 2.0f * dn)));
-        float th = fmaxf(rough, tc.p.min_spec_tan_half);
-        sp = cone<FMT, ANISO, COUNT>(g, lut, tc, o, rd, th, nullptr, 0u, cnt);
-    }
+    if (tc.p.specular) sp = cone<FMT, ANISO, COUNT>(g, lut, tc, o, rd, th, nullptr, 0u, cnt);
     store_out(v.out, v.out_format, npix + pi, sp);
 }
 

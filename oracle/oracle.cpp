@@ -757,6 +757,37 @@ void cone(const Chain<T>& ch, Vec3<T> o, Vec3<T> dir, T tan_half, const f184gi_c
     out[3] = alpha;
 }
 
+// Float-float depth rows of the FP32 path (the device's sequence, every operation rounded on its own): Knuth's
+// two-sum and the FMA two-product are exact, so a row of the inverse projection split into FP32 pairs evaluates to
+// ~2^-46 of its largest term; then 1 / w and z / w with one Newton correction each.
+inline void ff_two_sum(float a, float b, float& s, float& e) {
+    s = a + b;
+    const float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+inline void ff_row(const float* hi, const float* lo, float x, float y, float z, float& rh, float& rl) {
+    const float p0 = hi[0] * x, p1 = hi[1] * y, p2 = hi[2] * z;
+    const float e0 = std::fma(hi[0], x, -p0), e1 = std::fma(hi[1], y, -p1), e2 = std::fma(hi[2], z, -p2);
+    float s0, s1, s2, t0, t1, t2;
+    ff_two_sum(p0, p1, s0, t0);
+    ff_two_sum(s0, p2, s1, t1);
+    ff_two_sum(s1, hi[3], s2, t2);
+    const float small = (((t0 + t1) + t2) + ((e0 + e1) + e2)) + ((lo[0] * x + lo[1] * y) + (lo[2] * z + lo[3]));
+    rh = s2 + small;
+    rl = small - (rh - s2);
+}
+inline void ff_depth_zw(const float* hi, const float* lo, float nx, float ny, float d, float& rw, float& z) {
+    float zh, zl, wh, wl;
+    ff_row(hi, lo, nx, ny, d, zh, zl);
+    ff_row(hi + 4, lo + 4, nx, ny, d, wh, wl);
+    const float r = 1.0f / wh;
+    const float e = std::fma(-r, wl, std::fma(-r, wh, 1.0f));
+    rw = std::fma(r, e, r);
+    const float q = zh * rw;
+    const float qe = std::fma(-q, wh, zh) + std::fma(-q, wl, zl);
+    z = std::fma(qe, rw, q);
+}
+
 template <class T>
 int trace_impl(const f184gi_grid_frame* frame, uint32_t dim, uint32_t levels, uint32_t aniso, const T* chain,
                const float view[16], const float proj[16], uint32_t W, uint32_t H, const float* depth,
@@ -775,6 +806,11 @@ int trace_impl(const f184gi_grid_frame* frame, uint32_t dim, uint32_t levels, ui
     for (int i = 0; i < 16; ++i) {
         iv[i] = T(IV[i]);
         ip[i] = T(IP[i]);
+    }
+    float zw_hi[8], zw_lo[8];  // the FP32 path's depth rows: rows 2 and 3 of IP split into FP32 pairs
+    for (int k = 0; k < 8; ++k) {
+        zw_hi[k] = float(IP[8 + k]);
+        zw_lo[k] = float(IP[8 + k] - double(zw_hi[k]));
     }
     Chain<T> ch = make_chain(chain, dim, levels, aniso != 0);
     const T vs = T(frame->voxel_size);
@@ -808,12 +844,10 @@ int trace_impl(const f184gi_grid_frame* frame, uint32_t dim, uint32_t levels, ui
                 for (int r = 0; r < 4; ++r) vp[r] = ip[r * 4 + 0] * nx + ip[r * 4 + 1] * ny + ip[r * 4 + 2] * nz + ip[r * 4 + 3];
                 Vec3<T> cs{vp[0] / vp[3], vp[1] / vp[3], vp[2] / vp[3]};
                 if (std::is_same<T, float>::value) {
-                    // the device arithmetic: the projective rows (z, w) in FP64, x and y in FP32
-                    const double dnx = double(nx), dny = double(ny), ddz = double(nz);
-                    const double vz = IP[8] * dnx + IP[9] * dny + IP[10] * ddz + IP[11];
-                    const double vw = IP[12] * dnx + IP[13] * dny + IP[14] * ddz + IP[15];
-                    const double rw = 1.0 / vw;
-                    cs = Vec3<T>{vp[0] * T(rw), vp[1] * T(rw), T(vz * rw)};
+                    // the device arithmetic: the projective rows (z, w) as float-float pairs, x and y in FP32
+                    float rw, z;
+                    ff_depth_zw(zw_hi, zw_lo, float(nx), float(ny), float(nz), rw, z);
+                    cs = Vec3<T>{vp[0] * T(rw), vp[1] * T(rw), T(z)};
                 }
                 Vec3<T> wp{iv[0] * cs.x + iv[1] * cs.y + iv[2] * cs.z + iv[3],
                            iv[4] * cs.x + iv[5] * cs.y + iv[6] * cs.z + iv[7],
