@@ -300,24 +300,29 @@ class Server:
         check(self.lib.f184gi_server_add_scene(self.h, scene_id, C.byref(desc), tri.ctypes.data, alb.ctypes.data,
                                                tri.size // 9, C.byref(bounds), C.byref(light)))
 
-    def submit(self, scene_id, views, moves=(), host_buffers=False):
+    def submit(self, scene_id, views, moves=(), host_buffers=False, flags=0):
+        """flags: extra F184GI_REQ_* bits (e.g. the fault-injection test hooks _abi.REQ_INJECT_*)."""
         mv = (_abi.Move * max(1, len(moves)))(*[_abi.Move(int(f), int(c), (C.c_float * 3)(*o)) for f, c, o in moves])
         vw = (View * len(views))(*views)
-        req = _abi.Request(scene_id, _abi.REQ_HOST_BUFFERS if host_buffers else 0, mv, len(moves), len(views), vw)
+        req = _abi.Request(scene_id, (_abi.REQ_HOST_BUFFERS if host_buffers else 0) | flags, mv, len(moves),
+                           len(views), vw)
         t = C.c_uint64()
         check(self.lib.f184gi_server_submit(self.h, C.byref(req), C.byref(t)))
         return t.value
 
     def submit_many(self, requests, host_buffers=False):
-        """Queue [(scene_id, views, moves), ...] at once (one batch can take them all); returns the tickets."""
+        """Queue [(scene_id, views, moves[, flags]), ...] at once (one batch can take them all); returns the
+        tickets."""
         keep, reqs = [], []
-        for scene_id, views, moves in requests:
+        for req in requests:
+            scene_id, views, moves = req[:3]
+            flags = req[3] if len(req) > 3 else 0
             mv = (_abi.Move * max(1, len(moves)))(*[_abi.Move(int(f), int(c), (C.c_float * 3)(*o))
                                                      for f, c, o in moves])
             vw = (View * len(views))(*views)
             keep += [mv, vw]
-            reqs.append(_abi.Request(scene_id, _abi.REQ_HOST_BUFFERS if host_buffers else 0, mv, len(moves),
-                                     len(views), vw))
+            reqs.append(_abi.Request(scene_id, (_abi.REQ_HOST_BUFFERS if host_buffers else 0) | flags, mv,
+                                     len(moves), len(views), vw))
         arr = (_abi.Request * len(reqs))(*reqs)
         t = (C.c_uint64 * len(reqs))()
         check(self.lib.f184gi_server_submit_batch(self.h, arr, len(reqs), t))
@@ -332,6 +337,10 @@ class Server:
 
     def cancel(self, ticket):
         check(self.lib.f184gi_server_cancel(self.h, ticket))
+
+    def set_log(self, path):
+        """Append one JSON line per finished request to `path` (None: stop)."""
+        check(self.lib.f184gi_server_set_log(self.h, None if path is None else str(path).encode()))
 
     def stats(self):
         st = _abi.ServerStats()

@@ -23,7 +23,10 @@ ERR_OVERFLOW = -5
 ERR_TIMEOUT = -6
 ERR_NOTFOUND = -7
 ERR_CANCELLED = -8
+ERR_WORKER = -9
 REQ_HOST_BUFFERS = 1
+REQ_INJECT_FAIL = 0x100
+REQ_INJECT_WORKER_EXIT = 0x200
 
 
 class Vec3(C.Structure):
@@ -157,6 +160,7 @@ PROTOTYPES = {
     "f184gi_server_wait": (C.c_int, [P, U64, U32, C.POINTER(RequestResult)]),
     "f184gi_server_cancel": (C.c_int, [P, U64]),
     "f184gi_server_get_stats": (C.c_int, [P, C.POINTER(ServerStats)]),
+    "f184gi_server_set_log": (C.c_int, [P, C.c_char_p]),
     "f184gi_server_submit_batch": (C.c_int, [P, C.POINTER(Request), U32, C.POINTER(U64)]),
     "f184gi_scene_generate": (C.c_int, [U64, U64, U32, C.POINTER(C.POINTER(Scene))]),
     "f184gi_scene_free": (None, [C.POINTER(Scene)]),

@@ -3,6 +3,8 @@
 // A context owns device memory under an optional HBM budget: resident grids (mip chain + shadow map + frame)
 // and per-pass scratch that grows on demand and is reused.  Calls are stream-ordered on the caller's stream;
 // kernels report overflow/timeout through a device status word that f184gi_sync and the inspection calls read.
+#include <nvtx3/nvToolsExt.h>
+
 #include <atomic>
 #include <cmath>
 #include <cstring>
@@ -215,9 +217,19 @@ int read_status(f184gi_ctx* c) {
     cudaMemset(c->d_status, 0, 4);
     if (st & kStatusTimeout) return fail(F184GI_ERR_TIMEOUT, "a bounded device wait expired");
     if (st & kStatusOverflow) return fail(F184GI_ERR_OVERFLOW, "a bounded device structure overflowed");
+    if (st & kStatusNonFinite)
+        return fail(F184GI_ERR_INVALID, "triangles with a NaN or infinite coordinate were skipped");
     return fail(F184GI_ERR_INVALID, "geometry outside the fixed-point range was skipped");
 }
 
+}  // namespace
+
+namespace {
+// NVTX range over one pass of the C ABI (host-side issue of its kernels), for Nsight timelines
+struct PassRange {
+    explicit PassRange(const char* name) { nvtxRangePushA(name); }
+    ~PassRange() { nvtxRangePop(); }
+};
 }  // namespace
 
 extern "C" {
@@ -369,6 +381,7 @@ int f184gi_grid_destroy(f184gi_ctx* c, uint32_t grid) {
 int f184gi_voxelize(f184gi_ctx* c, uint32_t grid, const float* tri, const uint32_t* albedo, uint64_t ntris,
                     const f184gi_bounds* bounds, const f184gi_light* light, const uint32_t* dirty, uint32_t ndirty,
                     void* stream) {
+    PassRange range("f184gi_voxelize");
     if (!c || !light) return fail(F184GI_ERR_INVALID, "voxelize: null argument");
     GridObj* g = find_grid(c, grid);
     if (!g) return fail(F184GI_ERR_NOTFOUND, "voxelize: unknown grid");
@@ -450,6 +463,7 @@ int f184gi_apply_moves(f184gi_ctx* c, float* tri_xyz, const f184gi_move* moves, 
 }
 
 int f184gi_mip(f184gi_ctx* c, uint32_t grid, uint32_t levels, uint32_t anisotropic, void* stream) {
+    PassRange range("f184gi_mip");
     if (!c) return fail(F184GI_ERR_INVALID, "mip: null context");
     GridObj* g = find_grid(c, grid);
     if (!g) return fail(F184GI_ERR_NOTFOUND, "mip: unknown grid");
@@ -538,6 +552,7 @@ int trace_views(f184gi_ctx* c, uint32_t grid, const f184gi_view* views, uint32_t
 
 int f184gi_trace(f184gi_ctx* c, uint32_t grid, const f184gi_view* views, uint32_t nviews,
                  const f184gi_cone_params* params, void* stream) {
+    PassRange range("f184gi_trace");
     return trace_views(c, grid, views, nviews, params, stream, nullptr);
 }
 
@@ -634,6 +649,7 @@ int f184gi_blur(f184gi_ctx* c, const float* in, const float* depth, uint32_t wid
 
 int f184gi_gbuffer(f184gi_ctx* c, const float* tri, const float* rough, uint64_t ntris, const f184gi_view* view,
                    uint32_t* tri_id_out, void* stream) {
+    PassRange range("f184gi_gbuffer");
     if (!c || !view || !tri || !rough) return fail(F184GI_ERR_INVALID, "gbuffer: null argument");
     if (!view->depth || !view->normal || !view->roughness) return fail(F184GI_ERR_INVALID, "gbuffer: null G-buffer planes");
     if (view->width == 0 || view->height == 0 || view->width > kMaxRasterSide || view->height > kMaxRasterSide)

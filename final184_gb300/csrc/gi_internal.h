@@ -23,7 +23,8 @@ constexpr uint32_t kStatusTimeout = 2u;
 constexpr uint32_t kMaxViewSide = 16384;
 constexpr uint32_t kMaxRasterSide = 8192;  // rasterized images (shadow maps, G-buffers): 1/16-pixel snaps in range
 constexpr uint64_t kMaxTracePixels = 1ull << 36;
-constexpr uint32_t kStatusRange = 4u;  // geometry outside the fixed-point range was skipped
+constexpr uint32_t kStatusRange = 4u;      // geometry outside the fixed-point range was skipped
+constexpr uint32_t kStatusNonFinite = 8u;  // triangles with a NaN or infinite coordinate were skipped
 
 // process-wide count of kernels this library has launched (f184gi_kernel_launches)
 void note_launches(uint32_t n);

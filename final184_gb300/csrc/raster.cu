@@ -204,6 +204,14 @@ __global__ void __launch_bounds__(128) raster_setup(const float* __restrict__ tr
     __syncthreads();
     uint64_t t = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
     if (t >= ntris) return;
+    bool finite = true;  // a triangle with a NaN or infinite coordinate is skipped (and reported)
+#pragma unroll
+    for (int i = 0; i < 9; ++i) finite = finite && isfinite(tri[t * 9 + i]);
+    if (!finite) {
+        set_status(status, kStatusNonFinite);
+        sc.recs[t].tri = kNone;
+        return;
+    }
     V4f cf[3];
     bool inside = true;
 #pragma unroll

@@ -11,10 +11,17 @@
 //   - one trace launch over all views of the batch, replayed from the slot's CUDA graph.
 // A completer thread retires batches in launch order and records per-request latency.  Batches on different
 // slots overlap on the device; requests that arrive meanwhile join the next batch.
+// Failures are per request: a request whose staging, update or view set-up fails finishes with that status and the
+// rest of its batch runs.  If the scheduler thread stops (for any reason, or by the INJECT_WORKER_EXIT test hook),
+// its exit path fails the batch it was forming and every queued request with F184GI_ERR_WORKER and the server
+// refuses new requests, so no caller waits on a request nothing will run.
+#include <nvtx3/nvToolsExt.h>
+
 #include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <condition_variable>
+#include <cstdio>
 #include <cstring>
 #include <deque>
 #include <map>
@@ -74,6 +81,7 @@ struct Slot {
     cudaEvent_t done = nullptr;
     TraceGraph* graph = nullptr;
     std::vector<Request*> reqs;
+    std::vector<int> req_status;  // per request: a failure of its own staging / update / views (0 = ran)
     std::vector<Scene*> scenes;  // scene of each request, resolved under the server lock
     std::vector<TraceView> tv;
     uint32_t batch = 0;
@@ -104,6 +112,8 @@ struct f184gi_server {
     std::deque<int> launched;
     std::thread sched, completer;
     bool stop = false;
+    bool worker_lost = false;  // the scheduler thread has stopped while the server was running
+    FILE* log = nullptr;       // per-request JSON lines (f184gi_server_set_log)
     uint64_t next_ticket = 1, generation = 0;
     uint32_t next_batch = 1;
     uint64_t hbm_used = 0;
@@ -240,42 +250,68 @@ int stage_out(Request* r, const std::vector<void*>& host_out, cudaStream_t s) {
     return cuda_fail(e, "server: staging free");
 }
 
+// NVTX range for the duration of a scope (visible in Nsight Systems / ncu's NVTX filter)
+struct NvtxRange {
+    explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+};
+
+// The batch's device work on the slot's stream.  A request whose staging, scene update or view set-up fails gets
+// that status in slot.req_status and its views are left out; the others run.  The return value is a failure of
+// the batch itself (graph, launch, event), which fails every request of the batch.
 int issue_batch(f184gi_server* S, Slot& slot) {
+    NvtxRange range("f184gi server batch");
     cudaStream_t s = slot.stream;
     slot.tv.clear();
+    slot.req_status.assign(slot.reqs.size(), F184GI_OK);
     std::vector<std::vector<void*>> host_out(slot.reqs.size());
-    for (size_t k = 0; k < slot.reqs.size(); ++k) {
-        Request* r = slot.reqs[k];
-        Scene* sc = slot.scenes[k];
-        for (const f184gi_view& v : r->views) host_out[k].push_back(v.out);
-        int rc = stage_in(r, s);
-        if (!rc) rc = scene_update(sc, r, s);
-        if (rc) return rc;
-        for (const f184gi_view& v : r->views) {
-            TraceView t;
-            if ((rc = prepare_view(S, sc, v, t))) return rc;
-            slot.tv.push_back(t);
+    {
+        NvtxRange r_update("f184gi server: staging + scene updates");
+        for (size_t k = 0; k < slot.reqs.size(); ++k) {
+            Request* r = slot.reqs[k];
+            Scene* sc = slot.scenes[k];
+            for (const f184gi_view& v : r->views) host_out[k].push_back(v.out);
+            const size_t first_view = slot.tv.size();
+            int rc = (r->flags & F184GI_REQ_INJECT_FAIL)
+                         ? fail(F184GI_ERR_CUDA, "server: injected failure of the scene update (test hook)")
+                         : stage_in(r, s);
+            if (!rc) rc = scene_update(sc, r, s);
+            for (size_t v = 0; !rc && v < r->views.size(); ++v) {
+                TraceView t;
+                if (!(rc = prepare_view(S, sc, r->views[v], t))) slot.tv.push_back(t);
+            }
+            if (rc) {
+                slot.req_status[k] = rc;
+                slot.tv.resize(first_view);
+                if (r->d_stage) {
+                    cudaFreeAsync(r->d_stage, s);
+                    r->d_stage = nullptr;
+                }
+            }
         }
     }
-    if (!slot.graph) {
-        int rc = trace_graph_create(&slot.graph, uint32_t(S->fmt), S->aniso != 0, S->cfg.max_batch_views,
-                                    S->cfg.blocks_per_sm, S->tc);
-        if (rc) return rc;
-    }
     int rc = F184GI_OK;
-    if (S->variant < 0) {  // first batch: it runs alone (the scheduler issues nothing else meanwhile)
-        uint32_t best = trace_default_variant(uint32_t(S->fmt), S->aniso != 0);
-        float ms[kTraceVariantCount];
-        if ((rc = trace_graph_tune(slot.graph, slot.tv.data(), uint32_t(slot.tv.size()), s, &best, ms))) return rc;
-        std::lock_guard<std::mutex> lk(S->mu);
-        for (uint32_t v = 0; v < kTraceVariantCount; ++v) S->tune_ms[v] = ms[v];
-        S->variant = int(best);
-    } else {
-        rc = trace_graph_launch(slot.graph, slot.tv.data(), uint32_t(slot.tv.size()), uint32_t(S->variant), s);
-        if (rc) return rc;
+    if (!slot.tv.empty()) {
+        NvtxRange r_trace("f184gi server: batched trace");
+        if (!slot.graph) {
+            rc = trace_graph_create(&slot.graph, uint32_t(S->fmt), S->aniso != 0, S->cfg.max_batch_views,
+                                    S->cfg.blocks_per_sm, S->tc);
+            if (rc) return rc;
+        }
+        if (S->variant < 0) {  // first batch: it runs alone (the scheduler issues nothing else meanwhile)
+            uint32_t best = trace_default_variant(uint32_t(S->fmt), S->aniso != 0);
+            float ms[kTraceVariantCount];
+            if ((rc = trace_graph_tune(slot.graph, slot.tv.data(), uint32_t(slot.tv.size()), s, &best, ms))) return rc;
+            std::lock_guard<std::mutex> lk(S->mu);
+            for (uint32_t v = 0; v < kTraceVariantCount; ++v) S->tune_ms[v] = ms[v];
+            S->variant = int(best);
+        } else {
+            rc = trace_graph_launch(slot.graph, slot.tv.data(), uint32_t(slot.tv.size()), uint32_t(S->variant), s);
+            if (rc) return rc;
+        }
     }
     for (size_t k = 0; k < slot.reqs.size(); ++k)
-        if ((rc = stage_out(slot.reqs[k], host_out[k], s))) return rc;
+        if (slot.req_status[k] == F184GI_OK && (rc = stage_out(slot.reqs[k], host_out[k], s))) return rc;
     return cuda_fail(cudaEventRecord(slot.done, s), "server: batch event");
 }
 
@@ -295,9 +331,52 @@ void finish_request(f184gi_server* S, Request* r, int status, Clock::time_point 
         S->pixels += r->pixels;
     }
     S->hbm_used -= r->staging;
+    if (S->log) {
+        std::fprintf(S->log,
+                     "{\"ticket\": %llu, \"scene\": %u, \"status\": %d, \"batch\": %u, \"views\": %zu, "
+                     "\"moves\": %zu, \"pixels\": %llu, \"queued_ms\": %.3f, \"latency_ms\": %.3f}\n",
+                     (unsigned long long)r->ticket, r->scene, status, r->batch, r->views.size(), r->moves.size(),
+                     (unsigned long long)r->pixels, r->admitted ? ms_between(r->t_submit, r->t_admit) : 0.0,
+                     ms_between(r->t_submit, now));
+        std::fflush(S->log);
+    }
 }
 
+// Runs when the scheduler thread leaves its loop for any reason.  Unless the server is being destroyed, the worker
+// is lost: the batch it was forming (admitted, not issued) and every queued request fail with F184GI_ERR_WORKER,
+// and later submissions are refused; batches already issued are still retired by the completer.
+void scheduler_exit(f184gi_server* S) {
+    std::lock_guard<std::mutex> lk(S->mu);
+    if (S->stop) return;
+    S->worker_lost = true;
+    const Clock::time_point now = Clock::now();
+    for (Slot& sl : S->slots) {
+        if (!sl.busy || std::find(S->launched.begin(), S->launched.end(), int(&sl - S->slots.data())) != S->launched.end())
+            continue;
+        for (size_t k = 0; k < sl.reqs.size(); ++k) {
+            finish_request(S, sl.reqs[k], F184GI_ERR_WORKER, now);
+            sl.scenes[k]->busy = false;
+        }
+        sl.reqs.clear();
+        sl.busy = false;
+    }
+    for (Request* r : S->pending) finish_request(S, r, F184GI_ERR_WORKER, now);
+    S->pending.clear();
+    S->generation++;
+    S->cv_done.notify_all();
+}
+
+void scheduler_loop(f184gi_server* S);
+
 void scheduler(f184gi_server* S) {
+    try {
+        scheduler_loop(S);
+    } catch (...) {  // e.g. a host allocation failure: the worker is lost, the exit path below reports it
+    }
+    scheduler_exit(S);
+}
+
+void scheduler_loop(f184gi_server* S) {
     cudaSetDevice(S->cfg.device);
     std::unique_lock<std::mutex> lk(S->mu);
     uint64_t seen = S->generation;
@@ -344,6 +423,8 @@ void scheduler(f184gi_server* S) {
         for (Request* r : batch) slot.scenes.push_back(S->scenes.at(r->scene));
         slot.batch = S->next_batch++;
         for (Request* r : batch) r->admitted = true, r->t_admit = now, r->batch = slot.batch;
+        for (Request* r : batch)
+            if (r->flags & F184GI_REQ_INJECT_WORKER_EXIT) return;  // test hook: the worker is lost between stages
         lk.unlock();
         int rc = issue_batch(S, slot);
         lk.lock();
@@ -353,7 +434,7 @@ void scheduler(f184gi_server* S) {
             for (size_t k = 0; k < slot.reqs.size(); ++k) {
                 Request* r = slot.reqs[k];
                 if (r->d_stage) cudaFree(r->d_stage), r->d_stage = nullptr;
-                finish_request(S, r, rc, t);
+                finish_request(S, r, slot.req_status.size() > k && slot.req_status[k] ? slot.req_status[k] : rc, t);
                 slot.scenes[k]->busy = false;
             }
             slot.reqs.clear();
@@ -392,7 +473,7 @@ void completer(f184gi_server* S) {
         S->launched.pop_front();
         const Clock::time_point now = Clock::now();
         for (size_t k = 0; k < slot.reqs.size(); ++k) {
-            finish_request(S, slot.reqs[k], st, now);
+            finish_request(S, slot.reqs[k], slot.req_status[k] ? slot.req_status[k] : st, now);
             slot.scenes[k]->busy = false;
         }
         S->batches += 1;
@@ -472,6 +553,7 @@ int f184gi_server_destroy(f184gi_server* S) {
         delete sc;
     }
     for (auto& kv : S->reqs) delete kv.second;
+    if (S->log) std::fclose(S->log);
     delete S;
     return F184GI_OK;
 }
@@ -481,6 +563,10 @@ int f184gi_server_add_scene(f184gi_server* S, uint32_t id, const f184gi_grid_des
                             const f184gi_light* light) {
     if (!S || !desc || !tri || !albedo || !bounds || !light || ntris == 0)
         return fail(F184GI_ERR_INVALID, "server_add_scene: null argument");
+    for (uint64_t i = 0; i < ntris * 9; ++i)
+        if (!std::isfinite(tri[i]))
+            return fail(F184GI_ERR_INVALID, "server_add_scene: triangle " + std::to_string(i / 9) +
+                                                " has a NaN or infinite coordinate");
     {
         std::lock_guard<std::mutex> lk(S->mu);
         if (S->scenes.count(id)) return fail(F184GI_ERR_INVALID, "server_add_scene: scene id already registered");
@@ -613,6 +699,10 @@ int f184gi_server_submit_batch(f184gi_server* S, const f184gi_request* reqs, uin
         rs.push_back(r);
     }
     std::lock_guard<std::mutex> lk(S->mu);
+    if (S->worker_lost) {
+        for (Request* q : rs) delete q;
+        return fail(F184GI_ERR_WORKER, "server_submit: the server's scheduler thread has stopped");
+    }
     for (Request* r : rs) {
         int rc = admit_check(S, r);
         if (rc) {
@@ -666,6 +756,16 @@ int f184gi_server_cancel(f184gi_server* S, uint64_t ticket) {
     S->cancelled += 1;
     S->cv_done.notify_all();
     S->cv_sched.notify_all();
+    return F184GI_OK;
+}
+
+int f184gi_server_set_log(f184gi_server* S, const char* path) {
+    if (!S) return fail(F184GI_ERR_INVALID, "server_set_log: null server");
+    FILE* f = nullptr;
+    if (path && !(f = std::fopen(path, "a"))) return fail(F184GI_ERR_INVALID, std::string("server_set_log: cannot open ") + path);
+    std::lock_guard<std::mutex> lk(S->mu);
+    if (S->log) std::fclose(S->log);
+    S->log = f;
     return F184GI_OK;
 }
 

@@ -165,6 +165,14 @@ __global__ void __launch_bounds__(128) vox_setup(const float* __restrict__ tri, 
     TriRec r;
     bool ok = t < ntris;
     const float* p = tri + (ok ? t : 0) * 9;
+    if (ok) {  // a triangle with a NaN or infinite coordinate is skipped (and reported)
+        bool finite = true;
+        for (int i = 0; i < 9; ++i) finite = finite && isfinite(p[i]);
+        if (!finite) {
+            set_status(status, kStatusNonFinite);
+            ok = false;
+        }
+    }
     for (int i = 0; i < 9; ++i) {
         int a = i % 3;
         int64_t q = 0;

@@ -45,6 +45,7 @@ extern "C" {
 #define F184GI_ERR_TIMEOUT (-6)  /* a bounded wait expired */
 #define F184GI_ERR_NOTFOUND (-7) /* unknown grid / request id */
 #define F184GI_ERR_CANCELLED (-8)
+#define F184GI_ERR_WORKER (-9)   /* a server's scheduler thread stopped: its queued requests fail, new ones are refused */
 
 /* ---- boundary value types (layout-compatible with the reference Math library) ---- */
 
@@ -297,6 +298,14 @@ typedef struct f184gi_server_config {
 } f184gi_server_config;
 
 #define F184GI_REQ_HOST_BUFFERS 1u /* view G-buffers / outputs are host pointers: staged through the budget */
+/* Host-side fault injection (test hooks; no GPU fault is involved):
+ *   INJECT_FAIL: this request's scene update fails with F184GI_ERR_CUDA before any of its device work is issued, as
+ *     if a CUDA call had failed; the other requests of its batch run and the server keeps serving;
+ *   INJECT_WORKER_EXIT: the scheduler thread exits after admitting the batch that holds this request, before
+ *     issuing it (a worker lost between stages): that batch and every queued request fail with F184GI_ERR_WORKER,
+ *     batches already on the device complete, and later submissions are refused with F184GI_ERR_WORKER. */
+#define F184GI_REQ_INJECT_FAIL 0x100u
+#define F184GI_REQ_INJECT_WORKER_EXIT 0x200u
 
 typedef struct f184gi_request {
     uint32_t scene_id;
@@ -344,6 +353,10 @@ int f184gi_server_wait(f184gi_server* s, uint64_t ticket, uint32_t timeout_ms, f
 /* Cancel a request that has not been admitted yet (F184GI_ERR_INVALID once it is running or done). */
 int f184gi_server_cancel(f184gi_server* s, uint64_t ticket);
 int f184gi_server_get_stats(f184gi_server* s, f184gi_server_stats* out);
+/* Per-request metrics: one JSON line per finished request (ticket, scene, status, batch, views, pixels, queued and
+ * latency ms) appended to `path` (NULL closes the log).  No counterpart in the reference (stdout only,
+ * MegaPipeline.cpp:76). */
+int f184gi_server_set_log(f184gi_server* s, const char* path);
 
 /* ---- inspection (host copies; synchronise the stream) ---- */
 int f184gi_grid_get_frame(f184gi_ctx* ctx, uint32_t grid, f184gi_grid_frame* out);

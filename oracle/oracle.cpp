@@ -363,6 +363,8 @@ struct FixTri {
 };
 
 bool fix_tri(const f184gi_grid_frame& fr, uint32_t dim, const float* p, FixTri& t) {
+    for (int i = 0; i < 9; ++i)
+        if (!std::isfinite(p[i])) return false;  // triangles with a NaN or infinite coordinate are skipped
     for (int v = 0; v < 3; ++v)
         for (int a = 0; a < 3; ++a) {
             double d = double(p[v * 3 + a]) - fr.origin[a];
@@ -984,6 +986,9 @@ int orc_raster(const double M[16], uint32_t W, uint32_t H, const float* tri, uin
     for (int i = 0; i < 16; ++i) mf[i] = float(M[i]);
     for (uint64_t t = 0; t < ntris; ++t) {
         const float* p = tri + t * 9;
+        bool finite = true;  // triangles with a NaN or infinite coordinate are skipped
+        for (int i = 0; i < 9; ++i) finite = finite && std::isfinite(p[i]);
+        if (!finite) continue;
         V4f cf[3];
         bool inside = true;
         for (int v = 0; v < 3; ++v) {

@@ -216,3 +216,44 @@ def test_oversize_views_are_refused_before_any_launch(case):
         case.gi.gbuffer(case.tri_d.data_ptr(), case.rough_d.data_ptr(), case.ntris, wide)
     assert err.value.code == _abi.ERR_INVALID and "8192" in str(err.value)
     case.gi.sync()  # nothing was launched: no device status
+
+
+def test_non_finite_triangles_skipped_and_reported(lib, orc):
+    """Malformed triangle buffers: triangles with a NaN or infinite coordinate are skipped by the shadow raster, the
+    voxelizer and the G-buffer raster (as by the oracle), and the next sync reports F184GI_ERR_INVALID; the shadow
+    map, occupancy, counts and the G-buffer stay bit-exact.  The server refuses such a scene up front."""
+    import final184_gb300 as g
+
+    c = Case(ntris=5000, nobj=40, dim=32, levels=5, res=256, width=96, height=64)
+    tri = c.sc.tri_xyz.copy().reshape(-1, 9)
+    rng = np.random.default_rng(11)
+    bad = rng.choice(np.arange(12, len(tri)), 60, replace=False)
+    vals = np.array([np.nan, np.inf, -np.inf], np.float32)
+    for k, t in enumerate(bad):
+        tri[t, rng.integers(0, 9)] = vals[k % 3]
+    tri = tri.ravel()
+    c.upload(tri, c.sc.albedo)
+    c.gi.voxelize(c.grid, c.tri_d.data_ptr(), c.alb_d.data_ptr(), c.ntris, c.sc.light, bounds=c.sc.bounds)
+    with pytest.raises(g.F184Error) as e:
+        c.gi.sync()
+    assert e.value.code == g._abi.ERR_INVALID and "NaN or infinite" in str(e.value)
+    fo = c.oracle_frame()
+    sd = orc.shadow_depth(orc.raster(orc.frame_matrix(fo), c.res, c.res, tri))
+    assert np.array_equal(c.gi.read_shadow(c.grid).view(np.uint32), sd.view(np.uint32))
+    _, cnt = orc.voxelize(fo, c.dim, c.res, tri, c.sc.albedo, c.oracle_light(), sd)
+    assert np.array_equal(c.gi.read_counts(c.grid), cnt.astype(np.uint32))
+    c.gi.gbuffer(c.tri_d.data_ptr(), c.rough_d.data_ptr(), c.ntris, c.view, c.tri_id.data_ptr())
+    with pytest.raises(g.F184Error):
+        c.gi.sync()
+    from gi_case import clip_matrix
+
+    keys = orc.raster(clip_matrix(c.P, c.V), c.W, c.H, tri)
+    dep, _, _, tid = orc.gbuffer_resolve(keys, tri, c.sc.roughness, c.V)
+    gd, _, _, gt = c.gbuffer_host()
+    assert np.array_equal(gt, tid) and np.array_equal(gd.view(np.uint32), dep.view(np.uint32))
+    c.gi.sync()  # the status was consumed: the context keeps working
+    srv = g.Server(0)
+    with pytest.raises(g.F184Error) as e:
+        srv.add_scene(0, g.GridDesc(32, 5, g.FMT_F16, 0, 256, 0), tri, c.sc.albedo, c.sc.bounds, c.sc.light)
+    assert e.value.code == g._abi.ERR_INVALID
+    srv.close()
