@@ -235,9 +235,11 @@ class VoxelGI:
     def sync(self, stream=None):
         check(self.lib.f184gi_sync(self.ctx, _stream(stream)))
 
-    def selftest_bounded_wait(self, polls, complete, stream=None):
-        """One bounded device wait that expires unless `complete`; the expiry surfaces at the next sync()."""
-        check(self.lib.f184gi_selftest_bounded_wait(self.ctx, polls, 1 if complete else 0, _stream(stream)))
+    def selftest_bounded_wait(self, polls, complete, stream=None, as_copy_wait=False):
+        """One bounded device wait that expires unless `complete`; the expiry surfaces at the next sync().
+        as_copy_wait: the expiry is recorded as an expired bulk-copy wait, after which the context refuses calls."""
+        check(self.lib.f184gi_selftest_bounded_wait(self.ctx, polls, 2 if as_copy_wait else (1 if complete else 0),
+                                                    _stream(stream)))
 
     def frame(self, grid):
         f = GridFrame()

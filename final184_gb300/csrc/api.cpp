@@ -111,6 +111,7 @@ struct f184gi_ctx {
     uint32_t next_id = 1;
     Scratch raster, vox, trace, misc, keys, counts;
     uint32_t* d_status = nullptr;
+    bool failed = false;  // a bulk-copy wait expired (kStatusCopyTimeout): every later call is refused
     TraceStaging* trace_stage = nullptr;
     // voxelize forks the triangle lists onto aux (after the frame) beside the shadow raster on the caller's
     // stream, and joins before the bricks
@@ -204,6 +205,13 @@ uint64_t chain_elems(const f184gi_grid_desc& d) {
     return c.off[l] + c.vol[l] * ((d.anisotropic && l > 0) ? 6 : 1);
 }
 
+// A context whose bulk-copy wait expired refuses further work (kStatusCopyTimeout).
+int refused(const f184gi_ctx* c, const char* what) {
+    return c->failed ? fail(F184GI_ERR_TIMEOUT, std::string(what) + ": the context failed (a bounded wait on a bulk "
+                                                                      "copy expired); create a new one")
+                     : F184GI_OK;
+}
+
 GridObj* find_grid(f184gi_ctx* c, uint32_t id) {
     auto it = c->grids.find(id);
     return it == c->grids.end() ? nullptr : &it->second;
@@ -215,6 +223,11 @@ int read_status(f184gi_ctx* c) {
     if (e != cudaSuccess) return cuda_fail(e, "status read");
     if (!st) return F184GI_OK;
     cudaMemset(c->d_status, 0, 4);
+    if (st & kStatusCopyTimeout) {
+        c->failed = true;
+        return fail(F184GI_ERR_TIMEOUT, "a bounded wait on a bulk copy expired; the copy may still be in flight, so the "
+                                        "context refuses further calls");
+    }
     if (st & kStatusTimeout) return fail(F184GI_ERR_TIMEOUT, "a bounded device wait expired");
     if (st & kStatusOverflow) return fail(F184GI_ERR_OVERFLOW, "a bounded device structure overflowed");
     if (st & kStatusNonFinite)
@@ -383,6 +396,7 @@ int f184gi_voxelize(f184gi_ctx* c, uint32_t grid, const float* tri, const uint32
                     void* stream) {
     PassRange range("f184gi_voxelize");
     if (!c || !light) return fail(F184GI_ERR_INVALID, "voxelize: null argument");
+    if (int rc0 = refused(c, "voxelize")) return rc0;
     GridObj* g = find_grid(c, grid);
     if (!g) return fail(F184GI_ERR_NOTFOUND, "voxelize: unknown grid");
     if (ntris && (!tri || !albedo)) return fail(F184GI_ERR_INVALID, "voxelize: null triangle buffers");
@@ -465,6 +479,7 @@ int f184gi_apply_moves(f184gi_ctx* c, float* tri_xyz, const f184gi_move* moves, 
 int f184gi_mip(f184gi_ctx* c, uint32_t grid, uint32_t levels, uint32_t anisotropic, void* stream) {
     PassRange range("f184gi_mip");
     if (!c) return fail(F184GI_ERR_INVALID, "mip: null context");
+    if (int rc0 = refused(c, "mip")) return rc0;
     GridObj* g = find_grid(c, grid);
     if (!g) return fail(F184GI_ERR_NOTFOUND, "mip: unknown grid");
     if (anisotropic != g->desc.anisotropic) return fail(F184GI_ERR_INVALID, "mip: anisotropy differs from the grid's");
@@ -492,6 +507,7 @@ namespace {
 int trace_views(f184gi_ctx* c, uint32_t grid, const f184gi_view* views, uint32_t nviews,
                 const f184gi_cone_params* params, void* stream, unsigned long long* d_counts) {
     if (!c || (nviews && !views)) return fail(F184GI_ERR_INVALID, "trace: null argument");
+    if (int rc0 = refused(c, "trace")) return rc0;
     GridObj* g = find_grid(c, grid);
     if (!g) return fail(F184GI_ERR_NOTFOUND, "trace: unknown grid");
     if (g->desc.format == F184GI_FMT_RG16) return fail(F184GI_ERR_INVALID, "trace: an RG16 grid is marched (f184gi_march)");
@@ -594,6 +610,7 @@ void f184gi_march_params_default(f184gi_march_params* p) {
 int f184gi_march(f184gi_ctx* c, uint32_t grid, const f184gi_view* views, uint32_t nviews,
                  const f184gi_march_params* params, void* stream) {
     if (!c || (nviews && !views)) return fail(F184GI_ERR_INVALID, "march: null argument");
+    if (int rc0 = refused(c, "march")) return rc0;
     GridObj* g = find_grid(c, grid);
     if (!g) return fail(F184GI_ERR_NOTFOUND, "march: unknown grid");
     if (g->desc.format != F184GI_FMT_RG16) return fail(F184GI_ERR_INVALID, "march: the grid is not an RG16 grid");
@@ -640,6 +657,7 @@ int f184gi_march(f184gi_ctx* c, uint32_t grid, const f184gi_view* views, uint32_
 int f184gi_blur(f184gi_ctx* c, const float* in, const float* depth, uint32_t width, uint32_t height, float* out,
                 void* stream) {
     if (!c || !in || !depth || !out) return fail(F184GI_ERR_INVALID, "blur: null argument");
+    if (int rc0 = refused(c, "blur")) return rc0;
     if (width == 0 || height == 0 || width > 16384 || height > 16384) return fail(F184GI_ERR_INVALID, "blur: bad size");
     if (in == out) return fail(F184GI_ERR_INVALID, "blur: the output may not alias the input");
     int rc = scratch_get(c, c->keys, size_t(width) * height * 16);
@@ -651,6 +669,7 @@ int f184gi_gbuffer(f184gi_ctx* c, const float* tri, const float* rough, uint64_t
                    uint32_t* tri_id_out, void* stream) {
     PassRange range("f184gi_gbuffer");
     if (!c || !view || !tri || !rough) return fail(F184GI_ERR_INVALID, "gbuffer: null argument");
+    if (int rc0 = refused(c, "gbuffer")) return rc0;
     if (!view->depth || !view->normal || !view->roughness) return fail(F184GI_ERR_INVALID, "gbuffer: null G-buffer planes");
     if (view->width == 0 || view->height == 0 || view->width > kMaxRasterSide || view->height > kMaxRasterSide)
         return fail(F184GI_ERR_INVALID, "gbuffer: view sides must be 1.." + std::to_string(kMaxRasterSide) + " pixels");
@@ -795,6 +814,7 @@ int grid_internal(f184gi_ctx* c, uint32_t grid, ChainLayout* chain, const f184gi
 
 int ctx_internal(f184gi_ctx* c, int* device, uint32_t** d_status) {
     if (!c || !device || !d_status) return fail(F184GI_ERR_INVALID, "ctx_internal: null argument");
+    if (int rc0 = refused(c, "call")) return rc0;
     *device = c->device;
     *d_status = c->d_status;
     return F184GI_OK;

@@ -25,6 +25,10 @@ constexpr uint32_t kMaxRasterSide = 8192;  // rasterized images (shadow maps, G-
 constexpr uint64_t kMaxTracePixels = 1ull << 36;
 constexpr uint32_t kStatusRange = 4u;      // geometry outside the fixed-point range was skipped
 constexpr uint32_t kStatusNonFinite = 8u;  // triangles with a NaN or infinite coordinate were skipped
+// a bounded wait on a bulk copy into shared memory expired: the CTA waited a second bounded window for its copy and
+// returned, so the copy may still land in shared memory the SM has handed to another CTA.  The context that reads
+// this bit refuses every later call (F184GI_ERR_TIMEOUT), so nothing it launches runs beside such a copy.
+constexpr uint32_t kStatusCopyTimeout = 16u;
 
 // process-wide count of kernels this library has launched (f184gi_kernel_launches)
 void note_launches(uint32_t n);

@@ -94,7 +94,7 @@ __global__ void __launch_bounds__(512) mip_pass(ChainLayout c, uint32_t src, uin
             bulk_g2s(smem, gsrc, bytes, &bar);
         }
         if (!mbar_wait_bounded(&bar, 0, kWaitPolls)) {
-            if (threadIdx.x == 0) set_status(status, kStatusTimeout);
+            if (threadIdx.x == 0) set_status(status, kStatusTimeout | kStatusCopyTimeout);
             mbar_wait_bounded(&bar, 0, kWaitPolls);  // let the copy land before the CTA exits
             return;
         }
@@ -174,7 +174,7 @@ __global__ void __launch_bounds__(512, 2) mip_aniso_l0(ChainLayout c, uint32_t n
         bulk_g2s(smem, gsrc, bytes, &bar);
     }
     if (!mbar_wait_bounded(&bar, 0, kWaitPolls)) {
-        if (threadIdx.x == 0) set_status(status, kStatusTimeout);
+        if (threadIdx.x == 0) set_status(status, kStatusTimeout | kStatusCopyTimeout);
         mbar_wait_bounded(&bar, 0, kWaitPolls);  // let the copy land before the CTA exits
         return;
     }

@@ -8,7 +8,12 @@
 // __device__ array of kStaticScratchBytes, so a call allocates nothing on the device.
 //
 // Set-up: the first call on a device looks the array's address up (cudaGetSymbolAddress) with that device
-// current.  That first call can load this file's module and so should come before any stream capture.
+// current.  That first call can load this file's module and so should come before any stream capture.  Each call
+// makes the context's device current for its launches and restores the caller's device afterwards.
+//
+// Memory: the array's 48 MiB per device are not counted in f184gi_memory_used() nor in a request server's HBM
+// budget.  They are reserved when this file's module loads on a device: at the first f184gi_gbuffer_static call
+// under CUDA's default lazy module loading, at start-up of every device under CUDA_MODULE_LOADING=EAGER.
 //
 // Sharing: every call on a device uses the same array, which keeps the last call's contents.  The raster clears
 // the counters it needs (the per-tile counts and fills, the overflow and big-record counts) on the call's
@@ -35,25 +40,37 @@ __device__ __align__(256) unsigned char g_gbuffer_scratch[kStaticScratchBytes];
 std::mutex g_setup_mu;
 void* g_scratch_ptr[kMaxDevices] = {};
 
-// Once per device, with that device current: the array's device address.
+// Once per device, with that device current (the caller makes it so): the array's device address.
 int static_scratch(int device, void** ptr) {
     if (device < 0 || device >= kMaxDevices) return fail(F184GI_ERR_INVALID, "gbuffer_static: device out of range");
     std::lock_guard<std::mutex> lk(g_setup_mu);
     if (!g_scratch_ptr[device]) {
-        int prev = -1;
-        cudaError_t e = cudaGetDevice(&prev);
-        if (e != cudaSuccess) return cuda_fail(e, "gbuffer_static: cudaGetDevice");
-        if (prev != device && (e = cudaSetDevice(device)) != cudaSuccess)
-            return cuda_fail(e, "gbuffer_static: cudaSetDevice");
         void* p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_gbuffer_scratch);
-        if (prev != device) cudaSetDevice(prev);
+        cudaError_t e = cudaGetSymbolAddress(&p, g_gbuffer_scratch);
         if (e != cudaSuccess) return cuda_fail(e, "gbuffer_static: cudaGetSymbolAddress");
         g_scratch_ptr[device] = p;
     }
     *ptr = g_scratch_ptr[device];
     return F184GI_OK;
 }
+
+// The context's device current for the duration of a call, the caller's device restored at the end.
+struct DeviceScope {
+    int prev = -1;
+    bool switched = false;
+    int enter(int device) {
+        cudaError_t e = cudaGetDevice(&prev);
+        if (e != cudaSuccess) return cuda_fail(e, "gbuffer_static: cudaGetDevice");
+        if (prev != device) {
+            if ((e = cudaSetDevice(device)) != cudaSuccess) return cuda_fail(e, "gbuffer_static: cudaSetDevice");
+            switched = true;
+        }
+        return F184GI_OK;
+    }
+    ~DeviceScope() {
+        if (switched) cudaSetDevice(prev);
+    }
+};
 
 }  // namespace
 }  // namespace f184
@@ -89,6 +106,8 @@ extern "C" int f184gi_gbuffer_static(f184gi_ctx* c, const float* tri, const floa
     uint32_t* d_status = nullptr;
     int rc = ctx_internal(c, &device, &d_status);
     if (rc) return rc;
+    DeviceScope scope;  // the array's address and the launches belong to the context's device
+    if ((rc = scope.enter(device))) return rc;
     void* base = nullptr;
     if ((rc = static_scratch(device, &base))) return rc;
     cudaStream_t s = static_cast<cudaStream_t>(stream);

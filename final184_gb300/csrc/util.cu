@@ -254,9 +254,9 @@ __global__ void bounded_wait_selftest(uint32_t polls, uint32_t complete, uint32_
         fence_barrier_init();
     }
     __syncthreads();
-    if (complete && threadIdx.x == 0) mbar_arrive(&bar);
+    if (complete == 1 && threadIdx.x == 0) mbar_arrive(&bar);
     const bool done = mbar_wait_bounded(&bar, 0, polls);
-    if (!done && threadIdx.x == 0) set_status(status, kStatusTimeout);
+    if (!done && threadIdx.x == 0) set_status(status, kStatusTimeout | (complete == 2 ? kStatusCopyTimeout : 0u));
 }
 }  // namespace
 

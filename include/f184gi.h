@@ -159,9 +159,11 @@ int f184gi_abi_version(void);
 /* number of kernels this library has launched in this process (diagnostics) */
 uint64_t f184gi_kernel_launches(void);
 /* Diagnostic, with no counterpart in the reference: one device wait on a shared-memory mbarrier, bounded to
- * `polls` polls (1..2^24), whose phase completes only when `complete` is nonzero.  An expired wait is recorded in
- * the context's status exactly as the library's own bounded waits record theirs, so the next f184gi_sync returns
- * F184GI_ERR_TIMEOUT and the context stays usable: the failure path, exercised without a GPU fault. */
+ * `polls` polls (1..2^24), whose phase completes only when `complete` is 1.  An expired wait is recorded in the
+ * context's status exactly as the library's own bounded waits record theirs, so the next f184gi_sync returns
+ * F184GI_ERR_TIMEOUT and the context stays usable: the failure path, exercised without a GPU fault.  With
+ * `complete` = 2 the expired wait is recorded as the mip pass records an expired wait on its bulk copy (no copy is
+ * involved here): the next f184gi_sync returns F184GI_ERR_TIMEOUT and the context refuses every later call. */
 int f184gi_selftest_bounded_wait(f184gi_ctx* ctx, uint32_t polls, uint32_t complete, void* stream);
 int f184gi_create(const f184gi_config* cfg, f184gi_ctx** out);
 int f184gi_destroy(f184gi_ctx* ctx);
@@ -234,7 +236,10 @@ int f184gi_gbuffer(f184gi_ctx* ctx, const float* tri_xyz, const float* roughness
  * width*height <= 2097152 (1920x1080 fits); larger calls return F184GI_ERR_INVALID and name the limit.  The
  * first call on a device looks up the array's address (and can load its module): make it before any stream
  * capture.  Calls that overlap on the GPU race on the array; calls in order on one stream do not.  Errors that
- * kernels flag are reported by f184gi_sync(ctx, stream) as for f184gi_gbuffer. */
+ * kernels flag are reported by f184gi_sync(ctx, stream) as for f184gi_gbuffer.  The call runs on the context's
+ * device and restores the caller's current device.  The array's 48 MiB per device are counted neither in
+ * f184gi_memory_used nor in a server's HBM budget; they are reserved when the library's module holding it loads
+ * on a device (at the first call under CUDA's lazy module loading, at start-up under CUDA_MODULE_LOADING=EAGER). */
 int f184gi_gbuffer_static(f184gi_ctx* ctx, const float* tri_xyz, const float* roughness, uint64_t ntris,
                           const f184gi_view* view, uint32_t* tri_id_out, void* stream);
 

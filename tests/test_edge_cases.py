@@ -195,6 +195,29 @@ def test_expired_bounded_wait_is_reported_and_the_context_stays_usable(case):
     assert np.array_equal(before.view(np.uint32), after.view(np.uint32))
 
 
+def test_expired_copy_wait_retires_the_context(lib):
+    """An expired wait on a bulk copy (as the mip pass records one; the self-test's wait involves no copy) makes
+    the context refuse every later call, since such a copy may still be landing in shared memory."""
+    import final184_gb300 as g
+
+    c = Case(ntris=3000, nobj=30, dim=32, levels=5, res=256, width=64, height=32)
+    c.voxelize()
+    c.gi.selftest_bounded_wait(1000, complete=False, as_copy_wait=True)
+    with pytest.raises(g.F184Error) as err:
+        c.gi.sync()
+    assert err.value.code == g._abi.ERR_TIMEOUT and "bulk copy" in str(err.value)
+    for call in (lambda: c.gi.mip(c.grid), lambda: c.gi.trace(c.grid, [c.view]),
+                 lambda: c.gi.voxelize(c.grid, c.tri_d.data_ptr(), c.alb_d.data_ptr(), c.ntris, c.sc.light,
+                                       bounds=c.sc.bounds)):
+        with pytest.raises(g.F184Error) as err:
+            call()
+        assert err.value.code == g._abi.ERR_TIMEOUT
+    c.gi.close()
+    fresh = Case(ntris=3000, nobj=30, dim=32, levels=5, res=256, width=64, height=32)
+    fresh.voxelize()  # a new context works
+    fresh.mip()
+
+
 def test_oversize_views_are_refused_before_any_launch(case):
     import final184_gb300 as g
     from final184_gb300 import _abi

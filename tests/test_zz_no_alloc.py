@@ -54,16 +54,22 @@ def test_static_scratch_gbuffer_matches_gbuffer_twice_in_a_row(lib):
     used0 = gi.memory_used()
     got = []
     stream = torch.cuda.Stream()
-    for cs in cases:
-        pl = _planes(torch, cs)
+    planes = [_planes(torch, cs) for cs in cases]
+    torch.cuda.synchronize()  # the planes are initialised on torch's stream
+    free = []
+    for cs, pl in zip(cases, planes):
         v = _view(g, cs, pl)
-        torch.cuda.synchronize()  # the planes are initialised on torch's stream
+        free.append(torch.cuda.mem_get_info()[0])
         g.check(gi.lib.f184gi_gbuffer_static(gi.ctx, cs["tri"].data_ptr(), cs["rough"].data_ptr(), cs["sc"].ntris,
                                              C.byref(v), C.c_void_p(pl[3].data_ptr()),
                                              C.c_void_p(stream.cuda_stream)))
         got.append(pl)
     gi.sync(stream.cuda_stream)
+    free.append(torch.cuda.mem_get_info()[0])
     assert gi.memory_used() == used0  # nothing was allocated on the context
+    # nor on the device: after the first call (which may load the module holding the array), the second call
+    # leaves the device's free memory as it was
+    assert free[2] == free[1], (free[1], free[2])
     for a, b in zip(ref, got):
         for x, y in zip(a, b):
             assert torch.equal(x.view(torch.int32) if x.dtype == torch.float32 else x,
