@@ -544,8 +544,7 @@ int trace_views(f184gi_ctx* c, uint32_t grid, const f184gi_view* views, uint32_t
         for (int k = 0; k < 16; ++k) V[k] = v.view[k], P[k] = v.proj[k];
         if (!invert4(V, IV) || !invert4(P, IP)) return fail(F184GI_ERR_INVALID, "trace: singular view or projection");
         TraceView& t = tv[i];
-        for (int k = 0; k < 16; ++k) t.iview[k] = float(IV[k]), t.iproj[k] = float(IP[k]);
-        trace_view_set_depth_rows(t, IP);
+        trace_view_set_inverses(t, IP, IV);
         t.eye[0] = float(IV[3]);
         t.eye[1] = float(IV[7]);
         t.eye[2] = float(IV[11]);

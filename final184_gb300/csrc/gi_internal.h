@@ -110,8 +110,9 @@ int frame_launch(const float* tri, uint64_t ntris, const f184gi_bounds* bounds, 
 int mip_launch(const ChainLayout& chain, uint32_t levels, uint32_t* d_status, cudaStream_t s);
 
 struct TraceView {
-    float iview[16], iproj[16];     // inverses (FP32 of FP64 inverses)
-    float iproj_zw_hi[8], iproj_zw_lo[8];  // rows 2 and 3 of the FP64 inverse projection as FP32 pairs hi + lo
+    float iview[16];                     // inverse view (FP32 of the FP64 inverse: normals)
+    float iproj_h[16], iproj_l[16];      // FP64 inverse projection as FP32 pairs h + l (the float-float position)
+    float iview_h[12], iview_l[12];      // rows 0..2 of the FP64 inverse view as FP32 pairs
     float eye[3];
     uint32_t width, height;
     const float* depth;
@@ -143,11 +144,16 @@ struct TraceConsts {
     unsigned long long* counts;  // the counting kernel's totals: cone steps, level samples (null otherwise)
 };
 void trace_consts_schedule(TraceConsts& tc);  // fills tc.sched from tc.p
-// rows 2 and 3 of the FP64 inverse projection, split into FP32 pairs (the trace's float-float depth rows)
-inline void trace_view_set_depth_rows(TraceView& t, const double IP[16]) {
-    for (int k = 0; k < 8; ++k) {
-        t.iproj_zw_hi[k] = float(IP[8 + k]);
-        t.iproj_zw_lo[k] = float(IP[8 + k] - double(t.iproj_zw_hi[k]));
+// the FP64 inverse projection and inverse view split into FP32 pairs (the trace's float-float pixel set-up)
+inline void trace_view_set_inverses(TraceView& t, const double IP[16], const double IV[16]) {
+    for (int k = 0; k < 16; ++k) {
+        t.iview[k] = float(IV[k]);
+        t.iproj_h[k] = float(IP[k]);
+        t.iproj_l[k] = float(IP[k] - double(t.iproj_h[k]));
+    }
+    for (int k = 0; k < 12; ++k) {
+        t.iview_h[k] = float(IV[k]);
+        t.iview_l[k] = float(IV[k] - double(t.iview_h[k]));
     }
 }
 // Cone-trace kernel variants: the tile shape (tw x th pixels, one thread each) and the CTAs kept resident per SM

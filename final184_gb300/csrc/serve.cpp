@@ -199,8 +199,7 @@ int prepare_view(f184gi_server* S, const Scene* sc, const f184gi_view& v, TraceV
     for (int k = 0; k < 16; ++k) V[k] = v.view[k], P[k] = v.proj[k];
     if (!invert4(V, IV) || !invert4(P, IP)) return fail(F184GI_ERR_INVALID, "server: singular view or projection");
     t = TraceView{};
-    for (int k = 0; k < 16; ++k) t.iview[k] = float(IV[k]), t.iproj[k] = float(IP[k]);
-    trace_view_set_depth_rows(t, IP);
+    trace_view_set_inverses(t, IP, IV);
     t.eye[0] = float(IV[3]), t.eye[1] = float(IV[7]), t.eye[2] = float(IV[11]);
     t.width = v.width, t.height = v.height;
     t.depth = v.depth, t.normal = v.normal, t.rough = v.roughness, t.out = v.out, t.out_format = v.out_format;

@@ -86,41 +86,49 @@ __device__ __forceinline__ float4 load_vox_at(const unsigned char* p, int k) {
     return make_float4(fa.x, fa.y, fb.x, fb.y);
 }
 
-// Float-float (unevaluated pairs hi + lo of FP32) arithmetic for the depth reconstruction, every operation
-// explicitly rounded: Knuth's two-sum and the FMA two-product are exact, so a row of the inverse projection,
-// split into FP32 pairs on the host, is evaluated to ~2^-46 of its largest term.
+// Float-float arithmetic (unevaluated pairs h + l of FP32, ~2^-44 relative) for the pixel set-up, every
+// operation explicitly rounded: Knuth's two-sum and the FMA two-product are exact.  The cone origin in voxel units
+// comes out accurate to ~1e-9 voxel; an FP32 set-up (~1e-5 voxel at 256 voxels) moves the trilinear weights of a
+// grazing cone's first samples by 1e-5, which is a relative error of 1e-2 on a sample weighted 1e-3.
+struct FF {
+    float h, l;
+};
 __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
     s = __fadd_rn(a, b);
     const float bb = __fsub_rn(s, a);
     e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
 }
-// (hi[0..3] + lo[0..3]) . (x, y, z, 1) as a pair
-__device__ __forceinline__ void ff_row(const float* hi, const float* lo, float x, float y, float z, float& rh,
-                                       float& rl) {
-    const float p0 = __fmul_rn(hi[0], x), p1 = __fmul_rn(hi[1], y), p2 = __fmul_rn(hi[2], z);
-    const float e0 = __fmaf_rn(hi[0], x, -p0), e1 = __fmaf_rn(hi[1], y, -p1), e2 = __fmaf_rn(hi[2], z, -p2);
-    float s0, s1, s2, t0, t1, t2;
-    two_sum(p0, p1, s0, t0);
-    two_sum(s0, p2, s1, t1);
-    two_sum(s1, hi[3], s2, t2);
-    const float small = __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(t0, t1), t2), __fadd_rn(__fadd_rn(e0, e1), e2)),
-                                  __fadd_rn(__fadd_rn(__fmul_rn(lo[0], x), __fmul_rn(lo[1], y)),
-                                            __fadd_rn(__fmul_rn(lo[2], z), lo[3])));
-    rh = __fadd_rn(s2, small);
-    rl = __fsub_rn(small, __fsub_rn(rh, s2));
+__device__ __forceinline__ FF ff_norm(float s, float e) {  // |s| >= |e|
+    const float h = __fadd_rn(s, e);
+    return FF{h, __fsub_rn(e, __fsub_rn(h, s))};
 }
-// 1 / w and z / w of the view-space point (rows 2 and 3 of the inverse projection as FP32 pairs)
-__device__ __forceinline__ void depth_zw(const float* hi, const float* lo, float nx, float ny, float d, float& rw,
-                                         float& z) {
-    float zh, zl, wh, wl;
-    ff_row(hi, lo, nx, ny, d, zh, zl);
-    ff_row(hi + 4, lo + 4, nx, ny, d, wh, wl);
-    const float r = __frcp_rn(wh);
-    const float e = __fmaf_rn(-r, wl, __fmaf_rn(-r, wh, 1.0f));  // 1 - r (wh + wl)
-    rw = __fmaf_rn(r, e, r);
-    const float q = __fmul_rn(zh, rw);
-    const float qe = __fadd_rn(__fmaf_rn(-q, wh, zh), __fmaf_rn(-q, wl, zl));  // (zh + zl) - q (wh + wl)
-    z = __fmaf_rn(qe, rw, q);
+__device__ __forceinline__ FF ff_add(FF a, FF b) {
+    float s, e;
+    two_sum(a.h, b.h, s, e);
+    return ff_norm(s, __fadd_rn(e, __fadd_rn(a.l, b.l)));
+}
+__device__ __forceinline__ FF ff_mul(FF a, FF b) {
+    const float p = __fmul_rn(a.h, b.h);
+    const float e = __fmaf_rn(a.h, b.l, __fmaf_rn(a.l, b.h, __fmaf_rn(a.h, b.h, -p)));
+    return ff_norm(p, e);
+}
+__device__ __forceinline__ FF ff_div(FF a, FF b) {
+    const float q = __fdiv_rn(a.h, b.h);
+    const FF r = ff_add(a, ff_mul(FF{-q, 0.0f}, b));  // a - q b
+    return ff_norm(q, __fdiv_rn(r.h, b.h));
+}
+// (h[0..3] + l[0..3]) . (x, y, z, 1)
+__device__ __forceinline__ FF ff_row(const float* h, const float* l, FF x, FF y, FF z) {
+    FF s = ff_add(ff_mul(FF{h[0], l[0]}, x), ff_mul(FF{h[1], l[1]}, y));
+    s = ff_add(s, ff_mul(FF{h[2], l[2]}, z));
+    return ff_add(s, FF{h[3], l[3]});
+}
+// (2 k + 1) / n - 1: the normalised device coordinate of pixel k of n
+__device__ __forceinline__ FF ff_ndc(uint32_t k, uint32_t n) {
+    const float num = float(2u * k + 1u), den = float(n);  // exact: n <= 16384
+    const float q = __fdiv_rn(num, den);
+    const float ql = __fdiv_rn(__fmaf_rn(-q, den, num), den);
+    return ff_add(FF{q, ql}, FF{-1.0f, 0.0f});
 }
 
 // The grid a warp's tile traces against, staged in shared memory per warp: lanes index the level table with their
@@ -131,8 +139,8 @@ struct GridRef {
     const void* base;
     uint32_t dim, levels;
     float tmax;
-    float org[3];
-    float inv_vs;
+    float org_h[3], org_l[3];  // world -> L0 voxel units: (p - origin) * inv_vs, as float-float pairs
+    float ivs_h, ivs_l;
 };
 
 // Brick-offset table staged in shared memory: lut[a * kLut + b] = part1by2(b) << (9 + a), the element offset of
@@ -149,18 +157,25 @@ constexpr int kLut = 65;
 // folded into the z weights: acc += scale * sum_taps w_tap v_tap.
 template <int FMT, int NV>
 __device__ __forceinline__ void tri_sample(const void* base, int d, uint32_t l, const uint32_t (&vol_off)[NV],
-                                          float3 x, const uint32_t* lut, float scale, float4 (&acc)[NV]) {
+                                          float3 oi, float3 xr, const uint32_t* lut, float scale,
+                                          float4 (&acc)[NV]) {
     // NV volumes of the same level share the tap coordinates and weights (the three directions an anisotropic
     // sample blends); each volume accumulates its own taps in the single-volume order.
+    // The sample point is oi + xr (L0 voxel units): oi integer, xr small.  Its level coordinate
+    // u = (oi + xr) 2^-l - 0.5 is split as A = oi 2^-l - 0.5 (exact) = Ai + Af (integer + fraction, exact) and
+    // v = Af + xr 2^-l, so the fraction that weights the taps keeps the precision of xr, not of |oi|.
     const float s = __int_as_float((127 - int(l)) << 23);  // 2^-l
-    const float u[3] = {x.x * s - 0.5f, x.y * s - 0.5f, x.z * s - 0.5f};
+    const float oa[3] = {oi.x, oi.y, oi.z}, xa[3] = {xr.x, xr.y, xr.z};
     int c0[3];
     float f[3];
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
-        float fl = floorf(u[a]);
-        c0[a] = int(fl);
-        f[a] = u[a] - fl;
+        const float A = __fmaf_rn(oa[a], s, -0.5f);
+        const float Ai = floorf(A);
+        const float v = __fmaf_rn(xa[a], s, __fsub_rn(A, Ai));
+        const float fl = floorf(v);
+        c0[a] = int(__fadd_rn(Ai, fl));
+        f[a] = __fsub_rn(v, fl);
     }
     const float wx[2] = {1.0f - f[0], f[0]}, wy[2] = {1.0f - f[1], f[1]};
     const float wz[2] = {(1.0f - f[2]) * scale, f[2] * scale};
@@ -266,13 +281,13 @@ __device__ __forceinline__ void tri_sample(const void* base, int d, uint32_t l, 
 // acc += scale * (the sample of level l at x): isotropic, or the three direction volumes facing the cone
 // weighted by dir^2 (anisotropic levels >= 1)
 template <int FMT, bool ANISO>
-__device__ __forceinline__ void level_sample(const GridRef& g, const uint32_t* lut, uint32_t l, float3 x,
-                                             float3 dir, float scale, float4& acc) {
+__device__ __forceinline__ void level_sample(const GridRef& g, const uint32_t* lut, uint32_t l, float3 oi,
+                                             float3 x, float3 dir, float scale, float4& acc) {
     const int d = int(g.dim >> l);
     if (!ANISO || l == 0) {
         const uint32_t vo[1] = {g.off[l]};
         float4 a[1] = {acc};
-        tri_sample<FMT, 1>(g.base, d, l, vo, x, lut, scale, a);
+        tri_sample<FMT, 1>(g.base, d, l, vo, oi, x, lut, scale, a);
         acc = a[0];
         return;
     }
@@ -281,7 +296,7 @@ __device__ __forceinline__ void level_sample(const GridRef& g, const uint32_t* l
                             g.off[l] + (dir.y >= 0.0f ? 2u : 3u) * g.vol[l],
                             g.off[l] + (dir.z >= 0.0f ? 4u : 5u) * g.vol[l]};
     float4 sa[3] = {make_float4(0.f, 0.f, 0.f, 0.f), make_float4(0.f, 0.f, 0.f, 0.f), make_float4(0.f, 0.f, 0.f, 0.f)};
-    tri_sample<FMT, 3>(g.base, d, l, vo, x, lut, 1.0f, sa);
+    tri_sample<FMT, 3>(g.base, d, l, vo, oi, x, lut, 1.0f, sa);
 #pragma unroll
     for (int a = 0; a < 3; ++a) fma4(acc, w[a], sa[a]);
 }
@@ -289,7 +304,7 @@ __device__ __forceinline__ void level_sample(const GridRef& g, const uint32_t* l
 // sched: the first ns samples of this cone's march (the diffuse schedule; ns = 0 for the specular cone).
 // COUNT (the instrumented kernel): cnt[0] += steps, cnt[1] += level samples.
 template <int FMT, bool ANISO, bool COUNT>
-__device__ float4 cone(const GridRef& g, const uint32_t* lut, const TraceConsts& tc, float3 o, float3 dir,
+__device__ float4 cone(const GridRef& g, const uint32_t* lut, const TraceConsts& tc, float3 oi, float3 of, float3 dir,
                        float tan_half, const SchedEntry* sched, uint32_t ns, uint32_t* cnt) {
     float cr = 0.f, cg = 0.f, cb = 0.f, alpha = 0.f;
     // The march distance is the float pair t + tl, advanced with error-free sums: a cone of small aperture takes
@@ -310,10 +325,13 @@ __device__ float4 cone(const GridRef& g, const uint32_t* lut, const TraceConsts&
         }
         if (!(t < g.tmax || (t == g.tmax && tl <= 0.0f))) break;
         float lvl = fminf(lraw, maxl);
-        float3 x = f3(fmaf(dir.x, t, fmaf(dir.x, tl, o.x)), fmaf(dir.y, t, fmaf(dir.y, tl, o.y)),
-                      fmaf(dir.z, t, fmaf(dir.z, tl, o.z)));
+        // the sample point oi + x: x is the offset from the origin's integer voxel (small near the surface, where
+        // the weights of a grazing cone are most sensitive)
+        float3 x = f3(fmaf(dir.x, t, fmaf(dir.x, tl, of.x)), fmaf(dir.y, t, fmaf(dir.y, tl, of.y)),
+                      fmaf(dir.z, t, fmaf(dir.z, tl, of.z)));
         float m = 2.0f * diam;
-        if (x.x < -m || x.y < -m || x.z < -m || x.x > dimf + m || x.y > dimf + m || x.z > dimf + m) break;
+        const float3 xa = add3(oi, x);  // for the exit test only: samples out there read zero
+        if (xa.x < -m || xa.y < -m || xa.z < -m || xa.x > dimf + m || xa.y > dimf + m || xa.z > dimf + m) break;
         float fl = floorf(lvl);
         uint32_t l0 = uint32_t(fl);
         float f = lvl - fl;
@@ -330,10 +348,10 @@ __device__ float4 cone(const GridRef& g, const uint32_t* lut, const TraceConsts&
             const uint32_t nl = two ? 2u : 1u;
 #pragma unroll 1
             for (uint32_t k = 0; k < nl; ++k)
-                level_sample<FMT, ANISO>(g, lut, l0 + k, x, dir, k ? f : (two ? 1.0f - f : 1.0f), s);
+                level_sample<FMT, ANISO>(g, lut, l0 + k, oi, x, dir, k ? f : (two ? 1.0f - f : 1.0f), s);
         } else {
-            level_sample<FMT, ANISO>(g, lut, l0, x, dir, two ? 1.0f - f : 1.0f, s);
-            if (two) level_sample<FMT, ANISO>(g, lut, l0 + 1, x, dir, f, s);
+            level_sample<FMT, ANISO>(g, lut, l0, oi, x, dir, two ? 1.0f - f : 1.0f, s);
+            if (two) level_sample<FMT, ANISO>(g, lut, l0 + 1, oi, x, dir, f, s);
         }
         float tr = 1.0f - alpha;
         cr += tr * s.x;
@@ -375,25 +393,38 @@ __device__ void trace_pixel(const GridRef& g, const uint32_t* lut, const TraceCo
         store_out(v.out, v.out_format, npix + pi, make_float4(0.f, 0.f, 0.f, 0.f));
         return;
     }
-    const float* ip = v.iproj;
     const float* iv = v.iview;
-    float nx = (float(px) + 0.5f) / float(v.width) * 2.0f - 1.0f;
-    float ny = (float(py) + 0.5f) / float(v.height) * 2.0f - 1.0f;
-    // View-space position.  The projective rows (z, w) are float-float: for depths near 1, w is a small
-    // difference of O(1) terms and plain FP32 would lose ~5e-6 of it (a fraction of a voxel at 10 m); x and y
-    // are well conditioned and stay FP32.
-    float rwf, csz;
-    depth_zw(v.iproj_zw_hi, v.iproj_zw_lo, nx, ny, d, rwf, csz);
-    const float vx = ip[0] * nx + ip[1] * ny + ip[2] * d + ip[3], vy = ip[4] * nx + ip[5] * ny + ip[6] * d + ip[7];
-    float3 cs = f3(vx * rwf, vy * rwf, csz);
-    float3 wp = f3(iv[0] * cs.x + iv[1] * cs.y + iv[2] * cs.z + iv[3], iv[4] * cs.x + iv[5] * cs.y + iv[6] * cs.z + iv[7],
-                   iv[8] * cs.x + iv[9] * cs.y + iv[10] * cs.z + iv[11]);
+    // View-space and world position in float-float: clip (ndc x, ndc y, depth, 1) through the FP64 inverse
+    // projection (rows as FP32 pairs), the perspective division, then the inverse view (rows as FP32 pairs).
+    const FF ndx = ff_ndc(px, v.width), ndy = ff_ndc(py, v.height), dz = FF{d, 0.0f};
+    const FF vw = ff_row(v.iproj_h + 12, v.iproj_l + 12, ndx, ndy, dz);
+    const FF cx = ff_div(ff_row(v.iproj_h, v.iproj_l, ndx, ndy, dz), vw);
+    const FF cy = ff_div(ff_row(v.iproj_h + 4, v.iproj_l + 4, ndx, ndy, dz), vw);
+    const FF cz = ff_div(ff_row(v.iproj_h + 8, v.iproj_l + 8, ndx, ndy, dz), vw);
+    FF wpf[3];
+#pragma unroll
+    for (int r = 0; r < 3; ++r) wpf[r] = ff_row(v.iview_h + 4 * r, v.iview_l + 4 * r, cx, cy, cz);
+    const float3 wp = f3(wpf[0].h, wpf[1].h, wpf[2].h);
     float3 nv = oct_decode(v.normal[pi]);
     float3 nw = norm3(f3(iv[0] * nv.x + iv[1] * nv.y + iv[2] * nv.z, iv[4] * nv.x + iv[5] * nv.y + iv[6] * nv.z,
                          iv[8] * nv.x + iv[9] * nv.y + iv[10] * nv.z));
     float rough = __half2float(__ushort_as_half(v.rough[pi]));
-    float3 pv = f3((wp.x - g.org[0]) * g.inv_vs, (wp.y - g.org[1]) * g.inv_vs, (wp.z - g.org[2]) * g.inv_vs);
-    float3 o = add3(pv, mul3(nw, tc.p.start_offset));
+    // cone origin o = (wp - origin) * inv_vs + n * start_offset in voxel units, split as oi (integer) + of
+    float3 oi, of;
+    {
+        const float na[3] = {nw.x, nw.y, nw.z};
+        float oia[3], ofa[3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            const FF pv = ff_mul(ff_add(wpf[a], FF{-g.org_h[a], -g.org_l[a]}), FF{g.ivs_h, g.ivs_l});
+            const float q = __fmul_rn(na[a], tc.p.start_offset);
+            const FF o = ff_add(pv, FF{q, __fmaf_rn(na[a], tc.p.start_offset, -q)});
+            oia[a] = floorf(o.h);
+            ofa[a] = __fadd_rn(__fsub_rn(o.h, oia[a]), o.l);
+        }
+        oi = f3(oia[0], oia[1], oia[2]);
+        of = f3(ofa[0], ofa[1], ofa[2]);
+    }
     // the specular cone's direction and aperture first: the view position and normal die here
     float3 rd = f3(0.f, 0.f, 0.f);
     float th = 0.f;
@@ -407,7 +438,7 @@ __device__ void trace_pixel(const GridRef& g, const uint32_t* lut, const TraceCo
     coord_space(nw, bx, by, bz);
     float4 acc;
     if (tc.p.diffuse_cones >= 5) {
-        float4 c0 = cone<FMT, ANISO, COUNT>(g, lut, tc, o, bz, tc.p.diffuse_tan_half, sched, kDiffuseSched, cnt);
+        float4 c0 = cone<FMT, ANISO, COUNT>(g, lut, tc, oi, of, bz, tc.p.diffuse_tan_half, sched, kDiffuseSched, cnt);
         acc = make_float4(0.25f * c0.x, 0.25f * c0.y, 0.25f * c0.z, 0.25f * c0.w);
 #pragma unroll 1
         for (int k = 0; k < 4; ++k) {
@@ -415,18 +446,18 @@ __device__ void trace_pixel(const GridRef& g, const uint32_t* lut, const TraceCo
             float3 side = (k & 1) ? by : bx;
             if (k & 2) side = f3(-side.x, -side.y, -side.z);
             float3 dir = norm3(add3(mul3(bz, tc.cos_tilt), mul3(side, tc.sin_tilt)));
-            float4 ck = cone<FMT, ANISO, COUNT>(g, lut, tc, o, dir, tc.p.diffuse_tan_half, sched, kDiffuseSched, cnt);
+            float4 ck = cone<FMT, ANISO, COUNT>(g, lut, tc, oi, of, dir, tc.p.diffuse_tan_half, sched, kDiffuseSched, cnt);
             acc.x += 0.1875f * ck.x;
             acc.y += 0.1875f * ck.y;
             acc.z += 0.1875f * ck.z;
             acc.w += 0.1875f * ck.w;
         }
     } else {
-        acc = cone<FMT, ANISO, COUNT>(g, lut, tc, o, bz, tc.p.diffuse_tan_half, sched, kDiffuseSched, cnt);
+        acc = cone<FMT, ANISO, COUNT>(g, lut, tc, oi, of, bz, tc.p.diffuse_tan_half, sched, kDiffuseSched, cnt);
     }
     store_out(v.out, v.out_format, pi, acc);
     float4 sp = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (tc.p.specular) sp = cone<FMT, ANISO, COUNT>(g, lut, tc, o, rd, th, nullptr, 0u, cnt);
+    if (tc.p.specular) sp = cone<FMT, ANISO, COUNT>(g, lut, tc, oi, of, rd, th, nullptr, 0u, cnt);
     store_out(v.out, v.out_format, npix + pi, sp);
 }
 
@@ -481,9 +512,16 @@ __global__ void __launch_bounds__(TW * TH, MINB) trace_kernel(TraceConsts tc, co
                 g.dim = v.grid_dim;
                 g.levels = v.grid_levels;
                 g.tmax = v.tmax;
-                // world -> L0 voxel units: (p - origin) * (inv_voxel_fixed / 256), all scalings exact
-                for (int a = 0; a < 3; ++a) g.org[a] = float(v.frame->origin[a]);
-                g.inv_vs = float(v.frame->inv_voxel_fixed * (1.0 / 256.0));
+                // world -> L0 voxel units: (p - origin) * (inv_voxel_fixed / 256), the frame's FP64 values split
+                // into FP32 pairs once per view (the voxel-to-world set-up)
+                for (int a = 0; a < 3; ++a) {
+                    const double o = v.frame->origin[a];
+                    g.org_h[a] = float(o);
+                    g.org_l[a] = float(o - double(g.org_h[a]));
+                }
+                const double ivs = v.frame->inv_voxel_fixed * (1.0 / 256.0);
+                g.ivs_h = float(ivs);
+                g.ivs_l = float(ivs - double(g.ivs_h));
             }
             cur_view = vi;
             __syncwarp();

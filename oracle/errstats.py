@@ -21,17 +21,22 @@ FLOOR_FRAC = 1e-3
 
 
 class Err(NamedTuple):
-    max: float        # max true relative error over the values above the floor
-    rms: float        # RMS of the same
-    n: int            # values above the floor
-    below: int        # values at or below the floor (near-black), not in max / rms
-    below_abs: float  # max |got - ref| over those
-    below_ok: bool    # below_abs <= REL_TOL * floor of each group
-    floor: float      # the radiance (or single-group) floor
-    floor_a: float    # the alpha floor (RGBA data), else 0
+    max: float          # max true relative error over the values above the floor
+    rms: float          # RMS of the same
+    n: int              # values above the floor
+    below: int          # values at or below the floor (near-black), not in max / rms
+    below_abs: float    # max |got - ref| over those
+    below_ratio: float  # max over the groups of (max |got - ref| below the group's floor) / that floor
+    floor: float        # the radiance (or single-group) floor
+    floor_a: float      # the alpha floor (RGBA data), else 0
 
     def ok(self, tol=REL_TOL):
-        return self.max < tol and self.below_ok
+        """Every value above its floor within tol relative, every value below it within tol times the floor."""
+        return self.max < tol and self.below_ratio <= tol
+
+    @property
+    def below_ok(self):
+        return self.below_ratio <= REL_TOL
 
     def __str__(self):
         return ("max %.3e rms %.3e over %d values; %d near-black (floor %.2e%s) max abs %.2e"
@@ -45,13 +50,13 @@ def group_floor(ref, frac=FLOOR_FRAC):
     return float(frac * np.percentile(nz, 99)) if nz.size else 0.0
 
 
-def rel_err(got, ref, frac=FLOOR_FRAC, tol=REL_TOL):
+def rel_err(got, ref, frac=FLOOR_FRAC):
     got = np.asarray(got, dtype=np.float64)
     ref = np.asarray(ref, dtype=np.float64)
     assert got.shape == ref.shape, (got.shape, ref.shape)
     groups = [(got[..., :3], ref[..., :3]), (got[..., 3], ref[..., 3])] if ref.shape and ref.shape[-1] == 4 \
         else [(got, ref)]
-    errs, n, below, below_abs, below_ok, floors = [], 0, 0, 0.0, True, []
+    errs, n, below, below_abs, below_ratio, floors = [], 0, 0, 0.0, 0.0, []
     for g, r in groups:
         fl = group_floor(r, frac)
         floors.append(fl)
@@ -64,7 +69,8 @@ def rel_err(got, ref, frac=FLOOR_FRAC, tol=REL_TOL):
         below += int(b.size)
         if b.size:
             below_abs = max(below_abs, float(b.max()))
-            below_ok = below_ok and float(b.max()) <= tol * max(fl, 0.0)
+            if float(b.max()) > 0.0:
+                below_ratio = max(below_ratio, float(b.max()) / fl if fl > 0.0 else float("inf"))
     e = np.concatenate(errs) if errs else np.zeros(0)
     return Err(float(e.max()) if e.size else 0.0, float(np.sqrt(np.mean(e ** 2))) if e.size else 0.0, n, below,
-               below_abs, below_ok, floors[0], floors[1] if len(floors) > 1 else 0.0)
+               below_abs, below_ratio, floors[0], floors[1] if len(floors) > 1 else 0.0)

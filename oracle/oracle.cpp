@@ -759,35 +759,151 @@ void cone(const Chain<T>& ch, Vec3<T> o, Vec3<T> dir, T tan_half, const f184gi_c
     out[3] = alpha;
 }
 
-// Float-float depth rows of the FP32 path (the device's sequence, every operation rounded on its own): Knuth's
-// two-sum and the FMA two-product are exact, so a row of the inverse projection split into FP32 pairs evaluates to
-// ~2^-46 of its largest term; then 1 / w and z / w with one Newton correction each.
+// The FP32 path's pixel set-up and cone march, in the device's sequence (every operation rounded on its own).
+// Set-up in float-float (Knuth's two-sum and the FMA two-product are exact): the cone origin in voxel units to
+// ~1e-9 voxel, split into an integer voxel oi and an offset of.  The march keeps the sample point as oi + x with x
+// small, and forms each level coordinate as (oi 2^-l - 0.5) split exactly into integer + fraction, plus x 2^-l:
+// the tap weights then carry the precision of x, not of the grid-sized coordinate.
+struct FF32 {
+    float h, l;
+};
 inline void ff_two_sum(float a, float b, float& s, float& e) {
     s = a + b;
     const float bb = s - a;
     e = (a - (s - bb)) + (b - bb);
 }
-inline void ff_row(const float* hi, const float* lo, float x, float y, float z, float& rh, float& rl) {
-    const float p0 = hi[0] * x, p1 = hi[1] * y, p2 = hi[2] * z;
-    const float e0 = std::fma(hi[0], x, -p0), e1 = std::fma(hi[1], y, -p1), e2 = std::fma(hi[2], z, -p2);
-    float s0, s1, s2, t0, t1, t2;
-    ff_two_sum(p0, p1, s0, t0);
-    ff_two_sum(s0, p2, s1, t1);
-    ff_two_sum(s1, hi[3], s2, t2);
-    const float small = (((t0 + t1) + t2) + ((e0 + e1) + e2)) + ((lo[0] * x + lo[1] * y) + (lo[2] * z + lo[3]));
-    rh = s2 + small;
-    rl = small - (rh - s2);
+inline FF32 ff_norm(float s, float e) {
+    const float h = s + e;
+    return FF32{h, e - (h - s)};
 }
-inline void ff_depth_zw(const float* hi, const float* lo, float nx, float ny, float d, float& rw, float& z) {
-    float zh, zl, wh, wl;
-    ff_row(hi, lo, nx, ny, d, zh, zl);
-    ff_row(hi + 4, lo + 4, nx, ny, d, wh, wl);
-    const float r = 1.0f / wh;
-    const float e = std::fma(-r, wl, std::fma(-r, wh, 1.0f));
-    rw = std::fma(r, e, r);
-    const float q = zh * rw;
-    const float qe = std::fma(-q, wh, zh) + std::fma(-q, wl, zl);
-    z = std::fma(qe, rw, q);
+inline FF32 ff_add(FF32 a, FF32 b) {
+    float s, e;
+    ff_two_sum(a.h, b.h, s, e);
+    return ff_norm(s, e + (a.l + b.l));
+}
+inline FF32 ff_mul(FF32 a, FF32 b) {
+    const float p = a.h * b.h;
+    const float e = std::fma(a.h, b.l, std::fma(a.l, b.h, std::fma(a.h, b.h, -p)));
+    return ff_norm(p, e);
+}
+inline FF32 ff_div(FF32 a, FF32 b) {
+    const float q = a.h / b.h;
+    const FF32 r = ff_add(a, ff_mul(FF32{-q, 0.0f}, b));
+    return ff_norm(q, r.h / b.h);
+}
+inline FF32 ff_row(const float* h, const float* l, FF32 x, FF32 y, FF32 z) {
+    FF32 s = ff_add(ff_mul(FF32{h[0], l[0]}, x), ff_mul(FF32{h[1], l[1]}, y));
+    s = ff_add(s, ff_mul(FF32{h[2], l[2]}, z));
+    return ff_add(s, FF32{h[3], l[3]});
+}
+inline FF32 ff_ndc(uint32_t k, uint32_t n) {
+    const float num = float(2u * k + 1u), den = float(n);
+    const float q = num / den;
+    const float ql = std::fma(-q, den, num) / den;
+    return ff_add(FF32{q, ql}, FF32{-1.0f, 0.0f});
+}
+
+// 8-tap sample of one volume of level l at oi + x, added to out scaled by `scale`
+void tri_sample_rel(const float* vol, int64_t d, uint32_t l, const float oi[3], const float x[3], float scale,
+                    float out[4]) {
+    const float s = std::ldexp(1.0f, -int(l));
+    int64_t i0[3];
+    float f[3];
+    for (int a = 0; a < 3; ++a) {
+        const float A = std::fma(oi[a], s, -0.5f);
+        const float Ai = std::floor(A);
+        const float v = std::fma(x[a], s, A - Ai);
+        const float fl = std::floor(v);
+        i0[a] = int64_t(Ai + fl);
+        f[a] = v - fl;
+    }
+    for (int dz = 0; dz < 2; ++dz) {
+        const int64_t z = i0[2] + dz;
+        if (z < 0 || z >= d) continue;
+        const float wz = (dz ? f[2] : 1.0f - f[2]) * scale;
+        for (int dy = 0; dy < 2; ++dy) {
+            const int64_t y = i0[1] + dy;
+            if (y < 0 || y >= d) continue;
+            const float wyz = (dy ? f[1] : 1.0f - f[1]) * wz;
+            for (int dx = 0; dx < 2; ++dx) {
+                const int64_t xx = i0[0] + dx;
+                if (xx < 0 || xx >= d) continue;
+                const float w = (dx ? f[0] : 1.0f - f[0]) * wyz;
+                const float* v = vol + (((uint64_t(z) * d) + uint64_t(y)) * d + uint64_t(xx)) * 4;
+                for (int c = 0; c < 4; ++c) out[c] = std::fma(w, v[c], out[c]);
+            }
+        }
+    }
+}
+
+void level_sample_rel(const Chain<float>& ch, uint32_t l, const float oi[3], const float x[3], Vec3<float> dir,
+                      float scale, float out[4]) {
+    const int64_t d = ch.dim >> l;
+    if (!ch.aniso || l == 0) {
+        tri_sample_rel(ch.base + ch.off[l], d, l, oi, x, scale, out);
+        return;
+    }
+    const uint64_t vol = uint64_t(d) * d * d * 4;
+    const float w[3] = {dir.x * dir.x * scale, dir.y * dir.y * scale, dir.z * dir.z * scale};
+    const int sel[3] = {dir.x >= 0.0f ? 0 : 1, dir.y >= 0.0f ? 2 : 3, dir.z >= 0.0f ? 4 : 5};
+    for (int a = 0; a < 3; ++a) {
+        float sa[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+        tri_sample_rel(ch.base + ch.off[l] + vol * sel[a], d, l, oi, x, 1.0f, sa);
+        for (int c = 0; c < 4; ++c) out[c] = std::fma(w[a], sa[c], out[c]);
+    }
+}
+
+// The FP32 cone from the split origin oi + of (the device's march): quadrilinear as (1 - f) level l0 + f level l0+1
+// with the level weights folded into the tap weights; distance t + tl advanced with error-free sums.
+void cone_rel(const Chain<float>& ch, const float oi[3], const float of[3], Vec3<float> dir, float tan_half,
+              const f184gi_cone_params& p, float tmax, float out[4], uint64_t* cnt) {
+    float c[3] = {0.0f, 0.0f, 0.0f}, alpha = 0.0f;
+    float t = p.start_offset, tl = 0.0f;
+    const float dimf = float(ch.dim), maxl = float(ch.levels - 1), d2 = 2.0f * tan_half;
+    const float dv[3] = {dir.x, dir.y, dir.z};
+    while (t < tmax || (t == tmax && tl <= 0.0f)) {
+        const float diam = std::max(1.0f, std::fma(d2, t, d2 * tl));
+        const float lvl = std::min(std::max(std::log2(diam), 0.0f), maxl);
+        float x[3];
+        bool outside = false;
+        const float m = 2.0f * diam;
+        for (int a = 0; a < 3; ++a) {
+            x[a] = std::fma(dv[a], t, std::fma(dv[a], tl, of[a]));
+            const float xa = oi[a] + x[a];
+            outside = outside || xa < -m || xa > dimf + m;
+        }
+        if (outside) break;
+        const float fl = std::floor(lvl);
+        const uint32_t l0 = uint32_t(fl);
+        const float f = lvl - fl;
+        const bool two = f > 0.0f && l0 + 1 < ch.levels;
+        if (cnt) {
+            cnt[0] += 1;
+            cnt[1] += two ? 2 : 1;
+        }
+        float s[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+        level_sample_rel(ch, l0, oi, x, dir, two ? 1.0f - f : 1.0f, s);
+        if (two) level_sample_rel(ch, l0 + 1, oi, x, dir, f, s);
+        const float tr = 1.0f - alpha;
+        for (int k = 0; k < 3; ++k) c[k] += tr * s[k];
+        alpha += tr * s[3];
+        if (alpha >= p.alpha_stop) break;
+        const float step = p.step_factor * diam;
+        const float ts = t + step, tb = ts - t;
+        tl += (t - (ts - tb)) + (step - tb);
+        t = ts;
+    }
+    out[0] = c[0], out[1] = c[1], out[2] = c[2], out[3] = alpha;
+}
+
+// FP64: the definition (cone from the origin o); FP32: the device's march from the split origin
+inline void trace_cone(const Chain<double>& ch, const float*, const float*, Vec3<double> o, Vec3<double> dir,
+                       double tan_half, const f184gi_cone_params& p, double tmax, double out[4], uint64_t* cnt) {
+    cone(ch, o, dir, tan_half, p, tmax, out, cnt);
+}
+inline void trace_cone(const Chain<float>& ch, const float* oi, const float* of, Vec3<float>, Vec3<float> dir,
+                       float tan_half, const f184gi_cone_params& p, float tmax, float out[4], uint64_t* cnt) {
+    cone_rel(ch, oi, of, dir, tan_half, p, tmax, out, cnt);
 }
 
 template <class T>
@@ -809,11 +925,13 @@ int trace_impl(const f184gi_grid_frame* frame, uint32_t dim, uint32_t levels, ui
         iv[i] = T(IV[i]);
         ip[i] = T(IP[i]);
     }
-    float zw_hi[8], zw_lo[8];  // the FP32 path's depth rows: rows 2 and 3 of IP split into FP32 pairs
-    for (int k = 0; k < 8; ++k) {
-        zw_hi[k] = float(IP[8 + k]);
-        zw_lo[k] = float(IP[8 + k] - double(zw_hi[k]));
-    }
+    // the FP32 path's float-float set-up: IP, IV (rows 0..2), the grid origin and scale as FP32 pairs
+    float ip_h[16], ip_l[16], iv_h[12], iv_l[12], org_h[3], org_l[3];
+    for (int k = 0; k < 16; ++k) ip_h[k] = float(IP[k]), ip_l[k] = float(IP[k] - double(ip_h[k]));
+    for (int k = 0; k < 12; ++k) iv_h[k] = float(IV[k]), iv_l[k] = float(IV[k] - double(iv_h[k]));
+    for (int a = 0; a < 3; ++a) org_h[a] = float(frame->origin[a]), org_l[a] = float(frame->origin[a] - double(org_h[a]));
+    const double ivs_d = frame->inv_voxel_fixed * (1.0 / 256.0);
+    const float ivs_h = float(ivs_d), ivs_l = float(ivs_d - double(ivs_h));
     Chain<T> ch = make_chain(chain, dim, levels, aniso != 0);
     const T vs = T(frame->voxel_size);
     const T inv_vs = T(1.0 / frame->voxel_size);
@@ -845,11 +963,17 @@ int trace_impl(const f184gi_grid_frame* frame, uint32_t dim, uint32_t levels, ui
                 T vp[4];
                 for (int r = 0; r < 4; ++r) vp[r] = ip[r * 4 + 0] * nx + ip[r * 4 + 1] * ny + ip[r * 4 + 2] * nz + ip[r * 4 + 3];
                 Vec3<T> cs{vp[0] / vp[3], vp[1] / vp[3], vp[2] / vp[3]};
+                float oi[3] = {0, 0, 0}, of[3] = {0, 0, 0};  // FP32 path: the split cone origin
+                FF32 wpf[3] = {};
                 if (std::is_same<T, float>::value) {
-                    // the device arithmetic: the projective rows (z, w) as float-float pairs, x and y in FP32
-                    float rw, z;
-                    ff_depth_zw(zw_hi, zw_lo, float(nx), float(ny), float(nz), rw, z);
-                    cs = Vec3<T>{vp[0] * T(rw), vp[1] * T(rw), T(z)};
+                    // the device arithmetic: position in float-float
+                    const FF32 ndx = ff_ndc(px, W), ndy = ff_ndc(uint32_t(py), H), dzf = FF32{dd, 0.0f};
+                    const FF32 vwf = ff_row(ip_h + 12, ip_l + 12, ndx, ndy, dzf);
+                    const FF32 cxf = ff_div(ff_row(ip_h, ip_l, ndx, ndy, dzf), vwf);
+                    const FF32 cyf = ff_div(ff_row(ip_h + 4, ip_l + 4, ndx, ndy, dzf), vwf);
+                    const FF32 czf = ff_div(ff_row(ip_h + 8, ip_l + 8, ndx, ndy, dzf), vwf);
+                    for (int r = 0; r < 3; ++r) wpf[r] = ff_row(iv_h + 4 * r, iv_l + 4 * r, cxf, cyf, czf);
+                    cs = Vec3<T>{T(cxf.h), T(cyf.h), T(czf.h)};
                 }
                 Vec3<T> wp{iv[0] * cs.x + iv[1] * cs.y + iv[2] * cs.z + iv[3],
                            iv[4] * cs.x + iv[5] * cs.y + iv[6] * cs.z + iv[7],
@@ -859,25 +983,36 @@ int trace_impl(const f184gi_grid_frame* frame, uint32_t dim, uint32_t levels, ui
                                            iv[4] * nv.x + iv[5] * nv.y + iv[6] * nv.z,
                                            iv[8] * nv.x + iv[9] * nv.y + iv[10] * nv.z});
                 T r = T(h2f(rough[pi]));
+                if (std::is_same<T, float>::value) wp = Vec3<T>{T(wpf[0].h), T(wpf[1].h), T(wpf[2].h)};
                 Vec3<T> pv = vmul(vsub(wp, org), inv_vs);
                 Vec3<T> o = vadd(pv, vmul(nw, T(p.start_offset)));
+                if (std::is_same<T, float>::value) {
+                    const float na[3] = {float(nw.x), float(nw.y), float(nw.z)};
+                    for (int a = 0; a < 3; ++a) {
+                        const FF32 pf = ff_mul(ff_add(wpf[a], FF32{-org_h[a], -org_l[a]}), FF32{ivs_h, ivs_l});
+                        const float q = na[a] * p.start_offset;
+                        const FF32 of2 = ff_add(pf, FF32{q, std::fma(na[a], p.start_offset, -q)});
+                        oi[a] = std::floor(of2.h);
+                        of[a] = (of2.h - oi[a]) + of2.l;
+                    }
+                }
                 Vec3<T> bx, by, bz;
                 make_coord_space(nw, bx, by, bz);
                 T acc[4] = {T(0), T(0), T(0), T(0)};
                 if (p.diffuse_cones >= 5) {
                     T c0[4];
-                    cone(ch, o, bz, T(p.diffuse_tan_half), p, tmax, c0, cnt);
+                    trace_cone(ch, oi, of, o, bz, T(p.diffuse_tan_half), p, tmax, c0, cnt);
                     for (int k = 0; k < 4; ++k) acc[k] += T(0.25) * c0[k];
                     const T cphi[4] = {T(1), T(0), T(-1), T(0)}, sphi[4] = {T(0), T(1), T(0), T(-1)};
                     for (int s = 0; s < 4; ++s) {
                         Vec3<T> side = vadd(vmul(bx, cphi[s]), vmul(by, sphi[s]));
                         Vec3<T> d = vnorm(vadd(vmul(bz, ct), vmul(side, st)));
                         T cs4[4];
-                        cone(ch, o, d, T(p.diffuse_tan_half), p, tmax, cs4, cnt);
+                        trace_cone(ch, oi, of, o, d, T(p.diffuse_tan_half), p, tmax, cs4, cnt);
                         for (int k = 0; k < 4; ++k) acc[k] += T(0.1875) * cs4[k];
                     }
                 } else {
-                    cone(ch, o, bz, T(p.diffuse_tan_half), p, tmax, acc, cnt);
+                    trace_cone(ch, oi, of, o, bz, T(p.diffuse_tan_half), p, tmax, acc, cnt);
                 }
                 for (int k = 0; k < 4; ++k) od[k] = acc[k];
                 if (p.specular) {
@@ -886,7 +1021,7 @@ int trace_impl(const f184gi_grid_frame* frame, uint32_t dim, uint32_t levels, ui
                     Vec3<T> rd = vnorm(vsub(vdir, vmul(nw, T(2) * dn)));
                     T th = std::max(r, T(p.min_spec_tan_half));
                     T sc[4];
-                    cone(ch, o, rd, th, p, tmax, sc, cnt);
+                    trace_cone(ch, oi, of, o, rd, th, p, tmax, sc, cnt);
                     for (int k = 0; k < 4; ++k) os[k] = sc[k];
                 }
             }

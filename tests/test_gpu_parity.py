@@ -79,7 +79,7 @@ def test_mip_chain(case, orc):
     for lv in range(1, case.levels):
         got = case.gi.read_level(case.grid, lv)
         e = rel_err(got, levels[lv])
-        assert e.max < 1e-5 and e.below_ok, "level %d: %s" % (lv, e)
+        assert e.ok(1e-5), "level %d: %s" % (lv, e)
 
 
 def test_gbuffer_bit_exact(case, orc):
@@ -191,7 +191,7 @@ def test_anisotropic_chain_and_trace(lib, orc, fmt):
         for d in range(6):
             got = c.gi.read_level(c.grid, lv, direction=d)
             e = rel_err(got, levels[lv][d])
-            assert e.max < tol and e.below_ok, "level %d direction %d: %s" % (lv, d, e)
+            assert e.ok(tol), "level %d direction %d: %s" % (lv, d, e)
     got = c.trace()
     fo = c.oracle_frame()
     sd = orc.shadow_depth(orc.raster(orc.frame_matrix(fo), c.res, c.res, c.sc.tri_xyz))
