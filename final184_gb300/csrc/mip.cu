@@ -93,9 +93,11 @@ __global__ void __launch_bounds__(512) mip_pass(ChainLayout c, uint32_t src, uin
             mbar_expect_tx(&bar, bytes);
             bulk_g2s(smem, gsrc, bytes, &bar);
         }
-        if (!mbar_wait_bounded(&bar, 0, kWaitPolls)) {
-            if (threadIdx.x == 0) set_status(status, kStatusTimeout | kStatusCopyTimeout);
-            mbar_wait_bounded(&bar, 0, kWaitPolls);  // let the copy land before the CTA exits
+        if (__syncthreads_or(!mbar_wait_bounded(&bar, 0, kWaitPolls))) {  // one branch for the whole CTA
+            if (threadIdx.x == 0) {
+                set_status(status, kStatusTimeout | kStatusCopyTimeout);
+                mbar_wait_bounded(&bar, 0, kWaitPolls);  // let the copy land before the CTA exits (bounded)
+            }
             return;
         }
     } else {  // S rows of S x S from the ringed linear level: element e of row (y, z) -> smem (z S + y) S + e
@@ -151,6 +153,100 @@ __global__ void __launch_bounds__(512) mip_pass(ChainLayout c, uint32_t src, uin
     }
 }
 
+// Isotropic chains, level 0 -> levels 1 .. nout (<= 4), as a stream: one persistent CTA per SM walks the 16^3
+// blocks (b = blockIdx.x, += gridDim.x) through a ring of kStages shared-memory buffers, each filled by one bulk
+// copy (cp.async.bulk, completion on the buffer's mbarrier).  The copies of the next kStages - 1 blocks are in
+// flight while the CTA reduces the current one, so the SM keeps ~2 blocks (128 KB of FP32) of reads outstanding
+// instead of none between a block's load and its reduction.  The reductions are mip_pass's, in its order, so the
+// bytes are the same.  If a wait expires the CTA records kStatusCopyTimeout, waits (bounded) for every copy it
+// still has in flight, and returns.
+constexpr uint32_t kStages = 3;
+constexpr uint32_t kStageBytes = 4096u * 16u;  // one 16^3 block of FP32 voxels (FP16 blocks use half)
+
+__global__ void __launch_bounds__(512, 1) mip_l0_stream(ChainLayout c, uint32_t nout, uint32_t nblocks,
+                                                       uint32_t* status) {
+    extern __shared__ __align__(128) unsigned char smem[];  // kStages x kStageBytes
+    __shared__ float4 lvl[2][512];
+    __shared__ __align__(8) uint64_t bar[kStages];
+    const uint32_t t = threadIdx.x;
+    const uint32_t bytes = 4096u * c.esz;
+    const unsigned char* gbase = static_cast<const unsigned char*>(c.base) + c.off[0] * c.esz;
+    if (t == 0) {
+        for (uint32_t k = 0; k < kStages; ++k) mbar_init(&bar[k], 1);
+        fence_barrier_init();
+    }
+    __syncthreads();
+    uint32_t pending = 0;  // bit k: a copy into stage k is in flight (thread 0's view)
+    if (t == 0) {
+        for (uint32_t k = 0; k < kStages; ++k) {
+            const uint32_t blk = blockIdx.x + k * gridDim.x;
+            if (blk >= nblocks) break;
+            mbar_expect_tx(&bar[k], bytes);
+            bulk_g2s(smem + k * kStageBytes, gbase + uint64_t(blk) * bytes, bytes, &bar[k]);
+            pending |= 1u << k;
+        }
+    }
+    const uint32_t d1 = c.ldim[1];
+    for (uint32_t i = 0;; ++i) {
+        const uint32_t blk = blockIdx.x + i * gridDim.x;
+        if (blk >= nblocks) break;
+        const uint32_t st = i % kStages;
+        const uint32_t parity = (i / kStages) & 1u;
+        // every thread waits (bounded); the CTA then takes one branch (a vote), so no barrier below is missed
+        if (__syncthreads_or(!mbar_wait_bounded(&bar[st], parity, kWaitPolls))) {
+            if (t == 0) {
+                set_status(status, kStatusTimeout | kStatusCopyTimeout);
+                // let every copy still in flight land before the CTA exits (each wait bounded)
+                for (uint32_t k = 0; k < kStages; ++k) {
+                    if (!((pending >> k) & 1u)) continue;
+                    const uint32_t uses = (k < st) ? (i / kStages) + 1u : (i / kStages);  // waits done on stage k
+                    mbar_wait_bounded(&bar[k], uses & 1u, kWaitPolls);
+                }
+            }
+            return;
+        }
+        if (t == 0) pending &= ~(1u << st);
+        const unsigned char* src = smem + st * kStageBytes;
+        const uint32_t Bx = compact1by2(blk), By = compact1by2(blk >> 1), Bz = compact1by2(blk >> 2);
+        {  // level 1 from the staged block (512 outputs, one per thread)
+            const uint32_t x = t % 8u, y = (t / 8u) % 8u, z = t / 64u;
+            const float4 acc = reduce8<false>(0u, [&](int dx, int dy, int dz) {
+                const uint32_t sx = 2 * x + dx, sy = 2 * y + dy, sz = 2 * z + dz;
+                const uint32_t cb = ((sx >> 3) & 1u) | (((sy >> 3) & 1u) << 1) | (((sz >> 3) & 1u) << 2);
+                return raw_vox(src, c.format, cb * 512u + ((sz & 7u) << 6) + ((sy & 7u) << 3) + (sx & 7u));
+            });
+            lvl[0][t] = acc;
+            store_vox(c.base, c.format, c.off[1] + vox_index(1, d1, Bx * 8 + x, By * 8 + y, Bz * 8 + z), acc);
+        }
+        __syncthreads();  // the stage is read: refill it with the block kStages ahead
+        if (t == 0) {
+            const uint32_t nb = blk + kStages * gridDim.x;
+            if (nb < nblocks) {
+                mbar_expect_tx(&bar[st], bytes);
+                bulk_g2s(smem + st * kStageBytes, gbase + uint64_t(nb) * bytes, bytes, &bar[st]);
+                pending |= 1u << st;
+            }
+        }
+        int cur = 0;
+        uint32_t n = 8;
+        for (uint32_t k = 2; k <= nout; ++k) {
+            const uint32_t np = n;
+            n = n / 2;
+            if (t < n * n * n) {
+                const uint32_t x = t % n, y = (t / n) % n, z = t / (n * n);
+                const float4 acc = reduce8<false>(0u, [&](int dx, int dy, int dz) {
+                    return lvl[cur][((2 * z + dz) * np + (2 * y + dy)) * np + (2 * x + dx)];
+                });
+                lvl[cur ^ 1][t] = acc;
+                store_vox(c.base, c.format,
+                          c.off[k] + vox_index(k, c.ldim[k], Bx * n + x, By * n + y, Bz * n + z), acc);
+            }
+            __syncthreads();
+            cur ^= 1;
+        }
+    }
+}
+
 // Anisotropic chains, level 0 -> levels 1 .. nout: level 0 has one volume, so one CTA per 16^3 block stages it
 // once (bulk copy) and reduces it along all six directions (six CTAs of mip_pass per block would each stage it);
 // each thread keeps its voxel's six level-1 results, which then replace the staged block in shared memory as the
@@ -173,9 +269,11 @@ __global__ void __launch_bounds__(512, 2) mip_aniso_l0(ChainLayout c, uint32_t n
         mbar_expect_tx(&bar, bytes);
         bulk_g2s(smem, gsrc, bytes, &bar);
     }
-    if (!mbar_wait_bounded(&bar, 0, kWaitPolls)) {
-        if (threadIdx.x == 0) set_status(status, kStatusTimeout | kStatusCopyTimeout);
-        mbar_wait_bounded(&bar, 0, kWaitPolls);  // let the copy land before the CTA exits
+    if (__syncthreads_or(!mbar_wait_bounded(&bar, 0, kWaitPolls))) {  // one branch for the whole CTA
+        if (threadIdx.x == 0) {
+            set_status(status, kStatusTimeout | kStatusCopyTimeout);
+            mbar_wait_bounded(&bar, 0, kWaitPolls);  // let the copy land before the CTA exits (bounded)
+        }
         return;
     }
     const uint32_t t = threadIdx.x;
@@ -224,6 +322,13 @@ __global__ void __launch_bounds__(512, 2) mip_aniso_l0(ChainLayout c, uint32_t n
     }
 }
 
+uint32_t sm_count_current() {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    return uint32_t(sms > 0 ? sms : 1);
+}
+
 }  // namespace
 
 int mip_launch(const ChainLayout& c, uint32_t levels, uint32_t* d_status, cudaStream_t s) {
@@ -235,6 +340,9 @@ int mip_launch(const ChainLayout& c, uint32_t levels, uint32_t* d_status, cudaSt
             e = cudaFuncSetAttribute(mip_pass<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 4096 * 16);
         if (e == cudaSuccess)
             e = cudaFuncSetAttribute(mip_aniso_l0, cudaFuncAttributeMaxDynamicSharedMemorySize, 4096 * 16);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(mip_l0_stream, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     int(kStages * kStageBytes));
         if (e != cudaSuccess) return cuda_fail(e, "mip: smem attribute");
         attr_set = true;
     }
@@ -250,6 +358,9 @@ int mip_launch(const ChainLayout& c, uint32_t levels, uint32_t* d_status, cudaSt
         size_t smem = size_t(S) * S * S * c.esz;
         if (c.aniso && l == 0 && ds >= 16)  // one CTA per block for all six directions
             mip_aniso_l0<<<blocks / 6, 512, std::max<size_t>(smem, 6 * 512 * 16), s>>>(c, nout, d_status);
+        else if (!c.aniso && l == 0 && ds >= 16)  // the level-0 stream: one persistent CTA per SM
+            mip_l0_stream<<<std::min(blocks, sm_count_current()), 512, kStages * kStageBytes, s>>>(c, nout, blocks,
+                                                                                               d_status);
         else if (c.aniso)
             mip_pass<true><<<blocks, 512, smem, s>>>(c, l, nout, d_status);
         else
