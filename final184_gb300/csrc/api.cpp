@@ -709,7 +709,8 @@ int f184gi_transform(f184gi_ctx* c, const float* obj_xyz, uint64_t ntris, const 
 int f184gi_selftest_bounded_wait(f184gi_ctx* c, uint32_t polls, uint32_t complete, void* stream) {
     if (!c) return fail(F184GI_ERR_INVALID, "selftest_bounded_wait: null context");
     if (polls == 0 || polls > (1u << 24)) return fail(F184GI_ERR_INVALID, "selftest_bounded_wait: polls must be in 1..2^24");
-    return bounded_wait_selftest_launch(polls, complete ? 1u : 0u, c->d_status, static_cast<cudaStream_t>(stream));
+    if (complete > 2) return fail(F184GI_ERR_INVALID, "selftest_bounded_wait: complete must be 0, 1 or 2");
+    return bounded_wait_selftest_launch(polls, complete, c->d_status, static_cast<cudaStream_t>(stream));
 }
 
 int f184gi_sync(f184gi_ctx* c, void* stream) {

@@ -67,24 +67,37 @@ __host__ __device__ __forceinline__ uint64_t vox_index(uint32_t level, uint32_t 
 }
 
 // ---- voxel payload load/store ----
+// FP16 chains (8 B a voxel): R, G, B as binary16 and the opacity as 16-bit unorm, n / 65535.  Opacity is what the
+// cones composite as transmittance factors 1 - a: binary16 keeps 11 bits relative to a, so near a = 1 the factor
+// loses all its precision (a = 0.99 rounds by up to 2.4e-4, 2.4% of 1 - a), while unorm16 keeps 7.6e-6 absolute
+// everywhere.  Measured on the anisotropic test chain with the radiance left exact: max relative pixel error
+// 1.7e-3 with binary16 opacity, 7e-5 with unorm16 (3.3e-4 with binary16 radiance as well).
+constexpr float kUnorm16 = 1.0f / 65535.0f;
+__device__ __forceinline__ uint32_t alpha_to_unorm16(float a) {
+    return __float2uint_rn(fminf(fmaxf(a, 0.0f), 1.0f) * 65535.0f);
+}
+__device__ __forceinline__ float4 decode_f16_vox(uint2 raw) {
+    const float2 rg = __half22float2(*reinterpret_cast<const __half2*>(&raw.x));
+    const float b = __half2float(__ushort_as_half(uint16_t(raw.y & 0xffffu)));
+    return make_float4(rg.x, rg.y, b, float(raw.y >> 16) * kUnorm16);
+}
+__device__ __forceinline__ uint2 encode_f16_vox(float4 v) {
+    const __half2 rg = __floats2half2_rn(v.x, v.y);
+    uint2 raw;
+    raw.x = *reinterpret_cast<const uint32_t*>(&rg);
+    raw.y = uint32_t(__half_as_ushort(__float2half_rn(v.z))) | (alpha_to_unorm16(v.w) << 16);
+    return raw;
+}
 __device__ __forceinline__ float4 load_vox(const void* base, uint32_t format, uint64_t idx) {
     if (format == F184GI_FMT_F32) return __ldg(reinterpret_cast<const float4*>(base) + idx);
-    uint2 raw = __ldg(reinterpret_cast<const uint2*>(base) + idx);
-    __half2 a = *reinterpret_cast<__half2*>(&raw.x);
-    __half2 b = *reinterpret_cast<__half2*>(&raw.y);
-    float2 fa = __half22float2(a), fb = __half22float2(b);
-    return make_float4(fa.x, fa.y, fb.x, fb.y);
+    return decode_f16_vox(__ldg(reinterpret_cast<const uint2*>(base) + idx));
 }
 __device__ __forceinline__ void store_vox(void* base, uint32_t format, uint64_t idx, float4 v) {
     if (format == F184GI_FMT_F32) {
         reinterpret_cast<float4*>(base)[idx] = v;
         return;
     }
-    __half2 a = __floats2half2_rn(v.x, v.y), b = __floats2half2_rn(v.z, v.w);
-    uint2 raw;
-    raw.x = *reinterpret_cast<uint32_t*>(&a);
-    raw.y = *reinterpret_cast<uint32_t*>(&b);
-    reinterpret_cast<uint2*>(base)[idx] = raw;
+    reinterpret_cast<uint2*>(base)[idx] = encode_f16_vox(v);
 }
 
 __device__ __forceinline__ void set_status(uint32_t* st, uint32_t bit) {

@@ -165,12 +165,11 @@ struct TraceVariant {
 constexpr uint32_t kTraceVariantCount = 5;
 constexpr TraceVariant kTraceVariants[kTraceVariantCount] = {
     {16, 8, 4}, {8, 12, 7}, {4, 24, 7}, {8, 16, 5}, {4, 32, 5}};
-// The one-shot launch's variant per chain: isotropic FP32 chains take 96-thread CTAs of 4x8-pixel warp tiles at 7
-// per SM (1.69 ms per 1080p view; 8x4 tiles 1.71, 128-thread CTAs at 5 per SM 1.75); isotropic FP16 chains take
-// 128-thread CTAs of 4x8 tiles at 5 per SM (1.99 ms; 8x4 tiles 2.00); anisotropic chains take 128-thread CTAs of
-// 8x4 tiles at 5 per SM (the 512^3 anisotropic FP16 precision view: 18.9 against 19.5 ms at 7 per SM).
+// The one-shot launch's variant per chain: isotropic chains take 128-thread CTAs of 4x8-pixel warp tiles at 5 per
+// SM (the 96-register budget: FP32 1080p view 1.75 ms, against 1.81-1.85 ms for 96-thread CTAs at 7 per SM, whose
+// 80 registers spill the split-origin march); anisotropic chains take 128-thread CTAs of 8x4 tiles at 5 per SM.
 constexpr uint32_t trace_default_variant(uint32_t fmt, bool aniso) {
-    return aniso ? 3u : (fmt == F184GI_FMT_F32 ? 2u : 4u);
+    return aniso ? 3u : (fmt == F184GI_FMT_F32 ? 4u : 4u);
 }
 const void* trace_kernel_fn(uint32_t fmt, bool aniso, uint32_t variant);
 const void* trace_kernel_count_fn(uint32_t fmt, bool aniso);  // instrumented, default variant's tile shape

@@ -15,10 +15,7 @@ constexpr uint32_t kWaitPolls = 1u << 22;
 
 __device__ __forceinline__ float4 raw_vox(const unsigned char* smem, uint32_t format, uint32_t idx) {
     if (format == F184GI_FMT_F32) return reinterpret_cast<const float4*>(smem)[idx];
-    uint2 raw = reinterpret_cast<const uint2*>(smem)[idx];
-    float2 a = __half22float2(*reinterpret_cast<__half2*>(&raw.x));
-    float2 b = __half22float2(*reinterpret_cast<__half2*>(&raw.y));
-    return make_float4(a.x, a.y, b.x, b.y);
+    return decode_f16_vox(reinterpret_cast<const uint2*>(smem)[idx]);
 }
 
 __device__ __forceinline__ float4 f4add(float4 a, float4 b) { return make_float4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w); }

@@ -77,14 +77,22 @@ template <int FMT>
 __device__ __forceinline__ const unsigned char* vox_ptr(const void* base, uint32_t idx) {
     return static_cast<const unsigned char*>(base) + size_t(idx) * (FMT == F184GI_FMT_F32 ? 16u : 8u);
 }
+// FP16 chains: the opacity comes back as its unorm16 integer n (not n / 65535); the cone scales its opacity sum
+// once per step (kAlphaScale), so a tap costs one conversion per channel as with binary16.
 template <int FMT>
 __device__ __forceinline__ float4 load_vox_at(const unsigned char* p, int k) {
     if (FMT == F184GI_FMT_F32) return __ldg(reinterpret_cast<const float4*>(p) + k);
     const uint2 raw = __ldg(reinterpret_cast<const uint2*>(p) + k);
-    const float2 fa = __half22float2(*reinterpret_cast<const __half2*>(&raw.x));
-    const float2 fb = __half22float2(*reinterpret_cast<const __half2*>(&raw.y));
-    return make_float4(fa.x, fa.y, fb.x, fb.y);
+    const float2 rg = __half22float2(*reinterpret_cast<const __half2*>(&raw.x));
+    const float b = __half2float(__ushort_as_half(uint16_t(raw.y & 0xffffu)));
+    return make_float4(rg.x, rg.y, b, float(raw.y >> 16));
 }
+template <int FMT>
+__device__ __forceinline__ float4 load_vox_raw(const void* base, uint32_t idx) {
+    return load_vox_at<FMT>(static_cast<const unsigned char*>(base) + size_t(idx) * (FMT == F184GI_FMT_F32 ? 16u : 8u), 0);
+}
+template <int FMT>
+constexpr float kAlphaScale = FMT == F184GI_FMT_F32 ? 1.0f : kUnorm16;
 
 // Float-float arithmetic (unevaluated pairs h + l of FP32, ~2^-44 relative) for the pixel set-up, every
 // operation explicitly rounded: Knuth's two-sum and the FMA two-product are exact.  The cone origin in voxel units
@@ -231,7 +239,7 @@ __device__ __forceinline__ void tri_sample(const void* base, int d, uint32_t l, 
                     const uint32_t e = row + (tx ? dx : 0u);
 #pragma unroll
                     for (int k = 0; k < NV; ++k) {
-                        const float4 v = load_vox(base, FMT, vol_off[k] + e);
+                        const float4 v = load_vox_raw<FMT>(base, vol_off[k] + e);
                         fma4(acc[k], w, v);
                     }
                 }
@@ -270,7 +278,7 @@ __device__ __forceinline__ void tri_sample(const void* base, int d, uint32_t l, 
                     const float w = wx[tx] * wyz;
 #pragma unroll
                     for (int k = 0; k < NV; ++k) {
-                        const float4 v = load_vox(base, FMT, vol_off[k] + idx);
+                        const float4 v = load_vox_raw<FMT>(base, vol_off[k] + idx);
                         fma4(acc[k], w, v);
                     }
                 }
@@ -353,6 +361,7 @@ __device__ float4 cone(const GridRef& g, const uint32_t* lut, const TraceConsts&
             level_sample<FMT, ANISO>(g, lut, l0, oi, x, dir, two ? 1.0f - f : 1.0f, s);
             if (two) level_sample<FMT, ANISO>(g, lut, l0 + 1, oi, x, dir, f, s);
         }
+        if (FMT != F184GI_FMT_F32) s.w *= kAlphaScale<FMT>;  // the unorm16 opacity sum, scaled once
         float tr = 1.0f - alpha;
         cr += tr * s.x;
         cg += tr * s.y;

@@ -73,7 +73,8 @@ typedef struct f184gi_light {
 
 /* storage formats of the radiance/opacity grid (RGB = radiance premultiplied by opacity, A = opacity) */
 #define F184GI_FMT_F32 0u /* float4 per voxel, 16 B */
-#define F184GI_FMT_F16 1u /* half4  per voxel,  8 B */
+#define F184GI_FMT_F16 1u /* 8 B per voxel: R, G, B as IEEE binary16 and opacity as 16-bit unorm (n / 65535); as
+                          * a trace output format: half4 */
 #define F184GI_FMT_RG16 2u /* the reference's voxel volume (one level): uint32 per voxel = RGB565 albedo in the low
                             * 16 bits, the 5-6-5 packed normal in the high 16 (main.lua:269-272); for f184gi_march */
 

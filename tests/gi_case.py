@@ -3,7 +3,7 @@
 Tolerance used throughout (oracle/errstats.py): TRUE relative error |gpu - oracle| / |oracle| per value, below
 REL_TOL = 1e-3 over every value above the near-black floor (1e-3 of the 99th percentile of the nonzero |oracle|
 values of its channel group: radiance RGB, opacity A); values at or below the floor are counted and their
-absolute error must stay below REL_TOL times the floor.
+absolute error must stay below twice REL_TOL times the floor (oracle/errstats.py says why).
 """
 import numpy as np
 
