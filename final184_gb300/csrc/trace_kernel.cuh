@@ -322,6 +322,13 @@ __device__ float4 cone(const GridRef& g, const uint32_t* lut, const TraceConsts&
     const float dimf = float(g.dim);
     const float maxl = float(g.levels - 1);
     const float d2 = 2.0f * tan_half;
+    // The exit test (a sample more than 2 diameters outside the grid reads zero, so the cone stops there) can
+    // only fire for a cone that starts outside the grid or outruns the margin: the margin 2 diam = 4 t tan grows
+    // faster than the distance t travelled once tan >= 0.25, so a cone starting inside with tan >= 0.3 (the
+    // diffuse cones' 0.577 and wide specular cones) never meets it and skips it.
+    const float3 o0 = add3(oi, of);
+    const bool exit_test = !(tan_half >= 0.3f && o0.x >= 0.0f && o0.y >= 0.0f && o0.z >= 0.0f && o0.x <= dimf &&
+                             o0.y <= dimf && o0.z <= dimf);
     for (uint32_t k = 0;; ++k) {
         float diam, lraw;
         if (k < ns) {
@@ -337,9 +344,11 @@ __device__ float4 cone(const GridRef& g, const uint32_t* lut, const TraceConsts&
         // the weights of a grazing cone are most sensitive)
         float3 x = f3(fmaf(dir.x, t, fmaf(dir.x, tl, of.x)), fmaf(dir.y, t, fmaf(dir.y, tl, of.y)),
                       fmaf(dir.z, t, fmaf(dir.z, tl, of.z)));
-        float m = 2.0f * diam;
-        const float3 xa = add3(oi, x);  // for the exit test only: samples out there read zero
-        if (xa.x < -m || xa.y < -m || xa.z < -m || xa.x > dimf + m || xa.y > dimf + m || xa.z > dimf + m) break;
+        if (exit_test) {
+            const float m = 2.0f * diam;
+            const float3 xa = add3(oi, x);
+            if (xa.x < -m || xa.y < -m || xa.z < -m || xa.x > dimf + m || xa.y > dimf + m || xa.z > dimf + m) break;
+        }
         float fl = floorf(lvl);
         uint32_t l0 = uint32_t(fl);
         float f = lvl - fl;
