@@ -288,7 +288,7 @@ int f184gi_destroy(f184gi_ctx* c) {
         dev_free(c, g.shadow, g.shadow_bytes);
         dev_free(c, g.counts, g.counts_bytes);
         dev_free(c, g.weights, g.weights_bytes);
-        dev_free(c, g.d_frame, sizeof(f184gi_grid_frame));
+        dev_free(c, g.d_frame, kFrameAllocBytes);
     }
     for (Scratch* s : {&c->raster, &c->vox, &c->trace, &c->misc, &c->keys, &c->counts}) dev_free(c, s->ptr, s->bytes);
     trace_staging_destroy(c->trace_stage);
@@ -311,7 +311,7 @@ int f184gi_grid_bytes(const f184gi_grid_desc* d, uint64_t* bytes) {
     if (rc) return rc;
     if (!bytes) return fail(F184GI_ERR_INVALID, "grid_bytes: null output");
     uint64_t esz = format_bytes(d->format);
-    uint64_t b = chain_elems(*d) * esz + uint64_t(d->shadow_res) * d->shadow_res * 8 + sizeof(f184gi_grid_frame);
+    uint64_t b = chain_elems(*d) * esz + uint64_t(d->shadow_res) * d->shadow_res * 8 + kFrameAllocBytes;
     if (d->flags & F184GI_GRID_KEEP_COUNTS) b += uint64_t(d->dim) * d->dim * d->dim * 4;
     if (d->flags & F184GI_GRID_RESIDENT_WEIGHTS) b += uint64_t(d->dim) * d->dim * d->dim * 16;
     *bytes = b;
@@ -338,7 +338,7 @@ int f184gi_grid_create(f184gi_ctx* c, const f184gi_grid_desc* d, uint32_t* grid)
     }
     g.shadow = static_cast<unsigned long long*>(sh);
     void* fr = nullptr;
-    if ((rc = dev_alloc(c, &fr, sizeof(f184gi_grid_frame)))) {
+    if ((rc = dev_alloc(c, &fr, kFrameAllocBytes))) {
         dev_free(c, base, g.chain_bytes);
         dev_free(c, sh, g.shadow_bytes);
         return rc;
@@ -350,7 +350,7 @@ int f184gi_grid_create(f184gi_ctx* c, const f184gi_grid_desc* d, uint32_t* grid)
         if ((rc = dev_alloc(c, &cp, g.counts_bytes))) {
             dev_free(c, base, g.chain_bytes);
             dev_free(c, sh, g.shadow_bytes);
-            dev_free(c, fr, sizeof(f184gi_grid_frame));
+            dev_free(c, fr, kFrameAllocBytes);
             return rc;
         }
         g.counts = static_cast<uint32_t*>(cp);
@@ -362,7 +362,7 @@ int f184gi_grid_create(f184gi_ctx* c, const f184gi_grid_desc* d, uint32_t* grid)
         if ((rc = dev_alloc(c, &wp, g.weights_bytes))) {
             dev_free(c, base, g.chain_bytes);
             dev_free(c, sh, g.shadow_bytes);
-            dev_free(c, fr, sizeof(f184gi_grid_frame));
+            dev_free(c, fr, kFrameAllocBytes);
             dev_free(c, g.counts, g.counts_bytes);
             return rc;
         }
@@ -370,7 +370,7 @@ int f184gi_grid_create(f184gi_ctx* c, const f184gi_grid_desc* d, uint32_t* grid)
         cudaMemset(g.weights, 0, g.weights_bytes);
     }
     cudaMemset(base, 0, g.chain_bytes);
-    cudaMemset(fr, 0, sizeof(f184gi_grid_frame));
+    cudaMemset(fr, 0, kFrameAllocBytes);
     uint32_t id = c->next_id++;
     c->grids[id] = g;
     *grid = id;
@@ -386,7 +386,7 @@ int f184gi_grid_destroy(f184gi_ctx* c, uint32_t grid) {
     dev_free(c, g->shadow, g->shadow_bytes);
     dev_free(c, g->counts, g->counts_bytes);
     dev_free(c, g->weights, g->weights_bytes);
-    dev_free(c, g->d_frame, sizeof(f184gi_grid_frame));
+    dev_free(c, g->d_frame, kFrameAllocBytes);
     c->grids.erase(grid);
     return F184GI_OK;
 }

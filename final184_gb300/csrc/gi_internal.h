@@ -37,6 +37,18 @@ int fail(int code, const std::string& msg);
 int cuda_fail(cudaError_t e, const char* what);
 bool invert4(const double* m, double* inv);
 
+// The world -> L0 voxel map of a grid as FP32 pairs (h + l): p_voxel = (p - origin) * inv_vs.  Kept on the device
+// right after the grid's frame (the frame kernel writes both), so the per-pixel trace reads floats only and runs
+// no FP64.
+struct FramePairs {
+    float org_h[3], org_l[3];
+    float ivs_h, ivs_l;
+};
+constexpr size_t kFrameAllocBytes = sizeof(f184gi_grid_frame) + sizeof(FramePairs);
+inline const FramePairs* frame_pairs(const f184gi_grid_frame* d_frame) {
+    return reinterpret_cast<const FramePairs*>(d_frame + 1);
+}
+
 // Grid placement computed on the host in FP64 (same operation order as the device variant).
 int compute_frame(const f184gi_bounds& b, uint32_t dim, const float light_dir[3], f184gi_grid_frame* out);
 

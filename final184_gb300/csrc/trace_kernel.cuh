@@ -530,16 +530,12 @@ __global__ void __launch_bounds__(TW * TH, MINB) trace_kernel(TraceConsts tc, co
                 g.dim = v.grid_dim;
                 g.levels = v.grid_levels;
                 g.tmax = v.tmax;
-                // world -> L0 voxel units: (p - origin) * (inv_voxel_fixed / 256), the frame's FP64 values split
-                // into FP32 pairs once per view (the voxel-to-world set-up)
-                for (int a = 0; a < 3; ++a) {
-                    const double o = v.frame->origin[a];
-                    g.org_h[a] = float(o);
-                    g.org_l[a] = float(o - double(g.org_h[a]));
-                }
-                const double ivs = v.frame->inv_voxel_fixed * (1.0 / 256.0);
-                g.ivs_h = float(ivs);
-                g.ivs_l = float(ivs - double(g.ivs_h));
+                // world -> L0 voxel units: (p - origin) * (inv_voxel_fixed / 256) as FP32 pairs, written beside
+                // the frame when it was computed
+                const FramePairs* fp = reinterpret_cast<const FramePairs*>(v.frame + 1);
+                for (int a = 0; a < 3; ++a) g.org_h[a] = fp->org_h[a], g.org_l[a] = fp->org_l[a];
+                g.ivs_h = fp->ivs_h;
+                g.ivs_l = fp->ivs_l;
             }
             cur_view = vi;
             __syncwarp();

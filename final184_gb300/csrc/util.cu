@@ -146,6 +146,15 @@ __global__ void frame_kernel(const int32_t* mm, f184gi_bounds bounds, int use_mm
         }
     const float L[3] = {lx, ly, lz};
     frame_from_bounds(mn, mx, dim, L, out);
+    // the voxel map as FP32 pairs, after the frame (the trace's FP64-free set-up)
+    FramePairs* fp = reinterpret_cast<FramePairs*>(out + 1);
+    for (int a = 0; a < 3; ++a) {
+        fp->org_h[a] = __double2float_rn(out->origin[a]);
+        fp->org_l[a] = __double2float_rn(__dsub_rn(out->origin[a], double(fp->org_h[a])));
+    }
+    const double ivs = __dmul_rn(out->inv_voxel_fixed, 1.0 / 256.0);
+    fp->ivs_h = __double2float_rn(ivs);
+    fp->ivs_l = __double2float_rn(__dsub_rn(ivs, double(fp->ivs_h)));
 }
 
 }  // namespace

@@ -159,7 +159,8 @@ def test_grid_bytes_and_errors(lib):
     n = C.c_uint64()
     assert lib.f184gi_grid_bytes(C.byref(d), C.byref(n)) == 0
     levels = 256 ** 3 + sum(((256 >> l) + 2) ** 3 for l in range(1, 8))  # levels >= 1 carry a ring of zeros
-    assert n.value == levels * 16 + 2048 * 2048 * 8 + C.sizeof(_abi.GridFrame)
+    # the frame is followed on the device by its voxel map as FP32 pairs (8 floats)
+    assert n.value == levels * 16 + 2048 * 2048 * 8 + C.sizeof(_abi.GridFrame) + 32
     bad = _abi.GridDesc(100, 3, 0, 0, 1024, 0)
     assert lib.f184gi_grid_bytes(C.byref(bad), C.byref(n)) == _abi.ERR_INVALID
     assert b"power of two" in lib.f184gi_last_error()
