@@ -56,7 +56,8 @@ def peaks():
 
 
 def traffic_record(kernel):
-    """DRAM bytes per launch of `kernel` from the committed ncu summary (None when absent)."""
+    """DRAM bytes per launch of `kernel` (or another figure keyed `kernel`) from the committed ncu summary (None when
+    absent)."""
     path = os.path.join(ROOT, "profiles", "traffic.json")
     if not os.path.exists(path):
         return None
@@ -267,6 +268,24 @@ def run_reference(args, cfg):
 
 # ---------------------------------------------------------------- GPU arm
 
+def issue_roofline(warp_inst, ms, dev, clk):
+    """The trace kernel against the SM issue peak: warp instructions per launch (the committed ncu capture of the
+    same kernel on the same view) / its CUDA-event time, over SMs x 4 schedulers x the SM clock sampled during the
+    timed region (one warp instruction per scheduler per cycle)."""
+    if not warp_inst or not ms:
+        return None
+    import torch
+
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    mhz = (clk or {}).get("sm_mhz") or 2070.0
+    peak = sms * 4 * mhz * 1e6
+    achieved = warp_inst / (ms * 1e-3)
+    return {"bound": "issue", "achieved": round(achieved / 1e9, 2), "peak": round(peak / 1e9, 2),
+            "unit": "G warp instructions/s", "frac": round(achieved / peak, 4), "warp_instructions": int(warp_inst),
+            "source": "warp instructions from profiles/trace_kernel_plain-large.md (ncu, FP32 chain); peak = %d SMs x "
+                      "4 schedulers x %.0f MHz" % (sms, mhz)}
+
+
 def l2_copy_gbs(dev, stream, mib=40, reps=100):
     """Read + write GB/s of a device copy whose source and destination (2 x mib MiB) stay in L2."""
     import torch
@@ -447,6 +466,7 @@ def run_gpu(args, cfg):
     l2_gbs = l2_copy_gbs(dev, stream)
     kernel_names = {"voxelize": "vox_bricks", "mip": "mip_pass", "trace": "trace_kernel"}
     tr = traffic_record(kernel_names[top] + ("_f16" if args.storage == "f16" else ""))
+    tr_inst = traffic_record(kernel_names[top] + ("_f16" if args.storage == "f16" else "") + "_warp_instructions")
     line = {
         "metric": METRIC, "value": round(value, 4), "unit": "Mpix/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms_per_step, 4), "higher_is_better": True, "scaling": "weak",
@@ -461,9 +481,10 @@ def run_gpu(args, cfg):
                      "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_source": peak_kind,
                      "algorithmic_bytes": alg[top],
                      "traffic": (tr * 1.0 if isinstance(tr, (int, float)) else None),
-                     "note": "far below the HBM roof: the trace is instruction-issue bound (ncu: ~68% issue-active, "
-                             "L1 hit ~93%, L2 ~2% and DRAM ~0.4% of peak); algorithmic bytes = G-buffer 10 B + output 32 B per "
-                             "pixel + the whole chain once (upper bound of the touched part)",
+                     "note": "far below the HBM roof: the trace is instruction-issue bound (ncu: ~66% issue-active, "
+                             "L1 hit ~96%, DRAM ~0.35% of peak; see `issue`); algorithmic bytes = G-buffer 10 B + output "
+                             "32 B per pixel + the whole chain once (upper bound of the touched part)",
+                     "issue": issue_roofline(tr_inst, means[top], dev, clk),
                      "sampled": {"bytes": int(sampled), "achieved": round(sampled / (means[top] * 1e-3) / 1e9, 1),
                                  "unit": "GB/s", "l2_copy_gbs": round(l2_gbs, 1),
                                  "frac_of_l2_copy": round(sampled / (means[top] * 1e-3) / 1e9 / l2_gbs, 3),
