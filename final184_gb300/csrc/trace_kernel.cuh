@@ -156,11 +156,11 @@ struct GridRef {
 // three entries, and the step to the next brick along an axis is the difference of two.
 constexpr int kLut = 65;
 
-// 8-tap trilinear sample of one volume of level l (d voxels per axis) at x (L0 voxel units); taps outside the
-// volume read zero.  Levels >= 1 are linear inside a ring of zeros: a footprint that touches the volume is read
-// whole with deltas +1 / +(d+2) / +(d+2)^2, any other is zero.  Level 0 is bricked: interior samples address the
-// seven other taps from the first one with +1 / +8 / +64 inside a brick, or the Morton step to the next brick
-// when the tap crosses a brick face; samples touching its border test each tap.
+// 8-tap trilinear sample of one volume of level l (d voxels per axis) at the sample point (L0 voxel units); taps
+// outside the volume read zero.  Levels >= 1 are linear inside a ring of zeros: a footprint that touches the volume
+// is read whole with deltas +1 / +(d+2) / +(d+2)^2, any other is zero.  Level 0 is bricked: interior samples
+// address the seven other taps from the first one with +1 / +8 / +64 inside a brick, or the Morton step to the next
+// brick when the tap crosses a brick face; samples touching its border test each tap.
 // The sample is ADDED to acc scaled by `scale` (the weight of this level in the quadrilinear blend), which is
 // folded into the z weights: acc += scale * sum_taps w_tap v_tap.
 template <int FMT, int NV>
@@ -169,32 +169,34 @@ __device__ __forceinline__ void tri_sample(const void* base, int d, uint32_t l, 
                                           float4 (&acc)[NV]) {
     // NV volumes of the same level share the tap coordinates and weights (the three directions an anisotropic
     // sample blends); each volume accumulates its own taps in the single-volume order.
-    // The sample point is oi + xr (L0 voxel units): oi integer, xr small.  Its level coordinate
-    // u = (oi + xr) 2^-l - 0.5 is split as A = oi 2^-l - 0.5 (exact) = Ai + Af (integer + fraction, exact) and
-    // v = Af + xr 2^-l, so the fraction that weights the taps keeps the precision of xr, not of |oi|.
-    const float s = __int_as_float((127 - int(l)) << 23);  // 2^-l
+    // The sample point is oi + xr (oi integer, xr small).  Level l's coordinate is u = (oi + xr) 2^-l - 0.5.  At
+    // level 0 the tap fraction must keep the precision of xr (a grazing cone's first samples: the FP32 sum oi + xr
+    // alone costs 7e-3 relative error on a 512^3 view), so u is split exactly as (oi - 1) + (xr + 0.5).  Coarser
+    // levels scale the rounding of p = oi + xr (FP32) by 2^-l and take u + 1 = p 2^-l + 0.5 in FP32, whose floor is
+    // the footprint's first voxel in the ringed volume (measured in the FP32 restatement against the split at
+    // every level: the same maximum error on the 256^3 plain-large and the 512^3 anisotropic views).
     const float oa[3] = {oi.x, oi.y, oi.z}, xa[3] = {xr.x, xr.y, xr.z};
     int c0[3];
     float f[3];
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-        const float A = __fmaf_rn(oa[a], s, -0.5f);
-        const float Ai = floorf(A);
-        const float v = __fmaf_rn(xa[a], s, __fsub_rn(A, Ai));
-        const float fl = floorf(v);
-        c0[a] = int(__fadd_rn(Ai, fl));
-        f[a] = __fsub_rn(v, fl);
-    }
-    const float wx[2] = {1.0f - f[0], f[0]}, wy[2] = {1.0f - f[1], f[1]};
-    const float wz[2] = {(1.0f - f[2]) * scale, f[2] * scale};
     if (l > 0) {
+        const float sc = __int_as_float((127 - int(l)) << 23);  // 2^-l
+        int c1[3];  // c0 + 1: the footprint's first voxel in the ringed volume
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            const float u = __fmaf_rn(__fadd_rn(oa[a], xa[a]), sc, 0.5f);
+            const float fl = floorf(u);
+            c1[a] = int(fl);
+            f[a] = __fsub_rn(u, fl);
+        }
         // ringed linear level: footprints that touch the volume are read whole (the ring reads zero), the others
         // are zero outright
-        if (unsigned(c0[0] + 1) > unsigned(d) || unsigned(c0[1] + 1) > unsigned(d) || unsigned(c0[2] + 1) > unsigned(d))
+        if (unsigned(c1[0]) > unsigned(d) || unsigned(c1[1]) > unsigned(d) || unsigned(c1[2]) > unsigned(d))
             return;
+        const float wx[2] = {1.0f - f[0], f[0]}, wy[2] = {1.0f - f[1], f[1]};
+        const float wz[2] = {(1.0f - f[2]) * scale, f[2] * scale};
         // one address per x-row of the footprint: the row's second tap is the next element (an immediate offset)
         const uint32_t dp = uint32_t(d) + 2u;
-        const uint32_t i0 = (uint32_t(c0[2] + 1) * dp + uint32_t(c0[1] + 1)) * dp + uint32_t(c0[0] + 1);
+        const uint32_t i0 = (uint32_t(c1[2]) * dp + uint32_t(c1[1])) * dp + uint32_t(c1[0]);
         const uint32_t ry = dp, rz = dp * dp;
 #pragma unroll
         for (int tz = 0; tz < 2; ++tz)
@@ -212,6 +214,15 @@ __device__ __forceinline__ void tri_sample(const void* base, int d, uint32_t l, 
             }
         return;
     }
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const float v = __fadd_rn(xa[a], 0.5f);
+        const float fl = floorf(v);
+        c0[a] = int(__fadd_rn(__fsub_rn(oa[a], 1.0f), fl));
+        f[a] = __fsub_rn(v, fl);
+    }
+    const float wx[2] = {1.0f - f[0], f[0]}, wy[2] = {1.0f - f[1], f[1]};
+    const float wz[2] = {(1.0f - f[2]) * scale, f[2] * scale};
     const unsigned lim = unsigned(d - 1);
     if (unsigned(c0[0]) < lim && unsigned(c0[1]) < lim && unsigned(c0[2]) < lim) {
         uint32_t i0, dx, dy, dz;
@@ -346,8 +357,8 @@ __device__ float4 cone(const GridRef& g, const uint32_t* lut, const TraceConsts&
                       fmaf(dir.z, t, fmaf(dir.z, tl, of.z)));
         if (exit_test) {
             const float m = 2.0f * diam;
-            const float3 xa = add3(oi, x);
-            if (xa.x < -m || xa.y < -m || xa.z < -m || xa.x > dimf + m || xa.y > dimf + m || xa.z > dimf + m) break;
+            const float3 p = add3(oi, x);
+            if (p.x < -m || p.y < -m || p.z < -m || p.x > dimf + m || p.y > dimf + m || p.z > dimf + m) break;
         }
         float fl = floorf(lvl);
         uint32_t l0 = uint32_t(fl);

@@ -803,19 +803,26 @@ inline FF32 ff_ndc(uint32_t k, uint32_t n) {
     return ff_add(FF32{q, ql}, FF32{-1.0f, 0.0f});
 }
 
-// 8-tap sample of one volume of level l at oi + x, added to out scaled by `scale`
-void tri_sample_rel(const float* vol, int64_t d, uint32_t l, const float oi[3], const float x[3], float scale,
-                    float out[4]) {
+// 8-tap sample of one volume of level l at oi + x (p = oi + x rounded to FP32), added to out scaled by `scale`.
+// Level 0 splits its coordinate exactly as (oi - 1) + (x + 0.5), so the tap fraction keeps the precision of x;
+// coarser levels take u + 1 = p 2^-l + 0.5 in FP32 (the rounding of p shrinks by 2^-l there).
+void tri_sample_rel(const float* vol, int64_t d, uint32_t l, const float oi[3], const float x[3], const float p[3],
+                    float scale, float out[4]) {
     const float s = std::ldexp(1.0f, -int(l));
     int64_t i0[3];
     float f[3];
     for (int a = 0; a < 3; ++a) {
-        const float A = std::fma(oi[a], s, -0.5f);
-        const float Ai = std::floor(A);
-        const float v = std::fma(x[a], s, A - Ai);
-        const float fl = std::floor(v);
-        i0[a] = int64_t(Ai + fl);
-        f[a] = v - fl;
+        if (l == 0) {
+            const float v = x[a] + 0.5f;
+            const float fl = std::floor(v);
+            i0[a] = int64_t((oi[a] - 1.0f) + fl);
+            f[a] = v - fl;
+        } else {  // u + 1 = p 2^-l + 0.5: its floor is the first tap + 1
+            const float u1 = std::fma(p[a], s, 0.5f);
+            const float fl = std::floor(u1);
+            i0[a] = int64_t(fl) - 1;
+            f[a] = u1 - fl;
+        }
     }
     for (int dz = 0; dz < 2; ++dz) {
         const int64_t z = i0[2] + dz;
@@ -836,11 +843,11 @@ void tri_sample_rel(const float* vol, int64_t d, uint32_t l, const float oi[3], 
     }
 }
 
-void level_sample_rel(const Chain<float>& ch, uint32_t l, const float oi[3], const float x[3], Vec3<float> dir,
-                      float scale, float out[4]) {
+void level_sample_rel(const Chain<float>& ch, uint32_t l, const float oi[3], const float x[3], const float p[3],
+                      Vec3<float> dir, float scale, float out[4]) {
     const int64_t d = ch.dim >> l;
     if (!ch.aniso || l == 0) {
-        tri_sample_rel(ch.base + ch.off[l], d, l, oi, x, scale, out);
+        tri_sample_rel(ch.base + ch.off[l], d, l, oi, x, p, scale, out);
         return;
     }
     const uint64_t vol = uint64_t(d) * d * d * 4;
@@ -848,7 +855,7 @@ void level_sample_rel(const Chain<float>& ch, uint32_t l, const float oi[3], con
     const int sel[3] = {dir.x >= 0.0f ? 0 : 1, dir.y >= 0.0f ? 2 : 3, dir.z >= 0.0f ? 4 : 5};
     for (int a = 0; a < 3; ++a) {
         float sa[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-        tri_sample_rel(ch.base + ch.off[l] + vol * sel[a], d, l, oi, x, 1.0f, sa);
+        tri_sample_rel(ch.base + ch.off[l] + vol * sel[a], d, l, oi, x, p, 1.0f, sa);
         for (int c = 0; c < 4; ++c) out[c] = std::fma(w[a], sa[c], out[c]);
     }
 }
@@ -864,13 +871,13 @@ void cone_rel(const Chain<float>& ch, const float oi[3], const float of[3], Vec3
     while (t < tmax || (t == tmax && tl <= 0.0f)) {
         const float diam = std::max(1.0f, std::fma(d2, t, d2 * tl));
         const float lvl = std::min(std::max(std::log2(diam), 0.0f), maxl);
-        float x[3];
+        float x[3], pa[3];
         bool outside = false;
         const float m = 2.0f * diam;
         for (int a = 0; a < 3; ++a) {
             x[a] = std::fma(dv[a], t, std::fma(dv[a], tl, of[a]));
-            const float xa = oi[a] + x[a];
-            outside = outside || xa < -m || xa > dimf + m;
+            pa[a] = oi[a] + x[a];
+            outside = outside || pa[a] < -m || pa[a] > dimf + m;
         }
         if (outside) break;
         const float fl = std::floor(lvl);
@@ -882,8 +889,8 @@ void cone_rel(const Chain<float>& ch, const float oi[3], const float of[3], Vec3
             cnt[1] += two ? 2 : 1;
         }
         float s[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-        level_sample_rel(ch, l0, oi, x, dir, two ? 1.0f - f : 1.0f, s);
-        if (two) level_sample_rel(ch, l0 + 1, oi, x, dir, f, s);
+        level_sample_rel(ch, l0, oi, x, pa, dir, two ? 1.0f - f : 1.0f, s);
+        if (two) level_sample_rel(ch, l0 + 1, oi, x, pa, dir, f, s);
         const float tr = 1.0f - alpha;
         for (int k = 0; k < 3; ++k) c[k] += tr * s[k];
         alpha += tr * s[3];

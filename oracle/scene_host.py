@@ -52,6 +52,9 @@ class HostScene:
         self.tri_xyz = np.ctypeslib.as_array(s.tri_xyz, shape=(n * 9,)).copy()
         self.albedo = np.ctypeslib.as_array(s.albedo, shape=(n,)).copy()
         self.roughness = np.ctypeslib.as_array(s.roughness, shape=(n,)).copy()
+        no = self.nobjects
+        self.object_first = np.ctypeslib.as_array(s.object_first, shape=(no,)).copy()
+        self.object_count = np.ctypeslib.as_array(s.object_count, shape=(no,)).copy()
         self._ptr = ptr
 
     def camera(self, i, seed=None):
