@@ -330,8 +330,12 @@ __device__ float4 cone(const GridRef& g, const uint32_t* lut, const TraceConsts&
     // a hundred steps much shorter than t, and plain FP32 sums would drift by ~n/2 ulp(t) (5e-3 voxel at the far
     // end of a 512^3 grid), enough to move samples across opacity edges.
     float t = tc.p.start_offset, tl = 0.0f;
-    const float dimf = float(g.dim);
-    const float maxl = float(g.levels - 1);
+    // the grid's scalars in registers for the whole march: every shared-memory read is a load-pipe wavefront, and
+    // the kernel's load pipe is as busy as its issue slots
+    const uint32_t gdim = g.dim, glevels = g.levels;
+    const float gtmax = g.tmax;
+    const float dimf = float(gdim);
+    const float maxl = float(glevels - 1);
     const float d2 = 2.0f * tan_half;
     // The exit test (a sample more than 2 diameters outside the grid reads zero, so the cone stops there) can
     // only fire for a cone that starts outside the grid or outruns the margin: the margin 2 diam = 4 t tan grows
@@ -349,7 +353,7 @@ __device__ float4 cone(const GridRef& g, const uint32_t* lut, const TraceConsts&
             diam = fmaxf(1.0f, fmaf(d2, t, d2 * tl));
             lraw = fmaxf(log2f(diam), 0.0f);
         }
-        if (!(t < g.tmax || (t == g.tmax && tl <= 0.0f))) break;
+        if (!(t < gtmax || (t == gtmax && tl <= 0.0f))) break;
         float lvl = fminf(lraw, maxl);
         // the sample point oi + x: x is the offset from the origin's integer voxel (small near the surface, where
         // the weights of a grazing cone are most sensitive)
@@ -365,10 +369,10 @@ __device__ float4 cone(const GridRef& g, const uint32_t* lut, const TraceConsts&
         float f = lvl - fl;
         if constexpr (COUNT) {
             cnt[0] += 1u;
-            cnt[1] += (f > 0.0f && l0 + 1 < g.levels) ? 2u : 1u;
+            cnt[1] += (f > 0.0f && l0 + 1 < glevels) ? 2u : 1u;
         }
         // quadrilinear: (1 - f) * level l0 + f * level l0 + 1, the level weights folded into the tap weights
-        const bool two = f > 0.0f && l0 + 1 < g.levels;
+        const bool two = f > 0.0f && l0 + 1 < glevels;
         float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
         if (ANISO) {
             // the two levels share one copy of the (three-volume) sampling code: the instruction cache
@@ -497,20 +501,18 @@ __device__ void trace_pixel(const GridRef& g, const uint32_t* lut, const TraceCo
 // warp never waits for the other warps of its CTA: the only CTA barrier is the staging of the tables at the
 // start.  The CTA shape and the CTAs resident per SM (MINB) are the variants the tuner picks from.
 template <int FMT, bool ANISO, int TW, int TH, int MINB, bool COUNT = false>
-__global__ void __launch_bounds__(TW * TH, MINB) trace_kernel(TraceConsts tc, const TraceView* __restrict__ views,
+__global__ void __launch_bounds__(TW * TH, MINB) trace_kernel(const __grid_constant__ TraceConsts tc,
+                                                             const TraceView* __restrict__ views,
                                                              const uint32_t* __restrict__ tile_base, uint32_t nviews,
                                                              uint32_t* work) {
     constexpr int kWarps = TW * TH / 32, WW = TW, WH = 32 / TW;
     static_assert(TW * TH % 32 == 0 && 32 % TW == 0, "warp tiles of 32 pixels");
     uint32_t cnt[2] = {0u, 0u};  // COUNT only: this thread's steps and level samples
+    // The diffuse schedule is read from the parameter bank (`tc` is a grid constant): the step index is the same
+    // across the warp, so the constant cache broadcasts it without a load-pipe wavefront.
     __shared__ GridRef gs[kWarps];  // the grid of each warp's current view
     __shared__ uint32_t s_lut[3 * kLut];
-    __shared__ SchedEntry s_sched[kDiffuseSched];  // read by every lane at the same step: broadcast
     for (uint32_t i = threadIdx.x; i < 3 * kLut; i += TW * TH) s_lut[i] = part1by2(i % kLut) << (9 + i / kLut);
-    if (threadIdx.x == 0) {  // constant indices: the schedule is read straight from the parameter bank
-#pragma unroll
-        for (uint32_t i = 0; i < kDiffuseSched; ++i) s_sched[i] = tc.sched[i];
-    }
     __syncthreads();
     const uint32_t lane = threadIdx.x & 31u, wid = threadIdx.x >> 5;
     GridRef& g = gs[wid];
@@ -555,7 +557,7 @@ __global__ void __launch_bounds__(TW * TH, MINB) trace_kernel(TraceConsts tc, co
         const uint32_t tiles_x = (v.width + WW - 1) / WW;
         const uint32_t px = (local % tiles_x) * WW + (lane % WW);
         const uint32_t py = (local / tiles_x) * WH + (lane / WW);
-        if (px < v.width && py < v.height) trace_pixel<FMT, ANISO, COUNT>(g, s_lut, tc, v, px, py, s_sched, cnt);
+        if (px < v.width && py < v.height) trace_pixel<FMT, ANISO, COUNT>(g, s_lut, tc, v, px, py, tc.sched, cnt);
         if constexpr (COUNT) {  // warp totals, one atomic per warp and counter
             const unsigned long long a = __reduce_add_sync(0xffffffffu, cnt[0]), b = __reduce_add_sync(0xffffffffu, cnt[1]);
             if (lane == 0u) {
