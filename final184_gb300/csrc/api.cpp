@@ -217,12 +217,8 @@ GridObj* find_grid(f184gi_ctx* c, uint32_t id) {
     return it == c->grids.end() ? nullptr : &it->second;
 }
 
-int read_status(f184gi_ctx* c) {
-    uint32_t st = 0;
-    cudaError_t e = cudaMemcpy(&st, c->d_status, 4, cudaMemcpyDeviceToHost);
-    if (e != cudaSuccess) return cuda_fail(e, "status read");
+int decode_status(f184gi_ctx* c, uint32_t st) {
     if (!st) return F184GI_OK;
-    cudaMemset(c->d_status, 0, 4);
     if (st & kStatusCopyTimeout) {
         c->failed = true;
         return fail(F184GI_ERR_TIMEOUT, "a bounded wait on a bulk copy expired; the copy may still be in flight, so the "
@@ -233,6 +229,15 @@ int read_status(f184gi_ctx* c) {
     if (st & kStatusNonFinite)
         return fail(F184GI_ERR_INVALID, "triangles with a NaN or infinite coordinate were skipped");
     return fail(F184GI_ERR_INVALID, "geometry outside the fixed-point range was skipped");
+}
+
+int read_status(f184gi_ctx* c) {
+    uint32_t st = 0;
+    cudaError_t e = cudaMemcpy(&st, c->d_status, 4, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(e, "status read");
+    if (!st) return F184GI_OK;
+    cudaMemset(c->d_status, 0, 4);
+    return decode_status(c, st);
 }
 
 }  // namespace
@@ -818,6 +823,18 @@ int ctx_internal(f184gi_ctx* c, int* device, uint32_t** d_status) {
     *device = c->device;
     *d_status = c->d_status;
     return F184GI_OK;
+}
+
+int ctx_status_capture(f184gi_ctx* c, uint32_t* host_pinned, cudaStream_t s) {
+    if (!c || !host_pinned) return fail(F184GI_ERR_INVALID, "ctx_status_capture: null argument");
+    cudaError_t e = cudaMemcpyAsync(host_pinned, c->d_status, 4, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(c->d_status, 0, 4, s);
+    return cuda_fail(e, "status capture");
+}
+
+int ctx_status_report(f184gi_ctx* c, uint32_t status) {
+    if (!c) return fail(F184GI_ERR_INVALID, "ctx_status_report: null context");
+    return decode_status(c, status);
 }
 
 void view_clip_matrix(const f184gi_view* v, double M[16]) {

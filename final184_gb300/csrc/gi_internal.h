@@ -239,6 +239,10 @@ int blur_launch(const float* in, const float* depth, uint32_t W, uint32_t H, flo
 int grid_internal(f184gi_ctx* c, uint32_t grid, ChainLayout* chain, const f184gi_grid_frame** d_frame);
 // the context's device ordinal and device status word
 int ctx_internal(f184gi_ctx* c, int* device, uint32_t** d_status);
+// Stream-ordered status: copy the context's device status word to pinned host memory and clear it, on stream s
+// (ordered after the work issued before it); then decode a captured word as f184gi_sync would report it.
+int ctx_status_capture(f184gi_ctx* c, uint32_t* host_pinned, cudaStream_t s);
+int ctx_status_report(f184gi_ctx* c, uint32_t status);
 // clip = proj * view of a view in FP64, summed in index order without FMA contraction
 void view_clip_matrix(const f184gi_view* v, double M[16]);
 

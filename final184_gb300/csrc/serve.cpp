@@ -59,7 +59,12 @@ struct Scene {
     uint32_t* h_dirty = nullptr;  // pinned staging of the dirty list
     uint32_t nbricks = 0;
     std::vector<uint8_t> flag;
-    bool busy = false;
+    // Batches in flight that hold this scene (one request each, in admission order) and the slot of the latest:
+    // a later batch's update of the scene waits on that slot's completion event, so the scene's requests run in
+    // order without one in flight blocking the next one's admission.
+    uint32_t inflight = 0;
+    int last_slot = -1;
+    cudaEvent_t dirty_copied = nullptr;  // the last update's copy of h_dirty has been made (h_dirty reusable)
     uint64_t bytes = 0;
 };
 
@@ -83,6 +88,8 @@ struct Slot {
     std::vector<Request*> reqs;
     std::vector<int> req_status;  // per request: a failure of its own staging / update / views (0 = ran)
     std::vector<Scene*> scenes;  // scene of each request, resolved under the server lock
+    std::vector<cudaEvent_t> waits;  // per request: completion event of the scene's previous batch (or null)
+    uint32_t* h_status = nullptr;    // pinned: each scene context's status word, captured at the end of the batch
     std::vector<TraceView> tv;
     uint32_t batch = 0;
     bool busy = false;
@@ -181,13 +188,17 @@ int scene_update(Scene* sc, const Request* r, cudaStream_t s) {
         range_box(sc, m.first, m.count, mn, mx);
         mark_box(sc, mn, mx);
     }
+    // the previous update's copy of the dirty list may still be queued on another slot's stream
+    cudaError_t e = cudaEventSynchronize(sc->dirty_copied);
+    if (e != cudaSuccess) return cuda_fail(e, "server: dirty list reuse");
     uint32_t nd = 0;
     for (uint32_t m = 0; m < sc->nbricks; ++m)
         if (sc->flag[m]) sc->h_dirty[nd++] = m;
     int rc = f184gi_apply_moves(sc->ctx, sc->d_tri, r->moves.data(), uint32_t(r->moves.size()), sc->ntris, s);
     if (rc) return rc;
     if (nd == 0) return F184GI_OK;
-    cudaError_t e = cudaMemcpyAsync(sc->d_dirty, sc->h_dirty, size_t(nd) * 4, cudaMemcpyHostToDevice, s);
+    e = cudaMemcpyAsync(sc->d_dirty, sc->h_dirty, size_t(nd) * 4, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaEventRecord(sc->dirty_copied, s);
     if (e != cudaSuccess) return cuda_fail(e, "server: dirty list");
     rc = f184gi_voxelize(sc->ctx, sc->grid, sc->d_tri, sc->d_alb, sc->ntris, &sc->bounds, &sc->light, sc->d_dirty, nd, s);
     if (rc) return rc;
@@ -271,7 +282,10 @@ int issue_batch(f184gi_server* S, Slot& slot) {
             Scene* sc = slot.scenes[k];
             for (const f184gi_view& v : r->views) host_out[k].push_back(v.out);
             const size_t first_view = slot.tv.size();
-            int rc = (r->flags & F184GI_REQ_INJECT_FAIL)
+            // the scene's previous batch (another slot) reads the grid its update is about to rewrite
+            int rc = slot.waits[k] ? cuda_fail(cudaStreamWaitEvent(s, slot.waits[k], 0), "server: scene order") : 0;
+            if (!rc)
+                rc = (r->flags & F184GI_REQ_INJECT_FAIL)
                          ? fail(F184GI_ERR_CUDA, "server: injected failure of the scene update (test hook)")
                          : stage_in(r, s);
             if (!rc) rc = scene_update(sc, r, s);
@@ -311,6 +325,10 @@ int issue_batch(f184gi_server* S, Slot& slot) {
     }
     for (size_t k = 0; k < slot.reqs.size(); ++k)
         if (slot.req_status[k] == F184GI_OK && (rc = stage_out(slot.reqs[k], host_out[k], s))) return rc;
+    // each scene's status word, taken in stream order: flags raised by this batch's kernels are reported with
+    // this batch, not with a later batch of the same scene that may run by the time this one is retired
+    for (size_t k = 0; k < slot.scenes.size(); ++k)
+        if ((rc = ctx_status_capture(slot.scenes[k]->ctx, slot.h_status + k, s))) return rc;
     return cuda_fail(cudaEventRecord(slot.done, s), "server: batch event");
 }
 
@@ -354,7 +372,7 @@ void scheduler_exit(f184gi_server* S) {
             continue;
         for (size_t k = 0; k < sl.reqs.size(); ++k) {
             finish_request(S, sl.reqs[k], F184GI_ERR_WORKER, now);
-            sl.scenes[k]->busy = false;
+            sl.scenes[k]->inflight -= 1;
         }
         sl.reqs.clear();
         sl.busy = false;
@@ -390,9 +408,7 @@ void scheduler_loop(f184gi_server* S) {
         uint64_t npix = 0;
         for (auto it = S->pending.begin(); it != S->pending.end();) {
             Request* r = *it;
-            Scene* sc = S->scenes.at(r->scene);
-            if (sc->busy || blocked.count(r->scene)) {
-                blocked.insert(r->scene);
+            if (blocked.count(r->scene)) {  // one request per scene per batch, in order
                 ++it;
                 continue;
             }
@@ -404,7 +420,6 @@ void scheduler_loop(f184gi_server* S) {
             }
             batch.push_back(r);
             blocked.insert(r->scene);
-            sc->busy = true;
             nviews += uint32_t(r->views.size());
             npix += r->pixels;
             S->hbm_used += r->staging;
@@ -419,7 +434,16 @@ void scheduler_loop(f184gi_server* S) {
         slot.busy = true;
         slot.reqs = batch;
         slot.scenes.clear();
-        for (Request* r : batch) slot.scenes.push_back(S->scenes.at(r->scene));
+        slot.waits.clear();
+        for (Request* r : batch) {
+            Scene* sc = S->scenes.at(r->scene);
+            // the slot of the scene's latest batch in flight cannot be reused before this batch is issued (the
+            // scheduler issues batches in turn), so its event still marks that batch
+            slot.waits.push_back(sc->inflight && sc->last_slot >= 0 ? S->slots[sc->last_slot].done : nullptr);
+            sc->inflight += 1;
+            sc->last_slot = si;
+            slot.scenes.push_back(sc);
+        }
         slot.batch = S->next_batch++;
         for (Request* r : batch) r->admitted = true, r->t_admit = now, r->batch = slot.batch;
         for (Request* r : batch)
@@ -434,7 +458,7 @@ void scheduler_loop(f184gi_server* S) {
                 Request* r = slot.reqs[k];
                 if (r->d_stage) cudaFree(r->d_stage), r->d_stage = nullptr;
                 finish_request(S, r, slot.req_status.size() > k && slot.req_status[k] ? slot.req_status[k] : rc, t);
-                slot.scenes[k]->busy = false;
+                slot.scenes[k]->inflight -= 1;
             }
             slot.reqs.clear();
             slot.busy = false;
@@ -462,9 +486,9 @@ void completer(f184gi_server* S) {
         cudaError_t e = cudaEventSynchronize(slot.done);
         int st = e == cudaSuccess ? F184GI_OK : cuda_fail(e, "server: batch");
         if (st == F184GI_OK) {
-            // kernels flag overflow / timeout on each touched scene's context
-            for (Scene* sc : slot.scenes) {
-                int rs = f184gi_sync(sc->ctx, slot.stream);
+            // kernels flag overflow / timeout on each touched scene's context (captured in stream order)
+            for (size_t k = 0; k < slot.scenes.size(); ++k) {
+                int rs = ctx_status_report(slot.scenes[k]->ctx, slot.h_status[k]);
                 if (rs) st = rs;
             }
         }
@@ -473,7 +497,7 @@ void completer(f184gi_server* S) {
         const Clock::time_point now = Clock::now();
         for (size_t k = 0; k < slot.reqs.size(); ++k) {
             finish_request(S, slot.reqs[k], slot.req_status[k] ? slot.req_status[k] : st, now);
-            slot.scenes[k]->busy = false;
+            slot.scenes[k]->inflight -= 1;
         }
         S->batches += 1;
         S->batch_views += slot.tv.size();
@@ -515,7 +539,9 @@ int f184gi_server_create(const f184gi_server_config* cfg, f184gi_server** out) {
     S->slots.resize(c.slots);
     for (Slot& sl : S->slots) {
         if ((e = cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking)) != cudaSuccess ||
-            (e = cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming)) != cudaSuccess) {
+            (e = cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming)) != cudaSuccess ||
+            (e = cudaHostAlloc(reinterpret_cast<void**>(&sl.h_status), size_t(c.max_batch_views) * 4,
+                               cudaHostAllocDefault)) != cudaSuccess) {
             f184gi_server_destroy(S);
             return cuda_fail(e, "server_create: streams");
         }
@@ -541,6 +567,7 @@ int f184gi_server_destroy(f184gi_server* S) {
         trace_graph_destroy(sl.graph);
         if (sl.stream) cudaStreamDestroy(sl.stream);
         if (sl.done) cudaEventDestroy(sl.done);
+        if (sl.h_status) cudaFreeHost(sl.h_status);
     }
     for (auto& kv : S->scenes) {
         Scene* sc = kv.second;
@@ -548,6 +575,7 @@ int f184gi_server_destroy(f184gi_server* S) {
         cudaFree(sc->d_alb);
         cudaFree(sc->d_dirty);
         cudaFreeHost(sc->h_dirty);
+        if (sc->dirty_copied) cudaEventDestroy(sc->dirty_copied);
         if (sc->ctx) f184gi_destroy(sc->ctx);
         delete sc;
     }
@@ -596,7 +624,8 @@ int f184gi_server_add_scene(f184gi_server* S, uint32_t id, const f184gi_grid_des
     sc->nbricks = (d.dim / 8) * (d.dim / 8) * (d.dim / 8);
     if (!rc && ((e = cudaMalloc(&sc->d_tri, ntris * 36)) != cudaSuccess || (e = cudaMalloc(&sc->d_alb, ntris * 4)) != cudaSuccess ||
                 (e = cudaMalloc(&sc->d_dirty, size_t(sc->nbricks) * 4)) != cudaSuccess ||
-                (e = cudaHostAlloc(&sc->h_dirty, size_t(sc->nbricks) * 4, cudaHostAllocDefault)) != cudaSuccess))
+                (e = cudaHostAlloc(&sc->h_dirty, size_t(sc->nbricks) * 4, cudaHostAllocDefault)) != cudaSuccess ||
+                (e = cudaEventCreateWithFlags(&sc->dirty_copied, cudaEventDisableTiming)) != cudaSuccess))
         rc = cuda_fail(e, "server_add_scene: allocation");
     if (!rc) {
         sc->h_tri.assign(tri, tri + ntris * 9);
@@ -616,6 +645,7 @@ int f184gi_server_add_scene(f184gi_server* S, uint32_t id, const f184gi_grid_des
         cudaFree(sc->d_alb);
         cudaFree(sc->d_dirty);
         cudaFreeHost(sc->h_dirty);
+        if (sc->dirty_copied) cudaEventDestroy(sc->dirty_copied);
         if (sc->ctx) f184gi_destroy(sc->ctx);
         delete sc;
         return rc;

@@ -287,9 +287,11 @@ int f184gi_sync(f184gi_ctx* ctx, void* stream);
  * is free, the scheduler admits pending requests (one per scene per batch, HBM budget for their staging
  * buffers, at most max_batch_views views), re-voxelizes the moved objects' bricks, relights and rebuilds the
  * mips of each touched scene, and traces every view of the batch in one launch replayed from a CUDA
- * graph.  Requests that arrive while batches run join the next batch; batches on different slots overlap.
- * Results are the same as running each request alone (per scene, requests apply in submission order).  The
- * f184gi_server_* calls on one server may come from several host threads at once. */
+ * graph.  Requests that arrive while batches run join the next batch; batches on different slots overlap.  A
+ * scene's next request may be admitted while a batch holding the scene is in flight: its batch's update of the
+ * scene waits (on the device) for that batch to finish.  Results are the same as running each request alone
+ * (per scene, requests apply in submission order).  The f184gi_server_* calls on one server may come from several
+ * host threads at once. */
 typedef struct f184gi_server f184gi_server;
 
 typedef struct f184gi_server_config {

@@ -93,6 +93,14 @@ cudaError_t cudaEventRecord(cudaEvent_t e, cudaStream_t s) {
     g_event_done[e] = t < now ? now : t;
     return cudaSuccess;
 }
+cudaError_t cudaStreamWaitEvent(cudaStream_t s, cudaEvent_t e, unsigned int) {
+    // the stream's later work starts after the event's: its completion time moves past the event's
+    std::lock_guard<std::mutex> lk(g_mu);
+    const Clock::time_point te = g_event_done[e];
+    Clock::time_point& t = g_stream_done[s];
+    if (t < te) t = te;
+    return cudaSuccess;
+}
 cudaError_t cudaEventSynchronize(cudaEvent_t e) {
     Clock::time_point t;
     {
@@ -190,4 +198,10 @@ int trace_graph_tune(TraceGraph* g, const TraceView* v, uint32_t n, cudaStream_t
     return trace_graph_launch(g, v, n, 0, s);
 }
 void trace_graph_destroy(TraceGraph* g) { delete g; }
+int ctx_status_capture(f184gi_ctx*, uint32_t* host_pinned, cudaStream_t s) {
+    *host_pinned = 0;  // the fake's kernels raise no flags
+    add_work(s, 2);
+    return F184GI_OK;
+}
+int ctx_status_report(f184gi_ctx*, uint32_t status) { return status ? F184GI_ERR_INVALID : F184GI_OK; }
 }  // namespace f184

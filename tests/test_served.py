@@ -156,6 +156,45 @@ def test_concurrent_submitters_match_alone(fx):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("slots", [2, 4])
+def test_same_scene_requests_pipelined_in_order(fx, slots):
+    """Requests of one scene submitted at once run one per batch in order, each batch's update of the scene
+    waiting on the previous batch (another slot) instead of the scene blocking admission: every result equals the
+    same request run alone, after the moves of the requests before it."""
+    sc = fx.scenes[0]
+    rng = np.random.default_rng(17)
+    reqs = []  # every request on scene 0, each moving three of its objects
+    for _, vids, _ in fx.requests:
+        moves = [(int(sc.object_first[o]), int(sc.object_count[o]),
+                  [float(x) for x in rng.uniform(-0.3, 0.3, 3).astype(np.float32)])
+                 for o in rng.choice(np.arange(1, sc.nobjects), 3, replace=False)]
+        reqs.append((0, vids, moves))
+    srv = fx.server(slots=2, max_batch_views=32)
+    alone = []
+    for si, vids, moves in reqs:
+        views, outs = fx.make_views(si, vids)
+        assert srv.wait(srv.submit(si, views, moves)).status == 0
+        fx.torch.cuda.synchronize()
+        alone.append([o.cpu().numpy().copy() for o in outs])
+    srv.close()
+    srv = fx.server(slots=slots, max_batch_views=32)
+    keep, tickets = [], []
+    for si, vids, moves in reqs:
+        views, outs = fx.make_views(si, vids)
+        keep.append(outs)
+        tickets.append(srv.submit(si, views, moves))
+    res = [srv.wait(t) for t in tickets]
+    fx.torch.cuda.synchronize()
+    srv.close()
+    assert all(r.status == 0 for r in res)
+    batches = [r.batch for r in res]
+    assert batches == sorted(batches) and len(set(batches)) == len(batches)  # one per batch, in order
+    for a, outs in zip(alone, keep):
+        for x, y in zip(a, outs):
+            assert np.array_equal(x.view(np.uint32), y.cpu().numpy().view(np.uint32))
+
+
+@pytest.mark.gpu
 def test_dirty_updates_equal_full_voxelization(fx):
     g, torch = fx.g, fx.torch
     srv = fx.server(slots=1)
