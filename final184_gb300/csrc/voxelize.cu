@@ -295,7 +295,7 @@ __global__ void __launch_bounds__(256) relight_bricks(const float4* __restrict__
     }
 }
 
-// Exact tests of one (triangle, brick) item, prepared by one thread and shared through shared memory.  With
+// Exact tests of one (triangle, brick) item, prepared by 1, 2 or 4 threads and shared through shared memory.  With
 // m = 2 (voxel - brick origin) + 1 (odd, 1..15) the voxel centre is 128 m + brick offset and every separating-axis
 // test reads lo <= a . m <= hi in integers.  The nine edge x unit-axis tests each ignore one coordinate, so they
 // are evaluated once per cell of the three 8x8 projections of the item's voxel box into bit masks; a voxel is
@@ -308,17 +308,15 @@ struct ItemSetup {
     uint8_t l0[3], ext[3];       // voxel box inside the brick: first voxel and extent per axis
 };
 
-__device__ void item_setup(const TriRec& r, const int64_t base[3], const int32_t l0[3], const int32_t l1[3],
-                           ItemSetup& out) {
-    // brick-relative vertices and edges fit 32 bits (|q| < 2^19, base <= 2^17): products widen 32 x 32 -> 64
-    int32_t v[3][3];
-#pragma unroll
-    for (int a = 0; a < 3; ++a)
-#pragma unroll
-        for (int b = 0; b < 3; ++b) v[a][b] = r.q[a * 3 + b] - int32_t(base[b]);
-    unsigned long long mk[3] = {0ull, 0ull, 0ull};
+// The three projections' cell masks of an item (edge x unit-axis separating-axis tests), in integers of type T.
+template <class T>
+__device__ __forceinline__ T ceil_div128(T x) { return -((-x) >> 7); }
+template <class T>
+__device__ __forceinline__ void item_masks(const int32_t (&v)[3][3], const int32_t l0[3], const int32_t l1[3],
+                                           int part, int per, unsigned long long (&mks)[3]) {
 #pragma unroll
     for (int P = 0; P < 3; ++P) {
+        unsigned long long mk = 0ull;
         // the three edge axes of projection P: a = edge x unit(P); components on the two kept axes
         const int ku = (P + 1) % 3, kw = (P + 2) % 3;  // kept axes: u first, w second
         int32_t cu[3], cw[3], lo[3], hi[3];
@@ -331,18 +329,16 @@ __device__ void item_setup(const TriRec& r, const int64_t base[3], const int32_t
             if (P == 0) a[1] = ed[2], a[2] = -ed[1];
             if (P == 1) a[0] = -ed[2], a[2] = ed[0];
             if (P == 2) a[0] = ed[1], a[1] = -ed[0];
-            auto dotw = [&](const int32_t (&x)[3]) {
-                return int64_t(a[0]) * x[0] + int64_t(a[1]) * x[1] + int64_t(a[2]) * x[2];
-            };
-            int64_t p0 = dotw(v[0]), p1 = dotw(v[1]), p2 = dotw(v[2]);
-            int64_t rr = kHalf * (int64_t(abs(a[0])) + abs(a[1]) + abs(a[2]));
-            int64_t pmin = min(p0, min(p1, p2)), pmax = max(p0, max(p1, p2));
-            cu[e] = int32_t(a[ku]);
-            cw[e] = int32_t(a[kw]);
-            lo[e] = clamp32(sar7_ceil(pmin - rr));
-            hi[e] = clamp32(sar7_floor(pmax + rr));
+            auto dotw = [&](const int32_t (&x)[3]) { return T(a[0]) * x[0] + T(a[1]) * x[1] + T(a[2]) * x[2]; };
+            const T p0 = dotw(v[0]), p1 = dotw(v[1]), p2 = dotw(v[2]);
+            const T rr = T(kHalf) * (T(abs(a[0])) + abs(a[1]) + abs(a[2]));
+            const T pmin = min(p0, min(p1, p2)), pmax = max(p0, max(p1, p2));
+            cu[e] = a[ku];
+            cw[e] = a[kw];
+            lo[e] = clamp32(int64_t(ceil_div128<T>(pmin - rr)));
+            hi[e] = clamp32(int64_t((pmax + rr) >> 7));
         }
-        for (int w = l0[kw]; w <= l1[kw]; ++w) {
+        for (int w = l0[kw] + part; w <= l1[kw]; w += per) {  // this thread's share of the rows
             const int32_t mw = 2 * w + 1;
             for (int u = l0[ku]; u <= l1[ku]; ++u) {
                 const int32_t mu = 2 * u + 1;
@@ -352,10 +348,39 @@ __device__ void item_setup(const TriRec& r, const int64_t base[3], const int32_t
                     int32_t d = cu[e] * mu + cw[e] * mw;
                     pass = pass && d >= lo[e] && d <= hi[e];
                 }
-                if (pass) mk[P] |= 1ull << (u + 8 * w);
+                if (pass) mk |= 1ull << (u + 8 * w);
             }
         }
+        mks[P] = mk;
     }
+}
+
+// A share of one (triangle, brick) item's setup: the cells of rows w = l0 + part, l0 + part + per, .. of the
+// three projections' masks (OR-combined across the item's threads by the caller), and with do_plane the plane
+// test and the item's fields.  A chunk with few items spreads each item over 2 or 4 threads, so a large item's
+// cell loops (up to 8 x 8 cells per projection) do not hold its brick.
+__device__ void item_part(const TriRec& r, const int64_t base[3], const int32_t l0[3], const int32_t l1[3], int part,
+                          int per, bool do_plane, unsigned long long (&mks)[3], ItemSetup& out) {
+    // brick-relative vertices and edges fit 32 bits (|q| < 2^19, base <= 2^17): products widen 32 x 32 -> 64
+    int32_t v[3][3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int b = 0; b < 3; ++b) v[a][b] = r.q[a * 3 + b] - int32_t(base[b]);
+    // Items whose brick-relative vertices are below 2^14 in magnitude (a triangle within 64 voxels of the brick:
+    // all but the largest) take the edge tests in 32-bit integers: edge components < 2^15, each product < 2^29, a
+    // dot product (two nonzero terms) < 2^30, the box radius < 2^23, so nothing overflows and the bounds are the
+    // same integers the 64-bit form computes.
+    int32_t vmax = 0;
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int b = 0; b < 3; ++b) vmax = max(vmax, abs(v[a][b]));
+    if (vmax < (1 << 14))
+        item_masks<int32_t>(v, l0, l1, part, per, mks);
+    else
+        item_masks<int64_t>(v, l0, l1, part, per, mks);
+    if (!do_plane) return;
     int32_t e0[3], e1[3];
 #pragma unroll
     for (int b = 0; b < 3; ++b) e0[b] = v[1][b] - v[0][b], e1[b] = v[2][b] - v[0][b];
@@ -363,7 +388,6 @@ __device__ void item_setup(const TriRec& r, const int64_t base[3], const int32_t
                   n2 = int64_t(e0[0]) * e1[1] - int64_t(e0[1]) * e1[0];
     const int64_t sp = n0 * v[0][0] + n1 * v[0][1] + n2 * v[0][2];
     const int64_t rr = kHalf * (iabs64(n0) + iabs64(n1) + iabs64(n2));
-    out.mask[0] = mk[0], out.mask[1] = mk[1], out.mask[2] = mk[2];
     out.n[0] = n0, out.n[1] = n1, out.n[2] = n2;
     out.plo = sar7_ceil(sp - rr);  // overlap iff sp - rr <= 128 (n . m) <= sp + rr
     out.phi = sar7_floor(sp + rr);
@@ -372,7 +396,7 @@ __device__ void item_setup(const TriRec& r, const int64_t base[3], const int32_t
     for (int a = 0; a < 3; ++a) out.l0[a] = uint8_t(l0[a]), out.ext[a] = uint8_t(l1[a] - l0[a] + 1);
 }
 
-constexpr int kChunk = 128;  // items prepared per round (one per thread; = threads per CTA)
+constexpr int kChunk = 128;  // items prepared per round (at most one per thread; = threads per CTA)
 
 // Eight CTAs per SM (64 registers, 26 KB of shared memory each): a brick's phases are separated by barriers at
 // which most of its threads wait, so other bricks' CTAs are what keeps the SM busy (0.59 -> 0.40 ms per 256^3
@@ -411,20 +435,37 @@ __global__ void __launch_bounds__(kChunk, 8) vox_bricks(VoxScratch sc, const f18
     }
     const int64_t base[3] = {int64_t(bx) * kBrickFix, int64_t(by) * kBrickFix, int64_t(bz) * kBrickFix};
     for (uint32_t c0 = beg; c0 < end; c0 += kChunk) {
-        // phase 1: one thread prepares one item
-        const uint32_t it = c0 + threadIdx.x;
+        // phase 1: the chunk's items are prepared by 4, 2 or 1 threads each (at most 32, 64 or 128 items), each
+        // taking every per-th row of the projections' cell tests; the item's threads are adjacent lanes, whose
+        // partial masks are OR-combined by shuffles.  The item's first thread carries its row count and writes the
+        // masks; its last computes the plane.
+        const uint32_t nchunk = min(end - c0, uint32_t(kChunk));
+        const uint32_t per = nchunk <= kChunk / 4 ? 4u : (nchunk <= kChunk / 2 ? 2u : 1u);
+        const uint32_t slot = threadIdx.x / per, part = threadIdx.x % per;
         uint32_t nrows = 0;
-        if (it < end) {
-            const TriRec r = sc.recs[sc.list[it]];
+        unsigned long long mks[3] = {0ull, 0ull, 0ull};
+        bool valid = false;
+        if (slot < nchunk) {
+            const TriRec r = sc.recs[sc.list[c0 + slot]];
             int32_t lo[3], hi[3];
             voxel_range(r.q, dim, lo, hi);
             const int32_t l0[3] = {max(lo[0], bx * 8) - bx * 8, max(lo[1], by * 8) - by * 8, max(lo[2], bz * 8) - bz * 8};
             const int32_t l1[3] = {min(hi[0], bx * 8 + 7) - bx * 8, min(hi[1], by * 8 + 7) - by * 8,
                                    min(hi[2], bz * 8 + 7) - bz * 8};
-            if (l0[0] <= l1[0] && l0[1] <= l1[1] && l0[2] <= l1[2]) {
-                item_setup(r, base, l0, l1, s_item[threadIdx.x]);
-                nrows = uint32_t((l1[1] - l0[1] + 1) * (l1[2] - l0[2] + 1));
+            valid = l0[0] <= l1[0] && l0[1] <= l1[1] && l0[2] <= l1[2];
+            if (valid) {
+                item_part(r, base, l0, l1, int(part), int(per), part == per - 1, mks, s_item[slot]);
+                if (part == 0) nrows = uint32_t((l1[1] - l0[1] + 1) * (l1[2] - l0[2] + 1));
             }
+        }
+#pragma unroll
+        for (int P = 0; P < 3; ++P) {
+            uint32_t mlo = uint32_t(mks[P]), mhi = uint32_t(mks[P] >> 32);
+            for (uint32_t o = 1; o < per; o <<= 1) {
+                mlo |= __shfl_xor_sync(0xffffffffu, mlo, int(o));
+                mhi |= __shfl_xor_sync(0xffffffffu, mhi, int(o));
+            }
+            if (valid && part == 0) s_item[slot].mask[P] = (uint64_t(mhi) << 32) | mlo;
         }
         // exclusive scan of the row counts (warp shuffles + one pass over the 4 warp totals)
         {
@@ -454,7 +495,7 @@ __global__ void __launch_bounds__(kChunk, 8) vox_bricks(VoxScratch sc, const f18
                 uint32_t mid = (lo + hi) >> 1;
                 if (s_start[mid] <= rr) lo = mid; else hi = mid;
             }
-            const ItemSetup& is = s_item[lo];
+            const ItemSetup& is = s_item[lo / per];  // lo: the item's first thread
             const uint32_t local = rr - s_start[lo];
             const uint32_t ey = is.ext[1];
             // local / ey for local < 64, ey <= 8: the quotient's fraction stays >= 1/16 from an integer
