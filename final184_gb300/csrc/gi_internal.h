@@ -177,11 +177,12 @@ struct TraceVariant {
 constexpr uint32_t kTraceVariantCount = 5;
 constexpr TraceVariant kTraceVariants[kTraceVariantCount] = {
     {16, 8, 4}, {8, 12, 7}, {4, 24, 7}, {8, 16, 5}, {4, 32, 5}};
-// The one-shot launch's variant per chain: isotropic chains take 128-thread CTAs of 4x8-pixel warp tiles at 5 per
-// SM (the 96-register budget: FP32 1080p view 1.75 ms, against 1.81-1.85 ms for 96-thread CTAs at 7 per SM, whose
-// 80 registers spill the split-origin march); anisotropic chains take 128-thread CTAs of 8x4 tiles at 5 per SM.
+// The one-shot launch's variant per chain: isotropic chains take 96-thread CTAs of 4x8-pixel warp tiles at 7 per SM
+// (FP32 1080p view 1.60 ms against 1.67 at 5 per SM, FP16 1.85 against 1.88; with every cone marched from one call
+// site the kernel is half the size, and at 80 registers the pixel's state between cones goes to local memory,
+// reloaded once per cone), anisotropic chains take 128-thread CTAs of 8x4 tiles at 5 per SM.
 constexpr uint32_t trace_default_variant(uint32_t fmt, bool aniso) {
-    return aniso ? 3u : (fmt == F184GI_FMT_F32 ? 4u : 4u);
+    return aniso ? 3u : (fmt == F184GI_FMT_F32 ? 2u : 2u);
 }
 const void* trace_kernel_fn(uint32_t fmt, bool aniso, uint32_t variant);
 const void* trace_kernel_count_fn(uint32_t fmt, bool aniso);  // instrumented, default variant's tile shape

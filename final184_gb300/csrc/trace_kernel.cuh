@@ -469,28 +469,41 @@ __device__ void trace_pixel(const GridRef& g, const uint32_t* lut, const TraceCo
     }
     float3 bx, by, bz;
     coord_space(nw, bx, by, bz);
-    float4 acc;
-    if (tc.p.diffuse_cones >= 5) {
-        float4 c0 = cone<FMT, ANISO, COUNT>(g, lut, tc, oi, of, bz, tc.p.diffuse_tan_half, sched, kDiffuseSched, cnt);
-        acc = make_float4(0.25f * c0.x, 0.25f * c0.y, 0.25f * c0.z, 0.25f * c0.w);
+    // Every cone goes through one call site (one inlined copy of the march: the kernel's code stays small in the
+    // instruction cache): k < nd the diffuse cones (the normal, then four tilted 60 degrees at phi = 0, 90, 180,
+    // 270 degrees), k = nd the specular cone (no precomputed schedule: ns = 0).
+    const uint32_t nd = tc.p.diffuse_cones >= 5 ? 5u : 1u;
+    const uint32_t ncones = nd + (tc.p.specular ? 1u : 0u);
+    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f), sp = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll 1
-        for (int k = 0; k < 4; ++k) {
-            // bx cos(phi) + by sin(phi) for phi = k * 90 degrees (the products by 0 and +-1 are exact)
-            float3 side = (k & 1) ? by : bx;
-            if (k & 2) side = f3(-side.x, -side.y, -side.z);
-            float3 dir = norm3(add3(mul3(bz, tc.cos_tilt), mul3(side, tc.sin_tilt)));
-            float4 ck = cone<FMT, ANISO, COUNT>(g, lut, tc, oi, of, dir, tc.p.diffuse_tan_half, sched, kDiffuseSched, cnt);
-            acc.x += 0.1875f * ck.x;
-            acc.y += 0.1875f * ck.y;
-            acc.z += 0.1875f * ck.z;
-            acc.w += 0.1875f * ck.w;
+    for (uint32_t k = 0; k < ncones; ++k) {
+        float3 dir = bz;
+        float tan_half = tc.p.diffuse_tan_half;
+        uint32_t ns = kDiffuseSched;
+        if (k >= nd) {
+            dir = rd, tan_half = th, ns = 0u;
+        } else if (k > 0) {
+            // bx cos(phi) + by sin(phi) for phi = (k - 1) * 90 degrees (the products by 0 and +-1 are exact)
+            const uint32_t j = k - 1;
+            float3 side = (j & 1) ? by : bx;
+            if (j & 2) side = f3(-side.x, -side.y, -side.z);
+            dir = norm3(add3(mul3(bz, tc.cos_tilt), mul3(side, tc.sin_tilt)));
         }
-    } else {
-        acc = cone<FMT, ANISO, COUNT>(g, lut, tc, oi, of, bz, tc.p.diffuse_tan_half, sched, kDiffuseSched, cnt);
+        const float4 c = cone<FMT, ANISO, COUNT>(g, lut, tc, oi, of, dir, tan_half, sched, ns, cnt);
+        if (k >= nd) {
+            sp = c;
+        } else if (nd == 1) {
+            acc = c;
+        } else if (k == 0) {
+            acc = make_float4(0.25f * c.x, 0.25f * c.y, 0.25f * c.z, 0.25f * c.w);
+        } else {
+            acc.x += 0.1875f * c.x;
+            acc.y += 0.1875f * c.y;
+            acc.z += 0.1875f * c.z;
+            acc.w += 0.1875f * c.w;
+        }
     }
     store_out(v.out, v.out_format, pi, acc);
-    float4 sp = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (tc.p.specular) sp = cone<FMT, ANISO, COUNT>(g, lut, tc, oi, of, rd, th, nullptr, 0u, cnt);
     store_out(v.out, v.out_format, npix + pi, sp);
 }
 
