@@ -163,7 +163,7 @@ constexpr int kLut = 65;
 // brick when the tap crosses a brick face; samples touching its border test each tap.
 // The sample is ADDED to acc scaled by `scale` (the weight of this level in the quadrilinear blend), which is
 // folded into the z weights: acc += scale * sum_taps w_tap v_tap.
-template <int FMT, int NV>
+template <int FMT, int NV, bool COARSE = false>
 __device__ __forceinline__ void tri_sample(const void* base, int d, uint32_t l, const uint32_t (&vol_off)[NV],
                                           float3 oi, float3 xr, const uint32_t* lut, float scale,
                                           float4 (&acc)[NV]) {
@@ -178,7 +178,7 @@ __device__ __forceinline__ void tri_sample(const void* base, int d, uint32_t l, 
     const float oa[3] = {oi.x, oi.y, oi.z}, xa[3] = {xr.x, xr.y, xr.z};
     int c0[3];
     float f[3];
-    if (l > 0) {
+    if (COARSE || l > 0) {  // COARSE: the caller knows l >= 1 (the level-0 paths are not compiled)
         const float sc = __int_as_float((127 - int(l)) << 23);  // 2^-l
         int c1[3];  // c0 + 1: the footprint's first voxel in the ringed volume
 #pragma unroll
@@ -299,14 +299,14 @@ __device__ __forceinline__ void tri_sample(const void* base, int d, uint32_t l, 
 
 // acc += scale * (the sample of level l at x): isotropic, or the three direction volumes facing the cone
 // weighted by dir^2 (anisotropic levels >= 1)
-template <int FMT, bool ANISO>
+template <int FMT, bool ANISO, bool COARSE = false>
 __device__ __forceinline__ void level_sample(const GridRef& g, const uint32_t* lut, uint32_t l, float3 oi,
                                              float3 x, float3 dir, float scale, float4& acc) {
     const int d = int(g.dim >> l);
     if (!ANISO || l == 0) {
         const uint32_t vo[1] = {g.off[l]};
         float4 a[1] = {acc};
-        tri_sample<FMT, 1>(g.base, d, l, vo, oi, x, lut, scale, a);
+        tri_sample<FMT, 1, COARSE>(g.base, d, l, vo, oi, x, lut, scale, a);
         acc = a[0];
         return;
     }
@@ -315,7 +315,7 @@ __device__ __forceinline__ void level_sample(const GridRef& g, const uint32_t* l
                             g.off[l] + (dir.y >= 0.0f ? 2u : 3u) * g.vol[l],
                             g.off[l] + (dir.z >= 0.0f ? 4u : 5u) * g.vol[l]};
     float4 sa[3] = {make_float4(0.f, 0.f, 0.f, 0.f), make_float4(0.f, 0.f, 0.f, 0.f), make_float4(0.f, 0.f, 0.f, 0.f)};
-    tri_sample<FMT, 3>(g.base, d, l, vo, oi, x, lut, 1.0f, sa);
+    tri_sample<FMT, 3, COARSE>(g.base, d, l, vo, oi, x, lut, 1.0f, sa);
 #pragma unroll
     for (int a = 0; a < 3; ++a) fma4(acc, w[a], sa[a]);
 }
@@ -383,7 +383,8 @@ __device__ float4 cone(const GridRef& g, const uint32_t* lut, const TraceConsts&
                 level_sample<FMT, ANISO>(g, lut, l0 + k, oi, x, dir, k ? f : (two ? 1.0f - f : 1.0f), s);
         } else {
             level_sample<FMT, ANISO>(g, lut, l0, oi, x, dir, two ? 1.0f - f : 1.0f, s);
-            if (two) level_sample<FMT, ANISO>(g, lut, l0 + 1, oi, x, dir, f, s);
+            // the finer level's neighbour above is never level 0: its copy carries the ringed path only
+            if (two) level_sample<FMT, ANISO, true>(g, lut, l0 + 1, oi, x, dir, f, s);
         }
         if (FMT != F184GI_FMT_F32) s.w *= kAlphaScale<FMT>;  // the unorm16 opacity sum, scaled once
         float tr = 1.0f - alpha;
