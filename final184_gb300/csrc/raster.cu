@@ -322,7 +322,16 @@ __global__ void __launch_bounds__(256) raster_tiles(RasterScratch sc, uint32_t t
         const uint32_t n = min(end - c0, uint32_t(kStage));
         if (threadIdx.x < n) srec[threadIdx.x] = sc.recs[sc.list[c0 + threadIdx.x]];
         __syncthreads();
-        for (uint32_t r = warp; r < n; r += 8) {
+        // Each warp rasterizes GROUPS records at once, LANES lanes per record: the per-record set-up (clipping,
+        // the edge functions at the box corner, the row divisor) is spread over the warp's lanes instead of being
+        // repeated by all 32 for one record, and the record's pixels are walked LANES at a time (4 records of 8
+        // lanes: 0.82 -> 0.76 ms per 500k-triangle voxelization, whose shadow raster is on the critical path;
+        // 2 of 16: 0.77, 8 of 4: 0.81).
+        constexpr uint32_t GROUPS = 4, LANES = 32 / GROUPS;
+        const uint32_t grp = lane / LANES, sub = lane % LANES;
+        for (uint32_t r0 = warp * GROUPS; r0 < n; r0 += 8 * GROUPS) {
+            const uint32_t r = r0 + grp;
+            if (r >= n) continue;
             const SubTri& s = srec[r];
             int x0 = max(int(s.x0), tx * kTile), x1 = min(int(s.x1), tx * kTile + kTile - 1);
             int y0 = max(int(s.y0), ty * kTile), y1 = min(int(s.y1), ty * kTile + kTile - 1);
@@ -335,7 +344,7 @@ __global__ void __launch_bounds__(256) raster_tiles(RasterScratch sc, uint32_t t
             const int32_t ax0 = s.X[2] - s.X[1], ay0 = s.Y[2] - s.Y[1], ax1 = s.X[0] - s.X[2], ay1 = s.Y[0] - s.Y[2],
                           ax2 = s.X[1] - s.X[0], ay2 = s.Y[1] - s.Y[0];
             const uint32_t wmagic = (65536u + uint32_t(w) - 1u) / uint32_t(w);  // p / w = (p * wmagic) >> 16, p < 256
-            for (int p = int(lane); p < npx; p += 32) {
+            for (int p = int(sub); p < npx; p += int(LANES)) {
                 const int ly = int((uint32_t(p) * wmagic) >> 16), lx = p - ly * w;
                 const int px = x0 + lx, py = y0 + ly;
                 const int32_t ox = 16 * lx, oy = 16 * ly;
