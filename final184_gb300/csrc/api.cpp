@@ -68,6 +68,21 @@ int compute_frame(const f184gi_bounds& b, uint32_t dim, const float light_dir[3]
     return F184GI_OK;
 }
 
+// The frame and its FP32 pairs as the device's frame kernel writes them (same FP64 operations, no contraction in
+// this file; the pairs are conversions and one subtraction per axis).
+int compute_frame_block(const f184gi_bounds& b, uint32_t dim, const float light_dir[3], FrameBlock* out) {
+    std::memset(out, 0, sizeof(*out));
+    compute_frame(b, dim, light_dir, &out->frame);
+    for (int a = 0; a < 3; ++a) {
+        out->pairs.org_h[a] = float(out->frame.origin[a]);
+        out->pairs.org_l[a] = float(out->frame.origin[a] - double(out->pairs.org_h[a]));
+    }
+    const double ivs = out->frame.inv_voxel_fixed * (1.0 / 256.0);
+    out->pairs.ivs_h = float(ivs);
+    out->pairs.ivs_l = float(ivs - double(out->pairs.ivs_h));
+    return F184GI_OK;
+}
+
 // The diffuse cones' march recurrence, step by step as the kernel's cone loop advances it: diameter
 // max(1, 2 tan (t + tl)) with the low part's product rounded first, step = step_factor * diameter and the
 // error-free sum t + step (this file is compiled without floating-point contraction).

@@ -45,6 +45,13 @@ struct FramePairs {
     float ivs_h, ivs_l;
 };
 constexpr size_t kFrameAllocBytes = sizeof(f184gi_grid_frame) + sizeof(FramePairs);
+// A grid's frame and its FP32 pairs as they lie on the device (computed on the host when the bounds are given).
+struct FrameBlock {
+    f184gi_grid_frame frame;
+    FramePairs pairs;
+};
+static_assert(sizeof(FrameBlock) == kFrameAllocBytes, "the frame block is the frame followed by its pairs");
+int compute_frame_block(const f184gi_bounds& b, uint32_t dim, const float light_dir[3], FrameBlock* out);
 inline const FramePairs* frame_pairs(const f184gi_grid_frame* d_frame) {
     return reinterpret_cast<const FramePairs*>(d_frame + 1);
 }

@@ -157,6 +157,15 @@ __global__ void frame_kernel(const int32_t* mm, f184gi_bounds bounds, int use_mm
     fp->ivs_l = __double2float_rn(__dsub_rn(ivs, double(fp->ivs_h)));
 }
 
+// The frame block computed on the host, passed by value and stored by one warp.
+__global__ void frame_store(FrameBlock fb, f184gi_grid_frame* out) {
+    constexpr uint32_t kWords = uint32_t(sizeof(FrameBlock) / 4);
+    static_assert(sizeof(FrameBlock) % 4 == 0, "whole words");
+    const uint32_t* src = reinterpret_cast<const uint32_t*>(&fb);
+    uint32_t* dst = reinterpret_cast<uint32_t*>(out);
+    for (uint32_t i = threadIdx.x; i < kWords; i += blockDim.x) dst[i] = src[i];
+}
+
 }  // namespace
 
 int frame_launch(const float* tri, uint64_t ntris, const f184gi_bounds* bounds, uint32_t dim,
@@ -171,9 +180,16 @@ int frame_launch(const float* tri, uint64_t ntris, const f184gi_bounds* bounds, 
         bounds_reduce<<<blocks, 256, 0, s>>>(tri, ntris * 9, mm);
         note_launches(2);
     } else {
-        b = *bounds;
+        // Given bounds: the frame on the host (the same bytes as the device kernel, which is one thread of FP64
+        // work on the critical path of a voxelization), stored by a kernel that takes it as its argument.
+        FrameBlock fb;
+        int rc = compute_frame_block(*bounds, dim, light_dir, &fb);
+        if (rc) return rc;
+        frame_store<<<1, 32, 0, s>>>(fb, d_frame);
+        note_launches(1);
+        return cuda_fail(cudaGetLastError(), "frame");
     }
-    frame_kernel<<<1, 32, 0, s>>>(mm, b, bounds ? 0 : 1, dim, light_dir[0], light_dir[1], light_dir[2], d_frame);
+    frame_kernel<<<1, 32, 0, s>>>(mm, b, 1, dim, light_dir[0], light_dir[1], light_dir[2], d_frame);
     note_launches(1);
     return cuda_fail(cudaGetLastError(), "frame");
 }

@@ -39,11 +39,22 @@ def test_frame_host_device_oracle_identical(case, oracle_l0):
 
 
 def test_frame_from_device_bounds(lib):
-    """bounds=None: the AABB is reduced on the device; the scene AABB is the room, so the frame is the same."""
+    """bounds=None: the AABB is reduced on the device and the frame computed there (given bounds, the host computes
+    it); the scene AABB is the room, so the frame is the same, and so is the traced image (the trace reads the
+    frame's FP32 pairs, written by the device kernel here and by the host with given bounds)."""
     c = Case(ntris=5000, nobj=40, dim=32, levels=5, res=256, width=64, height=32)
+    c.gbuffer()
     c.voxelize(bounds=False)
     fo = c.oracle_frame()
     assert bytes(c.gi.frame(c.grid)) == bytes(fo)
+    c.mip()
+    img_device_frame = c.trace().copy()
+    c.voxelize(bounds=True)
+    assert bytes(c.gi.frame(c.grid)) == bytes(fo)
+    c.mip()
+    img_host_frame = c.trace()
+    assert float(np.abs(img_host_frame).sum()) > 0
+    assert np.array_equal(img_device_frame.view(np.uint32), img_host_frame.view(np.uint32))
 
 
 def test_shadow_map_bit_exact(case, oracle_l0):
