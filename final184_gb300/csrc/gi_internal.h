@@ -179,17 +179,18 @@ inline void trace_view_set_inverses(TraceView& t, const double IP[16], const dou
 // (the register budget).  Every variant computes each pixel with the same arithmetic, so results are identical;
 // the batched launch picks the fastest by timing them on the work it serves.
 struct TraceVariant {
-    uint32_t tw, th, minb;
+    uint32_t tw, th, minb;  // CTA of tw x th pixels (warp tiles of tw x 32/tw), at least minb CTAs per SM
 };
 constexpr uint32_t kTraceVariantCount = 5;
 constexpr TraceVariant kTraceVariants[kTraceVariantCount] = {
-    {16, 8, 4}, {8, 12, 7}, {4, 24, 7}, {8, 16, 5}, {4, 32, 5}};
-// The one-shot launch's variant per chain: isotropic chains take 96-thread CTAs of 4x8-pixel warp tiles at 7 per SM
-// (FP32 1080p view 1.60 ms against 1.67 at 5 per SM, FP16 1.85 against 1.88; with every cone marched from one call
-// site the kernel is half the size, and at 80 registers the pixel's state between cones goes to local memory,
-// reloaded once per cone), anisotropic chains take 128-thread CTAs of 8x4 tiles at 5 per SM.
+    {16, 8, 4}, {4, 24, 7}, {4, 32, 7}, {8, 16, 5}, {4, 24, 9}};
+// The one-shot launch's variant per chain (per 1080p view; the CTAs per SM set the register budget):
+// isotropic FP32 chains take 96-thread CTAs of 4x8-pixel warp tiles at 7 per SM (80 registers, 8 resident:
+// 1.60 ms), isotropic FP16 chains 128-thread CTAs of 4x8 tiles at 7 per SM (72 registers); anisotropic chains
+// 128-thread CTAs of 8x4 tiles at 5 per SM (96 registers).  With every cone marched from one call site the
+// pixel's state between cones goes to local memory at these budgets, reloaded once per cone.
 constexpr uint32_t trace_default_variant(uint32_t fmt, bool aniso) {
-    return aniso ? 3u : (fmt == F184GI_FMT_F32 ? 2u : 2u);
+    return aniso ? 3u : (fmt == F184GI_FMT_F32 ? 1u : 2u);
 }
 const void* trace_kernel_fn(uint32_t fmt, bool aniso, uint32_t variant);
 const void* trace_kernel_count_fn(uint32_t fmt, bool aniso);  // instrumented, default variant's tile shape
