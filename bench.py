@@ -481,8 +481,9 @@ def run_gpu(args, cfg):
                      "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_source": peak_kind,
                      "algorithmic_bytes": alg[top],
                      "traffic": (tr * 1.0 if isinstance(tr, (int, float)) else None),
-                     "note": "far below the HBM roof: the trace is instruction-issue bound (ncu: ~66% issue-active, "
-                             "L1 hit ~96%, DRAM ~0.35% of peak; see `issue`); algorithmic bytes = G-buffer 10 B + output "
+                     "note": "far below the HBM roof: the trace is bound by instruction issue and the L1 load pipe "
+                             "together (ncu: ~69% issue-active, load-pipe wavefronts ~75%, L1 hit ~96%, DRAM ~0.4% of "
+                             "peak; see `issue`); algorithmic bytes = G-buffer 10 B + output "
                              "32 B per pixel + the whole chain once (upper bound of the touched part)",
                      "issue": issue_roofline(tr_inst, means[top], dev, clk),
                      "sampled": {"bytes": int(sampled), "achieved": round(sampled / (means[top] * 1e-3) / 1e9, 1),
