@@ -186,11 +186,11 @@ constexpr TraceVariant kTraceVariants[kTraceVariantCount] = {
     {16, 8, 4}, {4, 24, 7}, {4, 32, 7}, {8, 16, 5}, {4, 24, 9}};
 // The one-shot launch's variant per chain (per 1080p view; the CTAs per SM set the register budget):
 // isotropic FP32 chains take 96-thread CTAs of 4x8-pixel warp tiles at 7 per SM (80 registers, 8 resident:
-// 1.60 ms), isotropic FP16 chains 128-thread CTAs of 4x8 tiles at 7 per SM (72 registers); anisotropic chains
-// 128-thread CTAs of 8x4 tiles at 5 per SM (96 registers).  With every cone marched from one call site the
-// pixel's state between cones goes to local memory at these budgets, reloaded once per cone.
+// 1.60 ms), FP16 and anisotropic chains 128-thread CTAs of 4x8 tiles at 7 per SM (72 registers; the 512^3
+// anisotropic FP16 4K view 15.3 ms against 15.7 with 8x4 tiles at 5 per SM).  With every cone marched from one
+// call site the pixel's state between cones goes to local memory at these budgets, reloaded once per cone.
 constexpr uint32_t trace_default_variant(uint32_t fmt, bool aniso) {
-    return aniso ? 3u : (fmt == F184GI_FMT_F32 ? 1u : 2u);
+    return aniso ? 2u : (fmt == F184GI_FMT_F32 ? 1u : 2u);
 }
 const void* trace_kernel_fn(uint32_t fmt, bool aniso, uint32_t variant);
 const void* trace_kernel_count_fn(uint32_t fmt, bool aniso);  // instrumented, default variant's tile shape

@@ -374,18 +374,9 @@ __device__ float4 cone(const GridRef& g, const uint32_t* lut, const TraceConsts&
         // quadrilinear: (1 - f) * level l0 + f * level l0 + 1, the level weights folded into the tap weights
         const bool two = f > 0.0f && l0 + 1 < glevels;
         float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (ANISO) {
-            // the two levels share one copy of the (three-volume) sampling code: the instruction cache
-            // outweighs the overlap of two inlined copies here, not in the single-volume kernel
-            const uint32_t nl = two ? 2u : 1u;
-#pragma unroll 1
-            for (uint32_t k = 0; k < nl; ++k)
-                level_sample<FMT, ANISO>(g, lut, l0 + k, oi, x, dir, k ? f : (two ? 1.0f - f : 1.0f), s);
-        } else {
-            level_sample<FMT, ANISO>(g, lut, l0, oi, x, dir, two ? 1.0f - f : 1.0f, s);
-            // the finer level's neighbour above is never level 0: its copy carries the ringed path only
-            if (two) level_sample<FMT, ANISO, true>(g, lut, l0 + 1, oi, x, dir, f, s);
-        }
+        level_sample<FMT, ANISO>(g, lut, l0, oi, x, dir, two ? 1.0f - f : 1.0f, s);
+        // the finer level's neighbour above is never level 0: its copy carries the ringed path only
+        if (two) level_sample<FMT, ANISO, true>(g, lut, l0 + 1, oi, x, dir, f, s);
         if (FMT != F184GI_FMT_F32) s.w *= kAlphaScale<FMT>;  // the unorm16 opacity sum, scaled once
         float tr = 1.0f - alpha;
         cr += tr * s.x;
