@@ -220,3 +220,33 @@ def test_anisotropic_chain_and_trace(lib, orc, fmt):
     print("anisotropic %s trace:" % ["fp32", "fp16"][fmt], e)
     assert e.ok(), str(e)
     assert ref[0, ..., :3].mean() > 1e-3  # lit scene
+
+
+@pytest.mark.parametrize("seed,ntris,nobj,dim,res", [(11, 20000, 20, 64, 512), (12, 30000, 8, 128, 1024),
+                                                     (14, 8000, 3, 64, 512), (16, 20000, 50, 32, 256)])
+def test_counts_and_shadow_bit_exact_across_scenes(lib, orc, seed, ntris, nobj, dim, res):
+    """Scenes of few large objects (long triangles crossing many bricks: the voxelizer's 64-bit edge tests and its
+    items spread over several threads) and of many small ones: occupancy/counts and the shadow map bit-exact."""
+    import torch
+
+    import final184_gb300 as g
+
+    dev = torch.device("cuda:0")
+    gi = g.VoxelGI(0)
+    sc = g.SyntheticScene(seed, ntris, nobj)
+    tri = torch.from_numpy(sc.tri_xyz).to(dev)
+    alb = torch.from_numpy(sc.albedo.view(np.int32)).to(dev)
+    grid = gi.create_grid(dim, 5, g.FMT_F32, 0, res, g.GRID_KEEP_COUNTS)
+    gi.voxelize(grid, tri.data_ptr(), alb.data_ptr(), sc.ntris, sc.light, bounds=sc.bounds)
+    gi.sync()
+    cnt, shadow = gi.read_counts(grid), gi.read_shadow(grid)
+    gi.close()
+    b = sc.bounds
+    fo = orc.grid_frame(orc.make_bounds((b.min.x, b.min.y, b.min.z), (b.max.x, b.max.y, b.max.z)), dim,
+                        np.array(sc.light.direction, np.float32))
+    sd = orc.shadow_depth(orc.raster(orc.frame_matrix(fo), res, res, sc.tri_xyz))
+    _, ocnt = orc.voxelize(fo, dim, res, sc.tri_xyz, sc.albedo,
+                           orc.make_light(list(sc.light.luminance), list(sc.light.direction)), sd)
+    assert int((ocnt > 0).sum()) > 1000
+    assert np.array_equal(cnt, ocnt), "counts differ in %d voxels" % int((cnt != ocnt).sum())
+    assert np.array_equal(shadow.view(np.uint32), sd.astype(np.float32).view(np.uint32))
