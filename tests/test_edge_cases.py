@@ -11,7 +11,8 @@
 - views past the size limits (a side over 16384 pixels for the trace, over 8192 for the G-buffer raster) are
   refused on the host with F184GI_ERR_INVALID, before any launch;
 - a bounded device wait that expires is reported as F184GI_ERR_TIMEOUT by the next sync, and the context goes on
-  working (the failure path of the library's bounded waits, without a GPU fault).
+  working (the failure path of the library's bounded waits, without a GPU fault);
+- the smallest grids (16^3, one to four levels; 32^3), FP32 and FP16: counts bit-exact, traces within REL_TOL.
 """
 import numpy as np
 import pytest
@@ -280,3 +281,26 @@ def test_non_finite_triangles_skipped_and_reported(lib, orc):
         srv.add_scene(0, g.GridDesc(32, 5, g.FMT_F16, 0, 256, 0), tri, c.sc.albedo, c.sc.bounds, c.sc.light)
     assert e.value.code == g._abi.ERR_INVALID
     srv.close()
+
+
+@pytest.mark.parametrize("dim,levels,fmt", [(16, 1, 0), (16, 4, 0), (16, 4, 1), (32, 5, 1)])
+def test_tiny_grids_against_oracle(lib, orc, dim, levels, fmt):
+    """The smallest grids (16^3: eight 8^3 bricks, the coarsest level 2^3), with one level (no quadrilinear blend
+    at all) up to the full chain, FP32 and FP16: occupancy and counts bit-exact, the traced view within REL_TOL of
+    the oracle."""
+    c = Case(ntris=4000, nobj=30, dim=dim, levels=levels, res=128, width=96, height=64, fmt=fmt)
+    c.voxelize()
+    c.mip()
+    c.gbuffer()
+    got = c.trace()
+    fo = c.oracle_frame()
+    sd = orc.shadow_depth(orc.raster(orc.frame_matrix(fo), c.res, c.res, c.sc.tri_xyz))
+    l0, cnt = orc.voxelize(fo, dim, c.res, c.sc.tri_xyz, c.sc.albedo, c.oracle_light(), sd)
+    assert np.array_equal(c.gi.read_counts(c.grid), cnt)
+    chain, _ = orc.mip(l0, levels)
+    dep, nrm, rgh, _ = c.gbuffer_host()
+    ref = orc.trace(fo, dim, levels, chain, c.V, c.P, c.W, c.H, dep, nrm, rgh)
+    assert ref[0, ..., :3].max() > 0
+    e = rel_err(got, ref)
+    print("dim %d, %d level(s), %s:" % (dim, levels, "FP16" if fmt else "FP32"), e)
+    assert e.ok(), str(e)
