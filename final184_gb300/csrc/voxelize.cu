@@ -397,6 +397,7 @@ __device__ void item_part(const TriRec& r, const int64_t base[3], const int32_t 
 }
 
 constexpr int kChunk = 128;  // items prepared per round (at most one per thread; = threads per CTA)
+constexpr uint32_t kRowCap = 1024;  // rows per round mapped to their item by table (later ones by search)
 
 // Eight CTAs per SM (64 registers, 26 KB of shared memory each): a brick's phases are separated by barriers at
 // which most of its threads wait, so other bricks' CTAs are what keeps the SM busy (0.59 -> 0.40 ms per 256^3
@@ -410,6 +411,7 @@ __global__ void __launch_bounds__(kChunk, 8) vox_bricks(VoxScratch sc, const f18
     __shared__ uint32_t s_cnt[512];
     __shared__ ItemSetup s_item[kChunk];
     __shared__ uint32_t s_start[kChunk + 1];       // prefix of x-rows per prepared item
+    __shared__ uint8_t s_rowitem[kRowCap];         // item slot of each of the first kRowCap rows
     const uint32_t m = dirty ? dirty[blockIdx.x] : blockIdx.x;
     const uint32_t nb = dim >> 3;
     if (m >= nb * nb * nb) return;
@@ -442,7 +444,7 @@ __global__ void __launch_bounds__(kChunk, 8) vox_bricks(VoxScratch sc, const f18
         const uint32_t nchunk = min(end - c0, uint32_t(kChunk));
         const uint32_t per = nchunk <= kChunk / 4 ? 4u : (nchunk <= kChunk / 2 ? 2u : 1u);
         const uint32_t slot = threadIdx.x / per, part = threadIdx.x % per;
-        uint32_t nrows = 0;
+        uint32_t nrows = 0, item_rows = 0;
         unsigned long long mks[3] = {0ull, 0ull, 0ull};
         bool valid = false;
         if (slot < nchunk) {
@@ -455,7 +457,8 @@ __global__ void __launch_bounds__(kChunk, 8) vox_bricks(VoxScratch sc, const f18
             valid = l0[0] <= l1[0] && l0[1] <= l1[1] && l0[2] <= l1[2];
             if (valid) {
                 item_part(r, base, l0, l1, int(part), int(per), part == per - 1, mks, s_item[slot]);
-                if (part == 0) nrows = uint32_t((l1[1] - l0[1] + 1) * (l1[2] - l0[2] + 1));
+                item_rows = uint32_t((l1[1] - l0[1] + 1) * (l1[2] - l0[2] + 1));
+                if (part == 0) nrows = item_rows;
             }
         }
 #pragma unroll
@@ -486,16 +489,28 @@ __global__ void __launch_bounds__(kChunk, 8) vox_bricks(VoxScratch sc, const f18
             __syncthreads();
         }
         const uint32_t total = s_start[kChunk];
+        // the item of each of the first kRowCap rows, written by the item's threads (its rows are contiguous)
+        if (item_rows) {
+            const uint32_t st = s_start[slot * per];
+            for (uint32_t j = part; j < item_rows && st + j < kRowCap; j += per) s_rowitem[st + j] = uint8_t(slot);
+        }
+        __syncthreads();
         // phase 2: all threads share the x-rows (item, y, z) of the chunk's voxel boxes evenly.  A row's candidate
         // voxels are the bits of one byte: projection 2 holds x + 8y (byte y), projection 1 holds z + 8x (the
         // bits z, z + 8, .., z + 56, gathered into a byte by one multiply), projection 0 one bit y + 8z.
         for (uint32_t rr = threadIdx.x; rr < total; rr += blockDim.x) {
-            uint32_t lo = 0, hi = kChunk;  // the item k with s_start[k] <= rr < s_start[k + 1]
-            while (hi - lo > 1) {
-                uint32_t mid = (lo + hi) >> 1;
-                if (s_start[mid] <= rr) lo = mid; else hi = mid;
+            uint32_t lo;  // the item's first thread: the k with s_start[k] <= rr < s_start[k + 1]
+            if (rr < kRowCap) {
+                lo = uint32_t(s_rowitem[rr]) * per;
+            } else {
+                lo = 0;
+                uint32_t hi = kChunk;
+                while (hi - lo > 1) {
+                    uint32_t mid = (lo + hi) >> 1;
+                    if (s_start[mid] <= rr) lo = mid; else hi = mid;
+                }
             }
-            const ItemSetup& is = s_item[lo / per];  // lo: the item's first thread
+            const ItemSetup& is = s_item[lo / per];
             const uint32_t local = rr - s_start[lo];
             const uint32_t ey = is.ext[1];
             // local / ey for local < 64, ey <= 8: the quotient's fraction stays >= 1/16 from an integer
