@@ -23,7 +23,10 @@ constexpr int kTile = 16;
 constexpr double kGuard = 16.0;
 constexpr uint32_t kNone = 0xffffffffu;
 constexpr int kBigCells = 8;  // records touching more tiles than this are binned by a whole CTA
-constexpr uint32_t kStage = 256;  // records staged per round by raster_tiles (one per thread)
+constexpr uint32_t kStage = 256;
+// ceil(65536 / w) for the clipped box widths w = 1..16 of a tile: p / w = (p * c_wmagic[w]) >> 16 for p < 256
+__constant__ uint32_t c_wmagic[17] = {0,    65536, 32768, 21846, 16384, 13108, 10923, 9363, 8192,
+                                      7282, 6554,  5958,  5462,  5042,  4682,  4370,  4096};  // records staged per round by raster_tiles (one per thread)
 
 struct SubTri {
     int32_t X[3], Y[3];
@@ -162,8 +165,12 @@ __device__ __forceinline__ bool snap_f(const V4f (&v)[3], uint32_t W, uint32_t H
 }
 
 // Edge function of edge (a -> b) at fixed-point point (px, py).
+// Edge function of (a, b) at p (1/16-pixel units): every factor fits 32 bits (snapped vertices and pixel centres
+// lie within the guard band, |difference| < 2^22), so each product is one 32 x 32 -> 64-bit multiply.
 __device__ __forceinline__ int64_t edge(const SubTri& s, int a, int b, int64_t px, int64_t py) {
-    return int64_t(s.X[b] - s.X[a]) * (py - s.Y[a]) - int64_t(s.Y[b] - s.Y[a]) * (px - s.X[a]);
+    const int32_t dx = s.X[b] - s.X[a], dy = s.Y[b] - s.Y[a];
+    const int32_t ry = int32_t(py) - s.Y[a], rx = int32_t(px) - s.X[a];
+    return int64_t(dx) * int64_t(ry) - int64_t(dy) * int64_t(rx);
 }
 
 // Can the triangle cover any pixel centre of tile (tx, ty)?  Rejects tiles wholly outside one edge.
@@ -343,7 +350,7 @@ __global__ void __launch_bounds__(256) raster_tiles(RasterScratch sc, uint32_t t
             const int64_t E0 = edge(s, 1, 2, Px0, Py0), E1 = edge(s, 2, 0, Px0, Py0), E2 = edge(s, 0, 1, Px0, Py0);
             const int32_t ax0 = s.X[2] - s.X[1], ay0 = s.Y[2] - s.Y[1], ax1 = s.X[0] - s.X[2], ay1 = s.Y[0] - s.Y[2],
                           ax2 = s.X[1] - s.X[0], ay2 = s.Y[1] - s.Y[0];
-            const uint32_t wmagic = (65536u + uint32_t(w) - 1u) / uint32_t(w);  // p / w = (p * wmagic) >> 16, p < 256
+            const uint32_t wmagic = c_wmagic[w];  // p / w = (p * wmagic) >> 16, p < 256
             for (int p = int(sub); p < npx; p += int(LANES)) {
                 const int ly = int((uint32_t(p) * wmagic) >> 16), lx = p - ly * w;
                 const int px = x0 + lx, py = y0 + ly;
