@@ -288,7 +288,12 @@ int f184gi_create(const f184gi_config* cfg, f184gi_ctx** out) {
     }
     c->d_status = static_cast<uint32_t*>(st);
     cudaMemset(c->d_status, 0, 4);
-    if ((e = cudaStreamCreateWithFlags(&c->aux, cudaStreamNonBlocking)) != cudaSuccess ||
+    // The lists chain is a run of short latency-bound kernels: at the highest stream priority its blocks are
+    // scheduled ahead of another request's trace when two requests overlap on the device (two request lanes:
+    // 2.35 -> 2.29 ms per plain-large request; one lane unchanged).
+    int least_prio = 0, greatest_prio = 0;
+    cudaDeviceGetStreamPriorityRange(&least_prio, &greatest_prio);
+    if ((e = cudaStreamCreateWithPriority(&c->aux, cudaStreamNonBlocking, greatest_prio)) != cudaSuccess ||
         (e = cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming)) != cudaSuccess ||
         (e = cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming)) != cudaSuccess) {
         f184gi_destroy(c);

@@ -23,10 +23,10 @@ constexpr int kTile = 16;
 constexpr double kGuard = 16.0;
 constexpr uint32_t kNone = 0xffffffffu;
 constexpr int kBigCells = 8;  // records touching more tiles than this are binned by a whole CTA
-constexpr uint32_t kStage = 256;
+constexpr uint32_t kStage = 256;  // records staged per round by raster_tiles (one per thread)
 // ceil(65536 / w) for the clipped box widths w = 1..16 of a tile: p / w = (p * c_wmagic[w]) >> 16 for p < 256
 __constant__ uint32_t c_wmagic[17] = {0,    65536, 32768, 21846, 16384, 13108, 10923, 9363, 8192,
-                                      7282, 6554,  5958,  5462,  5042,  4682,  4370,  4096};  // records staged per round by raster_tiles (one per thread)
+                                      7282, 6554,  5958,  5462,  5042,  4682,  4370,  4096};
 
 struct SubTri {
     int32_t X[3], Y[3];
@@ -164,7 +164,6 @@ __device__ __forceinline__ bool snap_f(const V4f (&v)[3], uint32_t W, uint32_t H
     return snap_finish(X, Y, Z, W, H, tri, s);
 }
 
-// Edge function of edge (a -> b) at fixed-point point (px, py).
 // Edge function of (a, b) at p (1/16-pixel units): every factor fits 32 bits (snapped vertices and pixel centres
 // lie within the guard band, |difference| < 2^22), so each product is one 32 x 32 -> 64-bit multiply.
 __device__ __forceinline__ int64_t edge(const SubTri& s, int a, int b, int64_t px, int64_t py) {
