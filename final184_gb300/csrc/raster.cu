@@ -22,7 +22,8 @@ namespace {
 constexpr int kTile = 16;
 constexpr double kGuard = 16.0;
 constexpr uint32_t kNone = 0xffffffffu;
-constexpr int kBigCells = 8;  // records touching more tiles than this are binned by a whole CTA
+constexpr int kBigCells = 8;     // records touching more tiles than this are binned by a warp ...
+constexpr int kHugeCells = 512;  // ... or, above this many tiles, by a whole CTA
 constexpr uint32_t kStage = 256;  // records staged per round by raster_tiles (one per thread)
 // ceil(65536 / w) for the clipped box widths w = 1..16 of a tile: p / w = (p * c_wmagic[w]) >> 16 for p < 256
 __constant__ uint32_t c_wmagic[17] = {0,    65536, 32768, 21846, 16384, 13108, 10923, 9363, 8192,
@@ -196,8 +197,10 @@ struct RasterScratch {
     uint32_t* total;       // [1]
     uint32_t* scan_tmp;
     uint32_t* list;
-    uint32_t* big;         // records with more than kBigCells tiles (binned by bin_big)
+    uint32_t* big;         // records with more than kHugeCells tiles (binned by raster_bin_big, a CTA each)
     uint32_t* big_count;   // [1]
+    uint32_t* mid;         // records with kBigCells < tiles <= kHugeCells (raster_bin_big, a warp each)
+    uint32_t* mid_count;   // [1]
     uint64_t list_cap;
     uint64_t ovf_cap;
 };
@@ -290,8 +293,9 @@ __global__ void __launch_bounds__(128) raster_bin(uint64_t ntris, RasterScratch 
     const int ntx = s.x1 / kTile - tx0 + 1, ncell = ntx * (s.y1 / kTile - ty0 + 1);
     if (ncell > kBigCells) {
         if (!emit) {
-            uint32_t k = atomicAdd(sc.big_count, 1u);
-            if (k < uint32_t(nrec)) sc.big[k] = uint32_t(r);
+            const bool huge = ncell > kHugeCells;
+            uint32_t k = atomicAdd(huge ? sc.big_count : sc.mid_count, 1u);
+            if (k < uint32_t(nrec)) (huge ? sc.big : sc.mid)[k] = uint32_t(r);
         }
         return;
     }
@@ -299,6 +303,9 @@ __global__ void __launch_bounds__(128) raster_bin(uint64_t ntris, RasterScratch 
         bin_cell(s, uint32_t(r), tx0 + c % ntx, ty0 + c / ntx, ncell > 2, tiles_x, sc, status, emit != 0);
 }
 
+// Records of more than kHugeCells tiles take a CTA each; the others above kBigCells take a warp each, all in one
+// wave (a record of a few dozen tiles would leave most of a CTA idle, and a CTA walking them one after another
+// waits on each record's loads in turn).
 __global__ void __launch_bounds__(256) raster_bin_big(RasterScratch sc, uint32_t tiles_x, uint32_t* status, int emit) {
     const uint32_t nbig = *sc.big_count;
     for (uint32_t i = blockIdx.x; i < nbig; i += gridDim.x) {
@@ -309,40 +316,97 @@ __global__ void __launch_bounds__(256) raster_bin_big(RasterScratch sc, uint32_t
         for (int c = int(threadIdx.x); c < ncell; c += int(blockDim.x))
             bin_cell(s, r, tx0 + c % ntx, ty0 + c / ntx, true, tiles_x, sc, status, emit != 0);
     }
+    const uint32_t nmid = *sc.mid_count, wpb = blockDim.x / 32, lane = threadIdx.x & 31;
+    for (uint32_t i = blockIdx.x * wpb + threadIdx.x / 32; i < nmid; i += gridDim.x * wpb) {
+        const uint32_t r = sc.mid[i];
+        const SubTri s = sc.recs[r];
+        const int tx0 = s.x0 / kTile, ty0 = s.y0 / kTile;
+        const int ntx = s.x1 / kTile - tx0 + 1, ncell = ntx * (s.y1 / kTile - ty0 + 1);
+        for (int c = int(lane); c < ncell; c += 32)
+            bin_cell(s, r, tx0 + c % ntx, ty0 + c / ntx, true, tiles_x, sc, status, emit != 0);
+    }
 }
+
+// The clipped pixel box of record s in tile (tx, ty): false when empty.
+__device__ __forceinline__ bool tile_box(const SubTri& s, int tx, int ty, int& x0, int& x1, int& y0, int& y1) {
+    x0 = max(int(s.x0), tx * kTile), x1 = min(int(s.x1), tx * kTile + kTile - 1);
+    y0 = max(int(s.y0), ty * kTile), y1 = min(int(s.y1), ty * kTile + kTile - 1);
+    return x0 <= x1 && y0 <= y1;
+}
+
+// Key of record s at pixel (px, py) when its centre is covered (inclusive edges), else ~0.
+__device__ __forceinline__ unsigned long long pixel_key(const SubTri& s, int px, int py, int64_t E0, int64_t E1,
+                                                        int64_t E2) {
+    if (E0 < 0 || E1 < 0 || E2 < 0) return ~0ull;
+    // |P - X0| < 2^21: the int32 -> float conversion is exact (an int64 conversion would use the FP64 pipe)
+    const int32_t dX = (16 * px + 8) - s.X[0], dY = (16 * py + 8) - s.Y[0];
+    float z = __fadd_rn(__fadd_rn(s.z0, __fmul_rn(s.a, float(dX))), __fmul_rn(s.b, float(dY)));
+    if (!(z > 0.0f)) z = 0.0f;  // also maps -0 and NaN to +0
+    if (z > 1.0f) z = 1.0f;
+    return (uint64_t(__float_as_uint(z)) << 32) | s.tri;
+}
+
+// Records whose box covers at least this many of a tile's 256 pixels are tested by every thread at its own pixel
+constexpr int kWidePx = 128;
 
 __global__ void __launch_bounds__(256) raster_tiles(RasterScratch sc, uint32_t tiles_x, uint32_t W, uint32_t H,
                                                     unsigned long long* __restrict__ keys) {
     __shared__ unsigned long long sk[kTile * kTile];
+    __shared__ SubTri srec[kStage];
+    __shared__ uint16_t s_wide[kStage], s_narrow[kStage];
+    __shared__ uint32_t s_cnt[2][2];  // [round parity][wide, narrow]
     const uint32_t tile = blockIdx.x;
     const int tx = int(tile % tiles_x), ty = int(tile / tiles_x);
     sk[threadIdx.x] = ~0ull;
+    if (threadIdx.x < 4) s_cnt[threadIdx.x >> 1][threadIdx.x & 1] = 0;
     __syncthreads();
     const uint32_t beg = sc.tile_start[tile], cnt = sc.tile_count[tile];
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t end = uint32_t(min(uint64_t(beg) + cnt, sc.list_cap));
-    // the tile's records are staged kStage at a time, one per thread (the two dependent loads of every record
-    // in flight together), then walked from shared memory by the warps
-    __shared__ SubTri srec[kStage];
-    for (uint32_t c0 = beg; c0 < end; c0 += kStage) {
+    // this thread's pixel, for the wide records
+    const int mpx = tx * kTile + int(threadIdx.x % kTile), mpy = ty * kTile + int(threadIdx.x / kTile);
+    unsigned long long mine = ~0ull;
+    uint32_t round = 0;
+    // The tile's records are staged kStage at a time, one per thread (the two dependent loads of every record in
+    // flight together), and sorted by their box in the tile: a wide record (a floor under the whole map covers
+    // every tile) is tested by all 256 threads at their own pixels, keeping the minimum in a register, so no
+    // warp walks 256 pixels alone while the others wait at the barrier; the narrow ones are walked by the warps.
+    for (uint32_t c0 = beg; c0 < end; c0 += kStage, ++round) {
         const uint32_t n = min(end - c0, uint32_t(kStage));
-        if (threadIdx.x < n) srec[threadIdx.x] = sc.recs[sc.list[c0 + threadIdx.x]];
+        uint32_t* cnts = s_cnt[round & 1];
+        if (threadIdx.x < n) {
+            const SubTri s = sc.recs[sc.list[c0 + threadIdx.x]];
+            srec[threadIdx.x] = s;
+            int x0, x1, y0, y1;
+            if (tile_box(s, tx, ty, x0, x1, y0, y1)) {
+                if ((x1 - x0 + 1) * (y1 - y0 + 1) >= kWidePx)
+                    s_wide[atomicAdd(&cnts[0], 1u)] = uint16_t(threadIdx.x);
+                else
+                    s_narrow[atomicAdd(&cnts[1], 1u)] = uint16_t(threadIdx.x);
+            }
+        }
         __syncthreads();
-        // Each warp rasterizes GROUPS records at once, LANES lanes per record: the per-record set-up (clipping,
-        // the edge functions at the box corner, the row divisor) is spread over the warp's lanes instead of being
-        // repeated by all 32 for one record, and the record's pixels are walked LANES at a time (4 records of 8
-        // lanes: 0.82 -> 0.76 ms per 500k-triangle voxelization, whose shadow raster is on the critical path;
-        // 2 of 16: 0.77, 8 of 4: 0.81).
+        const uint32_t nwide = cnts[0], nnarrow = cnts[1];
+        if (threadIdx.x < 2) s_cnt[(round + 1) & 1][threadIdx.x] = 0;  // the next round's counters
+        for (uint32_t k = 0; k < nwide; ++k) {
+            const SubTri& s = srec[s_wide[k]];
+            const int64_t Px = int64_t(mpx) * 16 + 8, Py = int64_t(mpy) * 16 + 8;
+            const unsigned long long key = pixel_key(s, mpx, mpy, edge(s, 1, 2, Px, Py), edge(s, 2, 0, Px, Py),
+                                                     edge(s, 0, 1, Px, Py));
+            mine = key < mine ? key : mine;
+        }
+        // Each warp rasterizes GROUPS narrow records at once, LANES lanes per record: the per-record set-up
+        // (clipping, the edge functions at the box corner, the row divisor) is spread over the warp's lanes
+        // instead of being repeated by all 32 for one record, and the record's pixels are walked LANES at a time.
         constexpr uint32_t GROUPS = 4, LANES = 32 / GROUPS;
         const uint32_t grp = lane / LANES, sub = lane % LANES;
-        for (uint32_t r0 = warp * GROUPS; r0 < n; r0 += 8 * GROUPS) {
+        for (uint32_t r0 = warp * GROUPS; r0 < nnarrow; r0 += 8 * GROUPS) {
             const uint32_t r = r0 + grp;
-            if (r >= n) continue;
-            const SubTri& s = srec[r];
-            int x0 = max(int(s.x0), tx * kTile), x1 = min(int(s.x1), tx * kTile + kTile - 1);
-            int y0 = max(int(s.y0), ty * kTile), y1 = min(int(s.y1), ty * kTile + kTile - 1);
-            if (x0 > x1 || y0 > y1) continue;
-            int w = x1 - x0 + 1, npx = w * (y1 - y0 + 1);
+            if (r >= nnarrow) continue;
+            const SubTri& s = srec[s_narrow[r]];
+            int x0, x1, y0, y1;
+            tile_box(s, tx, ty, x0, x1, y0, y1);
+            const int w = x1 - x0 + 1, npx = w * (y1 - y0 + 1);
             // Edge functions at the box's first pixel centre (int64), stepped exactly in int32 within the tile:
             // |edge delta| < 2^21 and the offsets are below 16 pixels (256 units), so each step term is < 2^29.
             const int64_t Px0 = int64_t(x0) * 16 + 8, Py0 = int64_t(y0) * 16 + 8;
@@ -354,23 +418,18 @@ __global__ void __launch_bounds__(256) raster_tiles(RasterScratch sc, uint32_t t
                 const int ly = int((uint32_t(p) * wmagic) >> 16), lx = p - ly * w;
                 const int px = x0 + lx, py = y0 + ly;
                 const int32_t ox = 16 * lx, oy = 16 * ly;
-                if (E0 + int64_t(ax0 * oy - ay0 * ox) < 0 || E1 + int64_t(ax1 * oy - ay1 * ox) < 0 ||
-                    E2 + int64_t(ax2 * oy - ay2 * ox) < 0)
-                    continue;
-                // |P - X0| < 2^21: the int32 -> float conversion is exact (an int64 conversion would use the FP64
-                // pipe)
-                const int32_t dX = (16 * px + 8) - s.X[0], dY = (16 * py + 8) - s.Y[0];
-                float z = __fadd_rn(__fadd_rn(s.z0, __fmul_rn(s.a, float(dX))), __fmul_rn(s.b, float(dY)));
-                if (!(z > 0.0f)) z = 0.0f;  // also maps -0 and NaN to +0
-                if (z > 1.0f) z = 1.0f;
-                unsigned long long key = (uint64_t(__float_as_uint(z)) << 32) | s.tri;
-                atomicMin(&sk[(py - ty * kTile) * kTile + (px - tx * kTile)], key);
+                const unsigned long long key =
+                    pixel_key(s, px, py, E0 + int64_t(ax0 * oy - ay0 * ox), E1 + int64_t(ax1 * oy - ay1 * ox),
+                              E2 + int64_t(ax2 * oy - ay2 * ox));
+                if (key != ~0ull) atomicMin(&sk[(py - ty * kTile) * kTile + (px - tx * kTile)], key);
             }
         }
         __syncthreads();  // srec is restaged for the next records
     }
-    int px = tx * kTile + int(threadIdx.x % kTile), py = ty * kTile + int(threadIdx.x / kTile);
-    if (px < int(W) && py < int(H)) keys[uint64_t(py) * W + px] = sk[threadIdx.x];
+    if (mpx < int(W) && mpy < int(H)) {
+        const unsigned long long k = sk[threadIdx.x];
+        keys[uint64_t(mpy) * W + mpx] = k < mine ? k : mine;
+    }
 }
 
 template <class T>
@@ -384,14 +443,14 @@ T* carve(char*& p, uint64_t n) {
 }  // namespace
 
 static uint64_t ovf_capacity(uint64_t ntris) { return ntris / 2 + 4096; }
-static constexpr uint32_t kBigBlocks = 2 * 152;
+static constexpr uint32_t kBigBlocks = 8 * 152;
 static uint64_t list_capacity(uint64_t ntris, uint32_t ntiles) { return ntris * 8 + uint64_t(ntiles) * 16 + 65536; }
 
 size_t raster_scratch_bytes(uint64_t ntris, uint32_t W, uint32_t H) {
     uint32_t tiles = ((W + kTile - 1) / kTile) * ((H + kTile - 1) / kTile);
     uint64_t recs = ntris + ovf_capacity(ntris);
     return recs * sizeof(SubTri) + uint64_t(tiles) * 12 + scan_scratch_bytes(tiles) + list_capacity(ntris, tiles) * 4 +
-           recs * 4 + 20 * 256;
+           2 * recs * 4 + 22 * 256;
 }
 
 int raster_launch(const RasterJob& job, void* scratch, size_t scratch_bytes, uint32_t* d_status, cudaStream_t s) {
@@ -416,7 +475,10 @@ int raster_launch(const RasterJob& job, void* scratch, size_t scratch_bytes, uin
     sc.list = carve<uint32_t>(p, sc.list_cap);
     sc.big = carve<uint32_t>(p, job.ntris + sc.ovf_cap);
     sc.big_count = carve<uint32_t>(p, 1);
+    sc.mid = carve<uint32_t>(p, job.ntris + sc.ovf_cap);
+    sc.mid_count = carve<uint32_t>(p, 1);
     cudaMemsetAsync(sc.big_count, 0, 4, s);
+    cudaMemsetAsync(sc.mid_count, 0, 4, s);
     cudaMemsetAsync(sc.ovf_count, 0, 4, s);
     cudaMemsetAsync(sc.tile_count, 0, size_t(ntiles) * 4, s);
     cudaMemsetAsync(sc.tile_fill, 0, size_t(ntiles) * 4, s);

@@ -40,8 +40,12 @@ struct VoxScratch {
     uint32_t* scan_tmp;
     uint32_t* dirty_mask;  // nbricks bits, null = all bricks
     uint32_t* list;
-    uint32_t* big;        // triangles with more than kWarpCells bricks (binned by vox_bin_big)
+    uint32_t* big;        // triangles with more than kMidCells bricks (binned by vox_bin_big, a CTA each)
     uint32_t* big_count;  // [1]
+    uint32_t* mid;        // triangles with kThreadCells < bricks <= kMidCells (vox_bin_big, a warp each)
+    uint32_t* mid_count;  // [1]
+    uint2* mid_bits;      // per mid entry: which of its (up to 64) bricks the count pass listed
+    uint8_t* bits;        // per triangle of at most kThreadCells bricks: which of them the count pass listed
     uint64_t list_cap;
 };
 
@@ -97,17 +101,20 @@ __device__ __forceinline__ void voxel_range(const int32_t* q, uint32_t dim, int3
     }
 }
 
-constexpr int kWarpCells = 8;  // triangles overlapping more bricks than this are binned by a whole CTA
+constexpr int kThreadCells = 8;  // triangles overlapping at most this many bricks are binned by one thread,
+constexpr int kMidCells = 64;    // at most this many by a warp, more by a whole CTA
 
-__device__ __forceinline__ void bin_brick(const int32_t* q, uint32_t t, int bx, int by, int bz, bool test,
-                                          const VoxScratch& sc, uint32_t* status, bool emit) {
-    uint32_t m = morton3(bx, by, bz);
-    if (sc.dirty_mask && !((sc.dirty_mask[m >> 5] >> (m & 31)) & 1u)) return;
-    if (test) {
-        const int64_t c[3] = {bx * kBrickFix + kBrickFix / 2, by * kBrickFix + kBrickFix / 2,
-                              bz * kBrickFix + kBrickFix / 2};
-        if (!tri_box_sat(q, c, kBrickFix / 2)) return;
-    }
+// Is brick (bx, by, bz) listed for the triangle: inside the dirty set and (test) overlapped by the triangle?
+__device__ __forceinline__ bool brick_hit(const int32_t* q, int bx, int by, int bz, bool test, const VoxScratch& sc) {
+    const uint32_t m = morton3(bx, by, bz);
+    if (sc.dirty_mask && !((sc.dirty_mask[m >> 5] >> (m & 31)) & 1u)) return false;
+    if (!test) return true;
+    const int64_t c[3] = {bx * kBrickFix + kBrickFix / 2, by * kBrickFix + kBrickFix / 2, bz * kBrickFix + kBrickFix / 2};
+    return tri_box_sat(q, c, kBrickFix / 2);
+}
+
+// Count (emit = false) or list (emit = true) triangle t in brick m.
+__device__ __forceinline__ void brick_add(uint32_t t, uint32_t m, const VoxScratch& sc, uint32_t* status, bool emit) {
     if (!emit) {
         atomicAdd(&sc.brick_count[m], 1u);
     } else {
@@ -119,6 +126,11 @@ __device__ __forceinline__ void bin_brick(const int32_t* q, uint32_t t, int bx, 
     }
 }
 
+__device__ __forceinline__ void bin_brick(const int32_t* q, uint32_t t, int bx, int by, int bz, bool test,
+                                          const VoxScratch& sc, uint32_t* status, bool emit) {
+    if (brick_hit(q, bx, by, bz, test, sc)) brick_add(t, morton3(bx, by, bz), sc, status, emit);
+}
+
 // brick box of a triangle: first brick and extent per axis
 __device__ __forceinline__ int brick_box(const int32_t* q, uint32_t dim, int32_t b0[3], int32_t nb[3]) {
     int32_t lo[3], hi[3];
@@ -127,24 +139,38 @@ __device__ __forceinline__ int brick_box(const int32_t* q, uint32_t dim, int32_t
     return nb[0] * nb[1] * nb[2];
 }
 
-// Count (emit = false) or list (emit = true) the bricks of a triangle with at most kWarpCells bricks; larger
-// triangles are queued on the count pass and binned by vox_bin_big (one CTA per triangle).
+// Count (emit = false) or list (emit = true) the bricks of a triangle with at most kThreadCells bricks; larger
+// triangles are queued on the count pass and binned by vox_bin_big.  The count pass keeps which bricks it listed
+// (one bit each), so the list pass repeats none of the overlap tests.
 __device__ __forceinline__ void bin_small(const TriRec& r, uint32_t t, uint32_t dim, const VoxScratch& sc,
                                           uint32_t* status, bool emit, uint64_t ntris) {
     int32_t b0[3], nb[3];
     const int ncell = brick_box(r.q, dim, b0, nb);
-    if (ncell > kWarpCells) {
+    if (ncell > kThreadCells) {
         if (!emit) {
-            uint32_t k = atomicAdd(sc.big_count, 1u);
-            if (k < ntris) sc.big[k] = t;
+            const bool huge = ncell > kMidCells;
+            uint32_t k = atomicAdd(huge ? sc.big_count : sc.mid_count, 1u);
+            if (k < ntris) (huge ? sc.big : sc.mid)[k] = t;
         }
         return;
     }
-    for (int c = 0; c < ncell; ++c)
-        bin_brick(r.q, t, b0[0] + c % nb[0], b0[1] + (c / nb[0]) % nb[1], b0[2] + c / (nb[0] * nb[1]), ncell > 1, sc,
-                  status, emit);
+    uint32_t bits = emit ? sc.bits[t] : 0u;
+    for (int c = 0; c < ncell; ++c) {
+        const int bx = b0[0] + c % nb[0], by = b0[1] + (c / nb[0]) % nb[1], bz = b0[2] + c / (nb[0] * nb[1]);
+        if (emit) {
+            if ((bits >> c) & 1u) brick_add(t, morton3(bx, by, bz), sc, status, true);
+        } else if (brick_hit(r.q, bx, by, bz, ncell > 1, sc)) {
+            brick_add(t, morton3(bx, by, bz), sc, status, false);
+            bits |= 1u << c;
+        }
+    }
+    if (!emit) sc.bits[t] = uint8_t(bits);
 }
 
+// Triangles of more than kMidCells bricks take a CTA each; the others above kThreadCells take a warp each, all in
+// one wave (a CTA walking triangles of a few dozen bricks one after another would wait on each one's loads and
+// overlap tests in turn with most of its threads idle).  A warp's count pass keeps its triangle's listed bricks
+// as two 32-bit ballots for the list pass.
 __global__ void __launch_bounds__(256) vox_bin_big(uint32_t dim, VoxScratch sc, uint32_t* status, int emit) {
     const uint32_t nbig = *sc.big_count;
     for (uint32_t i = blockIdx.x; i < nbig; i += gridDim.x) {
@@ -155,6 +181,24 @@ __global__ void __launch_bounds__(256) vox_bin_big(uint32_t dim, VoxScratch sc, 
         for (int c = int(threadIdx.x); c < n; c += int(blockDim.x))
             bin_brick(r.q, t, b0[0] + c % nb[0], b0[1] + (c / nb[0]) % nb[1], b0[2] + c / (nb[0] * nb[1]), true, sc,
                       status, emit != 0);
+    }
+    const uint32_t nmid = *sc.mid_count, wpb = blockDim.x / 32, lane = threadIdx.x & 31;
+    for (uint32_t i = blockIdx.x * wpb + threadIdx.x / 32; i < nmid; i += gridDim.x * wpb) {  // warp-uniform
+        const uint32_t t = sc.mid[i];
+        const TriRec r = sc.recs[t];
+        int32_t b0[3], nb[3];
+        const int n = brick_box(r.q, dim, b0, nb);
+        const uint2 listed = emit ? sc.mid_bits[i] : make_uint2(0u, 0u);
+        bool hit[2];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int c = int(lane) + 32 * h;
+            const int bx = b0[0] + c % nb[0], by = b0[1] + (c / nb[0]) % nb[1], bz = b0[2] + c / (nb[0] * nb[1]);
+            hit[h] = c < n && (emit ? (((h ? listed.y : listed.x) >> lane) & 1u) != 0u : brick_hit(r.q, bx, by, bz, true, sc));
+            if (hit[h]) brick_add(t, morton3(bx, by, bz), sc, status, emit != 0);
+        }
+        const uint32_t b0bits = __ballot_sync(0xffffffffu, hit[0]), b1bits = __ballot_sync(0xffffffffu, hit[1]);
+        if (!emit && lane == 0) sc.mid_bits[i] = make_uint2(b0bits, b1bits);
     }
 }
 
@@ -581,7 +625,7 @@ bool g_lut_ready = false;
 size_t voxelize_scratch_bytes(uint64_t ntris, uint32_t dim) {
     uint32_t nb = dim / 8, nbricks = nb * nb * nb;
     return ntris * sizeof(TriRec) + uint64_t(nbricks) * 12 + scan_scratch_bytes(nbricks) + (nbricks / 32 + 1) * 4 +
-           list_capacity(ntris, nbricks) * 4 + (ntris + 2) * 4 + 20 * 256;
+           list_capacity(ntris, nbricks) * 4 + (ntris + 2) * 4 + (ntris + 2) * 4 + (ntris + 1) * 8 + ntris + 24 * 256;
 }
 
 namespace {
@@ -602,6 +646,10 @@ VoxScratch carve_scratch(const VoxelizeJob& job, void* scratch, uint32_t** mask)
     sc.list = carve<uint32_t>(p, sc.list_cap);
     sc.big = carve<uint32_t>(p, job.ntris + 1);
     sc.big_count = carve<uint32_t>(p, 1);
+    sc.mid = carve<uint32_t>(p, job.ntris + 1);
+    sc.mid_count = carve<uint32_t>(p, 1);
+    sc.mid_bits = carve<uint2>(p, job.ntris + 1);
+    sc.bits = carve<uint8_t>(p, job.ntris);
     sc.dirty_mask = job.ndirty ? *mask : nullptr;
     return sc;
 }
@@ -632,6 +680,7 @@ int voxelize_lists_launch(const VoxelizeJob& job, void* scratch, size_t scratch_
     uint32_t* mask = nullptr;
     VoxScratch sc = carve_scratch(job, scratch, &mask);
     cudaMemsetAsync(sc.big_count, 0, 4, s);
+    cudaMemsetAsync(sc.mid_count, 0, 4, s);
     cudaMemsetAsync(sc.brick_count, 0, size_t(nbricks) * 4, s);
     cudaMemsetAsync(sc.brick_fill, 0, size_t(nbricks) * 4, s);
     if (job.ndirty) {
@@ -642,13 +691,13 @@ int voxelize_lists_launch(const VoxelizeJob& job, void* scratch, size_t scratch_
     if (job.ntris) {
         vox_setup<<<uint32_t((job.ntris + 127) / 128), 128, 0, s>>>(job.tri, job.albedo, job.ntris, job.d_frame, dim,
                                                                      sc, d_status);
-        vox_bin_big<<<2 * 152, 256, 0, s>>>(dim, sc, d_status, 0);
+        vox_bin_big<<<8 * 152, 256, 0, s>>>(dim, sc, d_status, 0);
         note_launches(2);
     }
     if ((rc = exclusive_scan(sc.brick_count, nbricks, sc.brick_start, sc.total, sc.scan_tmp, s))) return rc;
     if (job.ntris) {
         vox_emit<<<uint32_t((job.ntris + 127) / 128), 128, 0, s>>>(job.ntris, dim, sc, d_status);
-        vox_bin_big<<<2 * 152, 256, 0, s>>>(dim, sc, d_status, 1);
+        vox_bin_big<<<8 * 152, 256, 0, s>>>(dim, sc, d_status, 1);
         note_launches(2);
     }
     return cuda_fail(cudaGetLastError(), "voxelize lists");
