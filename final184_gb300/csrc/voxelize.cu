@@ -451,7 +451,9 @@ __global__ void __launch_bounds__(kChunk, 8) vox_bricks(VoxScratch sc, const f18
                                                   const unsigned long long* __restrict__ shadow, uint32_t res,
                                                   uint32_t* counts, const uint32_t* __restrict__ dirty,
                                                   float4* __restrict__ weights, uint32_t* status) {
-    __shared__ unsigned long long s_sum[3][512];  // 33.31 fixed point: exact, order-independent sums
+    // 33.31 fixed-point sums, exact and order-independent, as 32-bit words: the low word by atomic add, the high
+    // word counting the low word's carries (shared-memory 32-bit atomics run ~2.5x the rate of 64-bit ones)
+    __shared__ uint32_t s_lo[3][512], s_hi[3][512];
     __shared__ uint32_t s_cnt[512];
     __shared__ ItemSetup s_item[kChunk];
     __shared__ uint32_t s_start[kChunk + 1];       // prefix of x-rows per prepared item
@@ -476,7 +478,8 @@ __global__ void __launch_bounds__(kChunk, 8) vox_bricks(VoxScratch sc, const f18
         return;
     }
     for (int i = threadIdx.x; i < 512; i += kChunk) {
-        s_sum[0][i] = s_sum[1][i] = s_sum[2][i] = 0;
+        s_lo[0][i] = s_lo[1][i] = s_lo[2][i] = 0u;
+        s_hi[0][i] = s_hi[1][i] = s_hi[2][i] = 0u;
         s_cnt[i] = 0;
     }
     const int64_t base[3] = {int64_t(bx) * kBrickFix, int64_t(by) * kBrickFix, int64_t(bz) * kBrickFix};
@@ -571,9 +574,11 @@ __global__ void __launch_bounds__(kChunk, 8) vox_bricks(VoxScratch sc, const f18
                 const long long d = is.n[0] * (2 * lx + 1) + drow;
                 if (d < is.plo || d > is.phi) continue;
                 const int li = lz * 64 + ly * 8 + lx;
-                atomicAdd(&s_sum[0][li], (unsigned long long)is.wq[0]);
-                atomicAdd(&s_sum[1][li], (unsigned long long)is.wq[1]);
-                atomicAdd(&s_sum[2][li], (unsigned long long)is.wq[2]);
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    const uint32_t old = atomicAdd(&s_lo[c][li], is.wq[c]);
+                    if (old + is.wq[c] < old) atomicAdd(&s_hi[c][li], 1u);
+                }
                 atomicAdd(&s_cnt[li], 1u);
             }
         }
@@ -588,7 +593,9 @@ __global__ void __launch_bounds__(kChunk, 8) vox_bricks(VoxScratch sc, const f18
         if (cnt) {
             // mean injection weight (FP32), then radiance = luminance * (lit ? weight : 0)
             const float q = (1.0f / 2147483648.0f) / float(cnt);
-            const float4 w = make_float4(float(s_sum[0][li]) * q, float(s_sum[1][li]) * q, float(s_sum[2][li]) * q, 1.0f);
+            const float4 w = make_float4(float((uint64_t(s_hi[0][li]) << 32) | s_lo[0][li]) * q,
+                                         float((uint64_t(s_hi[1][li]) << 32) | s_lo[1][li]) * q,
+                                         float((uint64_t(s_hi[2][li]) << 32) | s_lo[2][li]) * q, 1.0f);
             if (weights) {
                 out = w;  // geometry only: relight_bricks applies the shadow test and the luminance
             } else {
