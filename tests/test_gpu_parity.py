@@ -82,6 +82,11 @@ def test_injected_radiance(case, oracle_l0):
     assert e.ok(), str(e)
     lit = (l0_ref[..., 0] > 0).sum()
     assert lit > 1000
+    # the scene exercises the carry of the 33.31 fixed-point sums past 32 bits: a lit voxel's sum is
+    # count * mean weight * 2^31 with mean weight = radiance / luminance
+    lum = np.array(case.oracle_light().luminance[:3], np.float64)
+    sums = oracle_l0[3][..., None] * l0_ref[..., :3] / lum * 2.0 ** 31
+    assert (sums >= 2.0 ** 32).sum() > 100
 
 
 def test_mip_chain(case, orc):
