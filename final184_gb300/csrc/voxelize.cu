@@ -10,8 +10,9 @@
 // compare with a two-voxel bias, evaluated as a fixed FP32 operation sequence (the same decision on any IEEE
 // machine) against the shadow map rasterized by raster.cu.  FP64 is used per vertex only (the snap).
 //
-// Pipeline: setup (snap, weight, count overlapped bricks) -> scan -> emit (triangle lists per brick) ->
-// one CTA per brick accumulates in shared memory, resolves and writes the brick once.
+// Pipeline: setup (snap, weight, count overlapped bricks) -> scan -> emit (triangle lists per brick) -> items
+// (each (triangle, brick) pair's exact-test setup) -> one CTA per brick accumulates in shared memory, resolves and
+// writes the brick once.
 #include "gi_device.cuh"
 #include "util.cuh"
 
@@ -31,6 +32,8 @@ struct TriRec {
     uint32_t wq[3];  // injection weight per channel, 1.31 fixed point (<= 2^31); wq[0] = kInvalid marks skipped
 };
 
+struct ItemSetup;
+
 struct VoxScratch {
     TriRec* recs;
     uint32_t* brick_count;
@@ -39,7 +42,9 @@ struct VoxScratch {
     uint32_t* total;
     uint32_t* scan_tmp;
     uint32_t* dirty_mask;  // nbricks bits, null = all bricks
-    uint32_t* list;
+    uint32_t* list;        // triangle of each (triangle, brick) item, grouped by brick
+    uint32_t* list_brick;  // brick of each item
+    ItemSetup* items;      // each item's exact-test setup (vox_items), in list order
     uint32_t* big;        // triangles with more than kMidCells bricks (binned by vox_bin_big, a CTA each)
     uint32_t* big_count;  // [1]
     uint32_t* mid;        // triangles with kThreadCells < bricks <= kMidCells (vox_bin_big, a warp each)
@@ -119,9 +124,10 @@ __device__ __forceinline__ void brick_add(uint32_t t, uint32_t m, const VoxScrat
         atomicAdd(&sc.brick_count[m], 1u);
     } else {
         uint64_t slot = uint64_t(sc.brick_start[m]) + atomicAdd(&sc.brick_fill[m], 1u);
-        if (slot < sc.list_cap)
+        if (slot < sc.list_cap) {
             sc.list[slot] = t;
-        else
+            sc.list_brick[slot] = m;
+        } else
             set_status(status, kStatusOverflow);
     }
 }
@@ -401,8 +407,8 @@ __device__ __forceinline__ void item_masks(const int32_t (&v)[3][3], const int32
 
 // A share of one (triangle, brick) item's setup: the cells of rows w = l0 + part, l0 + part + per, .. of the
 // three projections' masks (OR-combined across the item's threads by the caller), and with do_plane the plane
-// test and the item's fields.  A chunk with few items spreads each item over 2 or 4 threads, so a large item's
-// cell loops (up to 8 x 8 cells per projection) do not hold its brick.
+// test and the item's fields.  Each item is spread over kItemLanes threads, so a large item's cell loops (up to
+// 8 x 8 cells per projection) are not one thread's.
 __device__ void item_part(const TriRec& r, const int64_t base[3], const int32_t l0[3], const int32_t l1[3], int part,
                           int per, bool do_plane, unsigned long long (&mks)[3], ItemSetup& out) {
     // brick-relative vertices and edges fit 32 bits (|q| < 2^19, base <= 2^17): products widen 32 x 32 -> 64
@@ -440,13 +446,63 @@ __device__ void item_part(const TriRec& r, const int64_t base[3], const int32_t 
     for (int a = 0; a < 3; ++a) out.l0[a] = uint8_t(l0[a]), out.ext[a] = uint8_t(l1[a] - l0[a] + 1);
 }
 
-constexpr int kChunk = 128;  // items prepared per round (at most one per thread; = threads per CTA)
+// Adjacent lanes preparing one item in vox_items (per 500k-triangle voxelization: 4 lanes 0.615 ms, 2 lanes
+// 0.590, 1 lane 0.588 with the bricks' CTAs otherwise the same: the shared rows save less than the repeated
+// set-up of every lane costs)
+constexpr int kItemLanes = 1;
+
+// Every (triangle, brick) item of the lists, prepared apart from its brick: the three projections' cell masks
+// (each of an item's kItemLanes lanes a share of the rows, OR-combined by shuffles), the plane test and the
+// item's voxel box, written in list order for vox_bricks.  It needs the triangle records and the lists only, so it
+// runs on the lists' stream beside the shadow raster, at full occupancy and with no barrier: prepared inside the
+// brick's CTA, a large item's cell loops held the CTA's other threads at the barrier after them.
+__global__ void __launch_bounds__(256) vox_items(uint32_t dim, uint64_t ntris, VoxScratch sc) {
+    const uint32_t n = uint32_t(min(uint64_t(*sc.total), sc.list_cap));
+    const uint32_t lane = threadIdx.x & 31, part = lane % kItemLanes;
+    constexpr uint32_t kPerWarp = 32 / kItemLanes;
+    const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t i0 = gw * kPerWarp; i0 < n; i0 += nw * kPerWarp) {  // warp-uniform rounds (full-mask shuffles)
+        const uint32_t i = i0 + lane / kItemLanes;
+        unsigned long long mks[3] = {0ull, 0ull, 0ull};
+        ItemSetup it = {};  // an item whose voxel box misses its brick keeps ext = 0: no rows
+        const uint32_t t = i < n ? sc.list[i] : 0u;
+        if (i < n && t < ntris) {
+            const uint32_t m = sc.list_brick[i];
+            const TriRec r = sc.recs[t];
+            const int32_t bx = int32_t(compact1by2(m)), by = int32_t(compact1by2(m >> 1)),
+                          bz = int32_t(compact1by2(m >> 2));
+            const int64_t base[3] = {int64_t(bx) * kBrickFix, int64_t(by) * kBrickFix, int64_t(bz) * kBrickFix};
+            int32_t lo[3], hi[3];
+            voxel_range(r.q, dim, lo, hi);
+            const int32_t l0[3] = {max(lo[0], bx * 8) - bx * 8, max(lo[1], by * 8) - by * 8, max(lo[2], bz * 8) - bz * 8};
+            const int32_t l1[3] = {min(hi[0], bx * 8 + 7) - bx * 8, min(hi[1], by * 8 + 7) - by * 8,
+                                   min(hi[2], bz * 8 + 7) - bz * 8};
+            if (l0[0] <= l1[0] && l0[1] <= l1[1] && l0[2] <= l1[2])
+                item_part(r, base, l0, l1, int(part), kItemLanes, part == kItemLanes - 1, mks, it);
+        }
+#pragma unroll
+        for (int P = 0; P < 3; ++P) {
+            uint32_t mlo = uint32_t(mks[P]), mhi = uint32_t(mks[P] >> 32);
+#pragma unroll
+            for (int o = 1; o < kItemLanes; o <<= 1) {
+                mlo |= __shfl_xor_sync(0xffffffffu, mlo, o);
+                mhi |= __shfl_xor_sync(0xffffffffu, mhi, o);
+            }
+            it.mask[P] = (uint64_t(mhi) << 32) | mlo;
+        }
+        if (i < n && part == kItemLanes - 1) sc.items[i] = it;
+    }
+}
+
+constexpr int kChunk = 128;  // items staged per round (one per thread; = threads per CTA)
 constexpr uint32_t kRowCap = 1024;  // rows per round mapped to their item by table (later ones by search)
 
-// Eight CTAs per SM (64 registers, 26 KB of shared memory each): a brick's phases are separated by barriers at
-// which most of its threads wait, so other bricks' CTAs are what keeps the SM busy (0.59 -> 0.40 ms per 256^3
-// voxelization against four CTAs per SM).
-__global__ void __launch_bounds__(kChunk, 8) vox_bricks(VoxScratch sc, const f184gi_grid_frame* __restrict__ fr,
+// Fourteen CTAs per SM (32 registers, 16 KB of shared memory each: the prepared items are read from global memory
+// where a row needs them, not staged): a brick's phases are separated by barriers at which most of its threads
+// wait, so other bricks' CTAs are what keeps the SM busy (per 500k-triangle voxelization: 0.59 -> 0.40 ms at 8
+// CTAs per SM against 4, with the items prepared in the CTA; with the items prepared by vox_items, 8 CTAs staging
+// them 0.588 ms, 10 / 12 / 14 CTAs reading them from global memory 0.578 / 0.572 / 0.565 ms).
+__global__ void __launch_bounds__(kChunk, 14) vox_bricks(VoxScratch sc, const f184gi_grid_frame* __restrict__ fr,
                                                   uint32_t dim, ChainLayout chain, f184gi_light light,
                                                   const unsigned long long* __restrict__ shadow, uint32_t res,
                                                   uint32_t* counts, const uint32_t* __restrict__ dirty,
@@ -455,7 +511,6 @@ __global__ void __launch_bounds__(kChunk, 8) vox_bricks(VoxScratch sc, const f18
     // word counting the low word's carries (shared-memory 32-bit atomics run ~2.5x the rate of 64-bit ones)
     __shared__ uint32_t s_lo[3][512], s_hi[3][512];
     __shared__ uint32_t s_cnt[512];
-    __shared__ ItemSetup s_item[kChunk];
     __shared__ uint32_t s_start[kChunk + 1];       // prefix of x-rows per prepared item
     __shared__ uint8_t s_rowitem[kRowCap];         // item slot of each of the first kRowCap rows
     const uint32_t m = dirty ? dirty[blockIdx.x] : blockIdx.x;
@@ -482,40 +537,13 @@ __global__ void __launch_bounds__(kChunk, 8) vox_bricks(VoxScratch sc, const f18
         s_hi[0][i] = s_hi[1][i] = s_hi[2][i] = 0u;
         s_cnt[i] = 0;
     }
-    const int64_t base[3] = {int64_t(bx) * kBrickFix, int64_t(by) * kBrickFix, int64_t(bz) * kBrickFix};
     for (uint32_t c0 = beg; c0 < end; c0 += kChunk) {
-        // phase 1: the chunk's items are prepared by 4, 2 or 1 threads each (at most 32, 64 or 128 items), each
-        // taking every per-th row of the projections' cell tests; the item's threads are adjacent lanes, whose
-        // partial masks are OR-combined by shuffles.  The item's first thread carries its row count and writes the
-        // masks; its last computes the plane.
+        // phase 1: the x-row counts of the chunk's prepared items (vox_items), one item per thread
         const uint32_t nchunk = min(end - c0, uint32_t(kChunk));
-        const uint32_t per = nchunk <= kChunk / 4 ? 4u : (nchunk <= kChunk / 2 ? 2u : 1u);
-        const uint32_t slot = threadIdx.x / per, part = threadIdx.x % per;
-        uint32_t nrows = 0, item_rows = 0;
-        unsigned long long mks[3] = {0ull, 0ull, 0ull};
-        bool valid = false;
-        if (slot < nchunk) {
-            const TriRec r = sc.recs[sc.list[c0 + slot]];
-            int32_t lo[3], hi[3];
-            voxel_range(r.q, dim, lo, hi);
-            const int32_t l0[3] = {max(lo[0], bx * 8) - bx * 8, max(lo[1], by * 8) - by * 8, max(lo[2], bz * 8) - bz * 8};
-            const int32_t l1[3] = {min(hi[0], bx * 8 + 7) - bx * 8, min(hi[1], by * 8 + 7) - by * 8,
-                                   min(hi[2], bz * 8 + 7) - bz * 8};
-            valid = l0[0] <= l1[0] && l0[1] <= l1[1] && l0[2] <= l1[2];
-            if (valid) {
-                item_part(r, base, l0, l1, int(part), int(per), part == per - 1, mks, s_item[slot]);
-                item_rows = uint32_t((l1[1] - l0[1] + 1) * (l1[2] - l0[2] + 1));
-                if (part == 0) nrows = item_rows;
-            }
-        }
-#pragma unroll
-        for (int P = 0; P < 3; ++P) {
-            uint32_t mlo = uint32_t(mks[P]), mhi = uint32_t(mks[P] >> 32);
-            for (uint32_t o = 1; o < per; o <<= 1) {
-                mlo |= __shfl_xor_sync(0xffffffffu, mlo, int(o));
-                mhi |= __shfl_xor_sync(0xffffffffu, mhi, int(o));
-            }
-            if (valid && part == 0) s_item[slot].mask[P] = (uint64_t(mhi) << 32) | mlo;
+        uint32_t nrows = 0;
+        if (threadIdx.x < nchunk) {
+            const ItemSetup& it = sc.items[c0 + threadIdx.x];
+            nrows = uint32_t(it.ext[1]) * uint32_t(it.ext[2]);
         }
         // exclusive scan of the row counts (warp shuffles + one pass over the 4 warp totals)
         {
@@ -536,19 +564,19 @@ __global__ void __launch_bounds__(kChunk, 8) vox_bricks(VoxScratch sc, const f18
             __syncthreads();
         }
         const uint32_t total = s_start[kChunk];
-        // the item of each of the first kRowCap rows, written by the item's threads (its rows are contiguous)
-        if (item_rows) {
-            const uint32_t st = s_start[slot * per];
-            for (uint32_t j = part; j < item_rows && st + j < kRowCap; j += per) s_rowitem[st + j] = uint8_t(slot);
+        // the item of each of the first kRowCap rows, written by the item's thread (its rows are contiguous)
+        if (nrows) {
+            const uint32_t st = s_start[threadIdx.x];
+            for (uint32_t j = 0; j < nrows && st + j < kRowCap; ++j) s_rowitem[st + j] = uint8_t(threadIdx.x);
         }
         __syncthreads();
         // phase 2: all threads share the x-rows (item, y, z) of the chunk's voxel boxes evenly.  A row's candidate
         // voxels are the bits of one byte: projection 2 holds x + 8y (byte y), projection 1 holds z + 8x (the
         // bits z, z + 8, .., z + 56, gathered into a byte by one multiply), projection 0 one bit y + 8z.
         for (uint32_t rr = threadIdx.x; rr < total; rr += blockDim.x) {
-            uint32_t lo;  // the item's first thread: the k with s_start[k] <= rr < s_start[k + 1]
+            uint32_t lo;  // the row's item: the k with s_start[k] <= rr < s_start[k + 1]
             if (rr < kRowCap) {
-                lo = uint32_t(s_rowitem[rr]) * per;
+                lo = uint32_t(s_rowitem[rr]);
             } else {
                 lo = 0;
                 uint32_t hi = kChunk;
@@ -557,7 +585,7 @@ __global__ void __launch_bounds__(kChunk, 8) vox_bricks(VoxScratch sc, const f18
                     if (s_start[mid] <= rr) lo = mid; else hi = mid;
                 }
             }
-            const ItemSetup& is = s_item[lo / per];
+            const ItemSetup& is = sc.items[c0 + lo];
             const uint32_t local = rr - s_start[lo];
             const uint32_t ey = is.ext[1];
             // local / ey for local < 64, ey <= 8: the quotient's fraction stays >= 1/16 from an integer
@@ -632,7 +660,7 @@ bool g_lut_ready = false;
 size_t voxelize_scratch_bytes(uint64_t ntris, uint32_t dim) {
     uint32_t nb = dim / 8, nbricks = nb * nb * nb;
     return ntris * sizeof(TriRec) + uint64_t(nbricks) * 12 + scan_scratch_bytes(nbricks) + (nbricks / 32 + 1) * 4 +
-           list_capacity(ntris, nbricks) * 4 + (ntris + 2) * 4 + (ntris + 2) * 4 + (ntris + 1) * 8 + ntris + 24 * 256;
+           list_capacity(ntris, nbricks) * (8 + sizeof(ItemSetup)) + (ntris + 2) * 4 + (ntris + 2) * 4 + (ntris + 1) * 8 + ntris + 24 * 256;
 }
 
 namespace {
@@ -651,6 +679,8 @@ VoxScratch carve_scratch(const VoxelizeJob& job, void* scratch, uint32_t** mask)
     *mask = carve<uint32_t>(p, nbricks / 32 + 1);
     sc.list_cap = list_capacity(job.ntris, nbricks);
     sc.list = carve<uint32_t>(p, sc.list_cap);
+    sc.list_brick = carve<uint32_t>(p, sc.list_cap);
+    sc.items = carve<ItemSetup>(p, sc.list_cap);
     sc.big = carve<uint32_t>(p, job.ntris + 1);
     sc.big_count = carve<uint32_t>(p, 1);
     sc.mid = carve<uint32_t>(p, job.ntris + 1);
@@ -705,7 +735,8 @@ int voxelize_lists_launch(const VoxelizeJob& job, void* scratch, size_t scratch_
     if (job.ntris) {
         vox_emit<<<uint32_t((job.ntris + 127) / 128), 128, 0, s>>>(job.ntris, dim, sc, d_status);
         vox_bin_big<<<8 * 152, 256, 0, s>>>(dim, sc, d_status, 1);
-        note_launches(2);
+        vox_items<<<8 * 152, 256, 0, s>>>(dim, job.ntris, sc);
+        note_launches(3);
     }
     return cuda_fail(cudaGetLastError(), "voxelize lists");
 }
