@@ -246,6 +246,13 @@ class VoxelGI:
         check(self.lib.f184gi_grid_get_frame(self.ctx, grid.handle, C.byref(f)))
         return f
 
+    def level_ptr(self, grid, level):
+        """(device pointer, bytes) of one level of the chain (all six direction volumes of an anisotropic level).
+        The caller may write through it: the next mip() then builds the whole chain from level 0."""
+        ptr, nbytes = C.c_void_p(), C.c_uint64()
+        check(self.lib.f184gi_grid_level_ptr(self.ctx, grid.handle, level, C.byref(ptr), C.byref(nbytes)))
+        return int(ptr.value or 0), int(nbytes.value)
+
     def read_level(self, grid, level, direction=0):
         d = grid.level_dim(level)
         if grid.desc.format == FMT_RG16:  # packed uint32 per voxel (565 albedo | 565 normal << 16)

@@ -5,6 +5,7 @@
 // kernels report overflow/timeout through a device status word that f184gi_sync and the inspection calls read.
 #include <nvtx3/nvToolsExt.h>
 
+#include <algorithm>
 #include <atomic>
 #include <cmath>
 #include <cstring>
@@ -115,6 +116,9 @@ struct GridObj {
     size_t weights_bytes = 0;
     f184gi_grid_frame* d_frame = nullptr;
     bool voxelized = false;
+    // levels 1 .. min(3, levels - 1) agree with L0: written with it by the last voxelizations (isotropic FP32
+    // grids), or by a full mip build since; a pointer handed out by f184gi_grid_level_ptr clears it
+    bool low_levels_current = false;
     f184gi_light light{};  // the light of the last voxelization (the march shades with it)
 };
 
@@ -456,6 +460,11 @@ int f184gi_voxelize(f184gi_ctx* c, uint32_t grid, const float* tri, const uint32
     vj.dirty_bricks = dirty;
     vj.ndirty = ndirty;
     vj.weights = g->weights;
+    // isotropic FP32 grids written directly (no resident weights): each brick CTA also writes its block of levels
+    // 1..3, so f184gi_mip continues from level 3 instead of re-reading L0.  A dirty-brick update rewrites only its
+    // bricks' blocks, so the others must already agree with L0.
+    const bool fuse = d.format == F184GI_FMT_F32 && !d.anisotropic && !g->weights;
+    vj.mip_levels = fuse && (!ndirty || g->low_levels_current) ? std::min(3u, d.levels - 1) : 0u;
     const bool lists = d.format != F184GI_FMT_RG16;
     cudaError_t e;
     if (lists) {  // the triangle lists need the frame, not the shadow map: build them beside the raster
@@ -485,9 +494,11 @@ int f184gi_voxelize(f184gi_ctx* c, uint32_t grid, const float* tri, const uint32
         g->voxelized = true;
         return F184GI_OK;
     }
+    g->low_levels_current = false;
     if (!g->weights && (rc = voxelize_bricks_launch(vj, c->vox.ptr, c->vox.bytes, c->d_status, s))) return rc;
     if (g->weights && (rc = relight_launch(g->weights, g->d_frame, g->chain, *light, g->shadow, d.shadow_res, s)))
         return rc;
+    g->low_levels_current = vj.mip_levels > 0;
     g->voxelized = true;
     return F184GI_OK;
 }
@@ -510,7 +521,14 @@ int f184gi_mip(f184gi_ctx* c, uint32_t grid, uint32_t levels, uint32_t anisotrop
     if (anisotropic != g->desc.anisotropic) return fail(F184GI_ERR_INVALID, "mip: anisotropy differs from the grid's");
     if (g->desc.format == F184GI_FMT_RG16) return fail(F184GI_ERR_INVALID, "mip: an RG16 grid has one level");
     if (levels == 0 || levels > g->desc.levels) levels = g->desc.levels;
-    return mip_launch(g->chain, levels, c->d_status, static_cast<cudaStream_t>(stream));
+    const uint32_t low = std::min(3u, g->desc.levels - 1);
+    // levels 1..low written with L0 by the voxelization: the chain continues from level `low` (the same bytes as
+    // a build from L0, whose levels 1..4 come from the same 2x2x2 means of FP32 values)
+    const uint32_t from = g->low_levels_current ? std::min(low, levels - 1) : 0u;
+    int rc = mip_launch(g->chain, levels, from, c->d_status, static_cast<cudaStream_t>(stream));
+    if (!rc && levels - 1 >= low && g->desc.format == F184GI_FMT_F32 && !g->desc.anisotropic)
+        g->low_levels_current = true;
+    return rc;
 }
 
 void f184gi_cone_params_default(f184gi_cone_params* p) {
@@ -819,6 +837,7 @@ int f184gi_grid_level_ptr(f184gi_ctx* c, uint32_t grid, uint32_t level, void** p
     if (!g) return fail(F184GI_ERR_NOTFOUND, "grid_level_ptr: unknown grid");
     if (level >= g->desc.levels) return fail(F184GI_ERR_INVALID, "grid_level_ptr: level out of range");
     const ChainLayout& ch = g->chain;
+    g->low_levels_current = false;  // the caller may write through the pointer: the next mip builds from L0
     *ptr = static_cast<char*>(ch.base) + ch.off[level] * ch.esz;
     *bytes = ch.vol[level] * ch.esz * ((ch.aniso && level > 0) ? 6 : 1);
     return F184GI_OK;

@@ -100,6 +100,21 @@ __device__ __forceinline__ void store_vox(void* base, uint32_t format, uint64_t 
     reinterpret_cast<uint2*>(base)[idx] = encode_f16_vox(v);
 }
 
+// The isotropic mip value of a voxel: the mean of its 2x2x2 children, fetch(dx, dy, dz) returning child
+// (dx, dy, dz), summed in the order dz, dy, dx (one rounding per add, no multiply feeding an add) and scaled by
+// 1/8.  Every kernel that builds an isotropic level calls this, so the chain's bytes do not depend on which one did.
+template <class Fetch>
+__device__ __forceinline__ float4 iso_mean8(Fetch fetch) {
+    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int dz = 0; dz < 2; ++dz)
+        for (int dy = 0; dy < 2; ++dy)
+            for (int dx = 0; dx < 2; ++dx) {
+                const float4 v = fetch(dx, dy, dz);
+                acc = make_float4(acc.x + v.x, acc.y + v.y, acc.z + v.z, acc.w + v.w);
+            }
+    return make_float4(acc.x * 0.125f, acc.y * 0.125f, acc.z * 0.125f, acc.w * 0.125f);
+}
+
 __device__ __forceinline__ void set_status(uint32_t* st, uint32_t bit) {
     if (st) atomicOr(st, bit);
 }

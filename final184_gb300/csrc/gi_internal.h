@@ -105,6 +105,8 @@ struct VoxelizeJob {
     const uint32_t* dirty_bricks;       // optional list (Morton brick indices of L0)
     uint32_t ndirty;
     float4* weights;                    // optional: write the mean-weight grid W instead of L0 radiance
+    uint32_t mip_levels;                // with L0: also write levels 1 .. mip_levels (<= 3) of each brick's block
+                                        // (isotropic FP32 chains; 0 = L0 only)
 };
 // L0 = luminance * (lit ? W : 0) over the whole grid (after a shadow-map change); W as written by voxelize
 int relight_launch(const float4* weights, const f184gi_grid_frame* d_frame, const ChainLayout& chain,
@@ -126,7 +128,8 @@ int bounded_wait_selftest_launch(uint32_t polls, uint32_t complete, uint32_t* st
 int frame_launch(const float* tri, uint64_t ntris, const f184gi_bounds* bounds, uint32_t dim,
                  const float light_dir[3], f184gi_grid_frame* d_frame, void* scratch, cudaStream_t s);
 
-int mip_launch(const ChainLayout& chain, uint32_t levels, uint32_t* d_status, cudaStream_t s);
+// levels from+1 .. levels-1 from level `from` (0: the whole chain from L0)
+int mip_launch(const ChainLayout& chain, uint32_t levels, uint32_t from, uint32_t* d_status, cudaStream_t s);
 
 struct TraceView {
     float iview[16];                     // inverse view (FP32 of the FP64 inverse: normals)

@@ -18,7 +18,6 @@ __device__ __forceinline__ float4 raw_vox(const unsigned char* smem, uint32_t fo
     return decode_f16_vox(reinterpret_cast<const uint2*>(smem)[idx]);
 }
 
-__device__ __forceinline__ float4 f4add(float4 a, float4 b) { return make_float4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w); }
 __device__ __forceinline__ float4 f4mul(float4 a, float s) { return make_float4(a.x * s, a.y * s, a.z * s, a.w * s); }
 
 // One output voxel from its 2x2x2 children, fetch(dx, dy, dz) returning child (dx, dy, dz).
@@ -27,13 +26,8 @@ __device__ __forceinline__ float4 f4mul(float4 a, float s) { return make_float4(
 // f + (1 - f.alpha) b per channel) and the four columns across the axis are averaged.
 template <bool ANISO, class Fetch>
 __device__ __forceinline__ float4 reduce8(uint32_t dir, Fetch fetch) {
+    if (!ANISO) return iso_mean8(fetch);
     float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (!ANISO) {
-        for (int dz = 0; dz < 2; ++dz)
-            for (int dy = 0; dy < 2; ++dy)
-                for (int dx = 0; dx < 2; ++dx) acc = f4add(acc, fetch(dx, dy, dz));
-        return f4mul(acc, 0.125f);
-    }
     const int axis = int(dir >> 1);
     const int neg = int(dir & 1u);
     const int o1 = (axis + 1) % 3, o2 = (axis + 2) % 3;
@@ -328,7 +322,7 @@ uint32_t sm_count_current() {
 
 }  // namespace
 
-int mip_launch(const ChainLayout& c, uint32_t levels, uint32_t* d_status, cudaStream_t s) {
+int mip_launch(const ChainLayout& c, uint32_t levels, uint32_t from, uint32_t* d_status, cudaStream_t s) {
     if (levels > c.levels) levels = c.levels;
     static bool attr_set = false;
     if (!attr_set) {
@@ -344,7 +338,7 @@ int mip_launch(const ChainLayout& c, uint32_t levels, uint32_t* d_status, cudaSt
         attr_set = true;
     }
     const uint32_t ndir = c.aniso ? 6u : 1u;
-    uint32_t l = 0;
+    uint32_t l = from;
     while (l + 1 < levels) {
         uint32_t ds = c.ldim[l];
         uint32_t S = ds >= 16 ? 16u : ds;

@@ -506,11 +506,13 @@ __global__ void __launch_bounds__(kChunk, 14) vox_bricks(VoxScratch sc, const f1
                                                   uint32_t dim, ChainLayout chain, f184gi_light light,
                                                   const unsigned long long* __restrict__ shadow, uint32_t res,
                                                   uint32_t* counts, const uint32_t* __restrict__ dirty,
-                                                  float4* __restrict__ weights, uint32_t* status) {
-    // 33.31 fixed-point sums, exact and order-independent, as 32-bit words: the low word by atomic add, the high
-    // word counting the low word's carries (shared-memory 32-bit atomics run ~2.5x the rate of 64-bit ones)
-    __shared__ uint32_t s_lo[3][512], s_hi[3][512];
-    __shared__ uint32_t s_cnt[512];
+                                                  float4* __restrict__ weights, uint32_t nlow, uint32_t* status) {
+    // Per voxel, 33.31 fixed-point sums of the three channels, exact and order-independent, as 32-bit words: the
+    // low words (0..2) by atomic add, the high words (3..5) counting the low words' carries (shared-memory 32-bit
+    // atomics run ~2.5x the rate of 64-bit ones).  With nlow > 0 a voxel's six words then hold its FP32 output
+    // (two float2), which the brick's levels 1..nlow are reduced from.
+    __shared__ __align__(16) uint32_t s_acc[512][6];
+    __shared__ __align__(16) uint32_t s_cnt[512];  // then levels 1 and 2 of the brick (64 + 8 float4)
     __shared__ uint32_t s_start[kChunk + 1];       // prefix of x-rows per prepared item
     __shared__ uint8_t s_rowitem[kRowCap];         // item slot of each of the first kRowCap rows
     const uint32_t m = dirty ? dirty[blockIdx.x] : blockIdx.x;
@@ -520,6 +522,15 @@ __global__ void __launch_bounds__(kChunk, 14) vox_bricks(VoxScratch sc, const f1
     const uint32_t beg = sc.brick_start[m];
     const uint32_t end = uint32_t(min(uint64_t(beg) + sc.brick_count[m], sc.list_cap));
     if (beg == end) {  // an empty brick: zeros, without the shared-memory sums
+        for (uint32_t j = threadIdx.x; j < 64u + 8u + 1u; j += kChunk) {  // its blocks of levels 1..nlow
+            const uint32_t k = j < 64u ? 1u : (j < 72u ? 2u : 3u), e = j < 64u ? 1u << (3 - k) : j < 72u ? 2u : 1u;
+            const uint32_t r = j - (k == 1u ? 0u : k == 2u ? 64u : 72u);
+            if (k <= nlow)
+                store_vox(chain.base, F184GI_FMT_F32,
+                          chain.off[k] + vox_index(k, chain.ldim[k], uint32_t(bx) * e + r % e,
+                                                   uint32_t(by) * e + (r / e) % e, uint32_t(bz) * e + r / (e * e)),
+                          make_float4(0.f, 0.f, 0.f, 0.f));
+        }
         for (int li = threadIdx.x; li < 512; li += kChunk) {
             if (weights)
                 weights[(uint64_t(m) << 9) + li] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -533,8 +544,8 @@ __global__ void __launch_bounds__(kChunk, 14) vox_bricks(VoxScratch sc, const f1
         return;
     }
     for (int i = threadIdx.x; i < 512; i += kChunk) {
-        s_lo[0][i] = s_lo[1][i] = s_lo[2][i] = 0u;
-        s_hi[0][i] = s_hi[1][i] = s_hi[2][i] = 0u;
+#pragma unroll
+        for (int w = 0; w < 6; ++w) s_acc[i][w] = 0u;
         s_cnt[i] = 0;
     }
     for (uint32_t c0 = beg; c0 < end; c0 += kChunk) {
@@ -604,8 +615,8 @@ __global__ void __launch_bounds__(kChunk, 14) vox_bricks(VoxScratch sc, const f1
                 const int li = lz * 64 + ly * 8 + lx;
 #pragma unroll
                 for (int c = 0; c < 3; ++c) {
-                    const uint32_t old = atomicAdd(&s_lo[c][li], is.wq[c]);
-                    if (old + is.wq[c] < old) atomicAdd(&s_hi[c][li], 1u);
+                    const uint32_t old = atomicAdd(&s_acc[li][c], is.wq[c]);
+                    if (old + is.wq[c] < old) atomicAdd(&s_acc[li][3 + c], 1u);
                 }
                 atomicAdd(&s_cnt[li], 1u);
             }
@@ -621,9 +632,9 @@ __global__ void __launch_bounds__(kChunk, 14) vox_bricks(VoxScratch sc, const f1
         if (cnt) {
             // mean injection weight (FP32), then radiance = luminance * (lit ? weight : 0)
             const float q = (1.0f / 2147483648.0f) / float(cnt);
-            const float4 w = make_float4(float((uint64_t(s_hi[0][li]) << 32) | s_lo[0][li]) * q,
-                                         float((uint64_t(s_hi[1][li]) << 32) | s_lo[1][li]) * q,
-                                         float((uint64_t(s_hi[2][li]) << 32) | s_lo[2][li]) * q, 1.0f);
+            const float4 w = make_float4(float((uint64_t(s_acc[li][3]) << 32) | s_acc[li][0]) * q,
+                                         float((uint64_t(s_acc[li][4]) << 32) | s_acc[li][1]) * q,
+                                         float((uint64_t(s_acc[li][5]) << 32) | s_acc[li][2]) * q, 1.0f);
             if (weights) {
                 out = w;  // geometry only: relight_bricks applies the shadow test and the luminance
             } else {
@@ -640,6 +651,44 @@ __global__ void __launch_bounds__(kChunk, 14) vox_bricks(VoxScratch sc, const f1
             uint64_t lin = (uint64_t(bz * 8 + lz) * dim + uint64_t(by * 8 + ly)) * dim + uint64_t(bx * 8 + lx);
             counts[lin] = cnt;
         }
+        if (nlow) {  // the output over the voxel's own sums (read above by this thread only)
+            float2* slot = reinterpret_cast<float2*>(s_acc[li]);
+            slot[0] = make_float2(out.x, out.y);
+            slot[1] = make_float2(out.z, out.w);
+        }
+    }
+    if (!nlow) return;
+    // The brick's blocks of levels 1..nlow (4^3, 2^3, 1), each voxel the mean of its 2x2x2 children (iso_mean8,
+    // as the mip kernels compute them, hence the same bytes): level 1 from the brick's FP32 outputs, level 2 from
+    // level 1's FP32 values, level 3 from level 2's.
+    float4* s_l1 = reinterpret_cast<float4*>(s_cnt);
+    float4* s_l2 = s_l1 + 64;
+    __syncthreads();
+    if (threadIdx.x < 64) {
+        const uint32_t x = threadIdx.x & 3u, y = (threadIdx.x >> 2) & 3u, z = threadIdx.x >> 4;
+        const float4 v = iso_mean8([&](int dx, int dy, int dz) {
+            const float2* c = reinterpret_cast<const float2*>(s_acc[((2 * z + dz) << 6) + ((2 * y + dy) << 3) + 2 * x + dx]);
+            const float2 a = c[0], b = c[1];
+            return make_float4(a.x, a.y, b.x, b.y);
+        });
+        s_l1[threadIdx.x] = v;
+        store_vox(chain.base, F184GI_FMT_F32,
+                  chain.off[1] + vox_index(1, chain.ldim[1], uint32_t(bx) * 4 + x, uint32_t(by) * 4 + y, uint32_t(bz) * 4 + z), v);
+    }
+    if (nlow < 2) return;
+    __syncthreads();
+    if (threadIdx.x < 8) {
+        const uint32_t x = threadIdx.x & 1u, y = (threadIdx.x >> 1) & 1u, z = threadIdx.x >> 2;
+        const float4 v = iso_mean8([&](int dx, int dy, int dz) { return s_l1[((2 * z + dz) << 4) + ((2 * y + dy) << 2) + 2 * x + dx]; });
+        s_l2[threadIdx.x] = v;
+        store_vox(chain.base, F184GI_FMT_F32,
+                  chain.off[2] + vox_index(2, chain.ldim[2], uint32_t(bx) * 2 + x, uint32_t(by) * 2 + y, uint32_t(bz) * 2 + z), v);
+    }
+    if (nlow < 3) return;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const float4 v = iso_mean8([&](int dx, int dy, int dz) { return s_l2[(dz << 2) + (dy << 1) + dx]; });
+        store_vox(chain.base, F184GI_FMT_F32, chain.off[3] + vox_index(3, chain.ldim[3], uint32_t(bx), uint32_t(by), uint32_t(bz)), v);
     }
 }
 
@@ -750,7 +799,8 @@ int voxelize_bricks_launch(const VoxelizeJob& job, void* scratch, size_t scratch
     VoxScratch sc = carve_scratch(job, scratch, &mask);
     const uint32_t nblocks = job.ndirty ? job.ndirty : nbricks;
     vox_bricks<<<nblocks, kChunk, 0, s>>>(sc, job.d_frame, dim, job.chain, job.light, job.shadow_keys, job.shadow_res,
-                                       job.counts, job.ndirty ? job.dirty_bricks : nullptr, job.weights, d_status);
+                                       job.counts, job.ndirty ? job.dirty_bricks : nullptr, job.weights,
+                                       job.weights ? 0u : job.mip_levels, d_status);
     note_launches(1);
     return cuda_fail(cudaGetLastError(), "voxelize");
 }

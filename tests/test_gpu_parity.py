@@ -175,6 +175,33 @@ def test_dirty_brick_revoxelize_equals_full(lib):
     assert np.array_equal(inc.view(np.uint32), ref.view(np.uint32))
 
 
+def _chain_bytes(c):
+    return [c.gi.read_level(c.grid, lv).view(np.uint32).copy() for lv in range(c.levels)]
+
+
+@pytest.mark.parametrize("dim,levels", [(64, 6), (16, 4), (32, 2)])
+def test_mip_from_voxelized_low_levels_equals_build_from_l0(lib, dim, levels):
+    """Isotropic FP32 grids: the voxelization writes each brick's block of levels 1..3 with L0 and the mip goes on
+    from level 3.  The chain equals a build from L0 (forced by handing out a level pointer), after a full
+    voxelization and after dirty-brick updates (all bricks, and an arbitrary half of them)."""
+    c = Case(ntris=20000, nobj=200, dim=dim, levels=levels, res=1024, keep_counts=False)
+    nb = (dim // 8) ** 3
+    for dirty in (None, np.arange(nb, dtype=np.uint32), np.arange(0, nb, 2, dtype=np.uint32)):
+        if dirty is not None:
+            c.sc.move_objects(7 + len(dirty), 0.05, 1.0)
+            c.upload(c.sc.tri_xyz, c.sc.albedo)
+        c.voxelize(dirty=dirty)
+        c.mip()
+        continued = _chain_bytes(c)
+        assert np.abs(c.gi.read_level(c.grid, min(1, levels - 1))).sum() > 0
+        c.gi.level_ptr(c.grid, 0)
+        c.mip()
+        rebuilt = _chain_bytes(c)
+        for lv in range(levels):
+            assert np.array_equal(continued[lv], rebuilt[lv]), "level %d differs (dirty=%s)" % (
+                lv, None if dirty is None else len(dirty))
+
+
 def test_fp16_storage_trace_error(lib, orc):
     c = Case(fmt=1)
     c.voxelize()
