@@ -183,7 +183,9 @@ int f184gi_grid_bytes(const f184gi_grid_desc* desc, uint64_t* bytes);
  * (device, R in the low byte) into `grid`, injecting the directional light through a shadow map that this
  * call rasterizes.  bounds (host pointer) fixes the grid placement; NULL = the triangles' own AABB,
  * reduced on the device.  dirty_bricks (device, brick indices in Morton order) limits the rewrite to those
- * 8^3 bricks of L0 (ndirty = 0: whole grid); the shadow map is always rebuilt. */
+ * 8^3 bricks of L0 (ndirty = 0: whole grid); the shadow map is always rebuilt.  Isotropic FP32 grids without
+ * resident weights also get each rewritten brick's block of levels 1..3 (the mip values of L0), so the next
+ * f184gi_mip continues from level 3 with the same bytes as a build from L0. */
 int f184gi_voxelize(f184gi_ctx* ctx, uint32_t grid, const float* tri_xyz, const uint32_t* albedo,
                     uint64_t ntris, const f184gi_bounds* bounds, const f184gi_light* light,
                     const uint32_t* dirty_bricks, uint32_t ndirty, void* stream);
@@ -377,7 +379,8 @@ int f184gi_grid_read_counts(f184gi_ctx* ctx, uint32_t grid, uint32_t* host_count
 /* device pointer and byte size of one level (for callers that sample the chain themselves).  Layout: level 0 in
  * 8^3 bricks (voxels x fastest) in Morton order of brick coordinates; levels >= 1 linear, x fastest, inside a
  * one-voxel ring of zeros ((d + 2)^3 elements; voxel (x, y, z) at ((z + 1) (d + 2) + y + 1) (d + 2) + x + 1);
- * anisotropic levels hold six such volumes (+x, -x, +y, -y, +z, -z) back to back. */
+ * anisotropic levels hold six such volumes (+x, -x, +y, -y, +z, -z) back to back.  The caller may write through
+ * the pointer: the grid's next f184gi_mip then builds every level from L0. */
 int f184gi_grid_level_ptr(f184gi_ctx* ctx, uint32_t grid, uint32_t level, void** dev_ptr, uint64_t* bytes);
 
 /* Host computation of the grid frame that f184gi_voxelize derives from `bounds` (bit-identical to it). */
