@@ -27,7 +27,7 @@ PLAIN_LARGE = dict(name="plain-large", seed=1184, ntris=500000, nobjects=2000, d
                    width=1920, height=1080)
 SMALL = dict(name="plain-small-gpu", seed=184, ntris=20000, nobjects=200, dim=64, levels=6, shadow_res=1024,
              width=640, height=360)
-E2E_LANES = 3  # request lanes of the end-to-end measurement (each its own context, grid, buffers and stream)
+E2E_LANES = 1  # compute lanes of the end-to-end measurement (each its own context, grid and stream)
 
 
 def workload_desc(cfg, storage="f32"):
@@ -394,51 +394,70 @@ def run_gpu(args, cfg):
     value = replica_mpix(npix, ms_per_step, world)
 
     # ---- end to end through the API with host buffers ----
-    # E2E_LANES request lanes (each its own context, grid, device buffers and stream) take the steps in turn, so
-    # one request's copies overlap the others' kernels; every step still copies its inputs in from pinned host
-    # memory and its traced image out.  A lane runs its copy-in, kernels and copy-out in order, so with two lanes
-    # both tend to copy at once while the GPU idles (2.38 ms per plain-large request against 2.21 with three).
+    # E2E_LANES compute lanes (each its own context, grid and stream) take the requests in turn; the copies run on
+    # one copy-in and one copy-out stream, in request order, into and out of 2 x E2E_LANES sets of device buffers,
+    # so a request's inputs arrive and its image leaves while other requests compute.  Every step still copies its
+    # inputs in from pinned host memory and its traced image out.  Measured per plain-large request: one lane
+    # 2.253 ms (two runs), two lanes 2.251-2.277, three 2.271-2.308 (requests computing at the same time share the
+    # SMs badly: the bricks' shared memory takes L1 from a concurrent trace); lanes that carried their own copies
+    # in order on their streams 2.38 ms with two (both lanes copying at once while the GPU idles) and 2.20-2.31 ms
+    # with three.
     h2d = tri_h.numel() * 4 + alb_h.numel() * 4 + sum(x.numel() * x.element_size() for x in gbuf_h)
     d2h = out.numel() * 4
-    lanes = [dict(gi=gi, grid=grid, tri=tri, alb=alb, gbuf=[depth, normal, rgh], out=out, out_h=out_h, view=view,
-                  stream=stream)]
+    lanes = [dict(gi=gi, grid=grid, stream=stream)]
     for _ in range(E2E_LANES - 1):
         gl = g.VoxelGI(local)
+        lanes.append(dict(gi=gl, grid=gl.create_grid(dim, levels, fmt, 0, res), stream=torch.cuda.Stream(dev)))
+    sets = [dict(tri=tri, alb=alb, gbuf=[depth, normal, rgh], out=out, out_h=out_h, view=view)]
+    for _ in range(2 * E2E_LANES - 1):
         dl = [torch.empty_like(depth), torch.empty_like(normal), torch.empty_like(rgh)]
         ol = torch.empty_like(out)
-        lanes.append(dict(gi=gl, grid=gl.create_grid(dim, levels, fmt, 0, res), tri=torch.empty_like(tri),
-                          alb=torch.empty_like(alb), gbuf=dl, out=ol, out_h=torch.empty_like(out_h).pin_memory(),
-                          view=g.make_view(V, P, W, H, dl[0].data_ptr(), dl[1].data_ptr(), dl[2].data_ptr(),
-                                           ol.data_ptr()),
-                          stream=torch.cuda.Stream(dev)))
+        sets.append(dict(tri=torch.empty_like(tri), alb=torch.empty_like(alb), gbuf=dl, out=ol,
+                         out_h=torch.empty_like(out_h).pin_memory(),
+                         view=g.make_view(V, P, W, H, dl[0].data_ptr(), dl[1].data_ptr(), dl[2].data_ptr(),
+                                          ol.data_ptr())))
+    for S in sets:
+        S.update(in_ready=torch.cuda.Event(), in_free=torch.cuda.Event(), out_ready=torch.cuda.Event(),
+                 out_free=torch.cuda.Event())
+    cin, cout = torch.cuda.Stream(dev), torch.cuda.Stream(dev)
 
-    def e2e_step(L):
-        with torch.cuda.stream(L["stream"]):
-            L["tri"].copy_(tri_h, non_blocking=True)
-            L["alb"].copy_(alb_h, non_blocking=True)
-            for d_, h_ in zip(L["gbuf"], gbuf_h):
+    def e2e_step(k):
+        S, L = sets[k % len(sets)], lanes[k % len(lanes)]
+        with torch.cuda.stream(cin):  # inputs in, once the request that last used this set has read them
+            cin.wait_event(S["in_free"])
+            S["tri"].copy_(tri_h, non_blocking=True)
+            S["alb"].copy_(alb_h, non_blocking=True)
+            for d_, h_ in zip(S["gbuf"], gbuf_h):
                 d_.copy_(h_, non_blocking=True)
-            s_ = L["stream"].cuda_stream
-            L["gi"].voxelize(L["grid"], L["tri"].data_ptr(), L["alb"].data_ptr(), sc.ntris, light, bounds=sc.bounds,
-                             stream=s_)
-            L["gi"].mip(L["grid"], stream=s_)
-            L["gi"].trace(L["grid"], [L["view"]], stream=s_)
-            L["out_h"].copy_(L["out"], non_blocking=True)
+            S["in_ready"].record(cin)
+        ls = L["stream"]
+        ls.wait_event(S["in_ready"])
+        ls.wait_event(S["out_free"])  # its image buffer copied out
+        L["gi"].voxelize(L["grid"], S["tri"].data_ptr(), S["alb"].data_ptr(), sc.ntris, light, bounds=sc.bounds,
+                         stream=ls)
+        L["gi"].mip(L["grid"], stream=ls)
+        L["gi"].trace(L["grid"], [S["view"]], stream=ls)
+        S["in_free"].record(ls)
+        S["out_ready"].record(ls)
+        with torch.cuda.stream(cout):
+            cout.wait_event(S["out_ready"])
+            S["out_h"].copy_(S["out"], non_blocking=True)
+            S["out_free"].record(cout)
 
-    for L in lanes:  # warm every lane
-        e2e_step(L)
+    for k in range(len(sets)):  # warm every lane and buffer set
+        e2e_step(k)
     torch.cuda.synchronize(dev)
     barrier()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     e0.record(stream)
-    for L in lanes:
-        L["stream"].wait_event(e0)
+    for st in [cin, cout] + [L["stream"] for L in lanes[1:]]:
+        st.wait_event(e0)
     for k in range(args.steps):
-        e2e_step(lanes[k % len(lanes)])
-    for L in lanes[1:]:
+        e2e_step(k)
+    for st in [cout] + [L["stream"] for L in lanes[1:]]:
         done = torch.cuda.Event()
-        done.record(L["stream"])
+        done.record(st)
         stream.wait_event(done)
     e1.record(stream)
     barrier()
@@ -500,8 +519,9 @@ def run_gpu(args, cfg):
                                          "a torch copy of 2 x 40 MiB held in L2" % esz}},
         "e2e": {"value": round(e2e_value, 4), "unit": "Mpix/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "ms_per_step": round(e2e_ms, 4),
-                "note": "through the API from pinned host buffers; %d request lanes (context, grid, stream) take "
-                        "the steps in turn so one request's copies overlap the others' kernels" % len(lanes)},
+                "note": "through the API from pinned host buffers; %d compute lanes (context, grid, stream) take the "
+                        "requests in turn, their copies on a copy-in and a copy-out stream into and out of %d device "
+                        "buffer sets, so a request's copies overlap other requests' kernels" % (len(lanes), len(sets))},
         "gpu_launches": int(launches),
         "clocks": clk,
         # the traced image is lit (a black image would trace trivially short cones)
