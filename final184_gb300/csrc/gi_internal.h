@@ -187,13 +187,15 @@ struct TraceVariant {
 constexpr uint32_t kTraceVariantCount = 5;
 constexpr TraceVariant kTraceVariants[kTraceVariantCount] = {
     {16, 8, 4}, {4, 24, 7}, {4, 32, 7}, {8, 16, 5}, {4, 24, 9}};
-// The one-shot launch's variant per chain (per 1080p view; the CTAs per SM set the register budget):
-// isotropic FP32 chains take 96-thread CTAs of 4x8-pixel warp tiles at 7 per SM (80 registers, 8 resident:
-// 1.60 ms), FP16 and anisotropic chains 128-thread CTAs of 4x8 tiles at 7 per SM (72 registers; the 512^3
-// anisotropic FP16 4K view 15.3 ms against 15.7 with 8x4 tiles at 5 per SM).  With every cone marched from one
-// call site the pixel's state between cones goes to local memory at these budgets, reloaded once per cone.
+// The one-shot launch's variant (per 1080p view; the CTAs per SM set the register budget): 128-thread CTAs of
+// 4x8-pixel warp tiles at 7 per SM (72 registers) for every chain: FP32 1.622 ms against 1.628 for 96-thread CTAs
+// at 7 per SM (80 registers, 8 resident), FP16 1.848; the 512^3 anisotropic FP16 4K view 15.3 ms against 15.7 with
+// 8x4 tiles at 5 per SM.  With every cone marched from one call site the pixel's state between cones goes to local
+// memory at these budgets, reloaded once per cone.
 constexpr uint32_t trace_default_variant(uint32_t fmt, bool aniso) {
-    return aniso ? 2u : (fmt == F184GI_FMT_F32 ? 1u : 2u);
+    (void)fmt;
+    (void)aniso;
+    return 2u;
 }
 const void* trace_kernel_fn(uint32_t fmt, bool aniso, uint32_t variant);
 const void* trace_kernel_count_fn(uint32_t fmt, bool aniso);  // instrumented, default variant's tile shape

@@ -459,16 +459,18 @@ __device__ void trace_pixel(const GridRef& g, const uint32_t* lut, const TraceCo
         rd = norm3(sub3(vd, mul3(nw, 2.0f * dn)));
         th = fmaxf(rough, tc.p.min_spec_tan_half);
     }
-    float3 bx, by, bz;
-    coord_space(nw, bx, by, bz);
     // Every cone goes through one call site (one inlined copy of the march: the kernel's code stays small in the
     // instruction cache): k < nd the diffuse cones (the normal, then four tilted 60 degrees at phi = 0, 90, 180,
     // 270 degrees), k = nd the specular cone (no precomputed schedule: ns = 0).
     const uint32_t nd = tc.p.diffuse_cones >= 5 ? 5u : 1u;
     const uint32_t ncones = nd + (tc.p.specular ? 1u : 0u);
-    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f), sp = make_float4(0.f, 0.f, 0.f, 0.f);
+    // Carried between cones: the origin, the normal, the specular cone and the diffuse sum; the normal's frame
+    // is formed again for each diffuse cone (the same operations, so the same directions) rather than kept.
+    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll 1
     for (uint32_t k = 0; k < ncones; ++k) {
+        float3 bx, by, bz;
+        coord_space(nw, bx, by, bz);
         float3 dir = bz;
         float tan_half = tc.p.diffuse_tan_half;
         uint32_t ns = kDiffuseSched;
@@ -483,7 +485,7 @@ __device__ void trace_pixel(const GridRef& g, const uint32_t* lut, const TraceCo
         }
         const float4 c = cone<FMT, ANISO, COUNT>(g, lut, tc, oi, of, dir, tan_half, sched, ns, cnt);
         if (k >= nd) {
-            sp = c;
+            store_out(v.out, v.out_format, npix + pi, c);  // the specular cone is the last
         } else if (nd == 1) {
             acc = c;
         } else if (k == 0) {
@@ -496,7 +498,7 @@ __device__ void trace_pixel(const GridRef& g, const uint32_t* lut, const TraceCo
         }
     }
     store_out(v.out, v.out_format, pi, acc);
-    store_out(v.out, v.out_format, npix + pi, sp);
+    if (!tc.p.specular) store_out(v.out, v.out_format, npix + pi, make_float4(0.f, 0.f, 0.f, 0.f));
 }
 
 // Work is handed out per warp: a warp tile is TW x (32 / TW) pixels, one lane each, and the warp tiles of all
