@@ -13,13 +13,25 @@
 namespace f184 {
 namespace {
 
+// Vector helpers with every operation rounded on its own (the intrinsics are never contracted into FMAs): the
+// per-pixel set-up then computes the same bits in every kernel variant, however each is scheduled, and the same
+// bits as the FP32 restatement, which is compiled without contraction.
 __device__ __forceinline__ float3 f3(float x, float y, float z) { return make_float3(x, y, z); }
-__device__ __forceinline__ float3 add3(float3 a, float3 b) { return f3(a.x + b.x, a.y + b.y, a.z + b.z); }
-__device__ __forceinline__ float3 sub3(float3 a, float3 b) { return f3(a.x - b.x, a.y - b.y, a.z - b.z); }
-__device__ __forceinline__ float3 mul3(float3 a, float s) { return f3(a.x * s, a.y * s, a.z * s); }
-__device__ __forceinline__ float dot3(float3 a, float3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ float3 add3(float3 a, float3 b) {
+    return f3(__fadd_rn(a.x, b.x), __fadd_rn(a.y, b.y), __fadd_rn(a.z, b.z));
+}
+__device__ __forceinline__ float3 sub3(float3 a, float3 b) {
+    return f3(__fsub_rn(a.x, b.x), __fsub_rn(a.y, b.y), __fsub_rn(a.z, b.z));
+}
+__device__ __forceinline__ float3 mul3(float3 a, float s) {
+    return f3(__fmul_rn(a.x, s), __fmul_rn(a.y, s), __fmul_rn(a.z, s));
+}
+__device__ __forceinline__ float dot3(float3 a, float3 b) {
+    return __fadd_rn(__fadd_rn(__fmul_rn(a.x, b.x), __fmul_rn(a.y, b.y)), __fmul_rn(a.z, b.z));
+}
 __device__ __forceinline__ float3 cross3(float3 a, float3 b) {
-    return f3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+    return f3(__fsub_rn(__fmul_rn(a.y, b.z), __fmul_rn(a.z, b.y)), __fsub_rn(__fmul_rn(a.z, b.x), __fmul_rn(a.x, b.z)),
+              __fsub_rn(__fmul_rn(a.x, b.y), __fmul_rn(a.y, b.x)));
 }
 // acc += w * v per component as two packed FP32 FMAs (fma.rn.f32x2): each component is rounded once, exactly
 // as fmaf(w, v.c, acc.c), with half the instructions.
@@ -40,8 +52,8 @@ __device__ __forceinline__ void fma4(float4& acc, float w, const float4& v) {
     unpack2(hi, acc.z, acc.w);
 }
 __device__ __forceinline__ float3 norm3(float3 a) {
-    float l = sqrtf(dot3(a, a));
-    return l > 0.0f ? mul3(a, 1.0f / l) : a;
+    float l = __fsqrt_rn(dot3(a, a));
+    return l > 0.0f ? mul3(a, __fdiv_rn(1.0f, l)) : a;
 }
 
 // make_coord_space, indirect.frag:71-86
@@ -63,11 +75,11 @@ __device__ __forceinline__ void coord_space(float3 n, float3& x, float3& y, floa
 __device__ __forceinline__ float3 oct_decode(uint32_t p) {
     float x = __half2float(__ushort_as_half(uint16_t(p & 0xffffu)));
     float y = __half2float(__ushort_as_half(uint16_t(p >> 16)));
-    float3 v = f3(x, y, 1.0f - fabsf(x) - fabsf(y));
+    float3 v = f3(x, y, __fsub_rn(__fsub_rn(1.0f, fabsf(x)), fabsf(y)));
     if (v.z < 0.0f) {
         float ox = v.x, oy = v.y;
-        v.x = (1.0f - fabsf(oy)) * (ox >= 0.0f ? 1.0f : -1.0f);
-        v.y = (1.0f - fabsf(ox)) * (oy >= 0.0f ? 1.0f : -1.0f);
+        v.x = __fmul_rn(__fsub_rn(1.0f, fabsf(oy)), ox >= 0.0f ? 1.0f : -1.0f);
+        v.y = __fmul_rn(__fsub_rn(1.0f, fabsf(ox)), oy >= 0.0f ? 1.0f : -1.0f);
     }
     return norm3(v);
 }
@@ -378,11 +390,12 @@ __device__ float4 cone(const GridRef& g, const uint32_t* lut, const TraceConsts&
         // the finer level's neighbour above is never level 0: its copy carries the ringed path only
         if (two) level_sample<FMT, ANISO, true>(g, lut, l0 + 1, oi, x, dir, f, s);
         if (FMT != F184GI_FMT_F32) s.w *= kAlphaScale<FMT>;  // the unorm16 opacity sum, scaled once
-        float tr = 1.0f - alpha;
-        cr += tr * s.x;
-        cg += tr * s.y;
-        cb += tr * s.z;
-        alpha += tr * s.w;
+        // front-to-back composite, one fused multiply-add per channel (explicit: the same rounding in every variant)
+        const float tr = __fsub_rn(1.0f, alpha);
+        cr = __fmaf_rn(tr, s.x, cr);
+        cg = __fmaf_rn(tr, s.y, cg);
+        cb = __fmaf_rn(tr, s.z, cb);
+        alpha = __fmaf_rn(tr, s.w, alpha);
         if (alpha >= tc.p.alpha_stop) break;
         if (k + 1 >= ns) {
             // error-free sum t + step (explicit rounding: no contraction of the step's product into the sum)
@@ -431,8 +444,8 @@ __device__ void trace_pixel(const GridRef& g, const uint32_t* lut, const TraceCo
     for (int r = 0; r < 3; ++r) wpf[r] = ff_row(v.iview_h + 4 * r, v.iview_l + 4 * r, cx, cy, cz);
     const float3 wp = f3(wpf[0].h, wpf[1].h, wpf[2].h);
     float3 nv = oct_decode(v.normal[pi]);
-    float3 nw = norm3(f3(iv[0] * nv.x + iv[1] * nv.y + iv[2] * nv.z, iv[4] * nv.x + iv[5] * nv.y + iv[6] * nv.z,
-                         iv[8] * nv.x + iv[9] * nv.y + iv[10] * nv.z));
+    float3 nw = norm3(f3(dot3(f3(iv[0], iv[1], iv[2]), nv), dot3(f3(iv[4], iv[5], iv[6]), nv),
+                         dot3(f3(iv[8], iv[9], iv[10]), nv)));
     float rough = __half2float(__ushort_as_half(v.rough[pi]));
     // cone origin o = (wp - origin) * inv_vs + n * start_offset in voxel units, split as oi (integer) + of
     float3 oi, of;
@@ -456,7 +469,7 @@ __device__ void trace_pixel(const GridRef& g, const uint32_t* lut, const TraceCo
     if (tc.p.specular) {
         float3 vd = norm3(sub3(wp, f3(v.eye[0], v.eye[1], v.eye[2])));
         float dn = dot3(vd, nw);
-        rd = norm3(sub3(vd, mul3(nw, 2.0f * dn)));
+        rd = norm3(sub3(vd, mul3(nw, __fmul_rn(2.0f, dn))));
         th = fmaxf(rough, tc.p.min_spec_tan_half);
     }
     // Every cone goes through one call site (one inlined copy of the march: the kernel's code stays small in the
@@ -489,12 +502,12 @@ __device__ void trace_pixel(const GridRef& g, const uint32_t* lut, const TraceCo
         } else if (nd == 1) {
             acc = c;
         } else if (k == 0) {
-            acc = make_float4(0.25f * c.x, 0.25f * c.y, 0.25f * c.z, 0.25f * c.w);
+            acc = make_float4(__fmul_rn(0.25f, c.x), __fmul_rn(0.25f, c.y), __fmul_rn(0.25f, c.z), __fmul_rn(0.25f, c.w));
         } else {
-            acc.x += 0.1875f * c.x;
-            acc.y += 0.1875f * c.y;
-            acc.z += 0.1875f * c.z;
-            acc.w += 0.1875f * c.w;
+            acc.x = __fadd_rn(acc.x, __fmul_rn(0.1875f, c.x));
+            acc.y = __fadd_rn(acc.y, __fmul_rn(0.1875f, c.y));
+            acc.z = __fadd_rn(acc.z, __fmul_rn(0.1875f, c.z));
+            acc.w = __fadd_rn(acc.w, __fmul_rn(0.1875f, c.w));
         }
     }
     store_out(v.out, v.out_format, pi, acc);
