@@ -229,6 +229,17 @@ def test_dirty_updates_equal_full_voxelization(fx):
     gi.close()
 
 
+@pytest.fixture(scope="module")
+def fx32(lib):
+    return Fixture(fmt=0)
+
+
+@pytest.mark.gpu
+def test_every_trace_variant_matches_the_plain_path_fp32(fx32):
+    """As below on FP32 chains (the plain path's storage)."""
+    test_every_trace_variant_matches_the_plain_path(fx32)
+
+
 @pytest.mark.gpu
 def test_every_trace_variant_matches_the_plain_path(fx):
     """Each cone-trace kernel variant (tile shape, CTAs per SM), launched with a warp per tile or as a capped
