@@ -100,6 +100,37 @@ __device__ __forceinline__ void store_vox(void* base, uint32_t format, uint64_t 
     reinterpret_cast<uint2*>(base)[idx] = encode_f16_vox(v);
 }
 
+// Float-float arithmetic: unevaluated pairs h + l of FP32 (~2^-44 relative), every operation explicitly rounded
+// (Knuth's two-sum and the FMA two-product are exact), so a kernel and a restatement compiled without contraction
+// that run the same operations get the same bits.
+struct FF {
+    float h, l;
+};
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+    s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+__device__ __forceinline__ FF ff_norm(float s, float e) {  // |s| >= |e|
+    const float h = __fadd_rn(s, e);
+    return FF{h, __fsub_rn(e, __fsub_rn(h, s))};
+}
+__device__ __forceinline__ FF ff_add(FF a, FF b) {
+    float s, e;
+    two_sum(a.h, b.h, s, e);
+    return ff_norm(s, __fadd_rn(e, __fadd_rn(a.l, b.l)));
+}
+__device__ __forceinline__ FF ff_mul(FF a, FF b) {
+    const float p = __fmul_rn(a.h, b.h);
+    const float e = __fmaf_rn(a.h, b.l, __fmaf_rn(a.l, b.h, __fmaf_rn(a.h, b.h, -p)));
+    return ff_norm(p, e);
+}
+__device__ __forceinline__ FF ff_div(FF a, FF b) {
+    const float q = __fdiv_rn(a.h, b.h);
+    const FF r = ff_add(a, ff_mul(FF{-q, 0.0f}, b));  // a - q b
+    return ff_norm(q, __fdiv_rn(r.h, b.h));
+}
+
 // The isotropic mip value of a voxel: the mean of its 2x2x2 children, fetch(dx, dy, dz) returning child
 // (dx, dy, dz), summed in the order dz, dy, dx (one rounding per add, no multiply feeding an add) and scaled by
 // 1/8.  Every kernel that builds an isotropic level calls this, so the chain's bytes do not depend on which one did.

@@ -7,10 +7,10 @@
 //   0 <= z <= w, |x|,|y| <= 16 w is divided by w (skipped for w == 1) and snapped to 1/16 pixel in FP32; any
 //   other is clipped against those planes in FP64 (Sutherland-Hodgman on FP64 clip coordinates) and snapped in
 //   FP64; coverage by inclusive int64 edge functions at pixel centres; depth plane z0 + a (X - X0) + b (Y - Y0)
-//   solved in FP64 per triangle, rounded to FP32 and evaluated in FP32 in that operation order; per pixel the
-//   minimum of key = (depth bits << 32 | triangle index) wins.
-// Per-fragment work is FP32/int only and FP64 is left to the plane solve and to clipped triangles (the FP64
-// pipe of GB300 is narrow: an FP64 transform and snap of every triangle kept it 85% busy).
+//   solved per triangle in float-float arithmetic (clipped triangles: FP64), rounded to FP32 and evaluated in
+//   FP32 in that operation order; per pixel the minimum of key = (depth bits << 32 | triangle index) wins.
+// FP64 is left to clipped triangles (the FP64 pipe of GB300 is narrow: an FP64 transform and snap of every
+// triangle kept it 85% busy, and the FP64 plane solve alone cost ~0.02 ms of a 500k-triangle voxelization).
 // Work is binned into 16x16 pixel tiles (one CTA per tile, keys in shared memory).  Triangles spanning many
 // tiles are walked by a whole warp, so no thread serialises over a screen-sized triangle.
 #include "gi_device.cuh"
@@ -82,9 +82,13 @@ __device__ int clip_polygon(V4* poly, int n) {
 __device__ __forceinline__ double persp_div(double x, double w) { return w == 1.0 ? x : __ddiv_rn(x, w); }
 
 // Snapped triangle from its vertices in 1/16 pixel (X, Y) and NDC depth Z: orientation, the depth plane through
-// the three (FP64 solve, FP32 result) and the pixel range.
-__device__ __forceinline__ bool snap_finish(int64_t (&X)[3], int64_t (&Y)[3], double (&Z)[3], uint32_t W, uint32_t H,
-                                            uint32_t tri, SubTri& s) {
+// the three (FP32 result) and the pixel range.  With zf (the depths as the FP32 values they are, for triangles
+// inside the clip volume) the plane is solved in float-float arithmetic; a clipped triangle's FP64 depths are
+// solved in FP64.
+__device__ __forceinline__ bool snap_finish(int64_t (&X)[3], int64_t (&Y)[3], double (&Z)[3], const float* zf,
+                                            uint32_t W, uint32_t H, uint32_t tri, SubTri& s) {
+    float z[3] = {0.0f, 0.0f, 0.0f};
+    if (zf) z[0] = zf[0], z[1] = zf[1], z[2] = zf[2];
     int64_t area2 = (X[1] - X[0]) * (Y[2] - Y[0]) - (Y[1] - Y[0]) * (X[2] - X[0]);
     if (area2 == 0) return false;
     if (area2 < 0) {
@@ -93,6 +97,8 @@ __device__ __forceinline__ bool snap_finish(int64_t (&X)[3], int64_t (&Y)[3], do
         t = Y[1], Y[1] = Y[2], Y[2] = t;
         double tz = Z[1];
         Z[1] = Z[2], Z[2] = tz;
+        const float tzf = z[1];
+        z[1] = z[2], z[2] = tzf;
         area2 = -area2;
     }
     int64_t mnx = min(X[0], min(X[1], X[2])), mxx = max(X[0], max(X[1], X[2]));
@@ -102,16 +108,32 @@ __device__ __forceinline__ bool snap_finish(int64_t (&X)[3], int64_t (&Y)[3], do
     int64_t y0 = max(int64_t(0), -floor_div64(-(mny - 8), 16));
     int64_t y1 = min(int64_t(H) - 1, floor_div64(mxy - 8, 16));
     if (x0 > x1 || y0 > y1) return false;
-    // depth plane through the three snapped vertices (FP64 solve, FP32 result)
-    double dx1 = double(X[1] - X[0]), dy1 = double(Y[1] - Y[0]);
-    double dx2 = double(X[2] - X[0]), dy2 = double(Y[2] - Y[0]);
-    double dz1 = dsub(Z[1], Z[0]), dz2 = dsub(Z[2], Z[0]);
-    double D = double(area2);
-    double na = dsub(dmul(dz1, dy2), dmul(dz2, dy1));
-    double nb = dsub(dmul(dz2, dx1), dmul(dz1, dx2));
-    s.z0 = __double2float_rn(Z[0]);
-    s.a = __double2float_rn(__ddiv_rn(na, D));
-    s.b = __double2float_rn(__ddiv_rn(nb, D));
+    if (zf) {
+        // depth plane, float-float: dz exactly (two-sum of FP32 depths), the edge components exactly (|d| < 2^22),
+        // twice the area as an exact pair (< 2^45: the remainder of its FP32 rounding is below 2^21)
+        FF dz1, dz2;
+        two_sum(z[1], -z[0], dz1.h, dz1.l);
+        two_sum(z[2], -z[0], dz2.h, dz2.l);
+        const float dx1 = float(int32_t(X[1] - X[0])), dy1 = float(int32_t(Y[1] - Y[0]));
+        const float dx2 = float(int32_t(X[2] - X[0])), dy2 = float(int32_t(Y[2] - Y[0]));
+        const float dh = __ll2float_rn(area2);
+        const FF D{dh, float(int32_t(area2 - __float2ll_rn(dh)))};
+        const FF na = ff_add(ff_mul(dz1, FF{dy2, 0.0f}), ff_mul(dz2, FF{-dy1, 0.0f}));
+        const FF nb = ff_add(ff_mul(dz2, FF{dx1, 0.0f}), ff_mul(dz1, FF{-dx2, 0.0f}));
+        s.z0 = z[0];
+        s.a = ff_div(na, D).h;
+        s.b = ff_div(nb, D).h;
+    } else {  // depth plane through the three snapped vertices (FP64 solve, FP32 result)
+        double dx1 = double(X[1] - X[0]), dy1 = double(Y[1] - Y[0]);
+        double dx2 = double(X[2] - X[0]), dy2 = double(Y[2] - Y[0]);
+        double dz1 = dsub(Z[1], Z[0]), dz2 = dsub(Z[2], Z[0]);
+        double D = double(area2);
+        double na = dsub(dmul(dz1, dy2), dmul(dz2, dy1));
+        double nb = dsub(dmul(dz2, dx1), dmul(dz1, dx2));
+        s.z0 = __double2float_rn(Z[0]);
+        s.a = __double2float_rn(__ddiv_rn(na, D));
+        s.b = __double2float_rn(__ddiv_rn(nb, D));
+    }
     for (int i = 0; i < 3; ++i) {
         s.X[i] = int32_t(X[i]);
         s.Y[i] = int32_t(Y[i]);
@@ -133,12 +155,12 @@ __device__ bool snap(const V4& a, const V4& b, const V4& c, uint32_t W, uint32_t
         Y[i] = __double2ll_rn(dmul(dadd(ny, 1.0), 8.0 * double(H)));
         Z[i] = nz;
     }
-    return snap_finish(X, Y, Z, W, H, tri, s);
+    return snap_finish(X, Y, Z, nullptr, W, H, tri, s);
 }
 
 // The common case: a triangle inside the clip volume (0 <= z <= w, |x|, |y| <= 16 w), its clip coordinates in
 // FP32 (row . (x, y, z, 1) with the FP32-rounded matrix, each product and sum rounded in order), the perspective
-// division (skipped for w == 1) and the snap to 1/16 pixel in FP32.  FP64 is left to the plane solve.
+// division (skipped for w == 1) and the snap to 1/16 pixel in FP32; the plane in float-float.
 struct V4f {
     float x, y, z, w;
 };
@@ -154,15 +176,17 @@ __device__ __forceinline__ float persp_div_f(float x, float w) { return w == 1.0
 __device__ __forceinline__ bool snap_f(const V4f (&v)[3], uint32_t W, uint32_t H, uint32_t tri, SubTri& s) {
     int64_t X[3], Y[3];
     double Z[3];
+    float zf[3];
     const float sw = 8.0f * float(W), sh = 8.0f * float(H);  // exact: W, H <= 8192
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
         if (!(v[i].w > 0.0f)) return false;
         X[i] = __float2ll_rn(__fmul_rn(__fadd_rn(persp_div_f(v[i].x, v[i].w), 1.0f), sw));
         Y[i] = __float2ll_rn(__fmul_rn(__fadd_rn(persp_div_f(v[i].y, v[i].w), 1.0f), sh));
-        Z[i] = double(persp_div_f(v[i].z, v[i].w));
+        zf[i] = persp_div_f(v[i].z, v[i].w);
+        Z[i] = double(zf[i]);
     }
-    return snap_finish(X, Y, Z, W, H, tri, s);
+    return snap_finish(X, Y, Z, zf, W, H, tri, s);
 }
 
 // Edge function of (a, b) at p (1/16-pixel units): every factor fits 32 bits (snapped vertices and pixel centres

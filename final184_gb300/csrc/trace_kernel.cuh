@@ -106,37 +106,9 @@ __device__ __forceinline__ float4 load_vox_raw(const void* base, uint32_t idx) {
 template <int FMT>
 constexpr float kAlphaScale = FMT == F184GI_FMT_F32 ? 1.0f : kUnorm16;
 
-// Float-float arithmetic (unevaluated pairs h + l of FP32, ~2^-44 relative) for the pixel set-up, every
-// operation explicitly rounded: Knuth's two-sum and the FMA two-product are exact.  The cone origin in voxel units
-// comes out accurate to ~1e-9 voxel; an FP32 set-up (~1e-5 voxel at 256 voxels) moves the trilinear weights of a
-// grazing cone's first samples by 1e-5, which is a relative error of 1e-2 on a sample weighted 1e-3.
-struct FF {
-    float h, l;
-};
-__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
-    s = __fadd_rn(a, b);
-    const float bb = __fsub_rn(s, a);
-    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
-}
-__device__ __forceinline__ FF ff_norm(float s, float e) {  // |s| >= |e|
-    const float h = __fadd_rn(s, e);
-    return FF{h, __fsub_rn(e, __fsub_rn(h, s))};
-}
-__device__ __forceinline__ FF ff_add(FF a, FF b) {
-    float s, e;
-    two_sum(a.h, b.h, s, e);
-    return ff_norm(s, __fadd_rn(e, __fadd_rn(a.l, b.l)));
-}
-__device__ __forceinline__ FF ff_mul(FF a, FF b) {
-    const float p = __fmul_rn(a.h, b.h);
-    const float e = __fmaf_rn(a.h, b.l, __fmaf_rn(a.l, b.h, __fmaf_rn(a.h, b.h, -p)));
-    return ff_norm(p, e);
-}
-__device__ __forceinline__ FF ff_div(FF a, FF b) {
-    const float q = __fdiv_rn(a.h, b.h);
-    const FF r = ff_add(a, ff_mul(FF{-q, 0.0f}, b));  // a - q b
-    return ff_norm(q, __fdiv_rn(r.h, b.h));
-}
+// The pixel set-up runs in float-float arithmetic (FF, gi_device.cuh).  The cone origin in voxel units comes out
+// accurate to ~1e-9 voxel; an FP32 set-up (~1e-5 voxel at 256 voxels) moves the trilinear weights of a grazing
+// cone's first samples by 1e-5, which is a relative error of 1e-2 on a sample weighted 1e-3.
 // (h[0..3] + l[0..3]) . (x, y, z, 1)
 __device__ __forceinline__ FF ff_row(const float* h, const float* l, FF x, FF y, FF z) {
     FF s = ff_add(ff_mul(FF{h[0], l[0]}, x), ff_mul(FF{h[1], l[1]}, y));

@@ -121,17 +121,49 @@ int clip_polygon(V4* poly, int n) {
     return n;
 }
 
+// Float-float arithmetic (unevaluated FP32 pairs), the device's operations one for one (this file is compiled
+// without contraction, so each operation rounds once): the rasterizer's plane solve and the trace's pixel set-up.
+struct FF32 {
+    float h, l;
+};
+inline void ff_two_sum(float a, float b, float& s, float& e) {
+    s = a + b;
+    const float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+inline FF32 ff_norm(float s, float e) {
+    const float h = s + e;
+    return FF32{h, e - (h - s)};
+}
+inline FF32 ff_add(FF32 a, FF32 b) {
+    float s, e;
+    ff_two_sum(a.h, b.h, s, e);
+    return ff_norm(s, e + (a.l + b.l));
+}
+inline FF32 ff_mul(FF32 a, FF32 b) {
+    const float p = a.h * b.h;
+    const float e = std::fma(a.h, b.l, std::fma(a.l, b.h, std::fma(a.h, b.h, -p)));
+    return ff_norm(p, e);
+}
+inline FF32 ff_div(FF32 a, FF32 b) {
+    const float q = a.h / b.h;
+    const FF32 r = ff_add(a, ff_mul(FF32{-q, 0.0f}, b));
+    return ff_norm(q, r.h / b.h);
+}
+
 // Snapped triangle: vertices in 1/16 pixel, depth plane z(X, Y) = z0 + a (X - X0) + b (Y - Y0) with
-// z0, a, b rounded to FP32 from an FP64 plane solve.
+// z0, a, b rounded to FP32 from a float-float plane solve (FP32 depths) or an FP64 one (a clipped triangle).
 struct SnapTri {
     int64_t X[3], Y[3];
     double Z[3];
+    bool f32z = false;  // Z holds FP32 values (a triangle inside the clip volume)
     int64_t area2;
     float z0, a, b;
     int64_t x0, x1, y0, y1;  // pixel range, inclusive
 };
 
-// orientation, FP64 depth plane (rounded to FP32) and pixel range of a triangle already snapped to X, Y, Z
+// orientation, depth plane (rounded to FP32) and pixel range of a triangle already snapped to X, Y, Z
+// (raster.cu snap_finish)
 bool snap_finish(SnapTri& s, uint32_t W, uint32_t H) {
     int64_t area2 = (s.X[1] - s.X[0]) * (s.Y[2] - s.Y[0]) - (s.Y[1] - s.Y[0]) * (s.X[2] - s.X[0]);
     if (area2 == 0) return false;
@@ -142,7 +174,21 @@ bool snap_finish(SnapTri& s, uint32_t W, uint32_t H) {
         area2 = -area2;
     }
     s.area2 = area2;
-    {
+    if (s.f32z) {
+        const float z0 = float(s.Z[0]), z1 = float(s.Z[1]), z2 = float(s.Z[2]);
+        FF32 dz1, dz2;
+        ff_two_sum(z1, -z0, dz1.h, dz1.l);
+        ff_two_sum(z2, -z0, dz2.h, dz2.l);
+        const float dx1 = float(s.X[1] - s.X[0]), dy1 = float(s.Y[1] - s.Y[0]);
+        const float dx2 = float(s.X[2] - s.X[0]), dy2 = float(s.Y[2] - s.Y[0]);
+        const float dh = float(area2);
+        const FF32 D{dh, float(area2 - int64_t(dh))};
+        const FF32 na = ff_add(ff_mul(dz1, FF32{dy2, 0.0f}), ff_mul(dz2, FF32{-dy1, 0.0f}));
+        const FF32 nb = ff_add(ff_mul(dz2, FF32{dx1, 0.0f}), ff_mul(dz1, FF32{-dx2, 0.0f}));
+        s.z0 = z0;
+        s.a = ff_div(na, D).h;
+        s.b = ff_div(nb, D).h;
+    } else {
         double dx1 = double(s.X[1] - s.X[0]), dy1 = double(s.Y[1] - s.Y[0]);
         double dx2 = double(s.X[2] - s.X[0]), dy2 = double(s.Y[2] - s.Y[0]);
         double dz1 = s.Z[1] - s.Z[0], dz2 = s.Z[2] - s.Z[0];
@@ -206,6 +252,7 @@ bool snap_tri_f(const V4f v[3], uint32_t W, uint32_t H, SnapTri& s) {
         s.Y[i] = std::llrint(ny * sh);
         s.Z[i] = double(persp_div_f(v[i].z, v[i].w));
     }
+    s.f32z = true;
     return snap_finish(s, W, H);
 }
 
@@ -764,33 +811,6 @@ void cone(const Chain<T>& ch, Vec3<T> o, Vec3<T> dir, T tan_half, const f184gi_c
 // ~1e-9 voxel, split into an integer voxel oi and an offset of.  The march keeps the sample point as oi + x with x
 // small, and forms each level coordinate as (oi 2^-l - 0.5) split exactly into integer + fraction, plus x 2^-l:
 // the tap weights then carry the precision of x, not of the grid-sized coordinate.
-struct FF32 {
-    float h, l;
-};
-inline void ff_two_sum(float a, float b, float& s, float& e) {
-    s = a + b;
-    const float bb = s - a;
-    e = (a - (s - bb)) + (b - bb);
-}
-inline FF32 ff_norm(float s, float e) {
-    const float h = s + e;
-    return FF32{h, e - (h - s)};
-}
-inline FF32 ff_add(FF32 a, FF32 b) {
-    float s, e;
-    ff_two_sum(a.h, b.h, s, e);
-    return ff_norm(s, e + (a.l + b.l));
-}
-inline FF32 ff_mul(FF32 a, FF32 b) {
-    const float p = a.h * b.h;
-    const float e = std::fma(a.h, b.l, std::fma(a.l, b.h, std::fma(a.h, b.h, -p)));
-    return ff_norm(p, e);
-}
-inline FF32 ff_div(FF32 a, FF32 b) {
-    const float q = a.h / b.h;
-    const FF32 r = ff_add(a, ff_mul(FF32{-q, 0.0f}, b));
-    return ff_norm(q, r.h / b.h);
-}
 inline FF32 ff_row(const float* h, const float* l, FF32 x, FF32 y, FF32 z) {
     FF32 s = ff_add(ff_mul(FF32{h[0], l[0]}, x), ff_mul(FF32{h[1], l[1]}, y));
     s = ff_add(s, ff_mul(FF32{h[2], l[2]}, z));
