@@ -116,8 +116,10 @@ __device__ __forceinline__ bool snap_finish(int64_t (&X)[3], int64_t (&Y)[3], do
         two_sum(z[2], -z[0], dz2.h, dz2.l);
         const float dx1 = float(int32_t(X[1] - X[0])), dy1 = float(int32_t(Y[1] - Y[0]));
         const float dx2 = float(int32_t(X[2] - X[0])), dy2 = float(int32_t(Y[2] - Y[0]));
-        const float dh = __ll2float_rn(area2);
-        const FF D{dh, float(int32_t(area2 - __float2ll_rn(dh)))};
+        // area2 = hi 2^22 + lo with both parts exact in FP32: their two-sum is RN(area2) and its exact remainder,
+        // formed without the 64-bit conversions (FP64 pipe)
+        FF D;
+        two_sum(__fmul_rn(float(int32_t(area2 >> 22)), 4194304.0f), float(int32_t(area2 & 0x3fffff)), D.h, D.l);
         const FF na = ff_add(ff_mul(dz1, FF{dy2, 0.0f}), ff_mul(dz2, FF{-dy1, 0.0f}));
         const FF nb = ff_add(ff_mul(dz2, FF{dx1, 0.0f}), ff_mul(dz1, FF{-dx2, 0.0f}));
         s.z0 = z[0];
@@ -181,8 +183,10 @@ __device__ __forceinline__ bool snap_f(const V4f (&v)[3], uint32_t W, uint32_t H
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
         if (!(v[i].w > 0.0f)) return false;
-        X[i] = __float2ll_rn(__fmul_rn(__fadd_rn(persp_div_f(v[i].x, v[i].w), 1.0f), sw));
-        Y[i] = __float2ll_rn(__fmul_rn(__fadd_rn(persp_div_f(v[i].y, v[i].w), 1.0f), sh));
+        // inside the guard band |X|, |Y| < 17 * 8 * 8192 < 2^21: the 32-bit conversion rounds the same (the
+        // 64-bit one runs on the FP64 pipe)
+        X[i] = __float2int_rn(__fmul_rn(__fadd_rn(persp_div_f(v[i].x, v[i].w), 1.0f), sw));
+        Y[i] = __float2int_rn(__fmul_rn(__fadd_rn(persp_div_f(v[i].y, v[i].w), 1.0f), sh));
         zf[i] = persp_div_f(v[i].z, v[i].w);
         Z[i] = double(zf[i]);
     }
