@@ -340,7 +340,11 @@ __device__ V3 march_ray(const MarchShared& sh, const MarchJobDev& J, uint32_t pi
     return lo;
 }
 
-__global__ void __launch_bounds__(256) march_kernel(MarchJobDev J, MarchViewDev v) {
+// Eight CTAs of 256 threads per SM (32 registers, a few bytes spilled): each step of a ray is a dependent gather
+// from the volume, so the march wants warps to hide it (per 1080p view: 2.70 ms at 3 CTAs per SM and 68
+// registers, 2.32 / 2.08 / 1.98 at 4 / 5 / 6, 1.84 at 7 or 8).  Its arithmetic is written out operation by
+// operation, so the bits do not depend on the register budget.
+__global__ void __launch_bounds__(256, 8) march_kernel(MarchJobDev J, MarchViewDev v) {
     __shared__ MarchShared sh;
     if (threadIdx.x == 0 && threadIdx.y == 0) make_maps(J.frame_ptr, sh.maps);
     const uint32_t tid = threadIdx.y * blockDim.x + threadIdx.x;
