@@ -392,6 +392,7 @@ def run_gpu(args, cfg):
     stage = {"voxelize": [e[0].elapsed_time(e[1]) for e in evs], "mip": [e[1].elapsed_time(e[2]) for e in evs],
              "trace": [e[2].elapsed_time(e[3]) for e in evs]}
     value = replica_mpix(npix, ms_per_step, world)
+    ref_img = out.cpu().numpy().view(np.uint32).copy()  # the device-timed loop's image
 
     # ---- end to end through the API with host buffers ----
     # E2E_LANES compute lanes (each its own context, grid and stream) take the requests in turn; the copies run on
@@ -463,6 +464,9 @@ def run_gpu(args, cfg):
     barrier()
     e2e_ms = slowest_rank_ms(e0.elapsed_time(e1) / args.steps, dev)
     e2e_value = replica_mpix(npix, e2e_ms, world)
+    # every request traces the same inputs: the images copied out to the host equal the device-timed loop's
+    torch.cuda.synchronize(dev)
+    e2e_same = all(bool(np.array_equal(S["out_h"].numpy().view(np.uint32), ref_img)) for S in sets)
 
     # ---- roofline of the dominant kernel (HBM: nothing here is a dense contraction) ----
     # trace_kernel is the largest single kernel of a request (launch-list share ~42%); its stage is one launch
@@ -518,6 +522,7 @@ def run_gpu(args, cfg):
                                          "trace launch time; most are L1 hits, so it may exceed the L2 figure, "
                                          "a torch copy of 2 x 40 MiB held in L2" % esz}},
         "e2e": {"value": round(e2e_value, 4), "unit": "Mpix/s", "h2d_bytes_per_step": int(h2d),
+                "images_equal_device_loop": e2e_same,
                 "d2h_bytes_per_step": int(d2h), "ms_per_step": round(e2e_ms, 4),
                 "note": "through the API from pinned host buffers; %d compute lanes (context, grid, stream) take the "
                         "requests in turn, their copies on a copy-in and a copy-out stream into and out of %d device "
