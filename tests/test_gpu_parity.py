@@ -202,6 +202,21 @@ def test_mip_from_voxelized_low_levels_equals_build_from_l0(lib, dim, levels):
                 lv, None if dirty is None else len(dirty))
 
 
+def test_partial_mip_after_voxelized_low_levels(lib):
+    """f184gi_mip with fewer levels than the grid after a voxelization that wrote levels 1..3: the levels asked for
+    equal a build from L0, whether they end inside the voxelized ones (2) or beyond them (5)."""
+    c = Case(ntris=20000, nobj=200, dim=64, levels=6, res=1024, keep_counts=False)
+    c.voxelize()
+    c.mip()
+    full = _chain_bytes(c)
+    for n in (2, 5):
+        c.voxelize()
+        c.gi.mip(c.grid, levels=n)
+        c.gi.sync()
+        for lv in range(n):
+            assert np.array_equal(c.gi.read_level(c.grid, lv).view(np.uint32), full[lv]), (n, lv)
+
+
 def test_fp16_storage_trace_error(lib, orc):
     c = Case(fmt=1)
     c.voxelize()
