@@ -61,6 +61,30 @@ __device__ __forceinline__ int32_t clamp32(int64_t x) {
     return int32_t(x > int64_t(INT32_MAX) ? int64_t(INT32_MAX) : (x < int64_t(INT32_MIN) ? int64_t(INT32_MIN) : x));
 }
 
+// The nine edge x unit-axis tests of a triangle (box-relative vertices v) against the box of half size h.
+template <class T>
+__device__ __forceinline__ bool sat_edges(const T (&v)[3][3], T h) {
+#pragma unroll
+    for (int e = 0; e < 3; ++e) {
+        T ed[3];
+#pragma unroll
+        for (int b = 0; b < 3; ++b) ed[b] = v[(e + 1) % 3][b] - v[e][b];
+#pragma unroll
+        for (int ax = 0; ax < 3; ++ax) {
+            T a0 = 0, a1 = 0, a2 = 0;
+            if (ax == 0) a1 = ed[2], a2 = -ed[1];
+            if (ax == 1) a0 = -ed[2], a2 = ed[0];
+            if (ax == 2) a0 = ed[1], a1 = -ed[0];
+            const T p0 = a0 * v[0][0] + a1 * v[0][1] + a2 * v[0][2];
+            const T p1 = a0 * v[1][0] + a1 * v[1][1] + a2 * v[1][2];
+            const T p2 = a0 * v[2][0] + a1 * v[2][1] + a2 * v[2][2];
+            const T rr = h * ((a0 < 0 ? -a0 : a0) + (a1 < 0 ? -a1 : a1) + (a2 < 0 ? -a2 : a2));
+            if (min(p0, min(p1, p2)) > rr || max(p0, max(p1, p2)) < -rr) return false;
+        }
+    }
+    return true;
+}
+
 // Exact closed-set overlap of a triangle (fixed-point q) with the axis-aligned box of centre c, half size h.
 __device__ bool tri_box_sat(const int32_t* q, const int64_t c[3], int64_t h) {
     int64_t v[3][3];
@@ -79,22 +103,19 @@ __device__ bool tri_box_sat(const int32_t* q, const int64_t c[3], int64_t h) {
     int64_t s = n[0] * v[0][0] + n[1] * v[0][1] + n[2] * v[0][2];
     int64_t r = h * (iabs64(n[0]) + iabs64(n[1]) + iabs64(n[2]));
     if (s > r || s < -r) return false;
-    for (int e = 0; e < 3; ++e) {
-        int64_t ed[3];
-        for (int b = 0; b < 3; ++b) ed[b] = v[(e + 1) % 3][b] - v[e][b];
-        for (int ax = 0; ax < 3; ++ax) {
-            int64_t a0 = 0, a1 = 0, a2 = 0;
-            if (ax == 0) a1 = ed[2], a2 = -ed[1];
-            if (ax == 1) a0 = -ed[2], a2 = ed[0];
-            if (ax == 2) a0 = ed[1], a1 = -ed[0];
-            int64_t p0 = a0 * v[0][0] + a1 * v[0][1] + a2 * v[0][2];
-            int64_t p1 = a0 * v[1][0] + a1 * v[1][1] + a2 * v[1][2];
-            int64_t p2 = a0 * v[2][0] + a1 * v[2][1] + a2 * v[2][2];
-            int64_t rr = h * (iabs64(a0) + iabs64(a1) + iabs64(a2));
-            if (min(p0, min(p1, p2)) > rr || max(p0, max(p1, p2)) < -rr) return false;
-        }
+    // Vertices within 2^14 of the box centre (a triangle near its box: all but the largest) take the nine edge-axis
+    // tests in 32-bit integers: edge components < 2^15, each product < 2^29, a projection (two nonzero terms) < 2^30,
+    // the radius h (|a| + |a|) < 2^26 for h <= 2^10, so the bounds are the same integers the 64-bit form computes.
+    int64_t vmax = 0;
+    for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b) vmax = max(vmax, iabs64(v[a][b]));
+    if (vmax < (int64_t(1) << 14) && h <= 1024) {
+        int32_t w[3][3];
+        for (int a = 0; a < 3; ++a)
+            for (int b = 0; b < 3; ++b) w[a][b] = int32_t(v[a][b]);
+        return sat_edges<int32_t>(w, int32_t(h));
     }
-    return true;
+    return sat_edges<int64_t>(v, h);
 }
 
 // voxel range touched by the triangle's AABB (closed boxes), clamped to the grid
