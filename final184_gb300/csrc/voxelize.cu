@@ -377,6 +377,7 @@ struct ItemSetup {
     long long plo, phi;          // plane test bounds on n . m
     uint32_t wq[3];
     uint8_t l0[3], ext[3];       // voxel box inside the brick: first voxel and extent per axis
+    uint8_t small;               // |n| < 2^25 per component: the plane test of a voxel fits 32 bits
 };
 
 // The three projections' cell masks of an item (edge x unit-axis separating-axis tests), in integers of type T.
@@ -462,6 +463,8 @@ __device__ void item_part(const TriRec& r, const int64_t base[3], const int32_t 
     out.n[0] = n0, out.n[1] = n1, out.n[2] = n2;
     out.plo = sar7_ceil(sp - rr);  // overlap iff sp - rr <= 128 (n . m) <= sp + rr
     out.phi = sar7_floor(sp + rr);
+    const int64_t lim = int64_t(1) << 25;
+    out.small = (iabs64(n0) < lim && iabs64(n1) < lim && iabs64(n2) < lim) ? 1 : 0;
     out.wq[0] = r.wq[0], out.wq[1] = r.wq[1], out.wq[2] = r.wq[2];
 #pragma unroll
     for (int a = 0; a < 3; ++a) out.l0[a] = uint8_t(l0[a]), out.ext[a] = uint8_t(l1[a] - l0[a] + 1);
@@ -630,12 +633,30 @@ __global__ void __launch_bounds__(kChunk, 14) vox_bricks(VoxScratch sc, const f1
             const uint32_t col = uint32_t((((is.mask[1] >> lz) & 0x0101010101010101ull) * 0x0102040810204080ull) >> 56);
             uint32_t xm = uint32_t(is.mask[2] >> (8 * ly)) & col & 0xffu;
             if (!xm) continue;
-            const long long drow = is.n[1] * (2 * ly + 1) + is.n[2] * (2 * lz + 1);
-            while (xm) {
-                const int lx = __ffs(xm) - 1;
-                xm &= xm - 1;
-                const long long d = is.n[0] * (2 * lx + 1) + drow;
-                if (d < is.plo || d > is.phi) continue;
+            // the plane test n . m within [plo, phi] for the row's candidates; with |n| < 2^25 each term is below
+            // 15 * 2^25 and n . m below 2^31, so it runs in 32 bits against the bounds clamped to 32 bits (a bound
+            // beyond the 32-bit range decides nothing for a 32-bit value): the same decisions
+            uint32_t pass = 0;
+            if (is.small) {
+                const int32_t n0 = int32_t(is.n[0]);
+                const int32_t drow = int32_t(is.n[1]) * (2 * ly + 1) + int32_t(is.n[2]) * (2 * lz + 1);
+                const int32_t lo = int32_t(max(is.plo, (long long)INT32_MIN)), hi = int32_t(min(is.phi, (long long)INT32_MAX));
+                for (uint32_t m = xm; m; m &= m - 1) {
+                    const int lx = __ffs(m) - 1;
+                    const int32_t d = n0 * (2 * lx + 1) + drow;
+                    if (d >= lo && d <= hi) pass |= 1u << lx;
+                }
+            } else {
+                const long long drow = is.n[1] * (2 * ly + 1) + is.n[2] * (2 * lz + 1);
+                for (uint32_t m = xm; m; m &= m - 1) {
+                    const int lx = __ffs(m) - 1;
+                    const long long d = is.n[0] * (2 * lx + 1) + drow;
+                    if (d >= is.plo && d <= is.phi) pass |= 1u << lx;
+                }
+            }
+            while (pass) {
+                const int lx = __ffs(pass) - 1;
+                pass &= pass - 1;
                 const int li = lz * 64 + ly * 8 + lx;
 #pragma unroll
                 for (int c = 0; c < 3; ++c) {
