@@ -29,7 +29,9 @@ constexpr uint32_t kStage = 256;  // records staged per round by raster_tiles (o
 __constant__ uint32_t c_wmagic[17] = {0,    65536, 32768, 21846, 16384, 13108, 10923, 9363, 8192,
                                       7282, 6554,  5958,  5462,  5042,  4682,  4370,  4096};
 
-struct SubTri {
+// 48 bytes, 16-byte aligned: a record moves as three 16-byte loads or stores (the binning, staging and set-up
+// kernels read or write whole records; 0.562 -> 0.549 ms per 500k-triangle voxelization)
+struct __align__(16) SubTri {
     int32_t X[3], Y[3];
     float z0, a, b;
     uint32_t tri;

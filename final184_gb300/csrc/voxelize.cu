@@ -27,7 +27,8 @@ constexpr uint32_t kInvalid = 0xffffffffu;
 
 __constant__ float c_albedo_lut[256];  // (i / 255)^2.2
 
-struct TriRec {
+// 16-byte aligned (48 bytes): a record moves as three 16-byte loads or stores
+struct __align__(16) TriRec {
     int32_t q[9];    // snapped vertices (x0 y0 z0 x1 ...), 24.8 voxel fixed point
     uint32_t wq[3];  // injection weight per channel, 1.31 fixed point (<= 2^31); wq[0] = kInvalid marks skipped
 };
@@ -371,7 +372,8 @@ __global__ void __launch_bounds__(256) relight_bricks(const float4* __restrict__
 // test reads lo <= a . m <= hi in integers.  The nine edge x unit-axis tests each ignore one coordinate, so they
 // are evaluated once per cell of the three 8x8 projections of the item's voxel box into bit masks; a voxel is
 // covered when its three projection bits are set and the plane test passes.
-struct ItemSetup {
+// 16-byte aligned (96 bytes with the padding): a row reads its fields with 16-byte loads
+struct __align__(16) ItemSetup {
     unsigned long long mask[3];  // P = 0: bit y + 8z; P = 1: bit z + 8x; P = 2: bit x + 8y
     long long n[3];              // triangle normal (relative to the brick)
     long long plo, phi;          // plane test bounds on n . m
